@@ -1,0 +1,120 @@
+"""Initial conditions and drivers shared by the parity tests and bench.py.
+
+Cell centres follow samurai's Cell::center(): origin + length * (index + 0.5)
+(cell.hpp:130-138) with the unit box origin 0 and length 2^-level.
+"""
+import numpy as np
+
+
+def centers(level, coords):
+    length = 1.0 / np.left_shift(1, level.astype(np.int64)).astype(np.float64)
+    return length[:, None] * (coords.astype(np.float64) + 0.5)
+
+
+def disc(level, coords, xc=0.3, yc=0.3, radius=0.2):
+    """demos/FiniteVolume/advection_2d.cpp:22-44"""
+    c = centers(level, coords)
+    inside = ((c[:, 0] - xc) * (c[:, 0] - xc) + (c[:, 1] - yc) * (c[:, 1] - yc)) <= radius * radius
+    return np.where(inside, 1.0, 0.0)
+
+
+def readme_square(level, coords, length=0.2):
+    """README.md:110-118: u = 1 where |center - 0.5| <= length/2 in every direction"""
+    c = centers(level, coords)
+    inside = np.all(np.abs(c - 0.5) <= 0.5 * length, axis=1)
+    return np.where(inside, 1.0, 0.0)
+
+
+class SplitMix64:
+    """Fixed-algorithm RNG (SplitMix64) with a 53-bit uniform mapping, so the
+    synthetic inputs do not depend on a library's distribution code."""
+
+    def __init__(self, seed):
+        self.s = np.uint64(seed)
+
+    def next_u64(self):
+        with np.errstate(over="ignore"):
+            self.s = np.uint64(self.s + np.uint64(0x9E3779B97F4A7C15))
+            z = self.s
+            z = np.uint64((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9))
+            z = np.uint64((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB))
+            return np.uint64(z ^ (z >> np.uint64(31)))
+
+    def uniform(self, lo=0.0, hi=1.0):
+        u = float(self.next_u64() >> np.uint64(11)) * (1.0 / 9007199254740992.0)
+        return lo + (hi - lo) * u
+
+
+def shapes_2d(seed, n_squares=16, n_gauss=16):
+    """Seeded sum of indicator squares and Gaussians (the max_level-12 2D
+    workload: side U[0.02,0.1], centre U[0.2,0.8]^2, amplitude U[0.5,1],
+    Gaussian sigma U[0.005,0.03], centre U[0.2,0.8]^2, amplitude U[0.5,1])."""
+    rng = SplitMix64(seed)
+    sq = []
+    for _ in range(n_squares):
+        side = rng.uniform(0.02, 0.1)
+        cx, cy = rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8)
+        amp = rng.uniform(0.5, 1.0)
+        sq.append((side, cx, cy, amp))
+    ga = []
+    for _ in range(n_gauss):
+        sig = rng.uniform(0.005, 0.03)
+        cx, cy = rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8)
+        amp = rng.uniform(0.5, 1.0)
+        ga.append((sig, cx, cy, amp))
+
+    def f(level, coords):
+        c = centers(level, coords)
+        u = np.zeros(len(c))
+        for side, cx, cy, amp in sq:
+            inside = (np.abs(c[:, 0] - cx) <= 0.5 * side) & (np.abs(c[:, 1] - cy) <= 0.5 * side)
+            u = u + np.where(inside, amp, 0.0)
+        for sig, cx, cy, amp in ga:
+            r2 = (c[:, 0] - cx) * (c[:, 0] - cx) + (c[:, 1] - cy) * (c[:, 1] - cy)
+            u = u + amp * np.exp(-r2 / (2.0 * sig * sig))
+        return u
+
+    return f
+
+
+def ball_3d(seed, n_gauss=8):
+    """Seeded ball indicator (radius U[0.1,0.2], centre U[0.3,0.7]^3) plus
+    Gaussians (sigma U[0.01,0.05], centre U[0.3,0.7]^3, amplitude U[0.5,1])."""
+    rng = SplitMix64(seed)
+    rad = rng.uniform(0.1, 0.2)
+    bc = [rng.uniform(0.3, 0.7) for _ in range(3)]
+    ga = []
+    for _ in range(n_gauss):
+        sig = rng.uniform(0.01, 0.05)
+        cc = [rng.uniform(0.3, 0.7) for _ in range(3)]
+        amp = rng.uniform(0.5, 1.0)
+        ga.append((sig, cc, amp))
+
+    def f(level, coords):
+        c = centers(level, coords)
+        r2 = sum((c[:, d] - bc[d]) * (c[:, d] - bc[d]) for d in range(3))
+        u = np.where(r2 <= rad * rad, 1.0, 0.0)
+        for sig, cc, amp in ga:
+            r2 = sum((c[:, d] - cc[d]) * (c[:, d] - cc[d]) for d in range(3))
+            u = u + amp * np.exp(-r2 / (2.0 * sig * sig))
+        return u
+
+    return f
+
+
+def demo_time_loop(sim, dt, Tf, eps, regularity, a, scheme=0):
+    """The time loop of demos/FiniteVolume/advection_2d.cpp:124-156 (adapt,
+    clipped time step, ghost update, upwind), on any object exposing
+    adapt/update_ghost/upwind.  Returns the number of steps."""
+    t = 0.0
+    nt = 0
+    while t != Tf:
+        sim.adapt(eps, regularity)
+        t += dt
+        if t > Tf:
+            dt += Tf - t
+            t = Tf
+        sim.update_ghost()
+        sim.upwind(a, dt, scheme)
+        nt += 1
+    return nt
