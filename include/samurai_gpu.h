@@ -1,0 +1,117 @@
+/*
+ * C ABI of the GB300-native samurai MR advection path (libsamurai_gpu.so).
+ *
+ * samurai (hpc-maths/samurai v0.33.0) is a header-only C++ library with no
+ * FFI of its own; its "interface" for this path is the set of C++ calls a
+ * user program makes.  Each entry point below replaces one of them, cited
+ * next to it (paths relative to the samurai source tree).  The C++ drop-in
+ * headers under include/samurai/ and the Python package samurai_gb300 are
+ * thin layers over these functions.
+ *
+ * Conventions
+ *  - every call returns 0 (SG_OK) or a status code; sg_last_error() gives a
+ *    message for the calling thread.  No call aborts the process.
+ *  - host arrays are plain pointers with explicit sizes; field values in
+ *    host arrays use samurai's storage numbering of the reference mesh
+ *    (interval.index + x, level_cell_array.hpp:727-743).
+ *  - one mesh owns one CUDA stream; calls on a mesh are issued in order on
+ *    that stream by one host thread.
+ *  - there is no CPU fallback: without a usable sm_103a device every call
+ *    that computes returns SG_ERR_CUDA.
+ */
+#ifndef SAMURAI_GPU_H
+#define SAMURAI_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sg_mesh_s* sg_mesh_t;
+typedef struct sg_field_s* sg_field_t;
+
+enum sg_status
+{
+    SG_OK           = 0,
+    SG_ERR_ARG      = 1,
+    SG_ERR_CUDA     = 2,
+    SG_ERR_CAPACITY = 3,
+    SG_ERR_STATE    = 4,
+    SG_ERR_NOTFOUND = 5
+};
+
+/* MRMeshId (mr/mesh.hpp:25-33) */
+enum sg_mesh_id
+{
+    SG_CELLS            = 0,
+    SG_CELLS_AND_GHOSTS = 1,
+    SG_PROJ_CELLS       = 2,
+    SG_UNION_CELLS      = 3,
+    SG_REFERENCE        = 4
+};
+
+/* upwind variants */
+enum sg_scheme
+{
+    SG_UPWIND_OP = 0, /* unp1 = u - dt * samurai::upwind(a, u)  (stencil_field.hpp:91-179, demos/FiniteVolume/advection_2d.cpp:144) */
+    SG_README    = 1  /* the README for_each_interval lambda    (README.md:144-153) */
+};
+
+const char* sg_last_error(void);
+int sg_version(int* major, int* minor);
+
+/* Mesh on the unit box, uniform at max_level: samurai::mra::make_mesh(box, mesh_config<dim, prediction_radius>()
+ * .min_level().max_level().max_stencil_radius().graduation_width()) (mr/mesh.hpp:511-518, mesh_config.hpp:16-433),
+ * also the deprecated MRMesh<MRConfig<dim>>(box, min_level, max_level) (mr/mesh.hpp:166-181). */
+int sg_mesh_create(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width,
+                   sg_mesh_t* out);
+int sg_mesh_destroy(sg_mesh_t mesh);
+/* mesh.nb_cells(mesh_id_t::cells) and mesh.nb_cells() (= reference size) (mesh.hpp:530-550) */
+int sg_mesh_counts(sg_mesh_t mesh, long long* nb_cells, long long* nb_reference);
+/* for_each_cell(mesh, f) (algorithm.hpp:301-363): leaf cells in samurai order with their storage index */
+int sg_mesh_get_cells(sg_mesh_t mesh, int* level, int* coords, long long* index, long long capacity);
+/* LevelCellArray intervals of mesh[id][level] (level_cell_array.hpp:68-256): records (start, end, y[, z], index) */
+int sg_mesh_count_intervals(sg_mesh_t mesh, int mesh_id, int level, long long* n);
+int sg_mesh_get_intervals(sg_mesh_t mesh, int mesh_id, int level, long long* out, long long capacity);
+/* MRMesh(cl, cfg) from a leaf-cell list (mr/mesh.hpp:152-158); fields keep their storage but their values are void */
+int sg_mesh_set_cells(sg_mesh_t mesh, long long n, const int* level, const int* coords);
+/* the mesh's CUDA stream (cudaStream_t) for interop */
+int sg_mesh_stream(sg_mesh_t mesh, void** stream);
+int sg_mesh_synchronize(sg_mesh_t mesh);
+/* kernel launches issued on the mesh since the last reset (instrumentation) */
+int sg_mesh_launch_count(sg_mesh_t mesh, int reset, long long* count);
+
+/* samurai::make_scalar_field<double>(name, mesh) (field/scalar_field.hpp:173-216) */
+int sg_field_create(sg_mesh_t mesh, const char* name, sg_field_t* out);
+int sg_field_destroy(sg_field_t field);
+/* samurai::make_bc<samurai::Dirichlet<1>>(u, value) (bc/bc.hpp:786-800, bc/dirichlet.hpp:22-29) */
+int sg_field_set_dirichlet(sg_field_t field, double value);
+/* u.array() in the reference numbering, host memory (n = nb_reference) */
+int sg_field_upload(sg_field_t field, const double* values, long long n);
+int sg_field_download(sg_field_t field, double* values, long long n);
+/* the same with device memory (n = nb_reference), e.g. torch tensors */
+int sg_field_upload_device(sg_field_t field, const double* dvalues, long long n);
+int sg_field_download_device(sg_field_t field, double* dvalues, long long n);
+/* u[cell] for the leaf cells in for_each_cell order (n = nb_cells); other entries become 0 on upload */
+int sg_field_set_cells(sg_field_t field, const double* values, long long n);
+int sg_field_get_cells(sg_field_t field, double* values, long long n);
+/* std::swap(u.array(), unp1.array()) (demos/FiniteVolume/advection_2d.cpp:146) */
+int sg_field_swap(sg_field_t a, sg_field_t b);
+
+/* auto MRadaptation = samurai::make_MRAdapt(u); MRadaptation(mra_config().epsilon(eps).regularity(reg))
+ * (mr/adapt.hpp:147-203, 391-420); n_harten receives the number of Harten passes */
+int sg_adapt(sg_field_t u, double eps, double regularity, int* n_harten);
+/* one Harten pass (mr/adapt.hpp:276-389); converged = 1 at the fixed point */
+int sg_harten(sg_field_t u, int ite, double eps, double regularity, int* converged);
+/* samurai::update_ghost_mr(u) (algorithm/update_ghost_mr.hpp:261-270) */
+int sg_update_ghost_mr(sg_field_t u);
+/* unp1 = u - dt * samurai::upwind(a, u) on mesh[cells] (a has dim entries) */
+int sg_upwind(sg_field_t u, sg_field_t unp1, const double* a, double dt, int scheme);
+/* detail and tag fields of the last Harten pass, reference numbering (n = nb_reference) */
+int sg_detail_download(sg_field_t u, double* values, long long n);
+int sg_tag_download(sg_field_t u, unsigned char* values, long long n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SAMURAI_GPU_H */

@@ -1,0 +1,468 @@
+"""GB300-native MR advection path with samurai's API names.
+
+This package is the Python host side over the C ABI of libsamurai_gpu.so
+(include/samurai_gpu.h).  It mirrors the calls a samurai user program makes
+for the multiresolution advection path:
+
+    cfg  = mesh_config(2).min_level(4).max_level(10).max_stencil_size(2).disable_minimal_ghost_width()
+    mesh = mra.make_mesh(Box([0, 0], [1, 1]), cfg)        # mr/mesh.hpp:511-518
+    u    = make_scalar_field("u", mesh)                    # field/scalar_field.hpp:173-216
+    make_bc(Dirichlet(1), u, 0.)                           # bc/bc.hpp:786-800
+    MRadaptation = make_MRAdapt(u)                         # mr/adapt.hpp:391-397
+    MRadaptation(mra_config().epsilon(2e-4))               # mr/adapt.hpp:147-195
+    update_ghost_mr(u)                                     # algorithm/update_ghost_mr.hpp:261-270
+    unp1.assign_upwind(u, a, dt)                           # unp1 = u - dt * upwind(a, u)
+    swap(u, unp1)                                          # std::swap(u.array(), unp1.array())
+
+Everything that computes runs as sm_103a CUDA kernels; there is no CPU
+fallback, and a missing or unloadable library raises at first use.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBPATH = os.path.join(_HERE, "libsamurai_gpu.so")
+_lib = None
+
+SG_CELLS, SG_CELLS_AND_GHOSTS, SG_PROJ_CELLS, SG_UNION_CELLS, SG_REFERENCE = range(5)
+MESH_IDS = {"cells": 0, "cells_and_ghosts": 1, "proj_cells": 2, "union_cells": 3, "reference": 4, "all_cells": 4}
+UPWIND_OP, README = 0, 1
+
+
+class SamuraiGpuError(RuntimeError):
+    pass
+
+
+def library_path():
+    return _LIBPATH
+
+
+def lib():
+    """Load libsamurai_gpu.so (built in-tree by samurai_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIBPATH):
+        raise SamuraiGpuError("libsamurai_gpu.so is not built; run `python -m samurai_gb300.build` (there is no CPU fallback)")
+    L = ctypes.CDLL(_LIBPATH)
+    vp, i, d, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    pi, pl = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)
+    sig = {
+        "sg_last_error": (ctypes.c_char_p, []),
+        "sg_version": (i, [pi, pi]),
+        "sg_mesh_create": (i, [i, i, i, i, i, i, ctypes.POINTER(vp)]),
+        "sg_mesh_destroy": (i, [vp]),
+        "sg_mesh_counts": (i, [vp, pl, pl]),
+        "sg_mesh_get_cells": (i, [vp, vp, vp, vp, ll]),
+        "sg_mesh_count_intervals": (i, [vp, i, i, pl]),
+        "sg_mesh_get_intervals": (i, [vp, i, i, vp, ll]),
+        "sg_mesh_set_cells": (i, [vp, ll, vp, vp]),
+        "sg_mesh_stream": (i, [vp, ctypes.POINTER(vp)]),
+        "sg_mesh_synchronize": (i, [vp]),
+        "sg_mesh_launch_count": (i, [vp, i, pl]),
+        "sg_field_create": (i, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
+        "sg_field_destroy": (i, [vp]),
+        "sg_field_set_dirichlet": (i, [vp, d]),
+        "sg_field_upload": (i, [vp, vp, ll]),
+        "sg_field_download": (i, [vp, vp, ll]),
+        "sg_field_upload_device": (i, [vp, vp, ll]),
+        "sg_field_download_device": (i, [vp, vp, ll]),
+        "sg_field_set_cells": (i, [vp, vp, ll]),
+        "sg_field_get_cells": (i, [vp, vp, ll]),
+        "sg_field_swap": (i, [vp, vp]),
+        "sg_adapt": (i, [vp, d, d, pi]),
+        "sg_harten": (i, [vp, i, d, d, pi]),
+        "sg_update_ghost_mr": (i, [vp]),
+        "sg_upwind": (i, [vp, vp, vp, d, i]),
+        "sg_detail_download": (i, [vp, vp, ll]),
+        "sg_tag_download": (i, [vp, vp, ll]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(status, what):
+    if status != 0:
+        msg = lib().sg_last_error().decode(errors="replace")
+        raise SamuraiGpuError("%s failed (status %d): %s" % (what, status, msg))
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+# ---------------------------------------------------------------- configs
+class Box:
+    """samurai::Box<double, dim> (box.hpp); only the unit box is supported."""
+
+    def __init__(self, min_corner, max_corner):
+        self.min_corner = [float(v) for v in min_corner]
+        self.max_corner = [float(v) for v in max_corner]
+        if any(v != 0.0 for v in self.min_corner) or any(v != 1.0 for v in self.max_corner):
+            raise SamuraiGpuError("only the unit box [0,1]^dim is supported")
+
+    @property
+    def dim(self):
+        return len(self.min_corner)
+
+
+class mesh_config:
+    """samurai::mesh_config<dim, prediction_stencil_radius> (mesh_config.hpp:16-433)."""
+
+    def __init__(self, dim, prediction_stencil_radius=1):
+        self.dim = dim
+        self.prediction_stencil_radius = prediction_stencil_radius
+        self._min_level = 0
+        self._max_level = 6
+        self._max_stencil_radius = 1
+        self._graduation_width = 1
+        self._disable_minimal_ghost_width = False
+
+    def min_level(self, l):
+        self._min_level = l
+        return self
+
+    def max_level(self, l):
+        self._max_level = l
+        return self
+
+    def max_stencil_radius(self, r):
+        self._max_stencil_radius = r
+        return self
+
+    def max_stencil_size(self, s):
+        self._max_stencil_radius = s // 2 + (s % 2)
+        return self
+
+    def graduation_width(self, w):
+        self._graduation_width = w
+        return self
+
+    def disable_minimal_ghost_width(self):
+        self._disable_minimal_ghost_width = True
+        return self
+
+    def parse_args(self):
+        """mesh_config::parse_args without command-line overrides (mesh_config.hpp:358-396)."""
+        if self._max_level < self._min_level:
+            raise ValueError("Max level must be greater than min level.")
+        r = self._max_stencil_radius
+        if not self._disable_minimal_ghost_width:
+            r = max(r, 2)
+        return r
+
+
+class mra_config:
+    """samurai::mra_config (mr/config.hpp:10-67)."""
+
+    def __init__(self):
+        self._epsilon = 1e-4
+        self._regularity = 1.0
+        self._relative_detail = False
+
+    def epsilon(self, v=None):
+        if v is None:
+            return self._epsilon
+        self._epsilon = v
+        return self
+
+    def regularity(self, v=None):
+        if v is None:
+            return self._regularity
+        self._regularity = v
+        return self
+
+    def relative_detail(self, v=None):
+        if v is None:
+            return self._relative_detail
+        if v:
+            raise SamuraiGpuError("relative detail is not implemented")
+        return self
+
+
+# ------------------------------------------------------------------ mesh
+class MRMesh:
+    """samurai::MRMesh on the unit box (mr/mesh.hpp:74-211), device resident."""
+
+    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1):
+        self.dim = dim
+        self._min_level = min_level
+        self._max_level = max_level
+        self.max_stencil_radius = max_stencil_radius
+        self.prediction_radius = prediction_radius
+        self.graduation_width = graduation_width
+        h = ctypes.c_void_p()
+        _check(lib().sg_mesh_create(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, ctypes.byref(h)),
+               "sg_mesh_create")
+        self.h = h
+
+    @classmethod
+    def from_box(cls, box, min_level, max_level):
+        """Deprecated samurai constructor MRMesh<MRConfig<dim>>(box, min, max) (mr/mesh.hpp:166-181)."""
+        return cls(box.dim, min_level, max_level)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().sg_mesh_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    def min_level(self):
+        return self._min_level
+
+    def max_level(self):
+        return self._max_level
+
+    def cell_length(self, level):
+        """cell_length(1, level) (cell.hpp:17-20)"""
+        return 1.0 / (1 << level)
+
+    def min_cell_length(self):
+        return self.cell_length(self._max_level)
+
+    def counts(self):
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        _check(lib().sg_mesh_counts(self.h, ctypes.byref(a), ctypes.byref(b)), "sg_mesh_counts")
+        return a.value, b.value
+
+    def nb_cells(self, mesh_id="reference"):
+        nc, nr = self.counts()
+        return nr if MESH_IDS.get(mesh_id, mesh_id) == SG_REFERENCE else nc
+
+    def cells(self):
+        """for_each_cell order: (level, coords, storage index)"""
+        n, _ = self.counts()
+        level = np.empty(n, np.int32)
+        coords = np.empty((n, self.dim), np.int32)
+        index = np.empty(n, np.int64)
+        _check(lib().sg_mesh_get_cells(self.h, _ptr(level), _ptr(coords), _ptr(index), n), "sg_mesh_get_cells")
+        return level, coords, index
+
+    def intervals(self, mesh_id, level, with_index=False):
+        mid = MESH_IDS[mesh_id] if isinstance(mesh_id, str) else mesh_id
+        n = ctypes.c_longlong()
+        _check(lib().sg_mesh_count_intervals(self.h, mid, level, ctypes.byref(n)), "sg_mesh_count_intervals")
+        out = np.empty((n.value, self.dim + 2), np.int64)
+        _check(lib().sg_mesh_get_intervals(self.h, mid, level, _ptr(out), n.value), "sg_mesh_get_intervals")
+        return out if with_index else out[:, : self.dim + 1].astype(np.int32)
+
+    def set_cells(self, level, coords):
+        level = np.ascontiguousarray(level, np.int32)
+        coords = np.ascontiguousarray(coords, np.int32)
+        _check(lib().sg_mesh_set_cells(self.h, len(level), _ptr(level), _ptr(coords)), "sg_mesh_set_cells")
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(lib().sg_mesh_stream(self.h, ctypes.byref(s)), "sg_mesh_stream")
+        return s.value
+
+    def synchronize(self):
+        _check(lib().sg_mesh_synchronize(self.h), "sg_mesh_synchronize")
+
+    def launch_count(self, reset=False):
+        n = ctypes.c_longlong()
+        _check(lib().sg_mesh_launch_count(self.h, 1 if reset else 0, ctypes.byref(n)), "sg_mesh_launch_count")
+        return n.value
+
+
+class mra:
+    @staticmethod
+    def make_mesh(box, cfg):
+        """samurai::mra::make_mesh(box, cfg) (mr/mesh.hpp:511-518): uniform at max_level"""
+        if box.dim != cfg.dim:
+            raise ValueError("box and config dimensions differ")
+        r = cfg.parse_args()
+        return MRMesh(cfg.dim, cfg._min_level, cfg._max_level, r, cfg.prediction_stencil_radius, cfg._graduation_width)
+
+
+# ----------------------------------------------------------------- fields
+class ScalarField:
+    """samurai::ScalarField<MRMesh, double> (field/scalar_field.hpp:77-216)."""
+
+    def __init__(self, name, mesh):
+        self.name = name
+        self.mesh = mesh
+        h = ctypes.c_void_p()
+        _check(lib().sg_field_create(mesh.h, name.encode(), ctypes.byref(h)), "sg_field_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().sg_field_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    def array(self):
+        """u.array(): values in samurai's reference numbering (host copy)"""
+        n = self.mesh.nb_cells("reference")
+        out = np.empty(n, np.float64)
+        _check(lib().sg_field_download(self.h, _ptr(out), n), "sg_field_download")
+        return out
+
+    def set_array(self, values):
+        values = np.ascontiguousarray(values, np.float64)
+        _check(lib().sg_field_upload(self.h, _ptr(values), len(values)), "sg_field_upload")
+
+    def upload_device(self, ptr, n):
+        _check(lib().sg_field_upload_device(self.h, ctypes.c_void_p(ptr), n), "sg_field_upload_device")
+
+    def download_device(self, ptr, n):
+        _check(lib().sg_field_download_device(self.h, ctypes.c_void_p(ptr), n), "sg_field_download_device")
+
+    def set_cells(self, values):
+        """u[cell] = values for every leaf cell, in for_each_cell order"""
+        values = np.ascontiguousarray(values, np.float64)
+        _check(lib().sg_field_set_cells(self.h, _ptr(values), len(values)), "sg_field_set_cells")
+
+    def cell_values(self):
+        n = self.mesh.nb_cells("cells")
+        out = np.empty(n, np.float64)
+        _check(lib().sg_field_get_cells(self.h, _ptr(out), n), "sg_field_get_cells")
+        return out
+
+    def assign_upwind(self, u, a, dt, scheme=UPWIND_OP):
+        """self = u - dt * upwind(a, u) on mesh[cells]"""
+        a = np.ascontiguousarray(a, np.float64)
+        _check(lib().sg_upwind(u.h, self.h, _ptr(a), dt, scheme), "sg_upwind")
+
+    def detail(self):
+        n = self.mesh.nb_cells("reference")
+        out = np.empty(n, np.float64)
+        _check(lib().sg_detail_download(self.h, _ptr(out), n), "sg_detail_download")
+        return out
+
+    def tag(self):
+        n = self.mesh.nb_cells("reference")
+        out = np.empty(n, np.uint8)
+        _check(lib().sg_tag_download(self.h, _ptr(out), n), "sg_tag_download")
+        return out
+
+
+def make_scalar_field(name, mesh):
+    return ScalarField(name, mesh)
+
+
+make_field = make_scalar_field  # the README's make_field<double, 1>
+
+
+class Dirichlet:
+    """samurai::Dirichlet<order> (bc/dirichlet.hpp)"""
+
+    def __init__(self, order=1):
+        if order != 1:
+            raise SamuraiGpuError("only Dirichlet<1> is implemented")
+        self.order = order
+
+
+def make_bc(bc, field, value=0.0):
+    """samurai::make_bc<Dirichlet<1>>(u, value)"""
+    if not isinstance(bc, Dirichlet):
+        raise SamuraiGpuError("only Dirichlet boundary conditions are implemented")
+    _check(lib().sg_field_set_dirichlet(field.h, float(value)), "sg_field_set_dirichlet")
+    return bc
+
+
+def swap(a, b):
+    """std::swap(u.array(), unp1.array())"""
+    _check(lib().sg_field_swap(a.h, b.h), "sg_field_swap")
+
+
+def update_ghost_mr(u):
+    _check(lib().sg_update_ghost_mr(u.h), "sg_update_ghost_mr")
+
+
+class Adapt:
+    """samurai::Adapt for one field (mr/adapt.hpp:96-203)"""
+
+    def __init__(self, field):
+        self.field = field
+        self.last_harten = 0
+
+    def __call__(self, cfg_or_eps, regularity=None):
+        if isinstance(cfg_or_eps, mra_config):
+            eps, reg = cfg_or_eps.epsilon(), cfg_or_eps.regularity()
+        else:
+            eps, reg = float(cfg_or_eps), float(regularity)
+        n = ctypes.c_int()
+        _check(lib().sg_adapt(self.field.h, eps, reg, ctypes.byref(n)), "sg_adapt")
+        self.last_harten = n.value
+        return n.value
+
+    def harten(self, ite, eps, reg):
+        conv = ctypes.c_int()
+        _check(lib().sg_harten(self.field.h, ite, eps, reg, ctypes.byref(conv)), "sg_harten")
+        return bool(conv.value)
+
+
+def make_MRAdapt(field):
+    return Adapt(field)
+
+
+class AdvectionSim:
+    """One MR advection problem on the unit box with samurai's time-step
+    structure (adapt, update_ghost_mr, upwind, swap), used by the tests and
+    the benchmark; mirrors the oracle's driver interface."""
+
+    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1, dirichlet=0.0):
+        self.dim = dim
+        self.mesh = MRMesh(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width)
+        self.u = make_scalar_field("u", self.mesh)
+        self.unp1 = make_scalar_field("unp1", self.mesh)
+        make_bc(Dirichlet(1), self.u, dirichlet)
+        self.adaptation = make_MRAdapt(self.u)
+
+    def cells(self):
+        return self.mesh.cells()
+
+    def nb_cells(self):
+        return self.mesh.nb_cells("cells")
+
+    def nb_ref(self):
+        return self.mesh.nb_cells("reference")
+
+    def set_cell_values(self, values):
+        self.u.set_cells(values)
+
+    def cell_values(self):
+        return self.u.cell_values()
+
+    def field(self):
+        return self.u.array()
+
+    def set_field(self, values):
+        self.u.set_array(values)
+
+    def adapt(self, eps, regularity):
+        return self.adaptation(eps, regularity)
+
+    def harten(self, ite, eps, regularity):
+        return self.adaptation.harten(ite, eps, regularity)
+
+    def update_ghost(self):
+        update_ghost_mr(self.u)
+
+    def upwind(self, a, dt, scheme=UPWIND_OP):
+        self.unp1.assign_upwind(self.u, a, dt, scheme)
+        swap(self.u, self.unp1)
+
+    def intervals(self, mesh_id, level):
+        return self.mesh.intervals(mesh_id, level)
+
+    def detail(self):
+        return self.u.detail()
+
+    def tag(self):
+        return self.u.tag()
+
+    def set_cells(self, level, coords):
+        self.mesh.set_cells(level, coords)

@@ -1,0 +1,892 @@
+// C ABI of libsamurai_gpu.so (declared in include/samurai_gpu.h).
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/samurai_gpu.h"
+#include "sg_ctx.cuh"
+
+struct sg_mesh_s
+{
+    sg::Ctx ctx;
+    double* staging     = nullptr; // compact host<->device staging (nb_ref doubles)
+    long long staging_n = 0;
+};
+
+struct sg_field_s
+{
+    sg_mesh_s* mesh = nullptr;
+    sg::DeviceField f;
+};
+
+namespace
+{
+    thread_local std::string g_err;
+
+    int fail(int code, const std::string& msg)
+    {
+        g_err = msg;
+        return code;
+    }
+
+    int from_ctx(sg::Ctx& c, int st)
+    {
+        if (st != sg::SG_OK)
+        {
+            g_err = c.err.empty() ? "error" : c.err;
+        }
+        return st;
+    }
+
+    template <class T>
+    int dalloc(sg::Ctx& c, T** p, size_t n)
+    {
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T) + 256);
+        if (e != cudaSuccess)
+        {
+            c.err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+            *p    = nullptr;
+            return sg::SG_ERR_CUDA;
+        }
+        return sg::SG_OK;
+    }
+
+    template <class T>
+    void dfree(T*& p)
+    {
+        if (p)
+        {
+            cudaFree(p);
+            p = nullptr;
+        }
+    }
+
+    int alloc_mesh(sg::Ctx& c, sg::DeviceMesh& m)
+    {
+        const size_t n = static_cast<size_t>(c.g.total_words);
+        int st         = 0;
+        st |= dalloc(c, &m.cells, n);
+        st |= dalloc(c, &m.cag, n);
+        st |= dalloc(c, &m.proj, n);
+        st |= dalloc(c, &m.uni, n);
+        st |= dalloc(c, &m.ref, n);
+        st |= dalloc(c, &m.hc, n);
+        st |= dalloc(c, &m.hc2, n);
+        st |= dalloc(c, &m.rank, n);
+        return st ? sg::SG_ERR_CUDA : sg::SG_OK;
+    }
+
+    void free_mesh(sg::DeviceMesh& m)
+    {
+        dfree(m.cells);
+        dfree(m.cag);
+        dfree(m.proj);
+        dfree(m.uni);
+        dfree(m.ref);
+        dfree(m.hc);
+        dfree(m.hc2);
+        dfree(m.rank);
+    }
+
+    void destroy_ctx(sg_mesh_s* h)
+    {
+        sg::Ctx& c = h->ctx;
+        if (c.stream)
+        {
+            cudaStreamSynchronize(c.stream);
+        }
+        free_mesh(c.mesh[0]);
+        free_mesh(c.mesh[1]);
+        dfree(c.t0);
+        dfree(c.t1);
+        dfree(c.t2);
+        dfree(c.t3);
+        dfree(c.rf);
+        dfree(c.cf);
+        dfree(c.detail);
+        dfree(c.tag);
+        dfree(c.block_sums);
+        dfree(c.d_counts);
+        dfree(c.d_flags);
+        dfree(h->staging);
+        if (c.h_counts)
+        {
+            cudaFreeHost(c.h_counts);
+        }
+        if (c.h_flags)
+        {
+            cudaFreeHost(c.h_flags);
+        }
+        if (c.stream)
+        {
+            cudaStreamDestroy(c.stream);
+        }
+        delete h;
+    }
+
+    __global__ void k_box_cells(sg::Geom g, int l, uint32_t* cells)
+    {
+        const sg::LevelGeom& L = g.lv[l];
+        for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < L.nwords; w += static_cast<long long>(gridDim.x) * blockDim.x)
+        {
+            const long long row = w / L.W;
+            const int wi        = static_cast<int>(w - row * L.W);
+            cells[L.woff + w]   = sg::box_mask(g, l, row, wi, 0, 0);
+        }
+    }
+
+    int stage(sg_mesh_s* h, long long n)
+    {
+        if (n <= h->staging_n)
+        {
+            return sg::SG_OK;
+        }
+        dfree(h->staging);
+        h->staging_n = 0;
+        if (dalloc(h->ctx, &h->staging, static_cast<size_t>(n)))
+        {
+            return sg::SG_ERR_CUDA;
+        }
+        h->staging_n = n;
+        return sg::SG_OK;
+    }
+
+    struct HostMesh
+    {
+        std::vector<uint32_t> bm;
+        std::vector<uint32_t> ref;
+        std::vector<int> rank;
+    };
+
+    int pull(sg::Ctx& c, const uint32_t* dbm, HostMesh& hm, bool with_ref)
+    {
+        const size_t n = static_cast<size_t>(c.g.total_words);
+        hm.bm.resize(n);
+        cudaMemcpyAsync(hm.bm.data(), dbm, n * 4, cudaMemcpyDeviceToHost, c.stream);
+        if (with_ref)
+        {
+            hm.ref.resize(n);
+            hm.rank.resize(n);
+            cudaMemcpyAsync(hm.ref.data(), c.m().ref, n * 4, cudaMemcpyDeviceToHost, c.stream);
+            cudaMemcpyAsync(hm.rank.data(), c.m().rank, n * 4, cudaMemcpyDeviceToHost, c.stream);
+        }
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return sg::check(c, "pull");
+        }
+        return sg::SG_OK;
+    }
+
+    long long host_ref_index(const HostMesh& hm, long long w, int b)
+    {
+        return static_cast<long long>(hm.rank[w]) + __builtin_popcount(hm.ref[w] & ((1u << b) - 1u));
+    }
+
+    const uint32_t* mesh_bitmap(sg::Ctx& c, int id)
+    {
+        sg::DeviceMesh& m = c.m();
+        switch (id)
+        {
+            case SG_CELLS: return m.cells;
+            case SG_CELLS_AND_GHOSTS: return m.cag;
+            case SG_PROJ_CELLS: return m.proj;
+            case SG_UNION_CELLS: return m.uni;
+            case SG_REFERENCE: return m.ref;
+            default: return nullptr;
+        }
+    }
+} // namespace
+
+extern "C"
+{
+    const char* sg_last_error(void)
+    {
+        return g_err.c_str();
+    }
+
+    int sg_version(int* major, int* minor)
+    {
+        if (major)
+        {
+            *major = 0;
+        }
+        if (minor)
+        {
+            *minor = 1;
+        }
+        return SG_OK;
+    }
+
+    int sg_mesh_create(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width, sg_mesh_t* out)
+    {
+        if (!out)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_create: null output");
+        }
+        *out = nullptr;
+        if (dim != 2 && dim != 3)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_create: dim must be 2 or 3");
+        }
+        if (min_level < 1 || max_level < min_level || max_level + 2 > sg::MAXLEV)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_create: need 1 <= min_level <= max_level <= 21");
+        }
+        if (max_stencil_radius < 1 || prediction_radius < 0 || prediction_radius > 1 || graduation_width < 1 || graduation_width > 4)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_create: unsupported stencil radius / prediction radius / graduation width");
+        }
+        if (max_stencil_radius != 1)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_create: only max_stencil_radius 1 is implemented");
+        }
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        {
+            cudaGetLastError();
+            return fail(SG_ERR_CUDA, "sg_mesh_create: no CUDA device");
+        }
+        sg_mesh_s* h = new (std::nothrow) sg_mesh_s();
+        if (!h)
+        {
+            return fail(SG_ERR_CAPACITY, "sg_mesh_create: out of host memory");
+        }
+        sg::Ctx& c                 = h->ctx;
+        c.cfg.dim                  = dim;
+        c.cfg.min_level            = min_level;
+        c.cfg.max_level            = max_level;
+        c.cfg.max_stencil_radius   = max_stencil_radius;
+        c.cfg.prediction_radius    = prediction_radius;
+        c.cfg.graduation_width     = graduation_width;
+        c.cfg.ghost_width          = max_stencil_radius > prediction_radius ? max_stencil_radius : prediction_radius;
+        c.g                        = sg::make_geom(dim, min_level, max_level);
+        c.capacity                 = 32 * c.g.total_words;
+        if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
+        {
+            cudaGetLastError();
+            delete h;
+            return fail(SG_ERR_CUDA, "sg_mesh_create: cudaStreamCreate failed");
+        }
+        const size_t nw = static_cast<size_t>(c.g.total_words);
+        int st          = alloc_mesh(c, c.mesh[0]);
+        st |= alloc_mesh(c, c.mesh[1]);
+        st |= dalloc(c, &c.t0, nw);
+        st |= dalloc(c, &c.t1, nw);
+        st |= dalloc(c, &c.t2, nw);
+        st |= dalloc(c, &c.t3, nw);
+        st |= dalloc(c, &c.rf, nw);
+        st |= dalloc(c, &c.cf, nw);
+        st |= dalloc(c, &c.detail, static_cast<size_t>(c.capacity));
+        st |= dalloc(c, &c.tag, static_cast<size_t>(c.capacity));
+        c.n_scan_blocks = (c.g.total_words + 4095) / 4096;
+        st |= dalloc(c, &c.block_sums, static_cast<size_t>(c.n_scan_blocks) + 1);
+        st |= dalloc(c, &c.d_counts, 8);
+        st |= dalloc(c, &c.d_flags, 8);
+        if (!st)
+        {
+            if (cudaMallocHost(reinterpret_cast<void**>(&c.h_counts), 8 * sizeof(long long)) != cudaSuccess
+                || cudaMallocHost(reinterpret_cast<void**>(&c.h_flags), 8 * sizeof(int)) != cudaSuccess)
+            {
+                st = SG_ERR_CUDA;
+                c.err = "cudaMallocHost failed";
+            }
+        }
+        if (st)
+        {
+            std::string msg = c.err;
+            destroy_ctx(h);
+            return fail(SG_ERR_CUDA, "sg_mesh_create: " + msg);
+        }
+        for (int k = 0; k < 2; ++k)
+        {
+            cudaMemsetAsync(c.mesh[k].cells, 0, nw * 4, c.stream);
+        }
+        cudaMemsetAsync(c.detail, 0, static_cast<size_t>(c.capacity) * sizeof(double), c.stream);
+        cudaMemsetAsync(c.tag, 0, static_cast<size_t>(c.capacity), c.stream);
+        k_box_cells<<<sg::grid_for(c.g.lv[max_level].nwords), 256, 0, c.stream>>>(c.g, max_level, c.m().cells);
+        st = sg::check(c, "initial cells");
+        if (!st)
+        {
+            st = sg::build_mesh(c, c.m());
+        }
+        if (st)
+        {
+            std::string msg = c.err;
+            destroy_ctx(h);
+            return fail(st, "sg_mesh_create: " + msg);
+        }
+        *out = h;
+        return SG_OK;
+    }
+
+    int sg_mesh_destroy(sg_mesh_t mesh)
+    {
+        if (mesh)
+        {
+            destroy_ctx(mesh);
+        }
+        return SG_OK;
+    }
+
+    int sg_mesh_counts(sg_mesh_t mesh, long long* nb_cells, long long* nb_reference)
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_counts: null mesh");
+        }
+        if (nb_cells)
+        {
+            *nb_cells = mesh->ctx.m().nb_cells;
+        }
+        if (nb_reference)
+        {
+            *nb_reference = mesh->ctx.m().nb_ref;
+        }
+        return SG_OK;
+    }
+
+    int sg_mesh_get_cells(sg_mesh_t mesh, int* level, int* coords, long long* index, long long capacity)
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_get_cells: null mesh");
+        }
+        sg::Ctx& c = mesh->ctx;
+        if (capacity < c.m().nb_cells)
+        {
+            return fail(SG_ERR_CAPACITY, "sg_mesh_get_cells: output too small");
+        }
+        HostMesh hm;
+        if (int st = pull(c, c.m().cells, hm, true))
+        {
+            return from_ctx(c, st);
+        }
+        const int D  = c.g.dim;
+        long long k  = 0;
+        for (long long w = 0; w < c.g.total_words; ++w)
+        {
+            uint32_t v = hm.bm[w];
+            if (!v)
+            {
+                continue;
+            }
+            const int l = sg::level_of(c.g, w);
+            while (v)
+            {
+                const int b = __builtin_ctz(v);
+                v &= v - 1;
+                const sg::Cell cc = sg::cell_of(c.g, l, w, b);
+                if (level)
+                {
+                    level[k] = l;
+                }
+                if (coords)
+                {
+                    coords[D * k]     = cc.x;
+                    coords[D * k + 1] = cc.y;
+                    if (D == 3)
+                    {
+                        coords[D * k + 2] = cc.z;
+                    }
+                }
+                if (index)
+                {
+                    index[k] = host_ref_index(hm, w, b);
+                }
+                ++k;
+            }
+        }
+        return SG_OK;
+    }
+
+    int sg_mesh_count_intervals(sg_mesh_t mesh, int mesh_id, int level, long long* n)
+    {
+        if (!mesh || !n)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_count_intervals: null argument");
+        }
+        sg::Ctx& c = mesh->ctx;
+        const uint32_t* dbm = mesh_bitmap(c, mesh_id);
+        if (!dbm || level < 0 || level >= c.g.nlev)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_count_intervals: bad mesh id or level");
+        }
+        HostMesh hm;
+        if (int st = pull(c, dbm, hm, false))
+        {
+            return from_ctx(c, st);
+        }
+        const sg::LevelGeom& L = c.g.lv[level];
+        long long cnt          = 0;
+        for (long long r = 0; r < L.nrows; ++r)
+        {
+            bool prev = false;
+            for (int x = 0; x < 32 * L.W; ++x)
+            {
+                const long long w = L.woff + r * L.W + (x >> 5);
+                const bool on     = (hm.bm[w] >> (x & 31)) & 1u;
+                if (on && !prev)
+                {
+                    ++cnt;
+                }
+                prev = on;
+            }
+        }
+        *n = cnt;
+        return SG_OK;
+    }
+
+    int sg_mesh_get_intervals(sg_mesh_t mesh, int mesh_id, int level, long long* out, long long capacity)
+    {
+        if (!mesh || !out)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_get_intervals: null argument");
+        }
+        sg::Ctx& c = mesh->ctx;
+        const uint32_t* dbm = mesh_bitmap(c, mesh_id);
+        if (!dbm || level < 0 || level >= c.g.nlev)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_get_intervals: bad mesh id or level");
+        }
+        HostMesh hm;
+        if (int st = pull(c, dbm, hm, true))
+        {
+            return from_ctx(c, st);
+        }
+        const int D            = c.g.dim;
+        const int rec          = D + 2;
+        const sg::LevelGeom& L = c.g.lv[level];
+        long long k            = 0;
+        for (long long r = 0; r < L.nrows; ++r)
+        {
+            int start = 0;
+            bool prev = false;
+            for (int xb = 0; xb <= 32 * L.W; ++xb)
+            {
+                bool on = false;
+                if (xb < 32 * L.W)
+                {
+                    const long long w = L.woff + r * L.W + (xb >> 5);
+                    on                = (hm.bm[w] >> (xb & 31)) & 1u;
+                }
+                if (on && !prev)
+                {
+                    start = xb;
+                }
+                if (!on && prev)
+                {
+                    if (k >= capacity)
+                    {
+                        return fail(SG_ERR_CAPACITY, "sg_mesh_get_intervals: output too small");
+                    }
+                    const long long w0 = L.woff + r * L.W + (start >> 5);
+                    const int x0       = start - sg::PX;
+                    const sg::Cell cc  = sg::cell_of(c.g, level, w0, start & 31);
+                    long long idx      = -1;
+                    if ((hm.ref[w0] >> (start & 31)) & 1u)
+                    {
+                        idx = host_ref_index(hm, w0, start & 31) - x0;
+                    }
+                    out[rec * k]     = x0;
+                    out[rec * k + 1] = xb - sg::PX;
+                    out[rec * k + 2] = cc.y;
+                    if (D == 3)
+                    {
+                        out[rec * k + 3] = cc.z;
+                    }
+                    out[rec * k + D + 1] = idx;
+                    ++k;
+                }
+                prev = on;
+            }
+        }
+        return SG_OK;
+    }
+
+    int sg_mesh_set_cells(sg_mesh_t mesh, long long n, const int* level, const int* coords)
+    {
+        if (!mesh || (n > 0 && (!level || !coords)))
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_set_cells: null argument");
+        }
+        sg::Ctx& c = mesh->ctx;
+        const int D = c.g.dim;
+        std::vector<uint32_t> bm(static_cast<size_t>(c.g.total_words), 0u);
+        for (long long i = 0; i < n; ++i)
+        {
+            const int l = level[i];
+            if (l < c.cfg.min_level || l > c.cfg.max_level)
+            {
+                return fail(SG_ERR_ARG, "sg_mesh_set_cells: level out of [min_level, max_level]");
+            }
+            const int x = coords[D * i], y = coords[D * i + 1], z = D == 3 ? coords[D * i + 2] : 0;
+            const int nl = 1 << l;
+            if (x < 0 || x >= nl || y < 0 || y >= nl || z < 0 || (D == 3 && z >= nl))
+            {
+                return fail(SG_ERR_ARG, "sg_mesh_set_cells: cell outside the unit box");
+            }
+            const sg::Pos p = sg::pos_of(c.g, l, x, y, z);
+            bm[static_cast<size_t>(p.w)] |= 1u << p.b;
+        }
+        cudaMemcpyAsync(c.m().cells, bm.data(), bm.size() * 4, cudaMemcpyHostToDevice, c.stream);
+        return from_ctx(c, sg::build_mesh(c, c.m()));
+    }
+
+    int sg_mesh_stream(sg_mesh_t mesh, void** stream)
+    {
+        if (!mesh || !stream)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_stream: null argument");
+        }
+        *stream = mesh->ctx.stream;
+        return SG_OK;
+    }
+
+    int sg_mesh_synchronize(sg_mesh_t mesh)
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_synchronize: null mesh");
+        }
+        cudaError_t e = cudaStreamSynchronize(mesh->ctx.stream);
+        if (e != cudaSuccess)
+        {
+            return fail(SG_ERR_CUDA, std::string("sg_mesh_synchronize: ") + cudaGetErrorString(e));
+        }
+        return from_ctx(mesh->ctx, sg::device_error(mesh->ctx));
+    }
+
+    int sg_mesh_launch_count(sg_mesh_t mesh, int reset, long long* count)
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_launch_count: null mesh");
+        }
+        if (count)
+        {
+            *count = mesh->ctx.n_launches;
+        }
+        if (reset)
+        {
+            mesh->ctx.n_launches = 0;
+        }
+        return SG_OK;
+    }
+
+    int sg_field_create(sg_mesh_t mesh, const char* name, sg_field_t* out)
+    {
+        if (!mesh || !out)
+        {
+            return fail(SG_ERR_ARG, "sg_field_create: null argument");
+        }
+        sg_field_s* f = new (std::nothrow) sg_field_s();
+        if (!f)
+        {
+            return fail(SG_ERR_CAPACITY, "sg_field_create: out of host memory");
+        }
+        f->mesh  = mesh;
+        f->f.ctx = &mesh->ctx;
+        f->f.name = name ? name : "";
+        if (dalloc(mesh->ctx, &f->f.data, static_cast<size_t>(mesh->ctx.capacity)))
+        {
+            delete f;
+            return fail(SG_ERR_CUDA, "sg_field_create: " + mesh->ctx.err);
+        }
+        cudaMemsetAsync(f->f.data, 0, static_cast<size_t>(mesh->ctx.capacity) * sizeof(double), mesh->ctx.stream);
+        *out = f;
+        return SG_OK;
+    }
+
+    int sg_field_destroy(sg_field_t field)
+    {
+        if (field)
+        {
+            cudaStreamSynchronize(field->mesh->ctx.stream);
+            dfree(field->f.data);
+            dfree(field->f.spare);
+            delete field;
+        }
+        return SG_OK;
+    }
+
+    int sg_field_set_dirichlet(sg_field_t field, double value)
+    {
+        if (!field)
+        {
+            return fail(SG_ERR_ARG, "sg_field_set_dirichlet: null field");
+        }
+        field->f.has_bc   = true;
+        field->f.bc_value = value;
+        return SG_OK;
+    }
+
+    int sg_field_upload_device(sg_field_t field, const double* dvalues, long long n)
+    {
+        if (!field || !dvalues)
+        {
+            return fail(SG_ERR_ARG, "sg_field_upload_device: null argument");
+        }
+        sg::Ctx& c = field->mesh->ctx;
+        if (n != c.m().nb_ref)
+        {
+            return fail(SG_ERR_ARG, "sg_field_upload_device: size differs from the reference mesh");
+        }
+        return from_ctx(c, sg::scatter_compact(c, c.m(), dvalues, field->f.data));
+    }
+
+    int sg_field_download_device(sg_field_t field, double* dvalues, long long n)
+    {
+        if (!field || !dvalues)
+        {
+            return fail(SG_ERR_ARG, "sg_field_download_device: null argument");
+        }
+        sg::Ctx& c = field->mesh->ctx;
+        if (n != c.m().nb_ref)
+        {
+            return fail(SG_ERR_ARG, "sg_field_download_device: size differs from the reference mesh");
+        }
+        return from_ctx(c, sg::gather_compact(c, c.m(), field->f.data, dvalues));
+    }
+
+    int sg_field_upload(sg_field_t field, const double* values, long long n)
+    {
+        if (!field || !values)
+        {
+            return fail(SG_ERR_ARG, "sg_field_upload: null argument");
+        }
+        sg_mesh_s* h = field->mesh;
+        sg::Ctx& c   = h->ctx;
+        if (n != c.m().nb_ref)
+        {
+            return fail(SG_ERR_ARG, "sg_field_upload: size differs from the reference mesh");
+        }
+        if (stage(h, n))
+        {
+            return from_ctx(c, SG_ERR_CUDA);
+        }
+        cudaMemcpyAsync(h->staging, values, static_cast<size_t>(n) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        int st = sg::scatter_compact(c, c.m(), h->staging, field->f.data);
+        if (!st && cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            st = sg::check(c, "upload");
+        }
+        return from_ctx(c, st);
+    }
+
+    int sg_field_download(sg_field_t field, double* values, long long n)
+    {
+        if (!field || !values)
+        {
+            return fail(SG_ERR_ARG, "sg_field_download: null argument");
+        }
+        sg_mesh_s* h = field->mesh;
+        sg::Ctx& c   = h->ctx;
+        if (n != c.m().nb_ref)
+        {
+            return fail(SG_ERR_ARG, "sg_field_download: size differs from the reference mesh");
+        }
+        if (stage(h, n))
+        {
+            return from_ctx(c, SG_ERR_CUDA);
+        }
+        int st = sg::gather_compact(c, c.m(), field->f.data, h->staging);
+        if (st)
+        {
+            return from_ctx(c, st);
+        }
+        cudaMemcpyAsync(values, h->staging, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return from_ctx(c, sg::check(c, "download"));
+        }
+        return from_ctx(c, sg::device_error(c));
+    }
+
+    int sg_field_set_cells(sg_field_t field, const double* values, long long n)
+    {
+        if (!field || !values)
+        {
+            return fail(SG_ERR_ARG, "sg_field_set_cells: null argument");
+        }
+        sg::Ctx& c = field->mesh->ctx;
+        if (n != c.m().nb_cells)
+        {
+            return fail(SG_ERR_ARG, "sg_field_set_cells: size differs from the number of cells");
+        }
+        std::vector<long long> idx(static_cast<size_t>(n));
+        if (int st = sg_mesh_get_cells(field->mesh, nullptr, nullptr, idx.data(), n))
+        {
+            return st;
+        }
+        std::vector<double> full(static_cast<size_t>(c.m().nb_ref), 0.);
+        for (long long i = 0; i < n; ++i)
+        {
+            full[static_cast<size_t>(idx[i])] = values[i];
+        }
+        return sg_field_upload(field, full.data(), c.m().nb_ref);
+    }
+
+    int sg_field_get_cells(sg_field_t field, double* values, long long n)
+    {
+        if (!field || !values)
+        {
+            return fail(SG_ERR_ARG, "sg_field_get_cells: null argument");
+        }
+        sg::Ctx& c = field->mesh->ctx;
+        if (n != c.m().nb_cells)
+        {
+            return fail(SG_ERR_ARG, "sg_field_get_cells: size differs from the number of cells");
+        }
+        std::vector<long long> idx(static_cast<size_t>(n));
+        if (int st = sg_mesh_get_cells(field->mesh, nullptr, nullptr, idx.data(), n))
+        {
+            return st;
+        }
+        std::vector<double> full(static_cast<size_t>(c.m().nb_ref));
+        if (int st = sg_field_download(field, full.data(), c.m().nb_ref))
+        {
+            return st;
+        }
+        for (long long i = 0; i < n; ++i)
+        {
+            values[i] = full[static_cast<size_t>(idx[i])];
+        }
+        return SG_OK;
+    }
+
+    int sg_field_swap(sg_field_t a, sg_field_t b)
+    {
+        if (!a || !b || a->mesh != b->mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_field_swap: fields must live on the same mesh");
+        }
+        std::swap(a->f.data, b->f.data);
+        return SG_OK;
+    }
+
+    int sg_adapt(sg_field_t u, double eps, double regularity, int* n_harten)
+    {
+        if (!u)
+        {
+            return fail(SG_ERR_ARG, "sg_adapt: null field");
+        }
+        sg::Ctx& c = u->mesh->ctx;
+        if (!u->f.spare && dalloc(c, &u->f.spare, static_cast<size_t>(c.capacity)))
+        {
+            return from_ctx(c, SG_ERR_CUDA);
+        }
+        return from_ctx(c, sg::adapt(c, u->f, eps, regularity, n_harten));
+    }
+
+    int sg_harten(sg_field_t u, int ite, double eps, double regularity, int* converged)
+    {
+        if (!u)
+        {
+            return fail(SG_ERR_ARG, "sg_harten: null field");
+        }
+        sg::Ctx& c = u->mesh->ctx;
+        if (!u->f.spare && dalloc(c, &u->f.spare, static_cast<size_t>(c.capacity)))
+        {
+            return from_ctx(c, SG_ERR_CUDA);
+        }
+        bool conv = false;
+        int st    = sg::harten(c, u->f, ite, eps, regularity, &conv);
+        if (converged)
+        {
+            *converged = conv ? 1 : 0;
+        }
+        return from_ctx(c, st);
+    }
+
+    int sg_update_ghost_mr(sg_field_t u)
+    {
+        if (!u)
+        {
+            return fail(SG_ERR_ARG, "sg_update_ghost_mr: null field");
+        }
+        return from_ctx(u->mesh->ctx, sg::update_ghost_mr(u->mesh->ctx, u->f));
+    }
+
+    int sg_upwind(sg_field_t u, sg_field_t unp1, const double* a, double dt, int scheme)
+    {
+        if (!u || !unp1 || !a || u->mesh != unp1->mesh || u == unp1)
+        {
+            return fail(SG_ERR_ARG, "sg_upwind: need two distinct fields on the same mesh");
+        }
+        if (scheme != SG_UPWIND_OP && scheme != SG_README)
+        {
+            return fail(SG_ERR_ARG, "sg_upwind: unknown scheme");
+        }
+        sg::Ctx& c = u->mesh->ctx;
+        if (scheme == SG_README && c.g.dim != 2)
+        {
+            return fail(SG_ERR_ARG, "sg_upwind: the README scheme is two-dimensional");
+        }
+        return from_ctx(c, sg::upwind(c, u->f, unp1->f, a, dt, scheme));
+    }
+
+    int sg_detail_download(sg_field_t u, double* values, long long n)
+    {
+        if (!u || !values)
+        {
+            return fail(SG_ERR_ARG, "sg_detail_download: null argument");
+        }
+        sg_mesh_s* h = u->mesh;
+        sg::Ctx& c   = h->ctx;
+        if (n != c.m().nb_ref)
+        {
+            return fail(SG_ERR_ARG, "sg_detail_download: size differs from the reference mesh");
+        }
+        if (stage(h, n))
+        {
+            return from_ctx(c, SG_ERR_CUDA);
+        }
+        int st = sg::gather_compact(c, c.m(), c.detail, h->staging);
+        if (st)
+        {
+            return from_ctx(c, st);
+        }
+        cudaMemcpyAsync(values, h->staging, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return from_ctx(c, sg::check(c, "detail download"));
+        }
+        return SG_OK;
+    }
+
+    int sg_tag_download(sg_field_t u, unsigned char* values, long long n)
+    {
+        if (!u || !values)
+        {
+            return fail(SG_ERR_ARG, "sg_tag_download: null argument");
+        }
+        sg::Ctx& c = u->mesh->ctx;
+        if (n != c.m().nb_ref)
+        {
+            return fail(SG_ERR_ARG, "sg_tag_download: size differs from the reference mesh");
+        }
+        HostMesh hm;
+        if (int st = pull(c, c.m().ref, hm, true))
+        {
+            return from_ctx(c, st);
+        }
+        std::vector<uint8_t> dense(static_cast<size_t>(c.capacity));
+        cudaMemcpyAsync(dense.data(), c.tag, dense.size(), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return from_ctx(c, sg::check(c, "tag download"));
+        }
+        for (long long w = 0; w < c.g.total_words; ++w)
+        {
+            uint32_t v = hm.ref[w];
+            while (v)
+            {
+                const int b = __builtin_ctz(v);
+                v &= v - 1;
+                values[host_ref_index(hm, w, b)] = dense[static_cast<size_t>(32 * w + b)];
+            }
+        }
+        return SG_OK;
+    }
+}

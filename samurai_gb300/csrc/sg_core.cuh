@@ -1,0 +1,383 @@
+// Core device-side layout of the GB300 MR mesh.
+//
+// Every mesh id of samurai's MRMesh (cells, cells_and_ghosts, proj_cells,
+// union_cells, reference; mr/mesh.hpp:25-33) is held as a pyramid of
+// per-level bitmaps.  Level l covers the padded box
+//     x in [-PX, 32*W_l - PX),  y (and z) in [-PY, 2^l + PY)
+// with one bit per cell, rows ordered z-outer / y-inner and 32-bit words along
+// x.  Words of all levels are concatenated in level order, so a global word
+// index w identifies (level, row, x-word).
+//
+// FP64 fields use the same index space densely: the value of the cell at
+// (word w, bit b) lives at element 32*w + b.  A warp that owns one word
+// therefore reads/writes 32 consecutive doubles (256 B).
+//
+// samurai's storage numbering of the reference mesh (level-major, then rows,
+// then x: level_cell_array.hpp:775-784, mesh.hpp:894-911) is the exclusive
+// prefix popcount of the reference bitmap; rank[w] holds it per word.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sg
+{
+    constexpr int MAXLEV = 24; // levels 0..23 can be stored
+    constexpr int PX     = 32; // x padding in cells, one word on each side
+    constexpr int PY     = 8;  // y/z padding in rows on each side
+
+    struct LevelGeom
+    {
+        int n;   // 2^l cells per axis inside the unit box
+        int W;   // 32-bit words per row
+        int R;   // rows per axis: n + 2*PY
+        int pad_;
+        long long nrows;  // R^(dim-1)
+        long long woff;   // first word of the level
+        long long nwords; // nrows * W
+    };
+
+    struct Geom
+    {
+        int dim;
+        int nlev; // stored levels: 0..nlev-1 (= max_level + 2)
+        int min_level;
+        int max_level;
+        long long total_words;
+        LevelGeom lv[MAXLEV];
+    };
+
+    inline Geom make_geom(int dim, int min_level, int max_level)
+    {
+        Geom g{};
+        g.dim       = dim;
+        g.min_level = min_level;
+        g.max_level = max_level;
+        g.nlev      = max_level + 2;
+        long long off = 0;
+        for (int l = 0; l < g.nlev; ++l)
+        {
+            LevelGeom& L = g.lv[l];
+            L.n          = 1 << l;
+            L.W          = (L.n + 31) / 32 + 2;
+            L.R          = L.n + 2 * PY;
+            L.nrows      = (dim == 2) ? L.R : static_cast<long long>(L.R) * L.R;
+            L.woff       = off;
+            L.nwords     = L.nrows * L.W;
+            off += L.nwords;
+        }
+        g.total_words = off;
+        return g;
+    }
+
+    // --------------------------------------------------------- positions
+    struct Pos
+    {
+        long long w; // global word, -1 when outside the stored box
+        int b;       // bit
+    };
+
+    __host__ __device__ __forceinline__ Pos pos_of(const Geom& g, int l, int x, int y, int z)
+    {
+        const LevelGeom& L = g.lv[l];
+        const int xb       = x + PX;
+        const int ry       = y + PY;
+        const int rz       = z + PY;
+        if (xb < 0 || xb >= 32 * L.W || ry < 0 || ry >= L.R || (g.dim == 3 && (rz < 0 || rz >= L.R)))
+        {
+            return {-1, 0};
+        }
+        const long long row = (g.dim == 2) ? ry : static_cast<long long>(rz) * L.R + ry;
+        return {L.woff + row * L.W + (xb >> 5), xb & 31};
+    }
+
+    __device__ __forceinline__ bool test(const uint32_t* bm, const Pos& p)
+    {
+        return p.w >= 0 && ((__ldg(bm + p.w) >> p.b) & 1u);
+    }
+
+    __device__ __forceinline__ bool test(const uint32_t* bm, const Geom& g, int l, int x, int y, int z)
+    {
+        return test(bm, pos_of(g, l, x, y, z));
+    }
+
+    __host__ __device__ __forceinline__ long long elem(const Pos& p)
+    {
+        return 32 * p.w + p.b;
+    }
+
+    // coordinates of (word, bit) at level l
+    struct Cell
+    {
+        int x, y, z;
+    };
+
+    __host__ __device__ __forceinline__ Cell cell_of(const Geom& g, int l, long long w, int b)
+    {
+        const LevelGeom& L = g.lv[l];
+        const long long loc = w - L.woff;
+        const long long row = loc / L.W;
+        const int wi        = static_cast<int>(loc - row * L.W);
+        Cell c;
+        c.x = wi * 32 + b - PX;
+        if (g.dim == 2)
+        {
+            c.y = static_cast<int>(row) - PY;
+            c.z = 0;
+        }
+        else
+        {
+            c.y = static_cast<int>(row % L.R) - PY;
+            c.z = static_cast<int>(row / L.R) - PY;
+        }
+        return c;
+    }
+
+    // level of a global word (levels are few: linear scan)
+    __host__ __device__ __forceinline__ int level_of(const Geom& g, long long w)
+    {
+        int l = 0;
+        while (l + 1 < g.nlev && w >= g.lv[l + 1].woff)
+        {
+            ++l;
+        }
+        return l;
+    }
+
+    // storage index in samurai's reference numbering
+    __device__ __forceinline__ long long ref_index(const uint32_t* ref, const int* rank, const Pos& p)
+    {
+        return static_cast<long long>(__ldg(rank + p.w)) + __popc(__ldg(ref + p.w) & ((1u << p.b) - 1u));
+    }
+
+    // ------------------------------------------------------- bit kernels
+    // OR of bit pairs: 64 fine bits -> 32 coarse bits (bit j = b[2j] | b[2j+1])
+    __host__ __device__ __forceinline__ uint32_t compress_pairs(uint32_t lo, uint32_t hi)
+    {
+        uint64_t v = static_cast<uint64_t>(lo) | (static_cast<uint64_t>(hi) << 32);
+        v          = (v | (v >> 1)) & 0x5555555555555555ull;
+        v          = (v | (v >> 1)) & 0x3333333333333333ull;
+        v          = (v | (v >> 2)) & 0x0F0F0F0F0F0F0F0Full;
+        v          = (v | (v >> 4)) & 0x00FF00FF00FF00FFull;
+        v          = (v | (v >> 8)) & 0x0000FFFF0000FFFFull;
+        v          = (v | (v >> 16)) & 0x00000000FFFFFFFFull;
+        return static_cast<uint32_t>(v);
+    }
+
+    // even bits only: 64 fine bits -> 32 coarse bits (bit j = b[2j])
+    __host__ __device__ __forceinline__ uint32_t compress_even(uint32_t lo, uint32_t hi)
+    {
+        uint64_t v = (static_cast<uint64_t>(lo) | (static_cast<uint64_t>(hi) << 32)) & 0x5555555555555555ull;
+        v          = (v | (v >> 1)) & 0x3333333333333333ull;
+        v          = (v | (v >> 2)) & 0x0F0F0F0F0F0F0F0Full;
+        v          = (v | (v >> 4)) & 0x00FF00FF00FF00FFull;
+        v          = (v | (v >> 8)) & 0x0000FFFF0000FFFFull;
+        v          = (v | (v >> 16)) & 0x00000000FFFFFFFFull;
+        return static_cast<uint32_t>(v);
+    }
+
+    // 16 coarse bits -> 32 fine bits (bit j -> bits 2j, 2j+1)
+    __host__ __device__ __forceinline__ uint32_t spread16(uint32_t h)
+    {
+        uint32_t x = h & 0xFFFFu;
+        x          = (x | (x << 8)) & 0x00FF00FFu;
+        x          = (x | (x << 4)) & 0x0F0F0F0Fu;
+        x          = (x | (x << 2)) & 0x33333333u;
+        x          = (x | (x << 1)) & 0x55555555u;
+        return x | (x << 1);
+    }
+
+    // Word of the coarsened set (parent of any member) at level l from the
+    // bitmap `fine` at level l+1.  Coarse word wi of row (yc, zc) covers the
+    // fine words 2*wi-1 and 2*wi of the fine rows 2*yc+{0,1} (x 2*zc+{0,1}).
+    __device__ __forceinline__ uint32_t coarsen_word(const Geom& g, const uint32_t* fine, int l, long long row, int wi)
+    {
+        const LevelGeom& C = g.lv[l];
+        const LevelGeom& F = g.lv[l + 1];
+        int yc, zc;
+        if (g.dim == 2)
+        {
+            yc = static_cast<int>(row) - PY;
+            zc = 0;
+        }
+        else
+        {
+            yc = static_cast<int>(row % C.R) - PY;
+            zc = static_cast<int>(row / C.R) - PY;
+        }
+        uint32_t out = 0;
+        const int nz = (g.dim == 3) ? 2 : 1;
+        for (int sz = 0; sz < nz; ++sz)
+        {
+            for (int sy = 0; sy < 2; ++sy)
+            {
+                const int ry = 2 * yc + sy + PY;
+                const int rz = 2 * zc + sz + PY;
+                if (ry < 0 || ry >= F.R || (g.dim == 3 && (rz < 0 || rz >= F.R)))
+                {
+                    continue;
+                }
+                const long long frow = (g.dim == 2) ? ry : static_cast<long long>(rz) * F.R + ry;
+                const long long base = F.woff + frow * F.W;
+                const int k0         = 2 * wi - 1;
+                const uint32_t lo    = (k0 >= 0 && k0 < F.W) ? __ldg(fine + base + k0) : 0u;
+                const uint32_t hi    = (k0 + 1 >= 0 && k0 + 1 < F.W) ? __ldg(fine + base + k0 + 1) : 0u;
+                out |= compress_pairs(lo, hi);
+            }
+        }
+        return out;
+    }
+
+    // Word of the refined set (all children) at level l from `coarse` at
+    // level l-1.  Fine word k of row (yf, zf) reads coarse word (k+1)>>1 of
+    // row (yf>>1, zf>>1), low half when (k+1) is even, high half otherwise.
+    __device__ __forceinline__ uint32_t refine_word(const Geom& g, const uint32_t* coarse, int l, long long row, int k)
+    {
+        const LevelGeom& F = g.lv[l];
+        const LevelGeom& C = g.lv[l - 1];
+        int yf, zf;
+        if (g.dim == 2)
+        {
+            yf = static_cast<int>(row) - PY;
+            zf = 0;
+        }
+        else
+        {
+            yf = static_cast<int>(row % F.R) - PY;
+            zf = static_cast<int>(row / F.R) - PY;
+        }
+        const int ry = (yf >> 1) + PY;
+        const int rz = (zf >> 1) + PY;
+        if (ry < 0 || ry >= C.R || (g.dim == 3 && (rz < 0 || rz >= C.R)))
+        {
+            return 0u;
+        }
+        const int wc = (k + 1) >> 1;
+        if (wc >= C.W)
+        {
+            return 0u;
+        }
+        const long long crow = (g.dim == 2) ? ry : static_cast<long long>(rz) * C.R + ry;
+        const uint32_t cw    = __ldg(coarse + C.woff + crow * C.W + wc);
+        return spread16(((k + 1) & 1) ? (cw >> 16) : cw);
+    }
+
+    // x-dilation of one word by r (< 32) using its neighbours in the row
+    __device__ __forceinline__ uint32_t dilate_x(uint32_t left, uint32_t mid, uint32_t right, int r)
+    {
+        uint32_t out = mid;
+        for (int k = 1; k <= r; ++k)
+        {
+            out |= (mid << k) | (left >> (32 - k)) | (mid >> k) | (right << (32 - k));
+        }
+        return out;
+    }
+
+    // box dilation by r of bitmap `src` at level l, word (row, wi)
+    __device__ __forceinline__ uint32_t box_dilate_word(const Geom& g, const uint32_t* src, int l, long long row, int wi, int r)
+    {
+        const LevelGeom& L = g.lv[l];
+        int ry, rz;
+        if (g.dim == 2)
+        {
+            ry = static_cast<int>(row);
+            rz = 0;
+        }
+        else
+        {
+            ry = static_cast<int>(row % L.R);
+            rz = static_cast<int>(row / L.R);
+        }
+        uint32_t out = 0;
+        const int zlo = (g.dim == 3) ? -r : 0, zhi = (g.dim == 3) ? r : 0;
+        for (int dz = zlo; dz <= zhi; ++dz)
+        {
+            const int z2 = rz + dz;
+            if (g.dim == 3 && (z2 < 0 || z2 >= L.R))
+            {
+                continue;
+            }
+            for (int dy = -r; dy <= r; ++dy)
+            {
+                const int y2 = ry + dy;
+                if (y2 < 0 || y2 >= L.R)
+                {
+                    continue;
+                }
+                const long long base = L.woff + ((g.dim == 2) ? y2 : static_cast<long long>(z2) * L.R + y2) * L.W;
+                const uint32_t mid   = __ldg(src + base + wi);
+                const uint32_t left  = wi > 0 ? __ldg(src + base + wi - 1) : 0u;
+                const uint32_t right = wi + 1 < L.W ? __ldg(src + base + wi + 1) : 0u;
+                out |= dilate_x(left, mid, right, r);
+            }
+        }
+        return out;
+    }
+
+    // mask of the cells of word (row, wi) at level l inside the box
+    // [lo, 2^l + hi) in every direction
+    __host__ __device__ __forceinline__ uint32_t box_mask(const Geom& g, int l, long long row, int wi, int lo, int hi)
+    {
+        const LevelGeom& L = g.lv[l];
+        int y, z;
+        if (g.dim == 2)
+        {
+            y = static_cast<int>(row) - PY;
+            z = 0;
+        }
+        else
+        {
+            y = static_cast<int>(row % L.R) - PY;
+            z = static_cast<int>(row / L.R) - PY;
+        }
+        const int a = -lo, b = L.n + hi; // allowed range [a, b)
+        if (y < a || y >= b || (g.dim == 3 && (z < a || z >= b)))
+        {
+            return 0u;
+        }
+        const int x0 = wi * 32 - PX; // x of bit 0
+        int s        = a - x0;
+        int e        = b - x0;
+        if (s < 0)
+        {
+            s = 0;
+        }
+        if (e > 32)
+        {
+            e = 32;
+        }
+        if (e <= s)
+        {
+            return 0u;
+        }
+        const uint32_t hiMask = (e == 32) ? 0xFFFFFFFFu : ((1u << e) - 1u);
+        const uint32_t loMask = (1u << s) - 1u;
+        return hiMask & ~loMask;
+    }
+
+    // decompose a global word index within a known level
+    struct WordLoc
+    {
+        long long row;
+        int wi;
+    };
+
+    __host__ __device__ __forceinline__ WordLoc word_loc(const Geom& g, int l, long long w)
+    {
+        const LevelGeom& L = g.lv[l];
+        const long long loc = w - L.woff;
+        const long long row = loc / L.W;
+        return {row, static_cast<int>(loc - row * L.W)};
+    }
+
+    // status word shared with the host
+    enum Status : int
+    {
+        SG_OK           = 0,
+        SG_ERR_ARG      = 1,
+        SG_ERR_CUDA     = 2,
+        SG_ERR_CAPACITY = 3,
+        SG_ERR_STATE    = 4,
+        SG_ERR_NOTFOUND = 5
+    };
+} // namespace sg

@@ -1,0 +1,125 @@
+// Host-side state of one GB300 MR mesh and its fields (one stream, one GPU).
+#pragma once
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "sg_core.cuh"
+
+namespace sg
+{
+    struct MeshCfg
+    {
+        int dim                = 2;
+        int min_level          = 0;
+        int max_level          = 0;
+        int max_stencil_radius = 1; // mesh_config::max_stencil_radius (mesh_config.hpp:42-80)
+        int prediction_radius  = 1; // config_t::prediction_stencil_radius
+        int graduation_width   = 1;
+        int ghost_width        = 1; // max(max_stencil_radius, prediction_radius)
+    };
+
+    // One mesh: the bitmaps of the MRMesh ids plus helper sets and the rank.
+    struct DeviceMesh
+    {
+        uint32_t* cells = nullptr; // MRMeshId::cells
+        uint32_t* cag   = nullptr; // MRMeshId::cells_and_ghosts
+        uint32_t* proj  = nullptr; // MRMeshId::proj_cells
+        uint32_t* uni   = nullptr; // MRMeshId::union_cells
+        uint32_t* ref   = nullptr; // MRMeshId::reference (all_cells)
+        uint32_t* hc    = nullptr; // cells[l+1].on(l): cells with a leaf child
+        uint32_t* hc2   = nullptr; // cells[l+2].on(l)
+        int* rank       = nullptr; // exclusive popcount prefix of ref
+        long long nb_ref   = 0;    // host copy of the reference size
+        long long nb_cells = 0;    // host copy of the leaf count
+    };
+
+    struct Ctx
+    {
+        MeshCfg cfg;
+        Geom g{};
+        cudaStream_t stream = nullptr;
+        DeviceMesh mesh[2];
+        int cur = 0;
+        // scratch bitmaps
+        uint32_t* t0 = nullptr;
+        uint32_t* t1 = nullptr;
+        uint32_t* t2 = nullptr;
+        uint32_t* t3 = nullptr;
+        uint32_t* rf = nullptr; // refine flags of leaf cells
+        uint32_t* cf = nullptr; // coarsen (and not keep) flags of leaf cells
+        // adaptation fields (dense layout)
+        double* detail = nullptr;
+        uint8_t* tag   = nullptr;
+        // scan scratch
+        long long* block_sums = nullptr;
+        long long n_scan_blocks = 0;
+        // device/host flags and counters
+        long long* d_counts = nullptr; // [0] = popcount total, [1..] misc
+        long long* h_counts = nullptr; // pinned mirror
+        int* d_flags        = nullptr;
+        int* h_flags        = nullptr; // pinned mirror
+        long long capacity  = 0;       // dense elements per field (32 * total_words)
+        int n_launches      = 0;       // kernel launches since the last reset (instrumentation)
+        std::string err;
+
+        DeviceMesh& m()
+        {
+            return mesh[cur];
+        }
+
+        DeviceMesh& spare()
+        {
+            return mesh[1 - cur];
+        }
+    };
+
+    struct DeviceField
+    {
+        Ctx* ctx       = nullptr;
+        double* data   = nullptr;
+        double* spare  = nullptr; // second buffer for update_fields
+        bool has_bc    = false;
+        double bc_value = 0.;
+        std::string name;
+    };
+
+    // kernels and drivers (sg_mesh.cu / sg_field.cu)
+    int build_mesh(Ctx& c, DeviceMesh& m);           // from m.cells
+    int scan_rank(Ctx& c, DeviceMesh& m);            // rank + nb_ref
+    int update_ghost_mr(Ctx& c, DeviceField& f);     // update_ghost_mr(u)
+    int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten);
+    int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme);
+    int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact);
+    int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense);
+    int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value);
+    int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged);
+    int device_error(Ctx& c); // reads and clears the device error word (synchronises)
+
+    // launch helpers
+    inline int grid_for(long long n, int block = 256, long long cap = 152LL * 32)
+    {
+        long long b = (n + block - 1) / block;
+        if (b < 1)
+        {
+            b = 1;
+        }
+        if (b > cap)
+        {
+            b = cap;
+        }
+        return static_cast<int>(b);
+    }
+
+    inline int check(Ctx& c, const char* where)
+    {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+        {
+            c.err = std::string(where) + ": " + cudaGetErrorString(e);
+            return SG_ERR_CUDA;
+        }
+        return SG_OK;
+    }
+} // namespace sg

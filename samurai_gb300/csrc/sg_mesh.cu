@@ -1,0 +1,579 @@
+// Mesh construction on the device: the MRMesh ids from a leaf-cell bitmap,
+// and the integer kernels of the adaptation (tags -> new cells, graduation).
+//
+// Set algebra follows samurai's subset semantics: operators act on cells of
+// one level, coarser operands are refined, .on(l) coarsens to the parent of
+// any member (subset/projection.hpp:68-177).  On bitmaps these are word-wise
+// AND/OR/ANDNOT, bit-pair compression (coarsen) and bit spreading (refine).
+#include "sg_ctx.cuh"
+
+namespace sg
+{
+    namespace
+    {
+        // ------------------------------------------------------------- words
+        template <class F>
+        __global__ void k_words(Geom g, int l0, int l1, F f)
+        {
+            const long long begin = g.lv[l0].woff;
+            const long long end   = g.lv[l1].woff + g.lv[l1].nwords;
+            for (long long w = begin + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < end;
+                 w += static_cast<long long>(gridDim.x) * blockDim.x)
+            {
+                int l = l0;
+                while (l < l1 && w >= g.lv[l + 1].woff)
+                {
+                    ++l;
+                }
+                const WordLoc loc = word_loc(g, l, w);
+                f(l, w, loc.row, loc.wi);
+            }
+        }
+
+        template <class F>
+        int launch_words(Ctx& c, int l0, int l1, F f, const char* what)
+        {
+            if (l0 > l1)
+            {
+                return SG_OK;
+            }
+            const long long n = c.g.lv[l1].woff + c.g.lv[l1].nwords - c.g.lv[l0].woff;
+            k_words<<<grid_for(n), 256, 0, c.stream>>>(c.g, l0, l1, f);
+            ++c.n_launches;
+            return check(c, what);
+        }
+
+        // --------------------------------------------------------------- scan
+        constexpr int SCAN_T   = 256;
+        constexpr int SCAN_PER = 16;
+        constexpr int SCAN_CHUNK = SCAN_T * SCAN_PER;
+
+        __device__ __forceinline__ long long block_exclusive_scan(long long v, long long* total)
+        {
+            __shared__ long long warp_tot[32];
+            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            long long x    = v;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                long long y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o)
+                {
+                    x += y;
+                }
+            }
+            if (lane == 31)
+            {
+                warp_tot[wid] = x;
+            }
+            __syncthreads();
+            const int nw = blockDim.x >> 5;
+            if (wid == 0)
+            {
+                long long t = lane < nw ? warp_tot[lane] : 0;
+                for (int o = 1; o < 32; o <<= 1)
+                {
+                    long long y = __shfl_up_sync(0xffffffffu, t, o);
+                    if (lane >= o)
+                    {
+                        t += y;
+                    }
+                }
+                if (lane < nw)
+                {
+                    warp_tot[lane] = t;
+                }
+            }
+            __syncthreads();
+            const long long before = wid > 0 ? warp_tot[wid - 1] : 0;
+            if (total)
+            {
+                *total = warp_tot[nw - 1];
+            }
+            const long long r = before + x - v;
+            __syncthreads();
+            return r;
+        }
+
+        __global__ void k_scan_sums(const uint32_t* bm, long long n, long long* sums)
+        {
+            const long long base = static_cast<long long>(blockIdx.x) * SCAN_CHUNK + threadIdx.x * SCAN_PER;
+            long long s          = 0;
+            for (int k = 0; k < SCAN_PER; ++k)
+            {
+                if (base + k < n)
+                {
+                    s += __popc(bm[base + k]);
+                }
+            }
+            long long tot;
+            block_exclusive_scan(s, &tot);
+            if (threadIdx.x == 0)
+            {
+                sums[blockIdx.x] = tot;
+            }
+        }
+
+        __global__ void k_scan_top(long long* sums, long long nb, long long* total_out)
+        {
+            // one block: each thread scans a contiguous slice sequentially
+            const long long per = (nb + blockDim.x - 1) / blockDim.x;
+            const long long b0  = threadIdx.x * per;
+            long long s         = 0;
+            for (long long k = 0; k < per; ++k)
+            {
+                if (b0 + k < nb)
+                {
+                    s += sums[b0 + k];
+                }
+            }
+            long long tot;
+            long long off = block_exclusive_scan(s, &tot);
+            for (long long k = 0; k < per; ++k)
+            {
+                if (b0 + k < nb)
+                {
+                    long long v   = sums[b0 + k];
+                    sums[b0 + k]  = off;
+                    off += v;
+                }
+            }
+            if (threadIdx.x == 0)
+            {
+                *total_out = tot;
+            }
+        }
+
+        __global__ void k_scan_write(const uint32_t* bm, long long n, const long long* sums, int* rank)
+        {
+            const long long base = static_cast<long long>(blockIdx.x) * SCAN_CHUNK + threadIdx.x * SCAN_PER;
+            long long s          = 0;
+            for (int k = 0; k < SCAN_PER; ++k)
+            {
+                if (base + k < n)
+                {
+                    s += __popc(bm[base + k]);
+                }
+            }
+            long long off = block_exclusive_scan(s, nullptr) + sums[blockIdx.x];
+            for (int k = 0; k < SCAN_PER; ++k)
+            {
+                if (base + k < n)
+                {
+                    rank[base + k] = static_cast<int>(off);
+                    off += __popc(bm[base + k]);
+                }
+            }
+        }
+
+        __global__ void k_popcount(const uint32_t* bm, long long n, long long* out)
+        {
+            long long s = 0;
+            for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < n; w += static_cast<long long>(gridDim.x) * blockDim.x)
+            {
+                s += __popc(bm[w]);
+            }
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                s += __shfl_down_sync(0xffffffffu, s, o);
+            }
+            if ((threadIdx.x & 31) == 0 && s)
+            {
+                atomicAdd(reinterpret_cast<unsigned long long*>(out), static_cast<unsigned long long>(s));
+            }
+        }
+    } // namespace
+
+    int scan_rank(Ctx& c, DeviceMesh& m)
+    {
+        const long long n  = c.g.total_words;
+        const long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+        k_scan_sums<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, n, c.block_sums);
+        k_scan_top<<<1, 1024, 0, c.stream>>>(c.block_sums, nb, c.d_counts);
+        k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, n, c.block_sums, m.rank);
+        cudaMemsetAsync(c.d_counts + 1, 0, sizeof(long long), c.stream);
+        k_popcount<<<grid_for(n), 256, 0, c.stream>>>(m.cells, n, c.d_counts + 1);
+        c.n_launches += 4;
+        int st = check(c, "scan_rank");
+        if (st)
+        {
+            return st;
+        }
+        cudaMemcpyAsync(c.h_counts, c.d_counts, 2 * sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return check(c, "scan_rank sync");
+        }
+        m.nb_ref   = c.h_counts[0];
+        m.nb_cells = c.h_counts[1];
+        if (m.nb_ref >= (1LL << 31))
+        {
+            c.err = "reference mesh exceeds 2^31 cells";
+            return SG_ERR_CAPACITY;
+        }
+        return SG_OK;
+    }
+
+    // Mesh_base::finalize_mesh for the serial unit-box case:
+    // construct_union (mesh.hpp:1231-1262), MRMesh::update_sub_mesh_impl
+    // (mr/mesh.hpp:222-455) and renumbering (mesh.hpp:894-911).
+    int build_mesh(Ctx& c, DeviceMesh& m)
+    {
+        const Geom g       = c.g;
+        const int top      = g.nlev - 1;
+        const int maxl     = c.cfg.max_level;
+        const int r        = c.cfg.max_stencil_radius;
+        const int p        = c.cfg.prediction_radius;
+        const bool multi   = c.cfg.max_level != c.cfg.min_level;
+        uint32_t* cells    = m.cells;
+        uint32_t* hc       = m.hc;
+        uint32_t* hc2      = m.hc2;
+        uint32_t* uni      = m.uni;
+        uint32_t* cag      = m.cag;
+        uint32_t* ref      = m.ref;
+        uint32_t* proj     = m.proj;
+        uint32_t* t1       = c.t1;
+        const size_t bytes = static_cast<size_t>(g.total_words) * 4;
+        int st;
+
+        // cells with a leaf child / grandchild
+        st = launch_words(c, 0, top,
+                          [=] __device__(int l, long long w, long long row, int wi)
+                          { hc[w] = (l + 1 < g.nlev) ? coarsen_word(g, cells, l, row, wi) : 0u; },
+                          "hc");
+        if (st)
+        {
+            return st;
+        }
+        st = launch_words(c, 0, top,
+                          [=] __device__(int l, long long w, long long row, int wi)
+                          { hc2[w] = (l + 1 < g.nlev) ? coarsen_word(g, hc, l, row, wi) : 0u; },
+                          "hc2");
+        if (st)
+        {
+            return st;
+        }
+
+        // union cells, top-down: union[l] = (cells[l+1] | union[l+1]).on(l)
+        cudaMemsetAsync(uni, 0, bytes, c.stream);
+        for (int l = maxl - 1; l >= 0; --l)
+        {
+            st = launch_words(c, l, l,
+                              [=] __device__(int ll, long long w, long long row, int wi)
+                              { uni[w] = hc[w] | coarsen_word(g, uni, ll, row, wi); },
+                              "union");
+            if (st)
+            {
+                return st;
+            }
+        }
+
+        // cells_and_ghosts: box expansion of the cells by max_stencil_radius
+        st = launch_words(c, 0, top,
+                          [=] __device__(int l, long long w, long long row, int wi) { cag[w] = box_dilate_word(g, cells, l, row, wi, r); },
+                          "cag");
+        if (st)
+        {
+            return st;
+        }
+
+        if (!multi)
+        {
+            cudaMemcpyAsync(ref, cag, bytes, cudaMemcpyDeviceToDevice, c.stream);
+            cudaMemsetAsync(proj, 0, bytes, c.stream);
+            return scan_rank(c, m);
+        }
+
+        // prediction ghosts: cag[l+1].on(l) expanded by p within the expanded
+        // domain, and cells[l+2].on(l) expanded by p
+        st = launch_words(c, 0, top,
+                          [=] __device__(int l, long long w, long long row, int wi)
+                          { t1[w] = (l + 1 < g.nlev) ? coarsen_word(g, cag, l, row, wi) : 0u; },
+                          "cag_on");
+        if (st)
+        {
+            return st;
+        }
+        st = launch_words(c, 0, top,
+                          [=] __device__(int l, long long w, long long row, int wi)
+                          {
+                              uint32_t v = cag[w];
+                              v |= box_dilate_word(g, t1, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
+                              v |= box_dilate_word(g, hc2, l, row, wi, p);
+                              ref[w] = v;
+                          },
+                          "ref0");
+        if (st)
+        {
+            return st;
+        }
+
+        // children of the projection cells, bottom-up:
+        // reference[l+1] |= (reference[l] & union[l]) refined
+        for (int l = 0; l + 1 <= maxl; ++l)
+        {
+            st = launch_words(c, l + 1, l + 1,
+                              [=] __device__(int lf, long long w, long long row, int k)
+                              {
+                                  const LevelGeom& F = g.lv[lf];
+                                  const LevelGeom& C = g.lv[lf - 1];
+                                  int yf, zf;
+                                  if (g.dim == 2)
+                                  {
+                                      yf = static_cast<int>(row) - PY;
+                                      zf = 0;
+                                  }
+                                  else
+                                  {
+                                      yf = static_cast<int>(row % F.R) - PY;
+                                      zf = static_cast<int>(row / F.R) - PY;
+                                  }
+                                  const int ry = (yf >> 1) + PY, rz = (zf >> 1) + PY;
+                                  const int wc = (k + 1) >> 1;
+                                  if (ry < 0 || ry >= C.R || (g.dim == 3 && (rz < 0 || rz >= C.R)) || wc >= C.W)
+                                  {
+                                      return;
+                                  }
+                                  const long long cw = C.woff + ((g.dim == 2) ? ry : static_cast<long long>(rz) * C.R + ry) * C.W + wc;
+                                  const uint32_t pc  = ref[cw] & uni[cw];
+                                  const uint32_t add = spread16(((k + 1) & 1) ? (pc >> 16) : pc);
+                                  if (add)
+                                  {
+                                      ref[w] |= add;
+                                  }
+                              },
+                              "ref_children");
+            if (st)
+            {
+                return st;
+            }
+        }
+        st = launch_words(c, 0, top, [=] __device__(int, long long w, long long, int) { proj[w] = ref[w] & uni[w]; }, "proj");
+        if (st)
+        {
+            return st;
+        }
+        return scan_rank(c, m);
+    }
+
+    // ------------------------------------------------------------------
+    // adaptation: integer part
+    // ------------------------------------------------------------------
+    namespace
+    {
+        // refine / coarsen_even flags of leaf cells from the tags
+        // (update_cell_array_from_tag, algorithm/graduation.hpp:743-842)
+        __global__ void k_tag_flags(Geom g, const uint32_t* cells, const uint8_t* tag, uint32_t* rf, uint32_t* cf, int minl, int maxl)
+        {
+            for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < g.total_words;
+                 w += static_cast<long long>(gridDim.x) * blockDim.x)
+            {
+                const uint32_t cw = cells[w];
+                uint32_t r = 0, k = 0;
+                if (cw)
+                {
+                    const int l = level_of(g, w);
+                    const uint8_t* t = tag + 32 * w;
+                    for (int b = 0; b < 32; ++b)
+                    {
+                        if ((cw >> b) & 1u)
+                        {
+                            const uint8_t tv = t[b];
+                            const bool refine = (tv & 4) && l < maxl;
+                            const bool coarsen = (tv & 2) && !(tv & 1) && l > minl;
+                            if (refine)
+                            {
+                                r |= 1u << b;
+                            }
+                            else if (coarsen)
+                            {
+                                k |= 1u << b;
+                            }
+                        }
+                    }
+                }
+                rf[w] = r;
+                cf[w] = k;
+            }
+        }
+    } // namespace
+
+    int new_cells_from_tags(Ctx& c, const DeviceMesh& m, uint32_t* nc)
+    {
+        const Geom g = c.g;
+        k_tag_flags<<<grid_for(g.total_words), 256, 0, c.stream>>>(g, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
+        ++c.n_launches;
+        int st = check(c, "tag_flags");
+        if (st)
+        {
+            return st;
+        }
+        const uint32_t* cells = m.cells;
+        const uint32_t* rf    = c.rf;
+        const uint32_t* cf    = c.cf;
+        const int minl = c.cfg.min_level, maxl = c.cfg.max_level;
+        return launch_words(c, 0, g.nlev - 1,
+                            [=] __device__(int l, long long w, long long row, int wi)
+                            {
+                                uint32_t v = 0;
+                                if (l >= minl && l <= maxl)
+                                {
+                                    v = cells[w] & ~rf[w] & ~cf[w];
+                                    if (l >= 1)
+                                    {
+                                        v |= refine_word(g, rf, l, row, wi);
+                                    }
+                                    if (l + 1 < g.nlev)
+                                    {
+                                        // parent of the coarsened (even) child
+                                        const LevelGeom& C = g.lv[l];
+                                        const LevelGeom& F = g.lv[l + 1];
+                                        int yc, zc;
+                                        if (g.dim == 2)
+                                        {
+                                            yc = static_cast<int>(row) - PY;
+                                            zc = 0;
+                                        }
+                                        else
+                                        {
+                                            yc = static_cast<int>(row % C.R) - PY;
+                                            zc = static_cast<int>(row / C.R) - PY;
+                                        }
+                                        const int ry = 2 * yc + PY, rz = 2 * zc + PY;
+                                        if (ry >= 0 && ry < F.R && (g.dim == 2 || (rz >= 0 && rz < F.R)))
+                                        {
+                                            const long long base = F.woff + ((g.dim == 2) ? ry : static_cast<long long>(rz) * F.R + ry) * F.W;
+                                            const int k0         = 2 * wi - 1;
+                                            const uint32_t lo    = (k0 >= 0 && k0 < F.W) ? cf[base + k0] : 0u;
+                                            const uint32_t hi    = (k0 + 1 < F.W) ? cf[base + k0 + 1] : 0u;
+                                            v |= compress_even(lo, hi);
+                                        }
+                                    }
+                                }
+                                nc[w] = v;
+                            },
+                            "new_cells");
+    }
+
+    // make_graduation (algorithm/graduation.hpp:573-726, 245-330): the cells
+    // of level l that lie under the (2*grad_width)-expansion of a leaf cell
+    // two or more levels finer are refined, until a fixed point.  The
+    // contiguous-boundary pass (graduation.hpp:121-249) is a no-op for a
+    // max_stencil_radius of 1.
+    int graduate(Ctx& c, uint32_t* nc, int* iterations)
+    {
+        const Geom g   = c.g;
+        const int top  = g.nlev - 1;
+        const int maxl = c.cfg.max_level;
+        const int gw2  = 2 * c.cfg.graduation_width;
+        uint32_t* e    = c.t0;
+        uint32_t* ec1  = c.t1;
+        uint32_t* d    = c.t2;
+        uint32_t* rr   = c.t3;
+        int* flag      = c.d_flags;
+        const size_t bytes = static_cast<size_t>(g.total_words) * 4;
+        int nit        = 0;
+        for (;;)
+        {
+            ++nit;
+            int st = launch_words(c, 0, top,
+                                  [=] __device__(int l, long long w, long long row, int wi) { e[w] = box_dilate_word(g, nc, l, row, wi, gw2); },
+                                  "grad_expand");
+            if (st)
+            {
+                return st;
+            }
+            st = launch_words(c, 0, top,
+                              [=] __device__(int l, long long w, long long row, int wi)
+                              { ec1[w] = (l + 1 < g.nlev) ? coarsen_word(g, e, l, row, wi) : 0u; },
+                              "grad_coarsen");
+            if (st)
+            {
+                return st;
+            }
+            cudaMemsetAsync(d, 0, bytes, c.stream);
+            cudaMemsetAsync(rr, 0, bytes, c.stream);
+            cudaMemsetAsync(flag, 0, sizeof(int), c.stream);
+            // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. 0
+            for (int l = maxl - 2; l >= 0; --l)
+            {
+                st = launch_words(c, l, l,
+                                  [=] __device__(int ll, long long w, long long row, int wi)
+                                  {
+                                      const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | coarsen_word(g, d, ll, row, wi);
+                                      d[w]              = dv;
+                                      const uint32_t rv = nc[w] & dv;
+                                      rr[w]             = rv;
+                                      if (rv)
+                                      {
+                                          atomicOr(flag, 1);
+                                      }
+                                  },
+                                  "grad_down");
+                if (st)
+                {
+                    return st;
+                }
+            }
+            cudaMemcpyAsync(c.h_flags, flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+            if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+            {
+                return check(c, "graduate sync");
+            }
+            if (!c.h_flags[0])
+            {
+                break;
+            }
+            st = launch_words(c, 0, top,
+                              [=] __device__(int l, long long w, long long row, int wi)
+                              {
+                                  uint32_t v = nc[w] & ~rr[w];
+                                  if (l >= 1)
+                                  {
+                                      v |= refine_word(g, rr, l, row, wi);
+                                  }
+                                  nc[w] = v;
+                              },
+                              "grad_apply");
+            if (st)
+            {
+                return st;
+            }
+            if (nit > 64)
+            {
+                c.err = "graduation did not converge";
+                return SG_ERR_STATE;
+            }
+        }
+        if (iterations)
+        {
+            *iterations = nit - 1;
+        }
+        return SG_OK;
+    }
+
+    int bitmaps_equal(Ctx& c, const uint32_t* a, const uint32_t* b, bool* equal)
+    {
+        int* flag = c.d_flags;
+        cudaMemsetAsync(flag, 0, sizeof(int), c.stream);
+        int st = launch_words(c, 0, c.g.nlev - 1,
+                              [=] __device__(int, long long w, long long, int)
+                              {
+                                  if (a[w] != b[w])
+                                  {
+                                      atomicOr(flag, 1);
+                                  }
+                              },
+                              "compare");
+        if (st)
+        {
+            return st;
+        }
+        cudaMemcpyAsync(c.h_flags, flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return check(c, "compare sync");
+        }
+        *equal = c.h_flags[0] == 0;
+        return SG_OK;
+    }
+} // namespace sg

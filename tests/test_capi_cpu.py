@@ -1,0 +1,55 @@
+"""CPU-side checks of the C ABI: the library builds for sm_103a, loads, and
+exports every function that include/samurai_gpu.h declares.  No compute call
+is made here (there is no GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "samurai_gpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(sg_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ["sg_mesh_create", "sg_field_create", "sg_adapt", "sg_update_ghost_mr", "sg_upwind", "sg_last_error"]:
+        assert s in syms
+
+
+def test_library_exports_all_declared_symbols():
+    from samurai_gb300 import build
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_no_cpu_fallback_without_gpu():
+    import samurai_gb300 as sg
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(sg.SamuraiGpuError):
+        sg.MRMesh(2, 2, 5)
+
+
+def test_unit_box_only():
+    import samurai_gb300 as sg
+    with pytest.raises(sg.SamuraiGpuError):
+        sg.Box([0, 0], [2, 1])
+
+
+def test_minimal_ghost_width_rule():
+    import samurai_gb300 as sg
+    cfg = sg.mesh_config(2).min_level(2).max_level(5)
+    assert cfg.parse_args() == 2  # mesh_config.hpp:388-393
+    assert cfg.max_stencil_size(2).disable_minimal_ghost_width().parse_args() == 1

@@ -1,0 +1,169 @@
+"""Parity of the GB300 path with the CPU oracle, through the C ABI.
+
+Integer results (intervals of every mesh id, leaf cells, storage indices,
+tags) must be identical; FP64 fields must be bit-identical too, since every
+operation is rounded individually in the reference's order (the stated
+tolerance of the path is 1e-13 relative; these tests use 0).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from advection_cases import demo_time_loop, disc, readme_square, shapes_2d, ball_3d
+from gpu_util import compare_cells, compare_fields, compare_meshes
+from oracle.pyoracle import OracleSim
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def sg():
+    from samurai_gb300 import build
+
+    build.build()
+    import samurai_gb300
+
+    return samurai_gb300
+
+
+def pair(sg, dim, minl, maxl, pred=1):
+    g = sg.AdvectionSim(dim, minl, maxl, 1, pred)
+    o = OracleSim(dim, minl, maxl, 1, pred)
+    return g, o
+
+
+def init_both(g, o, f):
+    lv, co, _ = o.cells()
+    vals = f(lv, co)
+    o.set_cell_values(vals)
+    g.set_cell_values(vals)
+
+
+@pytest.mark.parametrize("dim,minl,maxl", [(2, 2, 6), (2, 4, 9), (3, 2, 5)])
+def test_uniform_mesh_ids(sg, dim, minl, maxl):
+    g, o = pair(sg, dim, minl, maxl)
+    compare_meshes(g, o, maxl + 1, "uniform")
+    compare_cells(g, o, "uniform")
+    assert g.nb_ref() == o.nb_ref()
+
+
+def test_ghost_update_uniform(sg):
+    g, o = pair(sg, 2, 2, 6)
+    init_both(g, o, readme_square)
+    o.update_ghost()
+    g.update_ghost()
+    compare_fields(g, o, "ghosts")
+
+
+@pytest.mark.parametrize("pred", [0, 1])
+def test_golden_replay(sg, pred):
+    """demos/FiniteVolume/advection_2d.cpp with --Tf 0.01 on the GPU: same
+    meshes as the reference's golden files, fields bit-identical to the
+    oracle at every step."""
+    g, o = pair(sg, 2, 4, 10, pred)
+    init_both(g, o, disc)
+    o.adapt(2e-4, 1.0)
+    g.adapt(2e-4, 1.0)
+    compare_cells(g, o, "init")
+    compare_fields(g, o, "init", cells_only=True)
+    gold = np.load(os.path.join(GOLD, "pred_%d_init.npz" % pred))
+    assert np.array_equal(g.cell_values(), gold["u"])
+    dt = 0.5 * (1.0 / (1 << 10))
+    t, Tf, nt = 0.0, 0.01, 0
+    while t != Tf:
+        o.adapt(2e-4, 1.0)
+        g.adapt(2e-4, 1.0)
+        t += dt
+        if t > Tf:
+            dt += Tf - t
+            t = Tf
+        o.update_ghost()
+        g.update_ghost()
+        compare_fields(g, o, "step %d ghosts" % nt)
+        o.upwind([1.0, 1.0], dt, 0)
+        g.upwind([1.0, 1.0], dt, 0)
+        nt += 1
+        compare_cells(g, o, "step %d" % nt)
+        compare_fields(g, o, "step %d" % nt, cells_only=True)
+    compare_meshes(g, o, 10, "final")
+    gold = np.load(os.path.join(GOLD, "pred_%d.npz" % pred))
+    lv, co, _ = g.cells()
+    assert np.array_equal(lv, gold["level"]) and np.array_equal(co[:, 0], gold["i"]) and np.array_equal(co[:, 1], gold["j"])
+    np.testing.assert_allclose(g.cell_values(), gold["u"], rtol=1e-14, atol=1e-7)
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_readme_demo(sg, scheme):
+    """README demo: min 2, max 8, square of side 0.2, eps 1e-4, regularity 2,
+    dt = 0.5 dx; 12 of its 50 iterations, both upwind forms."""
+    g, o = pair(sg, 2, 2, 8)
+    init_both(g, o, readme_square)
+    dt = 0.5 / (1 << 8)
+    for it in range(12):
+        o.adapt(1e-4, 2.0)
+        g.adapt(1e-4, 2.0)
+        compare_cells(g, o, "it %d adapt" % it)
+        o.update_ghost()
+        g.update_ghost()
+        o.upwind([1.0, 1.0], dt, scheme)
+        g.upwind([1.0, 1.0], dt, scheme)
+        compare_fields(g, o, "it %d" % it, cells_only=True)
+    compare_meshes(g, o, 8, "readme")
+
+
+def test_shapes_2d_small(sg):
+    """Seeded squares + Gaussians, a = (1, 0.5), min 3, max 8, eps 1e-4, reg 2."""
+    g, o = pair(sg, 2, 3, 8)
+    init_both(g, o, shapes_2d(7, 6, 6))
+    dt = 0.5 / (1 << 8)
+    for it in range(6):
+        o.adapt(1e-4, 2.0)
+        g.adapt(1e-4, 2.0)
+        compare_cells(g, o, "shapes it %d" % it)
+        o.update_ghost()
+        g.update_ghost()
+        compare_fields(g, o, "shapes ghosts %d" % it)
+        o.upwind([1.0, 0.5], dt, 0)
+        g.upwind([1.0, 0.5], dt, 0)
+        compare_fields(g, o, "shapes it %d" % it, cells_only=True)
+    compare_meshes(g, o, 8, "shapes")
+
+
+def test_details_and_tags(sg):
+    """Detail and tag fields of a converged Harten pass."""
+    g, o = pair(sg, 2, 3, 8)
+    init_both(g, o, shapes_2d(3, 4, 4))
+    o.adapt(1e-4, 2.0)
+    g.adapt(1e-4, 2.0)
+    # one more pass on the adapted mesh: usually the fixed point
+    for ite in range(5):
+        ro = o.harten(ite, 1e-4, 2.0)
+        rg = g.harten(ite, 1e-4, 2.0)
+        assert ro == rg
+        if ro:
+            do, dg = o.detail(), g.detail()
+            assert np.array_equal(do, dg)
+            assert np.array_equal(o.tag(), g.tag())
+            break
+    compare_cells(g, o, "after harten")
+
+
+def test_3d_small(sg):
+    """3D: ball + Gaussians, a = (1,1,1), min 2, max 5, eps 1e-3, reg 1."""
+    g, o = pair(sg, 3, 2, 5)
+    init_both(g, o, ball_3d(5, 3))
+    dt = 0.3 / (1 << 5)
+    for it in range(4):
+        o.adapt(1e-3, 1.0)
+        g.adapt(1e-3, 1.0)
+        compare_cells(g, o, "3d it %d" % it)
+        o.update_ghost()
+        g.update_ghost()
+        compare_fields(g, o, "3d ghosts %d" % it)
+        o.upwind([1.0, 1.0, 1.0], dt, 0)
+        g.upwind([1.0, 1.0, 1.0], dt, 0)
+        compare_fields(g, o, "3d it %d" % it, cells_only=True)
+    compare_meshes(g, o, 5, "3d")
