@@ -1,0 +1,415 @@
+"""Benchmark of the GB300 MR advection step (one JSON line on stdout).
+
+Workload (the max_level-12 2D configuration): linear advection
+u_t + a.grad(u) = 0 on [0,1]^2, a = (1, 0.5), MRMesh min level 4, max level 12
+(4096^2 finest-equivalent), max_stencil_size 2 with the minimal ghost width
+disabled (as demos/FiniteVolume/advection_2d.cpp), Dirichlet 0, FP64.  The
+initial condition is a seeded sum of 16 indicator squares and 16 Gaussians.
+One step = make_MRAdapt(eps=1e-4, regularity=2) + update_ghost_mr + the
+upwind step, dt = 0.5 dx(max_level).  The metric is active cell-updates/s:
+leaf cells advanced per second, adaptation and ghost work included.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU implementation of the same path (the oracle
+port of samurai's algorithm: the reference itself cannot be built here) on
+the host cores, on the same workload, metric and unit.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from advection_cases import shapes_2d  # noqa: E402
+
+CFG = dict(dim=2, min_level=4, max_level=12, a=(1.0, 0.5), eps=1e-4, regularity=2.0, seed=2026)
+METRIC = "active cell-updates/s"
+UNIT = "cell-updates/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def workload_config(extra=None):
+    c = {
+        "workload": "2D MR linear advection, min_level 4, max_level 12 (4096^2), a=(1,0.5), eps 1e-4, regularity 2, "
+        "16 squares + 16 Gaussians (seed %d), Dirichlet 0, dt=0.5*dx_min, upwind" % CFG["seed"],
+        "min_level": CFG["min_level"],
+        "max_level": CFG["max_level"],
+        "max_stencil_radius": 1,
+        "prediction_radius": 1,
+        "l2": "flushed (256 MiB write) before every timed step",
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+def initial_values(level, coords):
+    return shapes_2d(CFG["seed"])(level, coords)
+
+
+# ------------------------------------------------------------------ helpers
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_info():
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "processor\t")) and ":" in line and "model name" in line.lower():
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return model or os.uname().machine
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index, path):
+        self.path = path
+        self.proc = None
+        try:
+            self.f = open(path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if p[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def halo_count(level, coords):
+    """Distinct same-level non-leaf neighbours (+-1 along each axis) of the
+    leaf cells: the ghost values the upwind stencil reads."""
+    key_bits = 24
+    total = 0
+    for l in np.unique(level):
+        c = coords[level == l].astype(np.int64) + 64
+        keys = c[:, 0] | (c[:, 1] << key_bits)
+        nb = []
+        for dx, dy in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+            nb.append((c[:, 0] + dx) | ((c[:, 1] + dy) << key_bits))
+        nb = np.unique(np.concatenate(nb))
+        total += int(np.setdiff1d(nb, keys, assume_unique=True).size)
+    return total
+
+
+# --------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from samurai_gb300 import build as gpu_build
+
+    gpu_build.build()
+    import samurai_gb300 as sg
+
+    dim, minl, maxl = CFG["dim"], CFG["min_level"], CFG["max_level"]
+    a = list(CFG["a"])
+    dt = 0.5 / (1 << maxl)
+    sim = sg.AdvectionSim(dim, minl, maxl, 1, 1)
+    lv, co, _ = sim.cells()
+    sim.set_cell_values(initial_values(lv, co))
+    sim.adapt(CFG["eps"], CFG["regularity"])  # initial adaptation, as the demo does before its loop
+    stream_ptr = sim.mesh.stream()
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
+
+    def step():
+        sim.adapt(CFG["eps"], CFG["regularity"])
+        sim.update_ghost()
+        sim.upwind(a, dt)
+
+    for _ in range(args.warmup):
+        step()
+    sim.mesh.synchronize()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident timed region
+    sampler = ClockSampler(local, os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % rank)) if rank == 0 else None
+    barrier()
+    total_ms = 0.0
+    cell_updates = 0
+    sim.mesh.launch_count(reset=True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        n_cells = sim.nb_cells()
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+        step()
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+        cell_updates += n_cells
+    launches = sim.mesh.launch_count()
+    barrier()
+    clocks = sampler.stop() if sampler else None
+    ms = total_ms / args.steps
+    if world > 1:
+        t = torch.tensor([total_ms, float(cell_updates)], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        total_ms_max, cell_updates_all = float(tmax[0]), float(t[1])
+    else:
+        total_ms_max, cell_updates_all = total_ms, float(cell_updates)
+    value = cell_updates_all / (total_ms_max / 1e3)
+
+    # ---- end-to-end through the C ABI with host buffers
+    cap = sim.mesh.nb_cells("reference") * 4 + 1024
+    host = torch.empty(cap, dtype=torch.float64, pin_memory=True)
+    hbuf = host.numpy()
+    e2e_steps = max(1, min(args.steps, 50))
+    h2d = d2h = 0
+    e2e_updates = 0
+    n_ref = sim.nb_ref()
+    hbuf[:n_ref] = sim.u.array()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        n_ref = sim.nb_ref()
+        if n_ref > cap:
+            raise RuntimeError("pinned buffer too small")
+        sim.u.set_array(hbuf[:n_ref])
+        h2d += 8 * n_ref
+        e2e_updates += sim.nb_cells()
+        step()
+        n_ref = sim.nb_ref()
+        out = hbuf[:n_ref]
+
+
+        sg._check(sg.lib().sg_field_download(sim.u.h, out.ctypes.data_as(ctypes.c_void_p), n_ref), "download")
+        d2h += 8 * n_ref
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_updates * world / e2e_s
+
+    # ---- roofline of the upwind kernel, timed alone on its launch stream
+    nc, _ = sim.mesh.counts()
+    lv, co, _ = sim.cells()
+    halo = halo_count(lv, co)
+    alg_bytes = 16 * nc + 8 * halo
+    reps = 20
+    upw_ms = 0.0
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+            ev0.record(stream)
+        sim.unp1.assign_upwind(sim.u, a, dt)
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+        upw_ms += ev0.elapsed_time(ev1)
+    upw_ms /= reps
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = alg_bytes / (upw_ms / 1e3) / 1e9
+    traffic = None
+    try:
+        traffic_info = json.load(open(os.path.join(ROOT, "profiles", "upwind_traffic.json")))
+        traffic = traffic_info.get("bytes_per_launch")
+    except Exception:
+        pass
+
+    # ---- samurai's named timers over a few extra steps (per-phase GPU time)
+    phase_steps = 10
+    sim.mesh.timers(enable=True, reset=True)
+    for _ in range(phase_steps):
+        step()
+    phases = {k: round(v[0] / phase_steps, 4) for k, v in sim.mesh.timers(enable=False).items()}
+
+    cpu = cpu_baseline(sim, a, dt) if (rank == 0 and not args.no_cpu_baseline) else None
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": total_ms_max / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic: seeded squares + Gaussians (no dataset involved)",
+            "config": workload_config({"parallelism": "replicas" if world > 1 else "single GPU",
+                                       "cells_final": int(nc), "reference_cells_final": int(sim.nb_ref())}),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps),
+                    "steps": e2e_steps, "api": "sg_field_upload + sg_adapt + sg_update_ghost_mr + sg_upwind + sg_field_swap + sg_field_download"},
+            "roofline": {"bound": "hbm", "kernel": "k_upwind", "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": int(alg_bytes), "launch_ms": upw_ms,
+                         "cells": int(nc), "halo": int(halo)},
+            "gpu_launches": int(launches),
+            "launches_per_step": launches / args.steps,
+            "phases_ms_per_step": phases,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(sim, a, dt, budget_s=15.0):
+    """The CPU oracle advanced from the GPU's current state (same mesh, same
+    leaf values) for about budget_s seconds of steps, 1 thread."""
+    from oracle.pyoracle import OracleSim
+
+    lv, co, _ = sim.cells()
+    vals = sim.cell_values()
+    o = OracleSim(CFG["dim"], CFG["min_level"], CFG["max_level"], 1, 1)
+    o.set_cells(lv, co)
+    o.set_cell_values(vals)
+    t0 = time.perf_counter()
+    n = 0
+    updates = 0
+    while True:
+        updates += o.nb_cells()
+        o.adapt(CFG["eps"], CFG["regularity"])
+        o.update_ghost()
+        o.upwind(list(a), dt, 0)
+        n += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": updates / el, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_info(),
+            "sample": "%d steps of the same workload from the GPU run's final mesh and values (%.1f s)" % (n, el)}
+
+
+# --------------------------------------------------------- reference arm
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from oracle.pyoracle import OracleSim
+
+    dim, minl, maxl = CFG["dim"], CFG["min_level"], CFG["max_level"]
+    dt = 0.5 / (1 << maxl)
+    t_setup = time.perf_counter()
+    o = OracleSim(dim, minl, maxl, 1, 1)
+    lv, co, _ = o.cells()
+    o.set_cell_values(initial_values(lv, co))
+    o.adapt(CFG["eps"], CFG["regularity"])
+    for _ in range(min(args.warmup, 1)):
+        o.adapt(CFG["eps"], CFG["regularity"])
+        o.update_ghost()
+        o.upwind(list(CFG["a"]), dt, 0)
+    setup = time.perf_counter() - t_setup
+    budget = 90.0
+    t0 = time.perf_counter()
+    n = 0
+    updates = 0
+    while n < args.steps:
+        updates += o.nb_cells()
+        o.adapt(CFG["eps"], CFG["regularity"])
+        o.update_ghost()
+        o.upwind(list(CFG["a"]), dt, 0)
+        n += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    value = updates / el
+    sample = "%d of %d requested steps after the initial adaptation (setup %.0f s), 1 thread" % (n, args.steps, setup)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": n,
+        "warmup": min(args.warmup, 1),
+        "ms_per_step": 1e3 * el / n,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: seeded squares + Gaussians (no dataset involved)",
+        "config": workload_config({"parallelism": "sequential CPU (the reference MR path has no threading)"}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_info(), "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    args = p.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

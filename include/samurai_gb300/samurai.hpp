@@ -1,0 +1,595 @@
+// C++ drop-in for samurai's MR advection API, backed by libsamurai_gpu.so.
+//
+// A samurai program of the form of demos/FiniteVolume/advection_2d.cpp or
+// the README example compiles against this header with its calls unchanged:
+//
+//   auto config = samurai::mesh_config<2>().min_level(4).max_level(10)
+//                     .max_stencil_size(2).disable_minimal_ghost_width();   // mesh_config.hpp:16-433
+//   auto mesh   = samurai::mra::make_mesh(box, config);                      // mr/mesh.hpp:511-518
+//   auto u      = samurai::make_scalar_field<double>("u", mesh);             // field/scalar_field.hpp:173-216
+//   samurai::for_each_cell(mesh, [&](auto& cell) { u[cell] = ...; });        // algorithm.hpp:301-363 (host mirror)
+//   samurai::make_bc<samurai::Dirichlet<1>>(u, 0.);                          // bc/bc.hpp:786-800
+//   auto MRadaptation = samurai::make_MRAdapt(u);                            // mr/adapt.hpp:391-397
+//   MRadaptation(samurai::mra_config().epsilon(2e-4));                       // mr/adapt.hpp:147-195
+//   samurai::update_ghost_mr(u);                                             // algorithm/update_ghost_mr.hpp:261-270
+//   unp1 = u - dt * samurai::upwind(a, u);                                   // stencil_field.hpp:175-179
+//   std::swap(u.array(), unp1.array());                                      // advection_2d.cpp:146
+//
+// The mesh and the fields live on the GPU.  for_each_cell / for_each_interval
+// with user lambdas run on a host mirror (downloaded on demand); writes made
+// through u[cell] are uploaded at the next GPU call.  Errors raise
+// std::runtime_error with the library's message.
+#pragma once
+
+#include <array>
+#include <cstddef>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../samurai_gpu.h"
+
+namespace samurai
+{
+    namespace detail
+    {
+        inline void check(int status, const char* what)
+        {
+            if (status != SG_OK)
+            {
+                throw std::runtime_error(std::string(what) + ": " + sg_last_error());
+            }
+        }
+    }
+
+    template <class value_t, std::size_t dim>
+    struct Box
+    {
+        std::array<value_t, dim> min_corner, max_corner;
+
+        Box(const std::array<value_t, dim>& a, const std::array<value_t, dim>& b)
+            : min_corner(a)
+            , max_corner(b)
+        {
+            for (std::size_t d = 0; d < dim; ++d)
+            {
+                if (a[d] != 0 || b[d] != 1)
+                {
+                    throw std::invalid_argument("samurai_gb300: only the unit box is supported");
+                }
+            }
+        }
+    };
+
+    namespace default_config
+    {
+        static constexpr int prediction_stencil_radius = 1;
+    }
+
+    template <std::size_t dim_, int prediction_stencil_radius_ = default_config::prediction_stencil_radius>
+    class mesh_config
+    {
+      public:
+
+        static constexpr std::size_t dim            = dim_;
+        static constexpr int prediction_stencil_radius = prediction_stencil_radius_;
+
+        auto& min_level(std::size_t l)
+        {
+            m_min = l;
+            return *this;
+        }
+
+        auto& max_level(std::size_t l)
+        {
+            m_max = l;
+            return *this;
+        }
+
+        auto& max_stencil_radius(int r)
+        {
+            m_r = r;
+            return *this;
+        }
+
+        auto& max_stencil_size(int s)
+        {
+            m_r = s / 2 + (s % 2);
+            return *this;
+        }
+
+        auto& graduation_width(std::size_t w)
+        {
+            m_grad = w;
+            return *this;
+        }
+
+        auto& disable_minimal_ghost_width()
+        {
+            m_no_min_gw = true;
+            return *this;
+        }
+
+        auto& disable_args_parse()
+        {
+            return *this;
+        }
+
+        std::size_t min_level() const
+        {
+            return m_min;
+        }
+
+        std::size_t max_level() const
+        {
+            return m_max;
+        }
+
+        std::size_t graduation_width() const
+        {
+            return m_grad;
+        }
+
+        // mesh_config::parse_args (mesh_config.hpp:358-396), without CLI overrides
+        int parsed_stencil_radius() const
+        {
+            if (m_max < m_min)
+            {
+                throw std::invalid_argument("Max level must be greater than min level.");
+            }
+            return m_no_min_gw ? m_r : (m_r > 2 ? m_r : 2);
+        }
+
+      private:
+
+        std::size_t m_min = 0, m_max = 6, m_grad = 1;
+        int m_r           = 1;
+        bool m_no_min_gw  = false;
+    };
+
+    // deprecated MRConfig<dim> used by the README (mr/mesh.hpp:45-72)
+    template <std::size_t dim_>
+    struct MRConfig
+    {
+        static constexpr std::size_t dim               = dim_;
+        static constexpr int prediction_stencil_radius = 1;
+    };
+
+    template <std::size_t dim>
+    struct Cell
+    {
+        std::size_t level;
+        std::array<int, dim> indices;
+        long long index;
+        double length;
+
+        std::array<double, dim> center() const
+        {
+            std::array<double, dim> c;
+            for (std::size_t d = 0; d < dim; ++d)
+            {
+                c[d] = length * (indices[d] + 0.5); // cell.hpp:130-133 with a zero origin
+            }
+            return c;
+        }
+
+        std::array<double, dim> corner() const
+        {
+            std::array<double, dim> c;
+            for (std::size_t d = 0; d < dim; ++d)
+            {
+                c[d] = length * indices[d];
+            }
+            return c;
+        }
+    };
+
+    struct Interval
+    {
+        int start, end;
+        long long index;
+
+        int size() const
+        {
+            return end - start;
+        }
+    };
+
+    template <class Config>
+    class MRMesh
+    {
+      public:
+
+        static constexpr std::size_t dim = Config::dim;
+
+        MRMesh() = default;
+
+        MRMesh(int min_level, int max_level, int stencil_radius, int prediction_radius, int graduation_width)
+            : m_min(min_level)
+            , m_max(max_level)
+        {
+            sg_mesh_t h = nullptr;
+            detail::check(sg_mesh_create(static_cast<int>(dim), min_level, max_level, stencil_radius, prediction_radius, graduation_width, &h),
+                          "MRMesh");
+            m_h = std::shared_ptr<sg_mesh_s>(h, [](sg_mesh_t p) { sg_mesh_destroy(p); });
+        }
+
+        // deprecated constructor of the README (mr/mesh.hpp:166-181)
+        MRMesh(const Box<double, dim>&, std::size_t min_level, std::size_t max_level)
+            : MRMesh(static_cast<int>(min_level), static_cast<int>(max_level), 1, Config::prediction_stencil_radius, 1)
+        {
+        }
+
+        sg_mesh_t handle() const
+        {
+            return m_h.get();
+        }
+
+        std::size_t min_level() const
+        {
+            return static_cast<std::size_t>(m_min);
+        }
+
+        std::size_t max_level() const
+        {
+            return static_cast<std::size_t>(m_max);
+        }
+
+        double cell_length(std::size_t level) const
+        {
+            return 1.0 / static_cast<double>(1 << level);
+        }
+
+        double min_cell_length() const
+        {
+            return cell_length(max_level());
+        }
+
+        std::size_t nb_cells() const
+        {
+            long long nc = 0, nr = 0;
+            detail::check(sg_mesh_counts(handle(), &nc, &nr), "nb_cells");
+            return static_cast<std::size_t>(nr);
+        }
+
+        std::size_t nb_leaf_cells() const
+        {
+            long long nc = 0, nr = 0;
+            detail::check(sg_mesh_counts(handle(), &nc, &nr), "nb_cells");
+            return static_cast<std::size_t>(nc);
+        }
+
+        std::vector<Cell<dim>> cells() const
+        {
+            const std::size_t n = nb_leaf_cells();
+            std::vector<int> level(n), coords(n * dim);
+            std::vector<long long> index(n);
+            detail::check(sg_mesh_get_cells(handle(), level.data(), coords.data(), index.data(), static_cast<long long>(n)), "cells");
+            std::vector<Cell<dim>> out(n);
+            for (std::size_t k = 0; k < n; ++k)
+            {
+                out[k].level = static_cast<std::size_t>(level[k]);
+                for (std::size_t d = 0; d < dim; ++d)
+                {
+                    out[k].indices[d] = coords[k * dim + d];
+                }
+                out[k].index  = index[k];
+                out[k].length = cell_length(out[k].level);
+            }
+            return out;
+        }
+
+      private:
+
+        std::shared_ptr<sg_mesh_s> m_h;
+        int m_min = 0, m_max = 0;
+    };
+
+    namespace mra
+    {
+        template <class Cfg>
+        auto make_empty_mesh(const Cfg&)
+        {
+            return MRMesh<Cfg>();
+        }
+
+        template <class Cfg>
+        auto make_mesh(const Box<double, Cfg::dim>&, const Cfg& cfg)
+        {
+            return MRMesh<Cfg>(static_cast<int>(cfg.min_level()), static_cast<int>(cfg.max_level()), cfg.parsed_stencil_radius(),
+                               Cfg::prediction_stencil_radius, static_cast<int>(cfg.graduation_width()));
+        }
+    }
+
+    template <class Mesh>
+    class ScalarField;
+
+    // host mirror of u.array(): downloaded on demand, uploaded when dirty
+    class FieldArray
+    {
+      public:
+
+        std::vector<double> values;
+        bool valid = false;
+        bool dirty = false;
+    };
+
+    template <class Mesh>
+    struct UpwindExpr // u - dt * upwind(a, u)
+    {
+        const ScalarField<Mesh>* u;
+        std::array<double, Mesh::dim> a;
+        double dt;
+        int scheme;
+    };
+
+    template <class Mesh>
+    struct ScaledUpwind
+    {
+        const ScalarField<Mesh>* u;
+        std::array<double, Mesh::dim> a;
+        double dt;
+    };
+
+    template <class Mesh>
+    struct UpwindOp
+    {
+        const ScalarField<Mesh>* u;
+        std::array<double, Mesh::dim> a;
+    };
+
+    template <class Mesh>
+    class ScalarField
+    {
+      public:
+
+        static constexpr std::size_t dim = Mesh::dim;
+
+        ScalarField(std::string name, Mesh& mesh)
+            : m_mesh(&mesh)
+            , m_name(std::move(name))
+        {
+            sg_field_t h = nullptr;
+            detail::check(sg_field_create(mesh.handle(), m_name.c_str(), &h), "make_scalar_field");
+            m_h = std::shared_ptr<sg_field_s>(h, [](sg_field_t p) { sg_field_destroy(p); });
+        }
+
+        sg_field_t handle() const
+        {
+            return m_h.get();
+        }
+
+        Mesh& mesh() const
+        {
+            return *m_mesh;
+        }
+
+        // host mirror access (for_each_cell initialisation, inspection)
+        double& operator[](const Cell<dim>& cell)
+        {
+            pull();
+            m_host.dirty = true;
+            return m_host.values[static_cast<std::size_t>(cell.index)];
+        }
+
+        double operator[](const Cell<dim>& cell) const
+        {
+            const_cast<ScalarField*>(this)->pull();
+            return m_host.values[static_cast<std::size_t>(cell.index)];
+        }
+
+        void resize()
+        {
+        }
+
+        // u.array(): swapping arrays swaps the device storage
+        ScalarField& array()
+        {
+            return *this;
+        }
+
+        // push pending host writes before any GPU computation
+        void sync_to_device()
+        {
+            if (m_host.dirty)
+            {
+                detail::check(sg_field_upload(handle(), m_host.values.data(), static_cast<long long>(m_host.values.size())), "upload");
+                m_host.dirty = false;
+            }
+            m_host.valid = false;
+        }
+
+        ScalarField& operator=(const UpwindExpr<Mesh>& e)
+        {
+            const_cast<ScalarField<Mesh>*>(e.u)->sync_to_device();
+            detail::check(sg_upwind(e.u->handle(), handle(), e.a.data(), e.dt, e.scheme), "upwind");
+            m_host.valid = false;
+            return *this;
+        }
+
+        friend void swap(ScalarField& a, ScalarField& b)
+        {
+            a.sync_to_device();
+            b.sync_to_device();
+            detail::check(sg_field_swap(a.handle(), b.handle()), "swap");
+        }
+
+      private:
+
+        void pull()
+        {
+            if (m_host.valid)
+            {
+                return;
+            }
+            m_host.values.resize(m_mesh->nb_cells());
+            detail::check(sg_field_download(handle(), m_host.values.data(), static_cast<long long>(m_host.values.size())), "download");
+            m_host.valid = true;
+        }
+
+        Mesh* m_mesh;
+        std::string m_name;
+        std::shared_ptr<sg_field_s> m_h;
+        FieldArray m_host;
+    };
+
+    template <class value_t, class Mesh>
+    auto make_scalar_field(const std::string& name, Mesh& mesh)
+    {
+        static_assert(std::is_same_v<value_t, double>, "samurai_gb300 fields are FP64");
+        return ScalarField<Mesh>(name, mesh);
+    }
+
+    // README spelling make_field<double, 1>(name, mesh)
+    template <class value_t, std::size_t n_comp, class Mesh>
+    auto make_field(const std::string& name, Mesh& mesh)
+    {
+        static_assert(n_comp == 1, "samurai_gb300: vector fields are not implemented");
+        return make_scalar_field<value_t>(name, mesh);
+    }
+
+    template <std::size_t order = 1>
+    struct Dirichlet
+    {
+        static_assert(order == 1, "samurai_gb300 implements Dirichlet<1>");
+    };
+
+    template <class Bc, class Field>
+    void make_bc(Field& u, double value = 0.)
+    {
+        detail::check(sg_field_set_dirichlet(u.handle(), value), "make_bc");
+    }
+
+    template <class Mesh, class F>
+    void for_each_cell(const Mesh& mesh, F&& f)
+    {
+        for (auto& c : mesh.cells())
+        {
+            f(c);
+        }
+    }
+
+    class mra_config
+    {
+      public:
+
+        mra_config& epsilon(double e)
+        {
+            m_eps = e;
+            return *this;
+        }
+
+        double epsilon() const
+        {
+            return m_eps;
+        }
+
+        mra_config& regularity(double r)
+        {
+            m_reg = r;
+            return *this;
+        }
+
+        double regularity() const
+        {
+            return m_reg;
+        }
+
+        mra_config& relative_detail(bool r)
+        {
+            if (r)
+            {
+                throw std::invalid_argument("samurai_gb300: relative detail is not implemented");
+            }
+            return *this;
+        }
+
+      private:
+
+        double m_eps = 1e-4, m_reg = 1.;
+    };
+
+    template <class Field>
+    class Adapt
+    {
+      public:
+
+        explicit Adapt(Field& u)
+            : m_u(&u)
+        {
+        }
+
+        void operator()(const mra_config& cfg)
+        {
+            m_u->sync_to_device();
+            detail::check(sg_adapt(m_u->handle(), cfg.epsilon(), cfg.regularity(), &m_last), "MRadaptation");
+        }
+
+        void operator()(double eps, double regularity)
+        {
+            (*this)(mra_config().epsilon(eps).regularity(regularity));
+        }
+
+        int last_harten_passes() const
+        {
+            return m_last;
+        }
+
+      private:
+
+        Field* m_u;
+        int m_last = 0;
+    };
+
+    template <class Field>
+    auto make_MRAdapt(Field& u)
+    {
+        return Adapt<Field>(u);
+    }
+
+    template <class Field>
+    void update_ghost_mr(Field& u)
+    {
+        u.sync_to_device();
+        detail::check(sg_update_ghost_mr(u.handle()), "update_ghost_mr");
+    }
+
+    template <class Mesh, class A>
+    auto upwind(const A& a, const ScalarField<Mesh>& u)
+    {
+        UpwindOp<Mesh> op{&u, {}};
+        for (std::size_t d = 0; d < Mesh::dim; ++d)
+        {
+            op.a[d] = a[d];
+        }
+        return op;
+    }
+
+    template <class Mesh>
+    ScaledUpwind<Mesh> operator*(double dt, const UpwindOp<Mesh>& op)
+    {
+        return {op.u, op.a, dt};
+    }
+
+    template <class Mesh>
+    UpwindExpr<Mesh> operator-(const ScalarField<Mesh>& u, const ScaledUpwind<Mesh>& s)
+    {
+        if (&u != s.u)
+        {
+            throw std::invalid_argument("samurai_gb300: u - dt * upwind(a, v) needs v == u");
+        }
+        return {&u, s.a, s.dt, SG_UPWIND_OP};
+    }
+} // namespace samurai
+
+namespace std
+{
+    // std::swap(u.array(), unp1.array())
+    template <class Mesh>
+    void swap(samurai::ScalarField<Mesh>& a, samurai::ScalarField<Mesh>& b)
+    {
+        swap(a, b);
+    }
+}

@@ -80,6 +80,13 @@ int sg_mesh_synchronize(sg_mesh_t mesh);
 /* kernel launches issued on the mesh since the last reset (instrumentation) */
 int sg_mesh_launch_count(sg_mesh_t mesh, int reset, long long* count);
 
+/* samurai's named timers (timers.hpp:111-1036, printed with --timers): CUDA-event timers per phase.
+ * ids: 0 mesh adaptation, 1 ghost update, 2 detail computation, 3 tag cells, 4 tag finalization,
+ * 5 mesh update, 6 make_graduation, 7 mesh construction, 8 fields update, 9 field expressions (upwind). */
+int sg_timers_enable(sg_mesh_t mesh, int enable);
+int sg_timers_get(sg_mesh_t mesh, int timer_id, double* total_ms, long long* calls);
+int sg_timers_reset(sg_mesh_t mesh);
+
 /* samurai::make_scalar_field<double>(name, mesh) (field/scalar_field.hpp:173-216) */
 int sg_field_create(sg_mesh_t mesh, const char* name, sg_field_t* out);
 int sg_field_destroy(sg_field_t field);

@@ -62,6 +62,9 @@ def lib():
         "sg_mesh_stream": (i, [vp, ctypes.POINTER(vp)]),
         "sg_mesh_synchronize": (i, [vp]),
         "sg_mesh_launch_count": (i, [vp, i, pl]),
+        "sg_timers_enable": (i, [vp, i]),
+        "sg_timers_get": (i, [vp, i, ctypes.POINTER(d), pl]),
+        "sg_timers_reset": (i, [vp]),
         "sg_field_create": (i, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
         "sg_field_destroy": (i, [vp]),
         "sg_field_set_dirichlet": (i, [vp, d]),
@@ -266,6 +269,22 @@ class MRMesh:
 
     def synchronize(self):
         _check(lib().sg_mesh_synchronize(self.h), "sg_mesh_synchronize")
+
+    TIMER_NAMES = ["mesh adaptation", "ghost update", "detail computation", "tag cells", "tag finalization", "mesh update",
+                   "make_graduation", "mesh construction", "fields update", "field expressions"]
+
+    def timers(self, enable=None, reset=False):
+        """samurai's named timers as {name: (ms, calls)}; enable/reset on request"""
+        if enable is not None:
+            _check(lib().sg_timers_enable(self.h, 1 if enable else 0), "sg_timers_enable")
+        if reset:
+            _check(lib().sg_timers_reset(self.h), "sg_timers_reset")
+        out = {}
+        for k, name in enumerate(self.TIMER_NAMES):
+            ms, n = ctypes.c_double(), ctypes.c_longlong()
+            _check(lib().sg_timers_get(self.h, k, ctypes.byref(ms), ctypes.byref(n)), "sg_timers_get")
+            out[name] = (ms.value, n.value)
+        return out
 
     def launch_count(self, reset=False):
         n = ctypes.c_longlong()

@@ -74,6 +74,8 @@ namespace
         st |= dalloc(c, &m.hc, n);
         st |= dalloc(c, &m.hc2, n);
         st |= dalloc(c, &m.rank, n);
+        st |= dalloc(c, &m.wl_ref, n);
+        st |= dalloc(c, &m.wl_cells, n);
         return st ? sg::SG_ERR_CUDA : sg::SG_OK;
     }
 
@@ -87,6 +89,8 @@ namespace
         dfree(m.hc);
         dfree(m.hc2);
         dfree(m.rank);
+        dfree(m.wl_ref);
+        dfree(m.wl_cells);
     }
 
     void destroy_ctx(sg_mesh_s* h)
@@ -95,6 +99,11 @@ namespace
         if (c.stream)
         {
             cudaStreamSynchronize(c.stream);
+        }
+        sg::timers_flush(c);
+        for (cudaEvent_t e : c.timers.pool)
+        {
+            cudaEventDestroy(e);
         }
         free_mesh(c.mesh[0]);
         free_mesh(c.mesh[1]);
@@ -280,12 +289,12 @@ extern "C"
         st |= dalloc(c, &c.detail, static_cast<size_t>(c.capacity));
         st |= dalloc(c, &c.tag, static_cast<size_t>(c.capacity));
         c.n_scan_blocks = (c.g.total_words + 4095) / 4096;
-        st |= dalloc(c, &c.block_sums, static_cast<size_t>(c.n_scan_blocks) + 1);
-        st |= dalloc(c, &c.d_counts, 8);
+        st |= dalloc(c, &c.block_sums, 4 * static_cast<size_t>(c.n_scan_blocks) + 4);
+        st |= dalloc(c, &c.d_counts, static_cast<size_t>(sg::COUNTS));
         st |= dalloc(c, &c.d_flags, 8);
         if (!st)
         {
-            if (cudaMallocHost(reinterpret_cast<void**>(&c.h_counts), 8 * sizeof(long long)) != cudaSuccess
+            if (cudaMallocHost(reinterpret_cast<void**>(&c.h_counts), sg::COUNTS * sizeof(long long)) != cudaSuccess
                 || cudaMallocHost(reinterpret_cast<void**>(&c.h_flags), 8 * sizeof(int)) != cudaSuccess)
             {
                 st = SG_ERR_CUDA;
@@ -570,6 +579,49 @@ extern "C"
         if (reset)
         {
             mesh->ctx.n_launches = 0;
+        }
+        return SG_OK;
+    }
+
+    int sg_timers_enable(sg_mesh_t mesh, int enable)
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_timers_enable: null mesh");
+        }
+        mesh->ctx.timers.enabled = enable != 0;
+        return SG_OK;
+    }
+
+    int sg_timers_get(sg_mesh_t mesh, int timer_id, double* total_ms, long long* calls)
+    {
+        if (!mesh || timer_id < 0 || timer_id >= sg::T_COUNT)
+        {
+            return fail(SG_ERR_ARG, "sg_timers_get: bad mesh or timer id");
+        }
+        sg::timers_flush(mesh->ctx);
+        if (total_ms)
+        {
+            *total_ms = mesh->ctx.timers.ms[timer_id];
+        }
+        if (calls)
+        {
+            *calls = mesh->ctx.timers.calls[timer_id];
+        }
+        return SG_OK;
+    }
+
+    int sg_timers_reset(sg_mesh_t mesh)
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_timers_reset: null mesh");
+        }
+        sg::timers_flush(mesh->ctx);
+        for (int i = 0; i < sg::T_COUNT; ++i)
+        {
+            mesh->ctx.timers.ms[i]    = 0.;
+            mesh->ctx.timers.calls[i] = 0;
         }
         return SG_OK;
     }

@@ -31,12 +31,49 @@ namespace sg
         uint32_t* hc    = nullptr; // cells[l+1].on(l): cells with a leaf child
         uint32_t* hc2   = nullptr; // cells[l+2].on(l)
         int* rank       = nullptr; // exclusive popcount prefix of ref
+        int* wl_ref     = nullptr; // indices of the non-empty reference words, ascending
+        int* wl_cells   = nullptr; // indices of the non-empty leaf-cell words, ascending
         long long nb_ref   = 0;    // host copy of the reference size
         long long nb_cells = 0;    // host copy of the leaf count
+        // host copies: the words of level l are wl_*[lo_*[l] .. lo_*[l+1])
+        long long lo_ref[MAXLEV + 1]   = {};
+        long long lo_cells[MAXLEV + 1] = {};
+    };
+
+    constexpr int COUNTS = 4 + 2 * (MAXLEV + 1); // device counters filled by scan_rank
+
+    // Named phase timers with samurai's scope names (timers.hpp:111-1036;
+    // mr/adapt.hpp:151-387, update_ghost_mr.hpp:263, field/field_base.hpp:234).
+    // Disabled by default; when enabled, CUDA events on the mesh stream
+    // bracket each phase and the host sums the intervals on request.
+    enum TimerId : int
+    {
+        T_ADAPT = 0,      // "mesh adaptation"
+        T_GHOST,          // "ghost update"
+        T_DETAIL,         // "detail computation"
+        T_TAG,            // "tag cells"
+        T_FINALIZE,       // "tag finalization"
+        T_MESH_UPDATE,    // "mesh update" (tags -> cells, graduation, fixed-point test)
+        T_GRADUATION,     // "make_graduation"
+        T_CONSTRUCTION,   // "mesh construction"
+        T_FIELDS_UPDATE,  // "fields update"
+        T_UPWIND,         // "field expressions" (the upwind step)
+        T_COUNT
+    };
+
+    struct Timers
+    {
+        bool enabled = false;
+        std::vector<cudaEvent_t> pool;
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> open[T_COUNT];
+        double ms[T_COUNT]    = {};
+        long long calls[T_COUNT] = {};
+        cudaEvent_t pending[T_COUNT] = {};
     };
 
     struct Ctx
     {
+        Timers timers;
         MeshCfg cfg;
         Geom g{};
         cudaStream_t stream = nullptr;
@@ -96,6 +133,28 @@ namespace sg
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value);
     int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged);
     int device_error(Ctx& c); // reads and clears the device error word (synchronises)
+
+    void timer_start(Ctx& c, int id);
+    void timer_stop(Ctx& c, int id);
+    void timers_flush(Ctx& c); // synchronises and accumulates
+
+    struct ScopedTimer
+    {
+        Ctx& c;
+        int id;
+
+        ScopedTimer(Ctx& cc, int i)
+            : c(cc)
+            , id(i)
+        {
+            timer_start(c, id);
+        }
+
+        ~ScopedTimer()
+        {
+            timer_stop(c, id);
+        }
+    };
 
     // launch helpers
     inline int grid_for(long long n, int block = 256, long long cap = 152LL * 32)

@@ -37,31 +37,48 @@ namespace sg
     {
         constexpr int BLOCK = 256;
 
-        // Warp-cooperative traversal of the set bits of a computed subset:
-        // lane k evaluates word c0+k, the warp then visits every non-empty
-        // word with one lane per bit, so field accesses are 256 B coalesced.
+        constexpr int WARPS_PER_BLOCK = BLOCK / 32;
+
+        // One warp per listed word, lane b on bit b.  The list holds the
+        // non-empty words of a superset (reference or leaf cells) in
+        // ascending order; word_of(w) narrows it to the subset a kernel acts
+        // on.  Consecutive cells of a word are consecutive doubles, so every
+        // field access of a warp is one 256-byte segment.
         template <class WordF, class CellF>
-        __device__ __forceinline__ void warp_bits(long long wb, long long we, WordF word_of, CellF cell)
+        __device__ __forceinline__ void warp_list(const int* list, long long begin, long long end, long long warp0, long long nwarps, WordF word_of,
+                                                  CellF cell)
         {
-            const int lane         = threadIdx.x & 31;
-            const long long warp   = (blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) >> 5;
-            const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
-            for (long long c0 = wb + warp * 32; c0 < we; c0 += nwarps * 32)
+            const int lane = threadIdx.x & 31;
+            for (long long i = begin + warp0; i < end; i += nwarps)
             {
-                const long long w = c0 + lane;
-                const uint32_t v  = (w < we) ? word_of(w) : 0u;
-                uint32_t nz       = __ballot_sync(0xffffffffu, v != 0u);
-                while (nz)
+                const long long w = __ldg(list + i);
+                const uint32_t v  = word_of(w);
+                if ((v >> lane) & 1u)
                 {
-                    const int j = __ffs(nz) - 1;
-                    nz &= nz - 1;
-                    const uint32_t vj = __shfl_sync(0xffffffffu, v, j);
-                    if ((vj >> lane) & 1u)
-                    {
-                        cell(c0 + j, lane);
-                    }
+                    cell(w, lane);
                 }
             }
+        }
+
+        __device__ __forceinline__ long long warp_id()
+        {
+            return (blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) >> 5;
+        }
+
+        __device__ __forceinline__ long long warp_count()
+        {
+            return (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+        }
+
+        int blocks_for_items(long long items)
+        {
+            long long b = (items + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
+            if (b < 1)
+            {
+                b = 1;
+            }
+            const long long cap = 152LL * 64;
+            return static_cast<int>(b > cap ? cap : b);
         }
 
         // interp_coeffs<3> (numeric/prediction.hpp:32-36), parity 0: even
@@ -135,9 +152,9 @@ namespace sg
         }
 
         // ----------------------------------------------------------- tags
-        __global__ void k_tag_init(Geom g, const uint32_t* ref, const uint32_t* cells, uint8_t* tag, double* det)
+        __global__ void k_tag_init(Geom g, const int* wl, long long n, const uint32_t* ref, const uint32_t* cells, uint8_t* tag, double* det)
         {
-            warp_bits(0, g.total_words, [=](long long w) { return ref[w]; },
+            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; },
                       [=](long long w, int b)
                       {
                           const long long e = 32 * w + b;
@@ -179,12 +196,12 @@ namespace sg
 
         // update_outer_corners_by_polynomial_extrapolation for a ghost width
         // of 1 (bc/apply_field_bc.hpp:371-505) followed by project_corner_below
-        // (algorithm/update_outer_ghost.hpp:268-337).  One block per direction.
-        __global__ void k_corners(Geom g, Dirs dirs, int l, const uint32_t* cells, const uint32_t* ref, double* u)
+        // (algorithm/update_outer_ghost.hpp:268-337), one block per diagonal
+        // direction.
+        __device__ void corner_role(const Geom& g, const int* d, int l, const uint32_t* cells, const uint32_t* ref, double* u)
         {
-            const int* d  = dirs.d[blockIdx.x];
-            const int n   = g.lv[l].n;
-            int nfree     = 0;
+            const int n = g.lv[l].n;
+            int nfree   = 0;
             for (int k = 0; k < g.dim; ++k)
             {
                 nfree += (d[k] == 0);
@@ -256,7 +273,7 @@ namespace sg
                 }
                 if (a == axis)
                 {
-                    in[a] = sgn > 0 ? n - 1 : 0;
+                    in[a]  = sgn > 0 ? n - 1 : 0;
                     dir[a] = sgn;
                 }
                 else
@@ -266,33 +283,86 @@ namespace sg
             }
         }
 
-        // project_bc (algorithm/update_outer_ghost.hpp:20-155) and the
-        // Dirichlet<1> ghost u_g = 2 v - u_c (bc/dirichlet.hpp:22-29) for every
-        // Cartesian direction at level l.
-        __global__ void k_faces(Geom g, int l, int do_project, int do_dirichlet, double value, const uint32_t* cells, const uint32_t* uni,
-                                const uint32_t* ref, double* u)
+        struct GhostLevelArgs
         {
-            const int n          = g.lv[l].n;
-            const long long nf   = (g.dim == 2) ? n : static_cast<long long>(n) * n;
-            const long long ntot = nf * 2 * g.dim;
-            for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < ntot; t += static_cast<long long>(gridDim.x) * blockDim.x)
+            int l;
+            int do_corners;
+            int do_project;   // project_bc: level < max_level
+            int do_dirichlet; // apply_field_bc: level >= min_level and a BC is attached
+            int do_predict;   // predict_bc: min_level <= level < max_level
+            double value;
+            int nb_corner;    // blocks of the corner role
+            int nb_face;      // blocks of the face role
+            long long nfaces; // face positions (2*dim directions)
+            long long p_begin, p_end; // reference word list range of level l-1 (projection)
+        };
+
+        // One launch per level of the top-down pass of update_ghost_mr
+        // (algorithm/update_ghost_mr.hpp:206-222).  Within a level the
+        // reference's operations touch disjoint cells and read only cells
+        // finalised earlier, so they run concurrently as block roles:
+        //  - corners: outer corners and their projection two levels down;
+        //  - faces: per Cartesian direction, the Dirichlet ghost 2v - u
+        //    (bc/dirichlet.hpp:22-29) then predict_bc to level l+1
+        //    (update_outer_ghost.hpp:195-266) by the same thread, or project_bc
+        //    (update_outer_ghost.hpp:20-155) next to union cells;
+        //  - projection of the reference cells of level l onto proj_cells[l-1]
+        //    (numeric/projection.hpp:15-65).
+        __global__ void k_ghost_level(Geom g, Dirs dirs, GhostLevelArgs a, const int* wl_ref, const uint32_t* cells, const uint32_t* uni,
+                                      const uint32_t* proj, const uint32_t* ref, double* u)
+        {
+            const int l = a.l;
+            if (static_cast<int>(blockIdx.x) < a.nb_corner)
             {
-                const int k = static_cast<int>(t / nf);
+                corner_role(g, dirs.d[blockIdx.x], l, cells, ref, u);
+                return;
+            }
+            if (static_cast<int>(blockIdx.x) < a.nb_corner + a.nb_face)
+            {
+                const long long t = static_cast<long long>(blockIdx.x - a.nb_corner) * blockDim.x + threadIdx.x;
+                if (t >= a.nfaces)
+                {
+                    return;
+                }
+                const int n        = g.lv[l].n;
+                const long long nf = (g.dim == 2) ? n : static_cast<long long>(n) * n;
+                const int k        = static_cast<int>(t / nf);
                 int in[3], dir[3];
                 face_cell(g, l, k, t - k * nf, in, dir);
                 const Pos pi = pos_of(g, l, in[0], in[1], in[2]);
                 const int gx = in[0] + dir[0], gy = in[1] + dir[1], gz = in[2] + dir[2];
-                if (do_dirichlet && test(cells, pi))
+                if ((a.do_dirichlet || a.do_predict) && test(cells, pi))
                 {
                     const long long eg = elem_at(g, l, gx, gy, gz);
-                    u[eg]              = 2 * value - u[elem(pi)];
+                    if (a.do_dirichlet)
+                    {
+                        u[eg] = 2 * a.value - u[elem(pi)];
+                    }
+                    if (a.do_predict)
+                    {
+                        const double v = u[eg];
+                        for (int sz = 0; sz < (g.dim == 3 ? 2 : 1); ++sz)
+                        {
+                            for (int sy = 0; sy < 2; ++sy)
+                            {
+                                for (int sx = 0; sx < 2; ++sx)
+                                {
+                                    const Pos pf = pos_of(g, l + 1, 2 * gx + sx, 2 * gy + sy, g.dim == 3 ? 2 * gz + sz : 0);
+                                    if (test(ref, pf))
+                                    {
+                                        u[elem(pf)] = v;
+                                    }
+                                }
+                            }
+                        }
+                    }
                 }
-                else if (do_project && test(uni, pi))
+                else if (a.do_project && test(uni, pi))
                 {
                     const Pos pg = pos_of(g, l, gx, gy, gz);
                     if (!test(ref, pg))
                     {
-                        continue;
+                        return;
                     }
                     double sum = 0.;
                     int nch    = 0;
@@ -318,50 +388,14 @@ namespace sg
                     }
                     u[elem(pg)] = nch > 0 ? sum / static_cast<double>(nch) : 0.;
                 }
+                return;
             }
-        }
-
-        // predict_bc (algorithm/update_outer_ghost.hpp:195-266): the children
-        // at l+1 of the Dirichlet ghosts of level l copy their parent.
-        __global__ void k_faces_predict(Geom g, int l, const uint32_t* cells, const uint32_t* ref, double* u)
-        {
-            const int n          = g.lv[l].n;
-            const long long nf   = (g.dim == 2) ? n : static_cast<long long>(n) * n;
-            const long long ntot = nf * 2 * g.dim;
-            for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < ntot; t += static_cast<long long>(gridDim.x) * blockDim.x)
-            {
-                const int k = static_cast<int>(t / nf);
-                int in[3], dir[3];
-                face_cell(g, l, k, t - k * nf, in, dir);
-                if (!test(cells, g, l, in[0], in[1], in[2]))
-                {
-                    continue;
-                }
-                const int px = in[0] + dir[0], py = in[1] + dir[1], pz = in[2] + dir[2];
-                const double v = u[elem_at(g, l, px, py, pz)];
-                for (int sz = 0; sz < (g.dim == 3 ? 2 : 1); ++sz)
-                {
-                    for (int sy = 0; sy < 2; ++sy)
-                    {
-                        for (int sx = 0; sx < 2; ++sx)
-                        {
-                            const Pos pf = pos_of(g, l + 1, 2 * px + sx, 2 * py + sy, g.dim == 3 ? 2 * pz + sz : 0);
-                            if (test(ref, pf))
-                            {
-                                u[elem(pf)] = v;
-                            }
-                        }
-                    }
-                }
-            }
-        }
-
-        // projection of the reference cells of level l onto proj_cells[l-1]
-        // (algorithm/update_ghost_mr.hpp:217-221)
-        __global__ void k_project(Geom g, int l, const uint32_t* proj, const uint32_t* ref, double* u)
-        {
-            const int lc = l - 1;
-            warp_bits(g.lv[lc].woff, g.lv[lc].woff + g.lv[lc].nwords,
+            // projection role
+            const int lc              = l - 1;
+            const long long rb        = static_cast<long long>(blockIdx.x - a.nb_corner - a.nb_face);
+            const long long warp0     = (rb * blockDim.x + threadIdx.x) >> 5;
+            const long long nwarps    = (static_cast<long long>(gridDim.x - a.nb_corner - a.nb_face) * blockDim.x) >> 5;
+            warp_list(wl_ref, a.p_begin, a.p_end, warp0, nwarps,
                       [=](long long w)
                       {
                           const WordLoc loc = word_loc(g, lc, w);
@@ -369,16 +403,17 @@ namespace sg
                       },
                       [=](long long w, int b)
                       {
-                          const Cell c = cell_of(g, lc, w, b);
+                          const Cell c  = cell_of(g, lc, w, b);
                           u[32 * w + b] = project_one(g, u, l, c.x, c.y, c.z);
                       });
         }
 
         // prediction of the ghosts of level l from level l-1
         // (algorithm/update_ghost_mr.hpp:224-233)
-        __global__ void k_predict(Geom g, int l, int order, const uint32_t* cells, const uint32_t* proj, const uint32_t* ref, double* u)
+        __global__ void k_predict(Geom g, int l, int order, const int* wl_ref, long long begin, long long end, const uint32_t* cells, const uint32_t* proj,
+                                  const uint32_t* ref, double* u)
         {
-            warp_bits(g.lv[l].woff, g.lv[l].woff + g.lv[l].nwords,
+            warp_list(wl_ref, begin, end, warp_id(), warp_count(),
                       [=](long long w)
                       {
                           const WordLoc loc = word_loc(g, l, w);
@@ -386,7 +421,7 @@ namespace sg
                       },
                       [=](long long w, int b)
                       {
-                          const Cell c = cell_of(g, l, w, b);
+                          const Cell c  = cell_of(g, l, w, b);
                           u[32 * w + b] = predict_one(g, u, l, c.x, c.y, c.z, order);
                       });
         }
@@ -394,10 +429,10 @@ namespace sg
         // -------------------------------------------------------- details
         // compute_detail_op (mr/operators.hpp:139-540) on
         // intersection(all_cells[l], union(cells[l+1], cells[l+2])).on(l)
-        __global__ void k_detail(Geom g, int l0, int l1, int order, const uint32_t* ref, const uint32_t* hc, const uint32_t* hc2, const double* u,
-                                 double* det)
+        __global__ void k_detail(Geom g, int order, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
+                                 const uint32_t* hc2, const double* u, double* det)
         {
-            warp_bits(g.lv[l0].woff, g.lv[l1].woff + g.lv[l1].nwords, [=](long long w) { return ref[w] & (hc[w] | hc2[w]); },
+            warp_list(wl, begin, end, warp_id(), warp_count(), [=](long long w) { return ref[w] & (hc[w] | hc2[w]); },
                       [=](long long w, int b)
                       {
                           const int l    = level_of(g, w);
@@ -459,10 +494,10 @@ namespace sg
 
         // mr_criteria_op (mr/criteria.hpp:20-113) on
         // intersection(cells[l], all_cells[l-1]).on(l-1), fine levels l0..l1
-        __global__ void k_criteria(Geom g, int l0, int l1, Eps eps, const uint32_t* ref, const uint32_t* hc, const double* det, uint8_t* tag)
+        __global__ void k_criteria(Geom g, Eps eps, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
+                                   const double* det, uint8_t* tag)
         {
-            const int lc0 = l0 - 1, lc1 = l1 - 1;
-            warp_bits(g.lv[lc0].woff, g.lv[lc1].woff + g.lv[lc1].nwords, [=](long long w) { return ref[w] & hc[w]; },
+            warp_list(wl, begin, end, warp_id(), warp_count(), [=](long long w) { return ref[w] & hc[w]; },
                       [=](long long w, int b)
                       {
                           const int lc  = level_of(g, w);
@@ -511,10 +546,10 @@ namespace sg
         }
 
         // maximum_op (mr/operators.hpp:22-96), children at level l
-        __global__ void k_maximum(Geom g, int l, const uint32_t* ref, const uint32_t* hc, uint8_t* tag)
+        __global__ void k_maximum(Geom g, int l, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc, uint8_t* tag)
         {
             const int lc = l - 1;
-            warp_bits(g.lv[lc].woff, g.lv[lc].woff + g.lv[lc].nwords, [=](long long w) { return ref[w] & hc[w]; },
+            warp_list(wl, begin, end, warp_id(), warp_count(), [=](long long w) { return ref[w] & hc[w]; },
                       [=](long long w, int b)
                       {
                           const Cell c  = cell_of(g, lc, w, b);
@@ -554,10 +589,10 @@ namespace sg
         // update_fields (algorithm/update_fields.hpp:27-127): copy on
         // reference ∩ new cells, projection on coarsened cells, prediction on
         // refined cells; every other reference entry of the new field is 0.
-        __global__ void k_update_fields(Geom g, int order, const uint32_t* nref, const uint32_t* ncells, const uint32_t* oref, const uint32_t* ocells,
-                                        const uint32_t* ohc, const double* uo, double* un)
+        __global__ void k_update_fields(Geom g, int order, const int* wl, long long n, const uint32_t* nref, const uint32_t* ncells, const uint32_t* oref,
+                                        const uint32_t* ocells, const uint32_t* ohc, const double* uo, double* un)
         {
-            warp_bits(0, g.total_words, [=](long long w) { return nref[w]; },
+            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return nref[w]; },
                       [=](long long w, int b)
                       {
                           const long long e = 32 * w + b;
@@ -588,9 +623,10 @@ namespace sg
         // demos/FiniteVolume/advection_2d.cpp:144) or the README lambda
         // (README.md:144-153).  Neighbours at the same level are reference
         // cells, at fixed offsets in the dense slabs.
-        __global__ void k_upwind(Geom g, const uint32_t* cells, const double* u, double* unp1, double a0, double a1, double a2, double dt, int scheme)
+        __global__ void k_upwind(Geom g, const int* wl, long long n, const uint32_t* cells, const double* u, double* unp1, double a0, double a1, double a2,
+                                 double dt, int scheme)
         {
-            warp_bits(0, g.total_words, [=](long long w) { return cells[w]; },
+            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return cells[w]; },
                       [=](long long w, int b)
                       {
                           const int l          = level_of(g, w);
@@ -642,47 +678,44 @@ namespace sg
         }
 
         // --------------------------------------------------- layout moves
-        __global__ void k_gather(Geom g, const uint32_t* ref, const int* rank, const double* dense, double* compact)
+        __global__ void k_gather(const int* wl, long long n, const uint32_t* ref, const int* rank, const double* dense, double* compact)
         {
-            warp_bits(0, g.total_words, [=](long long w) { return ref[w]; },
+            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; },
                       [=](long long w, int b) { compact[ref_index(ref, rank, Pos{w, b})] = dense[32 * w + b]; });
         }
 
-        __global__ void k_scatter(Geom g, const uint32_t* ref, const int* rank, const double* compact, double* dense)
+        __global__ void k_scatter(const int* wl, long long n, const uint32_t* ref, const int* rank, const double* compact, double* dense)
         {
-            warp_bits(0, g.total_words, [=](long long w) { return ref[w]; },
+            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; },
                       [=](long long w, int b) { dense[32 * w + b] = compact[ref_index(ref, rank, Pos{w, b})]; });
         }
 
-        __global__ void k_fill(Geom g, const uint32_t* ref, double* dense, double v)
+        __global__ void k_fill(const int* wl, long long n, const uint32_t* ref, double* dense, double v)
         {
-            warp_bits(0, g.total_words, [=](long long w) { return ref[w]; }, [=](long long w, int b) { dense[32 * w + b] = v; });
-        }
-
-        int grid_words(long long nwords)
-        {
-            // one warp per 32 words, capped at 8 resident blocks per SM
-            return grid_for((nwords + 31) / 32 * 32, BLOCK, 152LL * 8);
+            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; }, [=](long long w, int b) { dense[32 * w + b] = v; });
         }
     } // namespace
 
     int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
     {
-        k_gather<<<grid_words(c.g.total_words), BLOCK, 0, c.stream>>>(c.g, m.ref, m.rank, dense, compact);
+        const long long n = m.lo_ref[c.g.nlev];
+        k_gather<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(m.wl_ref, n, m.ref, m.rank, dense, compact);
         ++c.n_launches;
         return check(c, "gather");
     }
 
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense)
     {
-        k_scatter<<<grid_words(c.g.total_words), BLOCK, 0, c.stream>>>(c.g, m.ref, m.rank, compact, dense);
+        const long long n = m.lo_ref[c.g.nlev];
+        k_scatter<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(m.wl_ref, n, m.ref, m.rank, compact, dense);
         ++c.n_launches;
         return check(c, "scatter");
     }
 
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value)
     {
-        k_fill<<<grid_words(c.g.total_words), BLOCK, 0, c.stream>>>(c.g, m.ref, dense, value);
+        const long long n = m.lo_ref[c.g.nlev];
+        k_fill<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(m.wl_ref, n, m.ref, dense, value);
         ++c.n_launches;
         return check(c, "fill");
     }
@@ -690,6 +723,7 @@ namespace sg
     // update_ghost_mr / update_ghost_mr_aggregated (algorithm/update_ghost_mr.hpp:195-270)
     int update_ghost_mr(Ctx& c, DeviceField& f)
     {
+        ScopedTimer timer(c, T_GHOST);
         const Geom& g   = c.g;
         DeviceMesh& m   = c.m();
         const int minl  = c.cfg.min_level;
@@ -706,39 +740,41 @@ namespace sg
         }
         for (int l = maxl; l >= lmin; --l)
         {
-            if (l >= minl && l <= maxl)
-            {
-                k_corners<<<diag.n, BLOCK, 0, c.stream>>>(g, diag, l, m.cells, m.ref, u);
-                ++c.n_launches;
-            }
-            const int n       = g.lv[l].n;
-            const long long nf = static_cast<long long>(2 * g.dim) * ((g.dim == 2) ? n : static_cast<long long>(n) * n);
-            const int do_proj = l < maxl;
-            const int do_bc   = (l >= minl) && f.has_bc;
-            if (do_proj || do_bc)
-            {
-                k_faces<<<grid_for(nf), BLOCK, 0, c.stream>>>(g, l, do_proj, do_bc, f.bc_value, m.cells, m.uni, m.ref, u);
-                ++c.n_launches;
-            }
-            if (l >= minl && l < maxl)
-            {
-                k_faces_predict<<<grid_for(nf), BLOCK, 0, c.stream>>>(g, l, m.cells, m.ref, u);
-                ++c.n_launches;
-            }
+            GhostLevelArgs a{};
+            a.l            = l;
+            a.do_corners   = (l >= minl && l <= maxl) ? 1 : 0;
+            a.do_project   = l < maxl;
+            a.do_dirichlet = (l >= minl) && f.has_bc;
+            a.do_predict   = (l >= minl && l < maxl);
+            a.value        = f.bc_value;
+            a.nb_corner    = a.do_corners ? diag.n : 0;
+            const int n    = g.lv[l].n;
+            a.nfaces       = (a.do_project || a.do_dirichlet || a.do_predict)
+                                 ? static_cast<long long>(2 * g.dim) * ((g.dim == 2) ? n : static_cast<long long>(n) * n)
+                                 : 0;
+            a.nb_face      = static_cast<int>((a.nfaces + BLOCK - 1) / BLOCK);
             if (l > lmin)
             {
-                k_project<<<grid_words(g.lv[l - 1].nwords), BLOCK, 0, c.stream>>>(g, l, m.proj, m.ref, u);
+                a.p_begin = m.lo_ref[l - 1];
+                a.p_end   = m.lo_ref[l];
+            }
+            const long long items = a.p_end - a.p_begin;
+            const int nb_proj     = items > 0 ? blocks_for_items(items) : 0;
+            const int grid        = a.nb_corner + a.nb_face + nb_proj;
+            if (grid > 0)
+            {
+                k_ghost_level<<<grid, BLOCK, 0, c.stream>>>(g, diag, a, m.wl_ref, m.cells, m.uni, m.proj, m.ref, u);
                 ++c.n_launches;
             }
         }
-        for (int l = 1; l <= maxl; ++l)
+        for (int l = (lmin > 1 ? lmin : 1); l <= maxl; ++l)
         {
-            if (l < lmin)
+            const long long b = m.lo_ref[l], e = m.lo_ref[l + 1];
+            if (e > b)
             {
-                continue;
+                k_predict<<<blocks_for_items(e - b), BLOCK, 0, c.stream>>>(g, l, c.cfg.prediction_radius, m.wl_ref, b, e, m.cells, m.proj, m.ref, u);
+                ++c.n_launches;
             }
-            k_predict<<<grid_words(g.lv[l].nwords), BLOCK, 0, c.stream>>>(g, l, c.cfg.prediction_radius, m.cells, m.proj, m.ref, u);
-            ++c.n_launches;
         }
         return check(c, "update_ghost_mr");
     }
@@ -753,7 +789,7 @@ namespace sg
         const int dim  = g.dim;
         int st;
 
-        k_tag_init<<<grid_words(g.total_words), BLOCK, 0, c.stream>>>(g, m.ref, m.cells, c.tag, c.detail);
+        k_tag_init<<<blocks_for_items(m.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(g, m.wl_ref, m.lo_ref[g.nlev], m.ref, m.cells, c.tag, c.detail);
         ++c.n_launches;
         if ((st = check(c, "tag_init")))
         {
@@ -766,13 +802,16 @@ namespace sg
 
         const int dl0 = minl > 0 ? minl - 1 : 0;
         const int dl1 = maxl - ite - 1;
-        if (dl1 >= dl0)
+        timer_start(c, T_DETAIL);
+        if (dl1 >= dl0 && m.lo_ref[dl1 + 1] > m.lo_ref[dl0])
         {
-            k_detail<<<grid_words(g.lv[dl1].woff + g.lv[dl1].nwords - g.lv[dl0].woff), BLOCK, 0, c.stream>>>(g, dl0, dl1, c.cfg.prediction_radius, m.ref,
-                                                                                                              m.hc, m.hc2, f.data, c.detail);
+            const long long b = m.lo_ref[dl0], e_ = m.lo_ref[dl1 + 1];
+            k_detail<<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(g, c.cfg.prediction_radius, m.wl_ref, b, e_, m.ref, m.hc, m.hc2, f.data,
+                                                                        c.detail);
             ++c.n_launches;
         }
-
+        timer_stop(c, T_DETAIL);
+        timer_start(c, T_TAG);
         Eps e{};
         for (int l = minl; l <= maxl - ite; ++l)
         {
@@ -782,22 +821,30 @@ namespace sg
             e.coarse[l]        = e.fine[l] / (1 << dim);
         }
         const int cl0 = minl, cl1 = maxl - ite;
-        if (cl1 >= cl0 && cl0 >= 1)
+        if (cl1 >= cl0 && cl0 >= 1 && m.lo_ref[cl1] > m.lo_ref[cl0 - 1])
         {
-            k_criteria<<<grid_words(g.lv[cl1 - 1].woff + g.lv[cl1 - 1].nwords - g.lv[cl0 - 1].woff), BLOCK, 0, c.stream>>>(g, cl0, cl1, e, m.ref, m.hc,
-                                                                                                                              c.detail, c.tag);
+            const long long b = m.lo_ref[cl0 - 1], e_ = m.lo_ref[cl1];
+            k_criteria<<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(g, e, m.wl_ref, b, e_, m.ref, m.hc, c.detail, c.tag);
             ++c.n_launches;
         }
+        timer_stop(c, T_TAG);
+        timer_start(c, T_FINALIZE);
         for (int l = maxl; l > 0; --l)
         {
-            k_maximum<<<grid_words(g.lv[l - 1].nwords), BLOCK, 0, c.stream>>>(g, l, m.ref, m.hc, c.tag);
-            ++c.n_launches;
+            const long long b = m.lo_ref[l - 1], e_ = m.lo_ref[l];
+            if (e_ > b)
+            {
+                k_maximum<<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(g, l, m.wl_ref, b, e_, m.ref, m.hc, c.tag);
+                ++c.n_launches;
+            }
         }
+        timer_stop(c, T_FINALIZE);
         if ((st = check(c, "criteria")))
         {
             return st;
         }
 
+        timer_start(c, T_MESH_UPDATE);
         DeviceMesh& nm = c.spare();
         if ((st = new_cells_from_tags(c, m, nm.cells)))
         {
@@ -814,6 +861,7 @@ namespace sg
         }
         if (same)
         {
+            timer_stop(c, T_MESH_UPDATE);
             *converged = true;
             return SG_OK;
         }
@@ -822,8 +870,10 @@ namespace sg
         {
             return st;
         }
-        k_update_fields<<<grid_words(g.total_words), BLOCK, 0, c.stream>>>(g, c.cfg.prediction_radius, nm.ref, nm.cells, m.ref, m.cells, m.hc, f.data,
-                                                                           f.spare);
+        timer_stop(c, T_MESH_UPDATE);
+        ScopedTimer tf(c, T_FIELDS_UPDATE);
+        k_update_fields<<<blocks_for_items(nm.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(g, c.cfg.prediction_radius, nm.wl_ref, nm.lo_ref[g.nlev], nm.ref,
+                                                                                      nm.cells, m.ref, m.cells, m.hc, f.data, f.spare);
         ++c.n_launches;
         if ((st = check(c, "update_fields")))
         {
@@ -837,6 +887,7 @@ namespace sg
     // Adapt::operator() (mr/adapt.hpp:147-195)
     int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten)
     {
+        ScopedTimer timer(c, T_ADAPT);
         const int minl = c.cfg.min_level, maxl = c.cfg.max_level;
         int it         = 0;
         if (minl != maxl)
@@ -865,8 +916,12 @@ namespace sg
 
     int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme)
     {
+        ScopedTimer timer(c, T_UPWIND);
         const Geom& g = c.g;
-        k_upwind<<<grid_words(g.total_words), BLOCK, 0, c.stream>>>(g, c.m().cells, u.data, unp1.data, a[0], a[1], g.dim == 3 ? a[2] : 0., dt, scheme);
+        const DeviceMesh& m = c.m();
+        const long long n   = m.lo_cells[g.nlev];
+        k_upwind<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(g, m.wl_cells, n, m.cells, u.data, unp1.data, a[0], a[1], g.dim == 3 ? a[2] : 0., dt,
+                                                                scheme);
         ++c.n_launches;
         return check(c, "upwind");
     }

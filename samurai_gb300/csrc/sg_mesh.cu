@@ -11,6 +11,66 @@ namespace sg
 {
     namespace
     {
+        cudaEvent_t take_event(Ctx& c)
+        {
+            if (!c.timers.pool.empty())
+            {
+                cudaEvent_t e = c.timers.pool.back();
+                c.timers.pool.pop_back();
+                return e;
+            }
+            cudaEvent_t e = nullptr;
+            cudaEventCreate(&e);
+            return e;
+        }
+    } // namespace
+
+    void timer_start(Ctx& c, int id)
+    {
+        if (!c.timers.enabled)
+        {
+            return;
+        }
+        cudaEvent_t e = take_event(c);
+        cudaEventRecord(e, c.stream);
+        c.timers.pending[id] = e;
+    }
+
+    void timer_stop(Ctx& c, int id)
+    {
+        if (!c.timers.enabled || !c.timers.pending[id])
+        {
+            return;
+        }
+        cudaEvent_t e = take_event(c);
+        cudaEventRecord(e, c.stream);
+        c.timers.open[id].push_back({c.timers.pending[id], e});
+        c.timers.pending[id] = nullptr;
+        ++c.timers.calls[id];
+    }
+
+    void timers_flush(Ctx& c)
+    {
+        cudaStreamSynchronize(c.stream);
+        for (int id = 0; id < T_COUNT; ++id)
+        {
+            for (auto& pr : c.timers.open[id])
+            {
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess)
+                {
+                    c.timers.ms[id] += ms;
+                }
+                c.timers.pool.push_back(pr.first);
+                c.timers.pool.push_back(pr.second);
+            }
+            c.timers.open[id].clear();
+        }
+        cudaGetLastError();
+    }
+
+    namespace
+    {
         // ------------------------------------------------------------- words
         template <class F>
         __global__ void k_words(Geom g, int l0, int l1, F f)
@@ -94,91 +154,116 @@ namespace sg
             return r;
         }
 
-        __global__ void k_scan_sums(const uint32_t* bm, long long n, long long* sums)
+        // Four scans in one pass over the words: popcount of the reference
+        // (rank), non-empty reference words, popcount of the cells and
+        // non-empty cell words (the word lists the field kernels iterate).
+        struct Quad
         {
-            const long long base = static_cast<long long>(blockIdx.x) * SCAN_CHUNK + threadIdx.x * SCAN_PER;
-            long long s          = 0;
+            long long v[4];
+        };
+
+        __device__ __forceinline__ Quad thread_quad(const uint32_t* ref, const uint32_t* cells, long long base, long long n)
+        {
+            Quad q{};
             for (int k = 0; k < SCAN_PER; ++k)
             {
                 if (base + k < n)
                 {
-                    s += __popc(bm[base + k]);
+                    const uint32_t r = ref[base + k], c = cells[base + k];
+                    q.v[0] += __popc(r);
+                    q.v[1] += (r != 0u);
+                    q.v[2] += __popc(c);
+                    q.v[3] += (c != 0u);
                 }
             }
-            long long tot;
-            block_exclusive_scan(s, &tot);
-            if (threadIdx.x == 0)
+            return q;
+        }
+
+        __global__ void k_scan_sums(const uint32_t* ref, const uint32_t* cells, long long n, long long nb, long long* sums)
+        {
+            const long long base = static_cast<long long>(blockIdx.x) * SCAN_CHUNK + threadIdx.x * SCAN_PER;
+            const Quad q         = thread_quad(ref, cells, base, n);
+            for (int k = 0; k < 4; ++k)
             {
-                sums[blockIdx.x] = tot;
+                long long tot;
+                block_exclusive_scan(q.v[k], &tot);
+                if (threadIdx.x == 0)
+                {
+                    sums[k * nb + blockIdx.x] = tot;
+                }
             }
         }
 
-        __global__ void k_scan_top(long long* sums, long long nb, long long* total_out)
+        __global__ void k_scan_top(long long* sums, long long nb, long long* counts)
         {
-            // one block: each thread scans a contiguous slice sequentially
             const long long per = (nb + blockDim.x - 1) / blockDim.x;
             const long long b0  = threadIdx.x * per;
-            long long s         = 0;
-            for (long long k = 0; k < per; ++k)
+            for (int k = 0; k < 4; ++k)
             {
-                if (b0 + k < nb)
+                long long* a = sums + k * nb;
+                long long s  = 0;
+                for (long long j = 0; j < per; ++j)
                 {
-                    s += sums[b0 + k];
+                    if (b0 + j < nb)
+                    {
+                        s += a[b0 + j];
+                    }
                 }
-            }
-            long long tot;
-            long long off = block_exclusive_scan(s, &tot);
-            for (long long k = 0; k < per; ++k)
-            {
-                if (b0 + k < nb)
+                long long tot;
+                long long off = block_exclusive_scan(s, &tot);
+                for (long long j = 0; j < per; ++j)
                 {
-                    long long v   = sums[b0 + k];
-                    sums[b0 + k]  = off;
-                    off += v;
+                    if (b0 + j < nb)
+                    {
+                        const long long v = a[b0 + j];
+                        a[b0 + j]         = off;
+                        off += v;
+                    }
                 }
-            }
-            if (threadIdx.x == 0)
-            {
-                *total_out = tot;
+                if (threadIdx.x == 0)
+                {
+                    counts[k] = tot;
+                }
             }
         }
 
-        __global__ void k_scan_write(const uint32_t* bm, long long n, const long long* sums, int* rank)
+        __global__ void k_scan_write(Geom g, const uint32_t* ref, const uint32_t* cells, long long n, long long nb, const long long* sums, int* rank,
+                                     int* wl_ref, int* wl_cells, long long* counts)
         {
             const long long base = static_cast<long long>(blockIdx.x) * SCAN_CHUNK + threadIdx.x * SCAN_PER;
-            long long s          = 0;
+            const Quad q         = thread_quad(ref, cells, base, n);
+            long long off[4];
+            for (int k = 0; k < 4; ++k)
+            {
+                off[k] = block_exclusive_scan(q.v[k], nullptr) + sums[k * nb + blockIdx.x];
+            }
             for (int k = 0; k < SCAN_PER; ++k)
             {
-                if (base + k < n)
+                const long long w = base + k;
+                if (w >= n)
                 {
-                    s += __popc(bm[base + k]);
+                    break;
                 }
-            }
-            long long off = block_exclusive_scan(s, nullptr) + sums[blockIdx.x];
-            for (int k = 0; k < SCAN_PER; ++k)
-            {
-                if (base + k < n)
+                for (int l = 0; l < g.nlev; ++l)
                 {
-                    rank[base + k] = static_cast<int>(off);
-                    off += __popc(bm[base + k]);
+                    if (g.lv[l].woff == w)
+                    {
+                        counts[4 + l]              = off[1];
+                        counts[4 + (MAXLEV + 1) + l] = off[3];
+                    }
                 }
-            }
-        }
-
-        __global__ void k_popcount(const uint32_t* bm, long long n, long long* out)
-        {
-            long long s = 0;
-            for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < n; w += static_cast<long long>(gridDim.x) * blockDim.x)
-            {
-                s += __popc(bm[w]);
-            }
-            for (int o = 16; o > 0; o >>= 1)
-            {
-                s += __shfl_down_sync(0xffffffffu, s, o);
-            }
-            if ((threadIdx.x & 31) == 0 && s)
-            {
-                atomicAdd(reinterpret_cast<unsigned long long*>(out), static_cast<unsigned long long>(s));
+                const uint32_t r = ref[w], c = cells[w];
+                rank[w]          = static_cast<int>(off[0]);
+                off[0] += __popc(r);
+                if (r)
+                {
+                    wl_ref[off[1]++] = static_cast<int>(w);
+                }
+                off[2] += __popc(c);
+                if (c)
+                {
+                    wl_cells[off[3]++] = static_cast<int>(w);
+                }
             }
         }
     } // namespace
@@ -187,24 +272,30 @@ namespace sg
     {
         const long long n  = c.g.total_words;
         const long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
-        k_scan_sums<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, n, c.block_sums);
+        k_scan_sums<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, m.cells, n, nb, c.block_sums);
         k_scan_top<<<1, 1024, 0, c.stream>>>(c.block_sums, nb, c.d_counts);
-        k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, n, c.block_sums, m.rank);
-        cudaMemsetAsync(c.d_counts + 1, 0, sizeof(long long), c.stream);
-        k_popcount<<<grid_for(n), 256, 0, c.stream>>>(m.cells, n, c.d_counts + 1);
-        c.n_launches += 4;
+        k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(c.g, m.ref, m.cells, n, nb, c.block_sums, m.rank, m.wl_ref, m.wl_cells,
+                                                                          c.d_counts);
+        c.n_launches += 3;
         int st = check(c, "scan_rank");
         if (st)
         {
             return st;
         }
-        cudaMemcpyAsync(c.h_counts, c.d_counts, 2 * sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
+        cudaMemcpyAsync(c.h_counts, c.d_counts, COUNTS * sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
         if (cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
             return check(c, "scan_rank sync");
         }
         m.nb_ref   = c.h_counts[0];
-        m.nb_cells = c.h_counts[1];
+        m.nb_cells = c.h_counts[2];
+        for (int l = 0; l < c.g.nlev; ++l)
+        {
+            m.lo_ref[l]   = c.h_counts[4 + l];
+            m.lo_cells[l] = c.h_counts[4 + (MAXLEV + 1) + l];
+        }
+        m.lo_ref[c.g.nlev]   = c.h_counts[1];
+        m.lo_cells[c.g.nlev] = c.h_counts[3];
         if (m.nb_ref >= (1LL << 31))
         {
             c.err = "reference mesh exceeds 2^31 cells";
@@ -218,6 +309,7 @@ namespace sg
     // (mr/mesh.hpp:222-455) and renumbering (mesh.hpp:894-911).
     int build_mesh(Ctx& c, DeviceMesh& m)
     {
+        ScopedTimer timer(c, T_CONSTRUCTION);
         const Geom g       = c.g;
         const int top      = g.nlev - 1;
         const int maxl     = c.cfg.max_level;
@@ -461,6 +553,7 @@ namespace sg
     // max_stencil_radius of 1.
     int graduate(Ctx& c, uint32_t* nc, int* iterations)
     {
+        ScopedTimer timer(c, T_GRADUATION);
         const Geom g   = c.g;
         const int top  = g.nlev - 1;
         const int maxl = c.cfg.max_level;

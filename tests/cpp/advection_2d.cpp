@@ -1,0 +1,102 @@
+// demos/FiniteVolume/advection_2d.cpp of samurai, written against the
+// GB300 drop-in header: the samurai calls are the demo's own (the output and
+// CLI parts are replaced by printing the final cells).  Usage:
+//   advection_2d <pred 0|1> <out.txt>
+#include <cstdio>
+#include <cstdlib>
+
+#include <samurai_gb300/samurai.hpp>
+
+template <class Field>
+void init(Field& u)
+{
+    auto& mesh = u.mesh();
+    u.resize();
+    samurai::for_each_cell(mesh,
+                           [&](auto& cell)
+                           {
+                               auto center           = cell.center();
+                               const double radius   = .2;
+                               const double x_center = 0.3;
+                               const double y_center = 0.3;
+                               if (((center[0] - x_center) * (center[0] - x_center) + (center[1] - y_center) * (center[1] - y_center))
+                                   <= radius * radius)
+                               {
+                                   u[cell] = 1;
+                               }
+                               else
+                               {
+                                   u[cell] = 0;
+                               }
+                           });
+}
+
+template <int pred>
+int run(const char* out_path)
+{
+    constexpr std::size_t dim = 2;
+    std::array<double, dim> a{{1, 1}};
+    double Tf  = .01;
+    double cfl = 0.5;
+    double t   = 0.;
+
+    const samurai::Box<double, dim> box({0., 0.}, {1., 1.});
+    auto config = samurai::mesh_config<dim, pred>().min_level(4).max_level(10).max_stencil_size(2).disable_minimal_ghost_width();
+    auto mesh   = samurai::mra::make_mesh(box, config);
+    auto u      = samurai::make_scalar_field<double>("u", mesh);
+    init(u);
+    samurai::make_bc<samurai::Dirichlet<1>>(u, 0.);
+
+    double dt = cfl * mesh.min_cell_length();
+    auto unp1 = samurai::make_scalar_field<double>("unp1", mesh);
+
+    auto MRadaptation = samurai::make_MRAdapt(u);
+    auto mra_config   = samurai::mra_config().epsilon(2e-4);
+    MRadaptation(mra_config);
+
+    std::size_t nt = 0;
+    while (t != Tf)
+    {
+        MRadaptation(mra_config);
+        t += dt;
+        if (t > Tf)
+        {
+            dt += Tf - t;
+            t = Tf;
+        }
+        samurai::update_ghost_mr(u);
+        unp1.resize();
+        unp1 = u - dt * samurai::upwind(a, u);
+        std::swap(u.array(), unp1.array());
+        ++nt;
+    }
+
+    FILE* f = std::fopen(out_path, "w");
+    if (!f)
+    {
+        return 1;
+    }
+    std::fprintf(f, "%zu\n", nt);
+    samurai::for_each_cell(mesh,
+                           [&](auto& cell) { std::fprintf(f, "%zu %d %d %.17g\n", cell.level, cell.indices[0], cell.indices[1], u[cell]); });
+    std::fclose(f);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 3)
+    {
+        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt>\n");
+        return 2;
+    }
+    try
+    {
+        return std::atoi(argv[1]) == 0 ? run<0>(argv[2]) : run<1>(argv[2]);
+    }
+    catch (const std::exception& e)
+    {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 1;
+    }
+}
