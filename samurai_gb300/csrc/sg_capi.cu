@@ -118,6 +118,12 @@ namespace
         dfree(c.block_sums);
         dfree(c.d_counts);
         dfree(c.d_flags);
+        dfree(c.d_geom);
+        dfree(c.d_eps);
+        if (c.h_eps)
+        {
+            cudaFreeHost(c.h_eps);
+        }
         dfree(h->staging);
         if (c.h_counts)
         {
@@ -134,8 +140,9 @@ namespace
         delete h;
     }
 
-    __global__ void k_box_cells(sg::Geom g, int l, uint32_t* cells)
+    __global__ void k_box_cells(const sg::Geom* __restrict__ gp, int l, uint32_t* cells)
     {
+        const sg::Geom& g      = *gp;
         const sg::LevelGeom& L = g.lv[l];
         for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < L.nwords; w += static_cast<long long>(gridDim.x) * blockDim.x)
         {
@@ -238,9 +245,9 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_mesh_create: dim must be 2 or 3");
         }
-        if (min_level < 1 || max_level < min_level || max_level + 2 > sg::MAXLEV)
+        if (min_level < 1 || max_level < min_level || max_level + 1 > sg::MAXLEV)
         {
-            return fail(SG_ERR_ARG, "sg_mesh_create: need 1 <= min_level <= max_level <= 21");
+            return fail(SG_ERR_ARG, "sg_mesh_create: need 1 <= min_level <= max_level <= 23");
         }
         if (max_stencil_radius < 1 || prediction_radius < 0 || prediction_radius > 1 || graduation_width < 1 || graduation_width > 4)
         {
@@ -292,9 +299,12 @@ extern "C"
         st |= dalloc(c, &c.block_sums, 4 * static_cast<size_t>(c.n_scan_blocks) + 4);
         st |= dalloc(c, &c.d_counts, static_cast<size_t>(sg::COUNTS));
         st |= dalloc(c, &c.d_flags, 8);
+        st |= dalloc(c, &c.d_geom, 1);
+        st |= dalloc(c, &c.d_eps, 3 * sg::MAXLEV);
         if (!st)
         {
-            if (cudaMallocHost(reinterpret_cast<void**>(&c.h_counts), sg::COUNTS * sizeof(long long)) != cudaSuccess
+            if (cudaMallocHost(reinterpret_cast<void**>(&c.h_eps), 3 * sg::MAXLEV * sizeof(double)) != cudaSuccess
+                || cudaMallocHost(reinterpret_cast<void**>(&c.h_counts), sg::COUNTS * sizeof(long long)) != cudaSuccess
                 || cudaMallocHost(reinterpret_cast<void**>(&c.h_flags), 8 * sizeof(int)) != cudaSuccess)
             {
                 st = SG_ERR_CUDA;
@@ -307,13 +317,14 @@ extern "C"
             destroy_ctx(h);
             return fail(SG_ERR_CUDA, "sg_mesh_create: " + msg);
         }
+        cudaMemcpyAsync(c.d_geom, &c.g, sizeof(sg::Geom), cudaMemcpyHostToDevice, c.stream);
         for (int k = 0; k < 2; ++k)
         {
             cudaMemsetAsync(c.mesh[k].cells, 0, nw * 4, c.stream);
         }
         cudaMemsetAsync(c.detail, 0, static_cast<size_t>(c.capacity) * sizeof(double), c.stream);
         cudaMemsetAsync(c.tag, 0, static_cast<size_t>(c.capacity), c.stream);
-        k_box_cells<<<sg::grid_for(c.g.lv[max_level].nwords), 256, 0, c.stream>>>(c.g, max_level, c.m().cells);
+        k_box_cells<<<sg::grid_for(c.g.lv[max_level].nwords), 256, 0, c.stream>>>(c.d_geom, max_level, c.m().cells);
         st = sg::check(c, "initial cells");
         if (!st)
         {

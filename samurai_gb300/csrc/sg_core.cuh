@@ -40,7 +40,7 @@ namespace sg
     struct Geom
     {
         int dim;
-        int nlev; // stored levels: 0..nlev-1 (= max_level + 2)
+        int nlev; // stored levels: 0..nlev-1 (= max_level + 1)
         int min_level;
         int max_level;
         long long total_words;
@@ -53,7 +53,7 @@ namespace sg
         g.dim       = dim;
         g.min_level = min_level;
         g.max_level = max_level;
-        g.nlev      = max_level + 2;
+        g.nlev      = max_level + 1;
         long long off = 0;
         for (int l = 0; l < g.nlev; ++l)
         {

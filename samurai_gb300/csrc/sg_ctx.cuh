@@ -75,7 +75,10 @@ namespace sg
     {
         Timers timers;
         MeshCfg cfg;
-        Geom g{};
+        Geom g{};                // host copy
+        Geom* d_geom = nullptr;  // device copy: kernels read the geometry through this pointer
+        double* d_eps = nullptr; // per-level thresholds of the criteria (3 x MAXLEV)
+        double* h_eps = nullptr; // pinned staging of d_eps
         cudaStream_t stream = nullptr;
         DeviceMesh mesh[2];
         int cur = 0;

@@ -152,10 +152,10 @@ namespace sg
         }
 
         // ----------------------------------------------------------- tags
-        __global__ void k_tag_init(Geom g, const int* wl, long long n, const uint32_t* ref, const uint32_t* cells, uint8_t* tag, double* det)
+        __global__ void k_tag_init(const Geom* __restrict__ gp, const int* wl, long long n, const uint32_t* ref, const uint32_t* cells, uint8_t* tag, double* det)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; },
-                      [=](long long w, int b)
+            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+                      [&](long long w, int b)
                       {
                           const long long e = 32 * w + b;
                           tag[e]            = static_cast<uint8_t>((cells[w] >> b) & 1u);
@@ -164,34 +164,29 @@ namespace sg
         }
 
         // ----------------------------------------------------- outer ghosts
-        struct Dirs
+        // k-th diagonal direction in for_each_diagonal_direction order
+        // (stencil.hpp:338-349): first coordinate fastest, at least two
+        // non-zero components
+        __device__ __forceinline__ void diagonal_dir(int dim, int k, int* d)
         {
-            int n;
-            int d[26][3];
-        };
-
-        // for_each_diagonal_direction order (stencil.hpp:338-349)
-        Dirs diagonal_dirs(int dim)
-        {
-            Dirs out{};
-            for (int z = (dim == 3 ? -1 : 0); z <= (dim == 3 ? 1 : 0); ++z)
+            int found = 0;
+            const int nz = (dim == 3) ? 3 : 1;
+            for (int t = 0; t < 9 * nz; ++t)
             {
-                for (int y = -1; y <= 1; ++y)
+                const int x = t % 3 - 1, y = (t / 3) % 3 - 1, z = (dim == 3) ? t / 9 - 1 : 0;
+                if ((x != 0) + (y != 0) + (z != 0) > 1)
                 {
-                    for (int x = -1; x <= 1; ++x)
+                    if (found == k)
                     {
-                        const int nnz = (x != 0) + (y != 0) + (z != 0);
-                        if (nnz > 1)
-                        {
-                            out.d[out.n][0] = x;
-                            out.d[out.n][1] = y;
-                            out.d[out.n][2] = z;
-                            ++out.n;
-                        }
+                        d[0] = x;
+                        d[1] = y;
+                        d[2] = z;
+                        return;
                     }
+                    ++found;
                 }
             }
-            return out;
+            d[0] = d[1] = d[2] = 0;
         }
 
         // update_outer_corners_by_polynomial_extrapolation for a ghost width
@@ -261,26 +256,29 @@ namespace sg
             const int axis = k >> 1;
             const int sgn  = (k & 1) ? -1 : 1;
             const int n    = g.lv[l].n;
-            int free_[2]   = {static_cast<int>(t % n), static_cast<int>(t / n)};
-            int f          = 0;
-            for (int a = 0; a < 3; ++a)
+            const int f0 = static_cast<int>(t % n), f1 = static_cast<int>(t / n);
+            // the free coordinates fill the non-normal axes in order
+            dir[0] = dir[1] = dir[2] = 0;
+            in[2]                    = 0;
+            if (axis == 0)
             {
-                dir[a] = 0;
-                if (a >= g.dim)
-                {
-                    in[a] = 0;
-                    continue;
-                }
-                if (a == axis)
-                {
-                    in[a]  = sgn > 0 ? n - 1 : 0;
-                    dir[a] = sgn;
-                }
-                else
-                {
-                    in[a] = free_[f++];
-                }
+                in[0] = sgn > 0 ? n - 1 : 0;
+                in[1] = f0;
+                in[2] = (g.dim == 3) ? f1 : 0;
             }
+            else if (axis == 1)
+            {
+                in[0] = f0;
+                in[1] = sgn > 0 ? n - 1 : 0;
+                in[2] = (g.dim == 3) ? f1 : 0;
+            }
+            else
+            {
+                in[0] = f0;
+                in[1] = f1;
+                in[2] = sgn > 0 ? n - 1 : 0;
+            }
+            dir[axis] = sgn;
         }
 
         struct GhostLevelArgs
@@ -308,13 +306,17 @@ namespace sg
         //    (update_outer_ghost.hpp:20-155) next to union cells;
         //  - projection of the reference cells of level l onto proj_cells[l-1]
         //    (numeric/projection.hpp:15-65).
-        __global__ void k_ghost_level(Geom g, Dirs dirs, GhostLevelArgs a, const int* wl_ref, const uint32_t* cells, const uint32_t* uni,
+        template <int DIM>
+        __global__ void k_ghost_level(const Geom* __restrict__ gp, GhostLevelArgs a, const int* wl_ref, const uint32_t* cells, const uint32_t* uni,
                                       const uint32_t* proj, const uint32_t* ref, double* u)
         {
+            const Geom& g = *gp;
             const int l = a.l;
             if (static_cast<int>(blockIdx.x) < a.nb_corner)
             {
-                corner_role(g, dirs.d[blockIdx.x], l, cells, ref, u);
+                int d[3];
+                diagonal_dir(DIM, static_cast<int>(blockIdx.x), d);
+                corner_role(g, d, l, cells, ref, u);
                 return;
             }
             if (static_cast<int>(blockIdx.x) < a.nb_corner + a.nb_face)
@@ -325,7 +327,7 @@ namespace sg
                     return;
                 }
                 const int n        = g.lv[l].n;
-                const long long nf = (g.dim == 2) ? n : static_cast<long long>(n) * n;
+                const long long nf = (DIM == 2) ? n : static_cast<long long>(n) * n;
                 const int k        = static_cast<int>(t / nf);
                 int in[3], dir[3];
                 face_cell(g, l, k, t - k * nf, in, dir);
@@ -341,13 +343,13 @@ namespace sg
                     if (a.do_predict)
                     {
                         const double v = u[eg];
-                        for (int sz = 0; sz < (g.dim == 3 ? 2 : 1); ++sz)
+                        for (int sz = 0; sz < (DIM == 3 ? 2 : 1); ++sz)
                         {
                             for (int sy = 0; sy < 2; ++sy)
                             {
                                 for (int sx = 0; sx < 2; ++sx)
                                 {
-                                    const Pos pf = pos_of(g, l + 1, 2 * gx + sx, 2 * gy + sy, g.dim == 3 ? 2 * gz + sz : 0);
+                                    const Pos pf = pos_of(g, l + 1, 2 * gx + sx, 2 * gy + sy, DIM == 3 ? 2 * gz + sz : 0);
                                     if (test(ref, pf))
                                     {
                                         u[elem(pf)] = v;
@@ -366,17 +368,17 @@ namespace sg
                     }
                     double sum = 0.;
                     int nch    = 0;
-                    for (int dl = 1; dl <= 2 && nch == 0; ++dl)
+                    for (int dl = 1; dl <= 2 && nch == 0 && l + dl < g.nlev; ++dl)
                     {
                         const int lc = l + dl;
                         const int m  = 1 << dl;
-                        for (int sz = 0; sz < (g.dim == 3 ? m : 1); ++sz)
+                        for (int sz = 0; sz < (DIM == 3 ? m : 1); ++sz)
                         {
                             for (int sy = 0; sy < m; ++sy)
                             {
                                 for (int sx = 0; sx < m; ++sx)
                                 {
-                                    const Pos pc = pos_of(g, lc, gx * m + sx, gy * m + sy, g.dim == 3 ? gz * m + sz : 0);
+                                    const Pos pc = pos_of(g, lc, gx * m + sx, gy * m + sy, DIM == 3 ? gz * m + sz : 0);
                                     if (test(ref, pc))
                                     {
                                         sum = sum + u[elem(pc)];
@@ -396,12 +398,12 @@ namespace sg
             const long long warp0     = (rb * blockDim.x + threadIdx.x) >> 5;
             const long long nwarps    = (static_cast<long long>(gridDim.x - a.nb_corner - a.nb_face) * blockDim.x) >> 5;
             warp_list(wl_ref, a.p_begin, a.p_end, warp0, nwarps,
-                      [=](long long w)
+                      [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, lc, w);
                           return proj[w] & coarsen_word(g, ref, lc, loc.row, loc.wi);
                       },
-                      [=](long long w, int b)
+                      [&](long long w, int b)
                       {
                           const Cell c  = cell_of(g, lc, w, b);
                           u[32 * w + b] = project_one(g, u, l, c.x, c.y, c.z);
@@ -410,16 +412,18 @@ namespace sg
 
         // prediction of the ghosts of level l from level l-1
         // (algorithm/update_ghost_mr.hpp:224-233)
-        __global__ void k_predict(Geom g, int l, int order, const int* wl_ref, long long begin, long long end, const uint32_t* cells, const uint32_t* proj,
+        template <int DIM>
+        __global__ void k_predict(const Geom* __restrict__ gp, int l, int order, const int* wl_ref, long long begin, long long end, const uint32_t* cells, const uint32_t* proj,
                                   const uint32_t* ref, double* u)
         {
+            const Geom& g = *gp;
             warp_list(wl_ref, begin, end, warp_id(), warp_count(),
-                      [=](long long w)
+                      [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, l, w);
                           return ref[w] & ~(cells[w] | proj[w]) & box_mask(g, l, loc.row, loc.wi, 0, 0) & refine_word(g, ref, l, loc.row, loc.wi);
                       },
-                      [=](long long w, int b)
+                      [&](long long w, int b)
                       {
                           const Cell c  = cell_of(g, l, w, b);
                           u[32 * w + b] = predict_one(g, u, l, c.x, c.y, c.z, order);
@@ -429,47 +433,48 @@ namespace sg
         // -------------------------------------------------------- details
         // compute_detail_op (mr/operators.hpp:139-540) on
         // intersection(all_cells[l], union(cells[l+1], cells[l+2])).on(l)
-        __global__ void k_detail(Geom g, int order, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
+        template <int DIM>
+        __global__ void k_detail(const Geom* __restrict__ gp, int order, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
                                  const uint32_t* hc2, const double* u, double* det)
         {
-            warp_list(wl, begin, end, warp_id(), warp_count(), [=](long long w) { return ref[w] & (hc[w] | hc2[w]); },
-                      [=](long long w, int b)
+            const Geom& g = *gp;
+            warp_list(wl, begin, end, warp_id(), warp_count(), [&](long long w) { return ref[w] & (hc[w] | hc2[w]); },
+                      [&](long long w, int b)
                       {
                           const int l    = level_of(g, w);
                           const Cell c   = cell_of(g, l, w, b);
-                          const int nch  = 1 << g.dim;
                           long long ce[8];
-                          for (int ch = 0; ch < nch; ++ch)
+                          for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
-                              ce[ch] = elem_at(g, l + 1, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), g.dim == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
+                              ce[ch] = elem_at(g, l + 1, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), DIM == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
                           }
                           if (order == 0)
                           {
                               const double uc = u[32 * w + b];
-                              for (int ch = 0; ch < nch; ++ch)
+                              for (int ch = 0; ch < (1 << DIM); ++ch)
                               {
                                   det[ce[ch]] = u[ce[ch]] - uc;
                               }
                               return;
                           }
                           double d[8];
-                          for (int ch = 0; ch < nch; ++ch)
+                          for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
                               d[ch] = u[ce[ch]];
                           }
-                          const int nz = (g.dim == 3) ? 3 : 1;
+                          const int nz = (DIM == 3) ? 3 : 1;
                           for (int sz = 0; sz < nz; ++sz)
                           {
                               for (int sy = 0; sy < 3; ++sy)
                               {
-                                  const long long base = elem_at(g, l, c.x - 1, c.y + sy - 1, g.dim == 3 ? c.z + sz - 1 : 0);
+                                  const long long base = elem_at(g, l, c.x - 1, c.y + sy - 1, DIM == 3 ? c.z + sz - 1 : 0);
                                   for (int sx = 0; sx < 3; ++sx)
                                   {
                                       const double src = u[base + sx];
-                                      for (int ch = 0; ch < nch; ++ch)
+                                      for (int ch = 0; ch < (1 << DIM); ++ch)
                                       {
                                           double cf = interp1(ch & 1, sx) * interp1((ch >> 1) & 1, sy);
-                                          if (g.dim == 3)
+                                          if (DIM == 3)
                                           {
                                               cf = cf * interp1((ch >> 2) & 1, sz);
                                           }
@@ -478,46 +483,40 @@ namespace sg
                                   }
                               }
                           }
-                          for (int ch = 0; ch < nch; ++ch)
+                          for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
                               det[ce[ch]] = d[ch];
                           }
                       });
         }
 
-        struct Eps
-        {
-            double eps[MAXLEV];    // eps_l, indexed by the fine level
-            double fine[MAXLEV];   // 2^(reg+dim) * eps_l
-            double coarse[MAXLEV]; // fine / 2^dim
-        };
-
         // mr_criteria_op (mr/criteria.hpp:20-113) on
         // intersection(cells[l], all_cells[l-1]).on(l-1), fine levels l0..l1
-        __global__ void k_criteria(Geom g, Eps eps, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
+        template <int DIM>
+        __global__ void k_criteria(const Geom* __restrict__ gp, const double* __restrict__ eps, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
                                    const double* det, uint8_t* tag)
         {
-            warp_list(wl, begin, end, warp_id(), warp_count(), [=](long long w) { return ref[w] & hc[w]; },
-                      [=](long long w, int b)
+            const Geom& g = *gp;
+            warp_list(wl, begin, end, warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
+                      [&](long long w, int b)
                       {
                           const int lc  = level_of(g, w);
                           const int lf  = lc + 1;
                           const Cell c  = cell_of(g, lc, w, b);
-                          const int nch = 1 << g.dim;
                           long long fo[8];
-                          for (int ch = 0; ch < nch; ++ch)
+                          for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
-                              fo[ch] = elem_at(g, lf, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), g.dim == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
+                              fo[ch] = elem_at(g, lf, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), DIM == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
                           }
                           if (lf > g.min_level)
                           {
-                              const bool cond = fabs(det[32 * w + b]) > eps.coarse[lf];
+                              const bool cond = fabs(det[32 * w + b]) > eps[2 * MAXLEV + lf];
                               if (!cond)
                               {
                                   bool ok = true;
-                                  for (int ch = 0; ch < nch; ++ch)
+                                  for (int ch = 0; ch < (1 << DIM); ++ch)
                                   {
-                                      if (fabs(det[fo[ch]]) > eps.eps[lf])
+                                      if (fabs(det[fo[ch]]) > eps[lf])
                                       {
                                           ok = false;
                                           break;
@@ -525,7 +524,7 @@ namespace sg
                                   }
                                   if (ok)
                                   {
-                                      for (int ch = 0; ch < nch; ++ch)
+                                      for (int ch = 0; ch < (1 << DIM); ++ch)
                                       {
                                           tag[fo[ch]] = 2;
                                       }
@@ -534,9 +533,9 @@ namespace sg
                           }
                           if (lf < g.max_level)
                           {
-                              for (int ch = 0; ch < nch; ++ch)
+                              for (int ch = 0; ch < (1 << DIM); ++ch)
                               {
-                                  if (fabs(det[fo[ch]]) > eps.fine[lf])
+                                  if (fabs(det[fo[ch]]) > eps[MAXLEV + lf])
                                   {
                                       tag[fo[ch]] |= 4;
                                   }
@@ -546,19 +545,20 @@ namespace sg
         }
 
         // maximum_op (mr/operators.hpp:22-96), children at level l
-        __global__ void k_maximum(Geom g, int l, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc, uint8_t* tag)
+        template <int DIM>
+        __global__ void k_maximum(const Geom* __restrict__ gp, int l, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc, uint8_t* tag)
         {
+            const Geom& g = *gp;
             const int lc = l - 1;
-            warp_list(wl, begin, end, warp_id(), warp_count(), [=](long long w) { return ref[w] & hc[w]; },
-                      [=](long long w, int b)
+            warp_list(wl, begin, end, warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
+                      [&](long long w, int b)
                       {
                           const Cell c  = cell_of(g, lc, w, b);
-                          const int nch = 1 << g.dim;
                           long long fo[8];
                           uint8_t keep = 0, coarsen = 2;
-                          for (int ch = 0; ch < nch; ++ch)
+                          for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
-                              fo[ch] = elem_at(g, l, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), g.dim == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
+                              fo[ch] = elem_at(g, l, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), DIM == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
                               const uint8_t t = tag[fo[ch]];
                               keep |= t & 1;
                               coarsen &= t & 2;
@@ -566,7 +566,7 @@ namespace sg
                           const long long co = 32 * w + b;
                           if (keep)
                           {
-                              for (int ch = 0; ch < nch; ++ch)
+                              for (int ch = 0; ch < (1 << DIM); ++ch)
                               {
                                   tag[fo[ch]] |= 1;
                               }
@@ -578,7 +578,7 @@ namespace sg
                           }
                           else
                           {
-                              for (int ch = 0; ch < nch; ++ch)
+                              for (int ch = 0; ch < (1 << DIM); ++ch)
                               {
                                   tag[fo[ch]] &= static_cast<uint8_t>(~2);
                               }
@@ -589,11 +589,13 @@ namespace sg
         // update_fields (algorithm/update_fields.hpp:27-127): copy on
         // reference ∩ new cells, projection on coarsened cells, prediction on
         // refined cells; every other reference entry of the new field is 0.
-        __global__ void k_update_fields(Geom g, int order, const int* wl, long long n, const uint32_t* nref, const uint32_t* ncells, const uint32_t* oref,
+        template <int DIM>
+        __global__ void k_update_fields(const Geom* __restrict__ gp, int order, const int* wl, long long n, const uint32_t* nref, const uint32_t* ncells, const uint32_t* oref,
                                         const uint32_t* ocells, const uint32_t* ohc, const double* uo, double* un)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return nref[w]; },
-                      [=](long long w, int b)
+            const Geom& g = *gp;
+            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return nref[w]; },
+                      [&](long long w, int b)
                       {
                           const long long e = 32 * w + b;
                           double v          = 0.;
@@ -623,11 +625,13 @@ namespace sg
         // demos/FiniteVolume/advection_2d.cpp:144) or the README lambda
         // (README.md:144-153).  Neighbours at the same level are reference
         // cells, at fixed offsets in the dense slabs.
-        __global__ void k_upwind(Geom g, const int* wl, long long n, const uint32_t* cells, const double* u, double* unp1, double a0, double a1, double a2,
+        template <int DIM>
+        __global__ void k_upwind(const Geom* __restrict__ gp, const int* wl, long long n, const uint32_t* cells, const double* u, double* unp1, double a0, double a1, double a2,
                                  double dt, int scheme)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return cells[w]; },
-                      [=](long long w, int b)
+            const Geom& g = *gp;
+            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return cells[w]; },
+                      [&](long long w, int b)
                       {
                           const int l          = level_of(g, w);
                           const LevelGeom& L   = g.lv[l];
@@ -642,7 +646,7 @@ namespace sg
                               double s = uc - u[e - 1];
                               s        = s + uc;
                               s        = s - u[e - sy];
-                              if (g.dim == 3)
+                              if (DIM == 3)
                               {
                                   s = s + uc;
                                   s = s - u[e - sz];
@@ -661,7 +665,7 @@ namespace sg
                               double s        = -lf + rf;
                               s               = s + -df;
                               s               = s + uf;
-                              if (g.dim == 3)
+                              if (DIM == 3)
                               {
                                   const double ha2 = .5 * a2, hb2 = .5 * fabs(a2);
                                   const double uf2 = u[e - sz], ub2 = u[e + sz];
@@ -680,19 +684,19 @@ namespace sg
         // --------------------------------------------------- layout moves
         __global__ void k_gather(const int* wl, long long n, const uint32_t* ref, const int* rank, const double* dense, double* compact)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; },
-                      [=](long long w, int b) { compact[ref_index(ref, rank, Pos{w, b})] = dense[32 * w + b]; });
+            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+                      [&](long long w, int b) { compact[ref_index(ref, rank, Pos{w, b})] = dense[32 * w + b]; });
         }
 
         __global__ void k_scatter(const int* wl, long long n, const uint32_t* ref, const int* rank, const double* compact, double* dense)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; },
-                      [=](long long w, int b) { dense[32 * w + b] = compact[ref_index(ref, rank, Pos{w, b})]; });
+            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+                      [&](long long w, int b) { dense[32 * w + b] = compact[ref_index(ref, rank, Pos{w, b})]; });
         }
 
         __global__ void k_fill(const int* wl, long long n, const uint32_t* ref, double* dense, double v)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [=](long long w) { return ref[w]; }, [=](long long w, int b) { dense[32 * w + b] = v; });
+            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; }, [&](long long w, int b) { dense[32 * w + b] = v; });
         }
     } // namespace
 
@@ -730,9 +734,7 @@ namespace sg
         const int maxl  = c.cfg.max_level;
         const int lmin  = minl >= 2 ? minl - 2 : 0; // no reference cell below min_level-2
         double* u       = f.data;
-        static const Dirs diag2 = diagonal_dirs(2);
-        static const Dirs diag3 = diagonal_dirs(3);
-        const Dirs& diag        = (g.dim == 2) ? diag2 : diag3;
+        const int ndiag = (g.dim == 2) ? 4 : 20;
         if (c.cfg.ghost_width != 1)
         {
             c.err = "update_ghost_mr: only a ghost width of 1 is implemented";
@@ -747,7 +749,7 @@ namespace sg
             a.do_dirichlet = (l >= minl) && f.has_bc;
             a.do_predict   = (l >= minl && l < maxl);
             a.value        = f.bc_value;
-            a.nb_corner    = a.do_corners ? diag.n : 0;
+            a.nb_corner    = a.do_corners ? ndiag : 0;
             const int n    = g.lv[l].n;
             a.nfaces       = (a.do_project || a.do_dirichlet || a.do_predict)
                                  ? static_cast<long long>(2 * g.dim) * ((g.dim == 2) ? n : static_cast<long long>(n) * n)
@@ -763,7 +765,14 @@ namespace sg
             const int grid        = a.nb_corner + a.nb_face + nb_proj;
             if (grid > 0)
             {
-                k_ghost_level<<<grid, BLOCK, 0, c.stream>>>(g, diag, a, m.wl_ref, m.cells, m.uni, m.proj, m.ref, u);
+                if (g.dim == 2)
+                {
+                    k_ghost_level<2><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.cells, m.uni, m.proj, m.ref, u);
+                }
+                else
+                {
+                    k_ghost_level<3><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.cells, m.uni, m.proj, m.ref, u);
+                }
                 ++c.n_launches;
             }
         }
@@ -772,7 +781,14 @@ namespace sg
             const long long b = m.lo_ref[l], e = m.lo_ref[l + 1];
             if (e > b)
             {
-                k_predict<<<blocks_for_items(e - b), BLOCK, 0, c.stream>>>(g, l, c.cfg.prediction_radius, m.wl_ref, b, e, m.cells, m.proj, m.ref, u);
+                if (g.dim == 2)
+                {
+                    k_predict<2><<<blocks_for_items(e - b), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, b, e, m.cells, m.proj, m.ref, u);
+                }
+                else
+                {
+                    k_predict<3><<<blocks_for_items(e - b), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, b, e, m.cells, m.proj, m.ref, u);
+                }
                 ++c.n_launches;
             }
         }
@@ -789,7 +805,7 @@ namespace sg
         const int dim  = g.dim;
         int st;
 
-        k_tag_init<<<blocks_for_items(m.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(g, m.wl_ref, m.lo_ref[g.nlev], m.ref, m.cells, c.tag, c.detail);
+        k_tag_init<<<blocks_for_items(m.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.lo_ref[g.nlev], m.ref, m.cells, c.tag, c.detail);
         ++c.n_launches;
         if ((st = check(c, "tag_init")))
         {
@@ -806,25 +822,42 @@ namespace sg
         if (dl1 >= dl0 && m.lo_ref[dl1 + 1] > m.lo_ref[dl0])
         {
             const long long b = m.lo_ref[dl0], e_ = m.lo_ref[dl1 + 1];
-            k_detail<<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(g, c.cfg.prediction_radius, m.wl_ref, b, e_, m.ref, m.hc, m.hc2, f.data,
+            if (g.dim == 2)
+            {
+                k_detail<2><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, b, e_, m.ref, m.hc, m.hc2, f.data,
                                                                         c.detail);
+            }
+            else
+            {
+                k_detail<3><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, b, e_, m.ref, m.hc, m.hc2, f.data,
+                                                                        c.detail);
+            }
             ++c.n_launches;
         }
         timer_stop(c, T_DETAIL);
         timer_start(c, T_TAG);
-        Eps e{};
+        double* e = c.h_eps;
+        cudaStreamSynchronize(c.stream); // h_eps may still feed an earlier copy
         for (int l = minl; l <= maxl - ite; ++l)
         {
-            const int exponent = dim * (maxl - l);
-            e.eps[l]           = eps / (1 << exponent);
-            e.fine[l]          = std::pow(2.0, regularity + dim) * e.eps[l];
-            e.coarse[l]        = e.fine[l] / (1 << dim);
+            const int exponent      = dim * (maxl - l);
+            e[l]                    = eps / (1 << exponent);
+            e[MAXLEV + l]           = std::pow(2.0, regularity + dim) * e[l];
+            e[2 * MAXLEV + l]       = e[MAXLEV + l] / (1 << dim);
         }
+        cudaMemcpyAsync(c.d_eps, e, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
         const int cl0 = minl, cl1 = maxl - ite;
         if (cl1 >= cl0 && cl0 >= 1 && m.lo_ref[cl1] > m.lo_ref[cl0 - 1])
         {
             const long long b = m.lo_ref[cl0 - 1], e_ = m.lo_ref[cl1];
-            k_criteria<<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(g, e, m.wl_ref, b, e_, m.ref, m.hc, c.detail, c.tag);
+            if (g.dim == 2)
+            {
+                k_criteria<2><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, b, e_, m.ref, m.hc, c.detail, c.tag);
+            }
+            else
+            {
+                k_criteria<3><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, b, e_, m.ref, m.hc, c.detail, c.tag);
+            }
             ++c.n_launches;
         }
         timer_stop(c, T_TAG);
@@ -834,7 +867,14 @@ namespace sg
             const long long b = m.lo_ref[l - 1], e_ = m.lo_ref[l];
             if (e_ > b)
             {
-                k_maximum<<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(g, l, m.wl_ref, b, e_, m.ref, m.hc, c.tag);
+                if (g.dim == 2)
+                {
+                    k_maximum<2><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, b, e_, m.ref, m.hc, c.tag);
+                }
+                else
+                {
+                    k_maximum<3><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, b, e_, m.ref, m.hc, c.tag);
+                }
                 ++c.n_launches;
             }
         }
@@ -872,8 +912,16 @@ namespace sg
         }
         timer_stop(c, T_MESH_UPDATE);
         ScopedTimer tf(c, T_FIELDS_UPDATE);
-        k_update_fields<<<blocks_for_items(nm.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(g, c.cfg.prediction_radius, nm.wl_ref, nm.lo_ref[g.nlev], nm.ref,
+        if (g.dim == 2)
+        {
+            k_update_fields<2><<<blocks_for_items(nm.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.lo_ref[g.nlev], nm.ref,
                                                                                       nm.cells, m.ref, m.cells, m.hc, f.data, f.spare);
+        }
+        else
+        {
+            k_update_fields<3><<<blocks_for_items(nm.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.lo_ref[g.nlev], nm.ref,
+                                                                                      nm.cells, m.ref, m.cells, m.hc, f.data, f.spare);
+        }
         ++c.n_launches;
         if ((st = check(c, "update_fields")))
         {
@@ -920,8 +968,16 @@ namespace sg
         const Geom& g = c.g;
         const DeviceMesh& m = c.m();
         const long long n   = m.lo_cells[g.nlev];
-        k_upwind<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(g, m.wl_cells, n, m.cells, u.data, unp1.data, a[0], a[1], g.dim == 3 ? a[2] : 0., dt,
+        if (g.dim == 2)
+        {
+            k_upwind<2><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, a[0], a[1], g.dim == 3 ? a[2] : 0., dt,
                                                                 scheme);
+        }
+        else
+        {
+            k_upwind<3><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, a[0], a[1], g.dim == 3 ? a[2] : 0., dt,
+                                                                scheme);
+        }
         ++c.n_launches;
         return check(c, "upwind");
     }

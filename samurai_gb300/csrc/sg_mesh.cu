@@ -73,8 +73,9 @@ namespace sg
     {
         // ------------------------------------------------------------- words
         template <class F>
-        __global__ void k_words(Geom g, int l0, int l1, F f)
+        __global__ void k_words(const Geom* __restrict__ gp, int l0, int l1, F f)
         {
+            const Geom& g         = *gp;
             const long long begin = g.lv[l0].woff;
             const long long end   = g.lv[l1].woff + g.lv[l1].nwords;
             for (long long w = begin + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < end;
@@ -86,7 +87,7 @@ namespace sg
                     ++l;
                 }
                 const WordLoc loc = word_loc(g, l, w);
-                f(l, w, loc.row, loc.wi);
+                f(g, l, w, loc.row, loc.wi);
             }
         }
 
@@ -98,7 +99,7 @@ namespace sg
                 return SG_OK;
             }
             const long long n = c.g.lv[l1].woff + c.g.lv[l1].nwords - c.g.lv[l0].woff;
-            k_words<<<grid_for(n), 256, 0, c.stream>>>(c.g, l0, l1, f);
+            k_words<<<grid_for(n), 256, 0, c.stream>>>(c.d_geom, l0, l1, f);
             ++c.n_launches;
             return check(c, what);
         }
@@ -227,9 +228,10 @@ namespace sg
             }
         }
 
-        __global__ void k_scan_write(Geom g, const uint32_t* ref, const uint32_t* cells, long long n, long long nb, const long long* sums, int* rank,
+        __global__ void k_scan_write(const Geom* __restrict__ gp, const uint32_t* ref, const uint32_t* cells, long long n, long long nb, const long long* sums, int* rank,
                                      int* wl_ref, int* wl_cells, long long* counts)
         {
+            const Geom& g = *gp;
             const long long base = static_cast<long long>(blockIdx.x) * SCAN_CHUNK + threadIdx.x * SCAN_PER;
             const Quad q         = thread_quad(ref, cells, base, n);
             long long off[4];
@@ -274,7 +276,7 @@ namespace sg
         const long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
         k_scan_sums<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, m.cells, n, nb, c.block_sums);
         k_scan_top<<<1, 1024, 0, c.stream>>>(c.block_sums, nb, c.d_counts);
-        k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(c.g, m.ref, m.cells, n, nb, c.block_sums, m.rank, m.wl_ref, m.wl_cells,
+        k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(c.d_geom, m.ref, m.cells, n, nb, c.block_sums, m.rank, m.wl_ref, m.wl_cells,
                                                                           c.d_counts);
         c.n_launches += 3;
         int st = check(c, "scan_rank");
@@ -329,7 +331,7 @@ namespace sg
 
         // cells with a leaf child / grandchild
         st = launch_words(c, 0, top,
-                          [=] __device__(int l, long long w, long long row, int wi)
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                           { hc[w] = (l + 1 < g.nlev) ? coarsen_word(g, cells, l, row, wi) : 0u; },
                           "hc");
         if (st)
@@ -337,7 +339,7 @@ namespace sg
             return st;
         }
         st = launch_words(c, 0, top,
-                          [=] __device__(int l, long long w, long long row, int wi)
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                           { hc2[w] = (l + 1 < g.nlev) ? coarsen_word(g, hc, l, row, wi) : 0u; },
                           "hc2");
         if (st)
@@ -350,7 +352,7 @@ namespace sg
         for (int l = maxl - 1; l >= 0; --l)
         {
             st = launch_words(c, l, l,
-                              [=] __device__(int ll, long long w, long long row, int wi)
+                              [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
                               { uni[w] = hc[w] | coarsen_word(g, uni, ll, row, wi); },
                               "union");
             if (st)
@@ -361,7 +363,7 @@ namespace sg
 
         // cells_and_ghosts: box expansion of the cells by max_stencil_radius
         st = launch_words(c, 0, top,
-                          [=] __device__(int l, long long w, long long row, int wi) { cag[w] = box_dilate_word(g, cells, l, row, wi, r); },
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = box_dilate_word(g, cells, l, row, wi, r); },
                           "cag");
         if (st)
         {
@@ -378,7 +380,7 @@ namespace sg
         // prediction ghosts: cag[l+1].on(l) expanded by p within the expanded
         // domain, and cells[l+2].on(l) expanded by p
         st = launch_words(c, 0, top,
-                          [=] __device__(int l, long long w, long long row, int wi)
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                           { t1[w] = (l + 1 < g.nlev) ? coarsen_word(g, cag, l, row, wi) : 0u; },
                           "cag_on");
         if (st)
@@ -386,7 +388,7 @@ namespace sg
             return st;
         }
         st = launch_words(c, 0, top,
-                          [=] __device__(int l, long long w, long long row, int wi)
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                           {
                               uint32_t v = cag[w];
                               v |= box_dilate_word(g, t1, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
@@ -404,7 +406,7 @@ namespace sg
         for (int l = 0; l + 1 <= maxl; ++l)
         {
             st = launch_words(c, l + 1, l + 1,
-                              [=] __device__(int lf, long long w, long long row, int k)
+                              [=] __device__(const Geom& g, int lf, long long w, long long row, int k)
                               {
                                   const LevelGeom& F = g.lv[lf];
                                   const LevelGeom& C = g.lv[lf - 1];
@@ -439,7 +441,7 @@ namespace sg
                 return st;
             }
         }
-        st = launch_words(c, 0, top, [=] __device__(int, long long w, long long, int) { proj[w] = ref[w] & uni[w]; }, "proj");
+        st = launch_words(c, 0, top, [=] __device__(const Geom&, int, long long w, long long, int) { proj[w] = ref[w] & uni[w]; }, "proj");
         if (st)
         {
             return st;
@@ -454,8 +456,9 @@ namespace sg
     {
         // refine / coarsen_even flags of leaf cells from the tags
         // (update_cell_array_from_tag, algorithm/graduation.hpp:743-842)
-        __global__ void k_tag_flags(Geom g, const uint32_t* cells, const uint8_t* tag, uint32_t* rf, uint32_t* cf, int minl, int maxl)
+        __global__ void k_tag_flags(const Geom* __restrict__ gp, const uint32_t* cells, const uint8_t* tag, uint32_t* rf, uint32_t* cf, int minl, int maxl)
         {
+            const Geom& g = *gp;
             for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < g.total_words;
                  w += static_cast<long long>(gridDim.x) * blockDim.x)
             {
@@ -492,7 +495,7 @@ namespace sg
     int new_cells_from_tags(Ctx& c, const DeviceMesh& m, uint32_t* nc)
     {
         const Geom g = c.g;
-        k_tag_flags<<<grid_for(g.total_words), 256, 0, c.stream>>>(g, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
+        k_tag_flags<<<grid_for(g.total_words), 256, 0, c.stream>>>(c.d_geom, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
         ++c.n_launches;
         int st = check(c, "tag_flags");
         if (st)
@@ -504,7 +507,7 @@ namespace sg
         const uint32_t* cf    = c.cf;
         const int minl = c.cfg.min_level, maxl = c.cfg.max_level;
         return launch_words(c, 0, g.nlev - 1,
-                            [=] __device__(int l, long long w, long long row, int wi)
+                            [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                             {
                                 uint32_t v = 0;
                                 if (l >= minl && l <= maxl)
@@ -569,14 +572,14 @@ namespace sg
         {
             ++nit;
             int st = launch_words(c, 0, top,
-                                  [=] __device__(int l, long long w, long long row, int wi) { e[w] = box_dilate_word(g, nc, l, row, wi, gw2); },
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = box_dilate_word(g, nc, l, row, wi, gw2); },
                                   "grad_expand");
             if (st)
             {
                 return st;
             }
             st = launch_words(c, 0, top,
-                              [=] __device__(int l, long long w, long long row, int wi)
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                               { ec1[w] = (l + 1 < g.nlev) ? coarsen_word(g, e, l, row, wi) : 0u; },
                               "grad_coarsen");
             if (st)
@@ -590,7 +593,7 @@ namespace sg
             for (int l = maxl - 2; l >= 0; --l)
             {
                 st = launch_words(c, l, l,
-                                  [=] __device__(int ll, long long w, long long row, int wi)
+                                  [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
                                   {
                                       const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | coarsen_word(g, d, ll, row, wi);
                                       d[w]              = dv;
@@ -617,7 +620,7 @@ namespace sg
                 break;
             }
             st = launch_words(c, 0, top,
-                              [=] __device__(int l, long long w, long long row, int wi)
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                               {
                                   uint32_t v = nc[w] & ~rr[w];
                                   if (l >= 1)
@@ -649,7 +652,7 @@ namespace sg
         int* flag = c.d_flags;
         cudaMemsetAsync(flag, 0, sizeof(int), c.stream);
         int st = launch_words(c, 0, c.g.nlev - 1,
-                              [=] __device__(int, long long w, long long, int)
+                              [=] __device__(const Geom&, int, long long w, long long, int)
                               {
                                   if (a[w] != b[w])
                                   {

@@ -45,7 +45,7 @@ def init_both(g, o, f):
 @pytest.mark.parametrize("dim,minl,maxl", [(2, 2, 6), (2, 4, 9), (3, 2, 5)])
 def test_uniform_mesh_ids(sg, dim, minl, maxl):
     g, o = pair(sg, dim, minl, maxl)
-    compare_meshes(g, o, maxl + 1, "uniform")
+    compare_meshes(g, o, maxl, "uniform")
     compare_cells(g, o, "uniform")
     assert g.nb_ref() == o.nb_ref()
 
