@@ -265,6 +265,13 @@ def run_gpu(args):
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
     achieved = alg_bytes / (upw_ms / 1e3) / 1e9
+    # FP64 roof: the upwind formula of the reference costs 5 FP64 operations
+    # per face flux plus 5 (2D) to assemble the update: 26 per cell in 2D
+    fp64_ops = 26 * nc
+    try:
+        fp64_peak = sg.device_fp64_rate()
+    except Exception:
+        fp64_peak = None
     traffic = None
     try:
         traffic_info = json.load(open(os.path.join(ROOT, "profiles", "upwind_traffic.json")))
@@ -301,7 +308,11 @@ def run_gpu(args):
                     "steps": e2e_steps, "api": "sg_field_upload + sg_adapt + sg_update_ghost_mr + sg_upwind + sg_field_swap + sg_field_download"},
             "roofline": {"bound": "hbm", "kernel": "k_upwind", "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": int(alg_bytes), "launch_ms": upw_ms,
-                         "cells": int(nc), "halo": int(halo)},
+                         "cells": int(nc), "halo": int(halo),
+                         "fp64": {"achieved_gflops": fp64_ops / (upw_ms / 1e3) / 1e9, "peak_gflops": fp64_peak,
+                                  "peak_source": "measured in this run (sg_device_fp64_rate probe)",
+                                  "frac": (fp64_ops / (upw_ms / 1e3) / 1e9 / fp64_peak) if fp64_peak else None,
+                                  "ops_per_launch": int(fp64_ops), "note": "26 FP64 operations per leaf cell in the reference's formula"}},
             "gpu_launches": int(launches),
             "launches_per_step": launches / args.steps,
             "phases_ms_per_step": phases,

@@ -87,6 +87,10 @@ int sg_timers_enable(sg_mesh_t mesh, int enable);
 int sg_timers_get(sg_mesh_t mesh, int timer_id, double* total_ms, long long* calls);
 int sg_timers_reset(sg_mesh_t mesh);
 
+/* Instrumentation without a samurai counterpart: the device's FP64 rate (non-fused adds and multiplies
+ * per second, in GFLOP/s), measured by a throughput probe kernel.  The FP64 pipe bounds this path on GB300. */
+int sg_device_fp64_rate(double* gflops);
+
 /* samurai::make_scalar_field<double>(name, mesh) (field/scalar_field.hpp:173-216) */
 int sg_field_create(sg_mesh_t mesh, const char* name, sg_field_t* out);
 int sg_field_destroy(sg_field_t field);

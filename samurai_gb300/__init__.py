@@ -65,6 +65,7 @@ def lib():
         "sg_timers_enable": (i, [vp, i]),
         "sg_timers_get": (i, [vp, i, ctypes.POINTER(d), pl]),
         "sg_timers_reset": (i, [vp]),
+        "sg_device_fp64_rate": (i, [ctypes.POINTER(d)]),
         "sg_field_create": (i, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
         "sg_field_destroy": (i, [vp]),
         "sg_field_set_dirichlet": (i, [vp, d]),
@@ -365,6 +366,13 @@ class ScalarField:
         out = np.empty(n, np.uint8)
         _check(lib().sg_tag_download(self.h, _ptr(out), n), "sg_tag_download")
         return out
+
+
+def device_fp64_rate():
+    """Measured FP64 rate of the current device (GFLOP/s, unfused add/mul)."""
+    v = ctypes.c_double()
+    _check(lib().sg_device_fp64_rate(ctypes.byref(v)), "sg_device_fp64_rate")
+    return v.value
 
 
 def make_scalar_field(name, mesh):

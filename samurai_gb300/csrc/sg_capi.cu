@@ -152,6 +152,29 @@ namespace
         }
     }
 
+    // FP64 throughput probe: independent multiply/add chains (built with
+    // --fmad=false, so each step is one DMUL and one DADD)
+    __global__ void k_fp64_probe(double* out, int iters, double a, double b)
+    {
+        double x0 = threadIdx.x * 1e-3, x1 = x0 + 1., x2 = x0 + 2., x3 = x0 + 3., x4 = x0 + 4., x5 = x0 + 5., x6 = x0 + 6., x7 = x0 + 7.;
+        for (int k = 0; k < iters; ++k)
+        {
+            x0 = x0 * a + b;
+            x1 = x1 * a + b;
+            x2 = x2 * a + b;
+            x3 = x3 * a + b;
+            x4 = x4 * a + b;
+            x5 = x5 * a + b;
+            x6 = x6 * a + b;
+            x7 = x7 * a + b;
+        }
+        const double r = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+        if (r == 12345.678)
+        {
+            out[0] = r; // keeps the chains alive
+        }
+    }
+
     int stage(sg_mesh_s* h, long long n)
     {
         if (n <= h->staging_n)
@@ -591,6 +614,44 @@ extern "C"
         {
             mesh->ctx.n_launches = 0;
         }
+        return SG_OK;
+    }
+
+    int sg_device_fp64_rate(double* gflops)
+    {
+        if (!gflops)
+        {
+            return fail(SG_ERR_ARG, "sg_device_fp64_rate: null output");
+        }
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return fail(SG_ERR_CUDA, "sg_device_fp64_rate: no CUDA device");
+        }
+        double* d = nullptr;
+        cudaMalloc(&d, 64);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        const int blocks = nsm * 8, threads = 256, iters = 4096;
+        k_fp64_probe<<<blocks, threads>>>(d, 64, 1.0000001, 1e-9); // warm up
+        cudaEventRecord(e0);
+        k_fp64_probe<<<blocks, threads>>>(d, iters, 1.0000001, 1e-9);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(d);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess)
+        {
+            return fail(SG_ERR_CUDA, std::string("sg_device_fp64_rate: ") + cudaGetErrorString(err));
+        }
+        const double ops = 2.0 * 8.0 * iters * static_cast<double>(blocks) * threads;
+        *gflops          = ops / (ms * 1e-3) / 1e9;
         return SG_OK;
     }
 

@@ -625,60 +625,101 @@ namespace sg
         // demos/FiniteVolume/advection_2d.cpp:144) or the README lambda
         // (README.md:144-153).  Neighbours at the same level are reference
         // cells, at fixed offsets in the dense slabs.
-        template <int DIM>
-        __global__ void k_upwind(const Geom* __restrict__ gp, const int* wl, long long n, const uint32_t* cells, const double* u, double* unp1, double a0, double a1, double a2,
-                                 double dt, int scheme)
+        // 2^l as a double from its exponent bits (no FP64 instruction)
+        __device__ __forceinline__ double pow2(int l)
         {
-            const Geom& g = *gp;
-            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return cells[w]; },
-                      [&](long long w, int b)
-                      {
-                          const int l          = level_of(g, w);
-                          const LevelGeom& L   = g.lv[l];
-                          const long long e    = 32 * w + b;
-                          const long long sy   = 32LL * L.W;
-                          const long long sz   = sy * L.R;
-                          const double dx      = 1.0 / static_cast<double>(1 << l);
-                          const double uc      = u[e];
-                          double out;
-                          if (scheme == 1)
-                          {
-                              double s = uc - u[e - 1];
-                              s        = s + uc;
-                              s        = s - u[e - sy];
-                              if (DIM == 3)
-                              {
-                                  s = s + uc;
-                                  s = s - u[e - sz];
-                              }
-                              out = uc - dt / dx * s;
-                          }
-                          else
-                          {
-                              const double ha0 = .5 * a0, hb0 = .5 * fabs(a0);
-                              const double ha1 = .5 * a1, hb1 = .5 * fabs(a1);
-                              const double ul = u[e - 1], ur = u[e + 1], ud = u[e - sy], uu = u[e + sy];
-                              const double lf = ha0 * (ul + uc) + hb0 * (ul - uc);
-                              const double rf = ha0 * (uc + ur) + hb0 * (uc - ur);
-                              const double df = ha1 * (ud + uc) + hb1 * (ud - uc);
-                              const double uf = ha1 * (uc + uu) + hb1 * (uc - uu);
-                              double s        = -lf + rf;
-                              s               = s + -df;
-                              s               = s + uf;
-                              if (DIM == 3)
-                              {
-                                  const double ha2 = .5 * a2, hb2 = .5 * fabs(a2);
-                                  const double uf2 = u[e - sz], ub2 = u[e + sz];
-                                  const double ff  = ha2 * (uf2 + uc) + hb2 * (uf2 - uc);
-                                  const double bf  = ha2 * (uc + ub2) + hb2 * (uc - ub2);
-                                  s                = s + -ff;
-                                  s                = s + bf;
-                              }
-                              const double up = s / dx;
-                              out             = uc - dt * up;
-                          }
-                          unp1[e] = out;
-                      });
+            return __longlong_as_double(static_cast<long long>(1023 + l) << 52);
+        }
+
+        struct UpwindArgs
+        {
+            double ha[3]; // .5 * a_d, as the reference's flux forms it
+            double hb[3]; // .5 * |a_d|
+            double dt;
+            int scheme;
+        };
+
+        // unp1 = u - dt * upwind(a, u) (stencil_field.hpp:38-44, 91-97;
+        // demos/FiniteVolume/advection_2d.cpp:144) or the README lambda
+        // (README.md:144-153).  Same-level neighbours are reference cells at
+        // fixed offsets in the dense slabs.  On GB300 the FP64 pipe, not HBM,
+        // bounds this kernel, so FP64 work is cut without changing a rounding:
+        //  - the x-face flux between two leaf cells of a word is computed once
+        //    (lane b's right flux is lane b+1's left flux: same operands, same
+        //    operations, same bits) and passed by a shuffle;
+        //  - /dx and dt/dx use dx = 2^-l exactly: x / 2^-l == x * 2^l.
+        template <int DIM>
+        __global__ void k_upwind(const Geom* __restrict__ gp, const int* wl, long long n, const uint32_t* cells, const double* __restrict__ u,
+                                 double* __restrict__ unp1, UpwindArgs p)
+        {
+            const Geom& g  = *gp;
+            const int lane = threadIdx.x & 31;
+            for (long long i = warp_id(); i < n; i += warp_count())
+            {
+                const long long w  = __ldg(wl + i);
+                const uint32_t v   = __ldg(cells + w);
+                const bool is_cell = (v >> lane) & 1u;
+                const int l        = level_of(g, w);
+                const LevelGeom& L = g.lv[l];
+                const long long e  = 32 * w + lane;
+                const long long sy = 32LL * L.W;
+                const long long sz = sy * L.R;
+                if (p.scheme == 1)
+                {
+                    if (is_cell)
+                    {
+                        const double uc = u[e];
+                        double s        = uc - u[e - 1];
+                        s               = s + uc;
+                        s               = s - u[e - sy];
+                        if (DIM == 3)
+                        {
+                            s = s + uc;
+                            s = s - u[e - sz];
+                        }
+                        unp1[e] = uc - (p.dt * pow2(l)) * s;
+                    }
+                    continue;
+                }
+                double uc = 0., rf = 0.;
+                if (is_cell)
+                {
+                    uc              = u[e];
+                    const double ur = u[e + 1];
+                    rf              = p.ha[0] * (uc + ur) + p.hb[0] * (uc - ur);
+                }
+                const double rf_left = __shfl_up_sync(0xffffffffu, rf, 1);
+                if (!is_cell)
+                {
+                    continue;
+                }
+                double lf;
+                if (lane > 0 && ((v >> (lane - 1)) & 1u))
+                {
+                    lf = rf_left;
+                }
+                else
+                {
+                    const double ul = u[e - 1];
+                    lf              = p.ha[0] * (ul + uc) + p.hb[0] * (ul - uc);
+                }
+                const double ud = u[e - sy], uu = u[e + sy];
+                const double df = p.ha[1] * (ud + uc) + p.hb[1] * (ud - uc);
+                const double uf = p.ha[1] * (uc + uu) + p.hb[1] * (uc - uu);
+                double s        = -lf + rf;
+                s               = s + -df;
+                s               = s + uf;
+                if (DIM == 3)
+                {
+                    const double uf2 = u[e - sz], ub2 = u[e + sz];
+                    const double ff  = p.ha[2] * (uf2 + uc) + p.hb[2] * (uf2 - uc);
+                    const double bf  = p.ha[2] * (uc + ub2) + p.hb[2] * (uc - ub2);
+                    s                = s + -ff;
+                    s                = s + bf;
+                }
+                const double up = s * pow2(l);
+                unp1[e]         = uc - p.dt * up;
+            }
         }
 
         // --------------------------------------------------- layout moves
@@ -968,15 +1009,21 @@ namespace sg
         const Geom& g = c.g;
         const DeviceMesh& m = c.m();
         const long long n   = m.lo_cells[g.nlev];
+        UpwindArgs p{};
+        for (int d = 0; d < g.dim; ++d)
+        {
+            p.ha[d] = .5 * a[d];
+            p.hb[d] = .5 * std::fabs(a[d]);
+        }
+        p.dt     = dt;
+        p.scheme = scheme;
         if (g.dim == 2)
         {
-            k_upwind<2><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, a[0], a[1], g.dim == 3 ? a[2] : 0., dt,
-                                                                scheme);
+            k_upwind<2><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, p);
         }
         else
         {
-            k_upwind<3><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, a[0], a[1], g.dim == 3 ? a[2] : 0., dt,
-                                                                scheme);
+            k_upwind<3><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, p);
         }
         ++c.n_launches;
         return check(c, "upwind");
