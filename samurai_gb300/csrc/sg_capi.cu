@@ -76,6 +76,12 @@ namespace
         st |= dalloc(c, &m.rank, n);
         st |= dalloc(c, &m.wl_ref, n);
         st |= dalloc(c, &m.wl_cells, n);
+        st |= dalloc(c, &m.d_lo, static_cast<size_t>(sg::COUNTS));
+        if (!st && cudaMallocHost(reinterpret_cast<void**>(&m.h_lo), sg::COUNTS * sizeof(long long)) != cudaSuccess)
+        {
+            m.h_lo = nullptr;
+            st     = sg::SG_ERR_CUDA;
+        }
         return st ? sg::SG_ERR_CUDA : sg::SG_OK;
     }
 
@@ -91,6 +97,12 @@ namespace
         dfree(m.rank);
         dfree(m.wl_ref);
         dfree(m.wl_cells);
+        dfree(m.d_lo);
+        if (m.h_lo)
+        {
+            cudaFreeHost(m.h_lo);
+            m.h_lo = nullptr;
+        }
     }
 
     void destroy_ctx(sg_mesh_s* h)
@@ -104,6 +116,16 @@ namespace
         for (cudaEvent_t e : c.timers.pool)
         {
             cudaEventDestroy(e);
+        }
+        for (auto& ge : c.graphs)
+        {
+            cudaGraphExecDestroy(ge.exec);
+        }
+        c.graphs.clear();
+        dfree(c.d_ite);
+        if (c.h_ite)
+        {
+            cudaFreeHost(c.h_ite);
         }
         free_mesh(c.mesh[0]);
         free_mesh(c.mesh[1]);
@@ -323,10 +345,12 @@ extern "C"
         st |= dalloc(c, &c.d_counts, static_cast<size_t>(sg::COUNTS));
         st |= dalloc(c, &c.d_flags, 8);
         st |= dalloc(c, &c.d_geom, 1);
+        st |= dalloc(c, &c.d_ite, 1);
         st |= dalloc(c, &c.d_eps, 3 * sg::MAXLEV);
         if (!st)
         {
-            if (cudaMallocHost(reinterpret_cast<void**>(&c.h_eps), 3 * sg::MAXLEV * sizeof(double)) != cudaSuccess
+            if (cudaMallocHost(reinterpret_cast<void**>(&c.h_ite), sizeof(int)) != cudaSuccess
+                || cudaMallocHost(reinterpret_cast<void**>(&c.h_eps), 3 * sg::MAXLEV * sizeof(double)) != cudaSuccess
                 || cudaMallocHost(reinterpret_cast<void**>(&c.h_counts), sg::COUNTS * sizeof(long long)) != cudaSuccess
                 || cudaMallocHost(reinterpret_cast<void**>(&c.h_flags), 8 * sizeof(int)) != cudaSuccess)
             {
@@ -353,6 +377,10 @@ extern "C"
         {
             st = sg::build_mesh(c, c.m());
         }
+        if (!st)
+        {
+            st = sg::host_counts(c, c.m());
+        }
         if (st)
         {
             std::string msg = c.err;
@@ -378,6 +406,10 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_mesh_counts: null mesh");
         }
+        if (int st = sg::host_counts(mesh->ctx, mesh->ctx.m()))
+        {
+            return from_ctx(mesh->ctx, st);
+        }
         if (nb_cells)
         {
             *nb_cells = mesh->ctx.m().nb_cells;
@@ -396,6 +428,10 @@ extern "C"
             return fail(SG_ERR_ARG, "sg_mesh_get_cells: null mesh");
         }
         sg::Ctx& c = mesh->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (capacity < c.m().nb_cells)
         {
             return fail(SG_ERR_CAPACITY, "sg_mesh_get_cells: output too small");
@@ -573,7 +609,12 @@ extern "C"
             bm[static_cast<size_t>(p.w)] |= 1u << p.b;
         }
         cudaMemcpyAsync(c.m().cells, bm.data(), bm.size() * 4, cudaMemcpyHostToDevice, c.stream);
-        return from_ctx(c, sg::build_mesh(c, c.m()));
+        int st = sg::build_mesh(c, c.m());
+        if (!st)
+        {
+            st = sg::host_counts(c, c.m());
+        }
+        return from_ctx(c, st);
     }
 
     int sg_mesh_stream(sg_mesh_t mesh, void** stream)
@@ -752,6 +793,10 @@ extern "C"
             return fail(SG_ERR_ARG, "sg_field_upload_device: null argument");
         }
         sg::Ctx& c = field->mesh->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_ref)
         {
             return fail(SG_ERR_ARG, "sg_field_upload_device: size differs from the reference mesh");
@@ -766,6 +811,10 @@ extern "C"
             return fail(SG_ERR_ARG, "sg_field_download_device: null argument");
         }
         sg::Ctx& c = field->mesh->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_ref)
         {
             return fail(SG_ERR_ARG, "sg_field_download_device: size differs from the reference mesh");
@@ -781,6 +830,10 @@ extern "C"
         }
         sg_mesh_s* h = field->mesh;
         sg::Ctx& c   = h->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_ref)
         {
             return fail(SG_ERR_ARG, "sg_field_upload: size differs from the reference mesh");
@@ -806,6 +859,10 @@ extern "C"
         }
         sg_mesh_s* h = field->mesh;
         sg::Ctx& c   = h->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_ref)
         {
             return fail(SG_ERR_ARG, "sg_field_download: size differs from the reference mesh");
@@ -834,6 +891,10 @@ extern "C"
             return fail(SG_ERR_ARG, "sg_field_set_cells: null argument");
         }
         sg::Ctx& c = field->mesh->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_cells)
         {
             return fail(SG_ERR_ARG, "sg_field_set_cells: size differs from the number of cells");
@@ -858,6 +919,10 @@ extern "C"
             return fail(SG_ERR_ARG, "sg_field_get_cells: null argument");
         }
         sg::Ctx& c = field->mesh->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_cells)
         {
             return fail(SG_ERR_ARG, "sg_field_get_cells: size differs from the number of cells");
@@ -958,6 +1023,10 @@ extern "C"
         }
         sg_mesh_s* h = u->mesh;
         sg::Ctx& c   = h->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_ref)
         {
             return fail(SG_ERR_ARG, "sg_detail_download: size differs from the reference mesh");
@@ -986,6 +1055,10 @@ extern "C"
             return fail(SG_ERR_ARG, "sg_tag_download: null argument");
         }
         sg::Ctx& c = u->mesh->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
         if (n != c.m().nb_ref)
         {
             return fail(SG_ERR_ARG, "sg_tag_download: size differs from the reference mesh");

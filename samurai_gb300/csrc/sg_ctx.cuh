@@ -33,14 +33,33 @@ namespace sg
         int* rank       = nullptr; // exclusive popcount prefix of ref
         int* wl_ref     = nullptr; // indices of the non-empty reference words, ascending
         int* wl_cells   = nullptr; // indices of the non-empty leaf-cell words, ascending
-        long long nb_ref   = 0;    // host copy of the reference size
-        long long nb_cells = 0;    // host copy of the leaf count
-        // host copies: the words of level l are wl_*[lo_*[l] .. lo_*[l+1])
-        long long lo_ref[MAXLEV + 1]   = {};
-        long long lo_cells[MAXLEV + 1] = {};
+        // Counters written by scan_rank on the device (layout below) and
+        // mirrored asynchronously into pinned host memory; kernels read the
+        // device copy, so no launch waits for the host.
+        long long* d_lo = nullptr;
+        long long* h_lo = nullptr;
+        bool host_valid = false; // h_lo reflects d_lo (after a synchronisation)
+        long long nb_ref   = 0;  // host copies, valid when host_valid
+        long long nb_cells = 0;
     };
 
-    constexpr int COUNTS = 4 + 2 * (MAXLEV + 1); // device counters filled by scan_rank
+    // counters of a mesh: [0] reference size, [1] non-empty reference words,
+    // [2] leaf cells, [3] non-empty leaf words, then the word-list offsets:
+    // the reference words of level l are wl_ref[lo[LO_REF+l] .. lo[LO_REF+l+1]),
+    // the leaf words wl_cells[lo[LO_CELLS+l] .. lo[LO_CELLS+l+1]).
+    constexpr int LO_REF   = 4;
+    constexpr int LO_CELLS = LO_REF + MAXLEV + 1;
+    constexpr int COUNTS   = LO_CELLS + MAXLEV + 1;
+
+    // flags written by the adaptation kernels (device, mirrored to pinned host)
+    enum FlagSlot : int
+    {
+        F_GRAD0 = 0,  // graduation pass 1 found cells to refine
+        F_GRAD1 = 1,  // graduation pass 2 found cells to refine (more passes needed)
+        F_DIFFER = 2, // new leaf cells differ from the current ones
+        F_GRADX = 3,  // scratch for extra graduation passes
+        F_COUNT = 8
+    };
 
     // Named phase timers with samurai's scope names (timers.hpp:111-1036;
     // mr/adapt.hpp:151-387, update_ghost_mr.hpp:263, field/field_base.hpp:234).
@@ -101,6 +120,16 @@ namespace sg
         int* d_flags        = nullptr;
         int* h_flags        = nullptr; // pinned mirror
         long long capacity  = 0;       // dense elements per field (32 * total_words)
+        int* d_ite          = nullptr; // Harten pass index seen by the detail/criteria kernels
+        int* h_ite          = nullptr; // pinned staging
+        bool use_graphs     = true;    // replay captured launch sequences
+        struct GraphEntry
+        {
+            unsigned long long key[4];
+            cudaGraphExec_t exec;
+            int kernels;
+        };
+        std::vector<GraphEntry> graphs;
         int n_launches      = 0;       // kernel launches since the last reset (instrumentation)
         std::string err;
 
@@ -126,8 +155,9 @@ namespace sg
     };
 
     // kernels and drivers (sg_mesh.cu / sg_field.cu)
-    int build_mesh(Ctx& c, DeviceMesh& m);           // from m.cells
-    int scan_rank(Ctx& c, DeviceMesh& m);            // rank + nb_ref
+    int build_mesh(Ctx& c, DeviceMesh& m);           // from m.cells; asynchronous
+    int scan_rank(Ctx& c, DeviceMesh& m);            // rank, word lists, counters; asynchronous
+    int host_counts(Ctx& c, DeviceMesh& m);          // synchronises and refreshes nb_ref / nb_cells
     int update_ghost_mr(Ctx& c, DeviceField& f);     // update_ghost_mr(u)
     int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten);
     int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme);
@@ -158,6 +188,19 @@ namespace sg
             timer_stop(c, id);
         }
     };
+
+    // blocks of 256 threads (8 warps) for a warp-per-item loop over at most
+    // max_items list entries: one wave of resident warps at most
+    inline int blocks_for_items(long long max_items)
+    {
+        long long b = (max_items + 7) / 8;
+        if (b < 1)
+        {
+            b = 1;
+        }
+        const long long cap = 152LL * 8;
+        return static_cast<int>(b > cap ? cap : b);
+    }
 
     // launch helpers
     inline int grid_for(long long n, int block = 256, long long cap = 152LL * 32)

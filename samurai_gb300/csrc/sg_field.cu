@@ -4,6 +4,8 @@
 // first-order upwind step.  Built with --fmad=false: every FP64 operation is
 // rounded on its own, in the reference's association order, so that the
 // detail thresholds take the same decisions as the CPU implementation.
+#include <cstring>
+
 #include "sg_ctx.cuh"
 
 namespace sg
@@ -31,13 +33,12 @@ namespace sg
 
     int new_cells_from_tags(Ctx& c, const DeviceMesh& m, uint32_t* nc);
     int graduate(Ctx& c, uint32_t* nc, int* iterations);
-    int bitmaps_equal(Ctx& c, const uint32_t* a, const uint32_t* b, bool* equal);
+    int grad_pass(Ctx& c, uint32_t* nc, int slot);
+    int bitmaps_differ(Ctx& c, const uint32_t* a, const uint32_t* b, int slot);
 
     namespace
     {
         constexpr int BLOCK = 256;
-
-        constexpr int WARPS_PER_BLOCK = BLOCK / 32;
 
         // One warp per listed word, lane b on bit b.  The list holds the
         // non-empty words of a superset (reference or leaf cells) in
@@ -70,16 +71,6 @@ namespace sg
             return (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
         }
 
-        int blocks_for_items(long long items)
-        {
-            long long b = (items + WARPS_PER_BLOCK - 1) / WARPS_PER_BLOCK;
-            if (b < 1)
-            {
-                b = 1;
-            }
-            const long long cap = 152LL * 64;
-            return static_cast<int>(b > cap ? cap : b);
-        }
 
         // interp_coeffs<3> (numeric/prediction.hpp:32-36), parity 0: even
         __device__ __forceinline__ double interp1(int parity, int k)
@@ -152,9 +143,10 @@ namespace sg
         }
 
         // ----------------------------------------------------------- tags
-        __global__ void k_tag_init(const Geom* __restrict__ gp, const int* wl, long long n, const uint32_t* ref, const uint32_t* cells, uint8_t* tag, double* det)
+        __global__ void k_tag_init(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* cells,
+                                   uint8_t* tag, double* det)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+            warp_list(wl, lo[LO_REF], lo[LO_REF + gp->nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; },
                       [&](long long w, int b)
                       {
                           const long long e = 32 * w + b;
@@ -292,7 +284,7 @@ namespace sg
             int nb_corner;    // blocks of the corner role
             int nb_face;      // blocks of the face role
             long long nfaces; // face positions (2*dim directions)
-            long long p_begin, p_end; // reference word list range of level l-1 (projection)
+            int do_proj;      // project the reference of level l onto proj_cells[l-1]
         };
 
         // One launch per level of the top-down pass of update_ghost_mr
@@ -307,7 +299,8 @@ namespace sg
         //  - projection of the reference cells of level l onto proj_cells[l-1]
         //    (numeric/projection.hpp:15-65).
         template <int DIM>
-        __global__ void k_ghost_level(const Geom* __restrict__ gp, GhostLevelArgs a, const int* wl_ref, const uint32_t* cells, const uint32_t* uni,
+        __global__ void k_ghost_level(const Geom* __restrict__ gp, GhostLevelArgs a, const int* wl_ref, const long long* lo, const uint32_t* cells,
+                                      const uint32_t* uni,
                                       const uint32_t* proj, const uint32_t* ref, double* u)
         {
             const Geom& g = *gp;
@@ -397,7 +390,11 @@ namespace sg
             const long long rb        = static_cast<long long>(blockIdx.x - a.nb_corner - a.nb_face);
             const long long warp0     = (rb * blockDim.x + threadIdx.x) >> 5;
             const long long nwarps    = (static_cast<long long>(gridDim.x - a.nb_corner - a.nb_face) * blockDim.x) >> 5;
-            warp_list(wl_ref, a.p_begin, a.p_end, warp0, nwarps,
+            if (!a.do_proj)
+            {
+                return;
+            }
+            warp_list(wl_ref, lo[LO_REF + lc], lo[LO_REF + lc + 1], warp0, nwarps,
                       [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, lc, w);
@@ -413,11 +410,11 @@ namespace sg
         // prediction of the ghosts of level l from level l-1
         // (algorithm/update_ghost_mr.hpp:224-233)
         template <int DIM>
-        __global__ void k_predict(const Geom* __restrict__ gp, int l, int order, const int* wl_ref, long long begin, long long end, const uint32_t* cells, const uint32_t* proj,
+        __global__ void k_predict(const Geom* __restrict__ gp, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells, const uint32_t* proj,
                                   const uint32_t* ref, double* u)
         {
             const Geom& g = *gp;
-            warp_list(wl_ref, begin, end, warp_id(), warp_count(),
+            warp_list(wl_ref, lo[LO_REF + l], lo[LO_REF + l + 1], warp_id(), warp_count(),
                       [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, l, w);
@@ -434,11 +431,17 @@ namespace sg
         // compute_detail_op (mr/operators.hpp:139-540) on
         // intersection(all_cells[l], union(cells[l+1], cells[l+2])).on(l)
         template <int DIM>
-        __global__ void k_detail(const Geom* __restrict__ gp, int order, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
-                                 const uint32_t* hc2, const double* u, double* det)
+        __global__ void k_detail(const Geom* __restrict__ gp, int order, const int* wl, const long long* lo, int l0, int l1, const int* d_ite,
+                                 const uint32_t* ref, const uint32_t* hc, const uint32_t* hc2, const double* u, double* det)
         {
             const Geom& g = *gp;
-            warp_list(wl, begin, end, warp_id(), warp_count(), [&](long long w) { return ref[w] & (hc[w] | hc2[w]); },
+            // levels l0 .. min(l1, max_level - ite - 1) (mr/adapt.hpp:310-317)
+            const int le = min(l1, g.max_level - *d_ite - 1);
+            if (le < l0)
+            {
+                return;
+            }
+            warp_list(wl, lo[LO_REF + l0], lo[LO_REF + le + 1], warp_id(), warp_count(), [&](long long w) { return ref[w] & (hc[w] | hc2[w]); },
                       [&](long long w, int b)
                       {
                           const int l    = level_of(g, w);
@@ -493,11 +496,18 @@ namespace sg
         // mr_criteria_op (mr/criteria.hpp:20-113) on
         // intersection(cells[l], all_cells[l-1]).on(l-1), fine levels l0..l1
         template <int DIM>
-        __global__ void k_criteria(const Geom* __restrict__ gp, const double* __restrict__ eps, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc,
-                                   const double* det, uint8_t* tag)
+        __global__ void k_criteria(const Geom* __restrict__ gp, const double* __restrict__ eps, const int* wl, const long long* lo, int l0, int l1,
+                                   const int* d_ite, const uint32_t* ref, const uint32_t* hc, const double* det, uint8_t* tag)
         {
             const Geom& g = *gp;
-            warp_list(wl, begin, end, warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
+            // fine levels l0 .. min(l1, max_level - ite) (mr/adapt.hpp:325-339); the
+            // operator runs on their parents
+            const int le = min(l1, g.max_level - *d_ite);
+            if (le < l0)
+            {
+                return;
+            }
+            warp_list(wl, lo[LO_REF + l0 - 1], lo[LO_REF + le], warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
                       [&](long long w, int b)
                       {
                           const int lc  = level_of(g, w);
@@ -546,11 +556,12 @@ namespace sg
 
         // maximum_op (mr/operators.hpp:22-96), children at level l
         template <int DIM>
-        __global__ void k_maximum(const Geom* __restrict__ gp, int l, const int* wl, long long begin, long long end, const uint32_t* ref, const uint32_t* hc, uint8_t* tag)
+        __global__ void k_maximum(const Geom* __restrict__ gp, int l, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
+                                  uint8_t* tag)
         {
             const Geom& g = *gp;
             const int lc = l - 1;
-            warp_list(wl, begin, end, warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
+            warp_list(wl, lo[LO_REF + lc], lo[LO_REF + l], warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
                       [&](long long w, int b)
                       {
                           const Cell c  = cell_of(g, lc, w, b);
@@ -590,11 +601,11 @@ namespace sg
         // reference ∩ new cells, projection on coarsened cells, prediction on
         // refined cells; every other reference entry of the new field is 0.
         template <int DIM>
-        __global__ void k_update_fields(const Geom* __restrict__ gp, int order, const int* wl, long long n, const uint32_t* nref, const uint32_t* ncells, const uint32_t* oref,
-                                        const uint32_t* ocells, const uint32_t* ohc, const double* uo, double* un)
+        __global__ void k_update_fields(const Geom* __restrict__ gp, int order, const int* wl, const long long* lo, const uint32_t* nref,
+                                        const uint32_t* ncells, const uint32_t* oref, const uint32_t* ocells, const uint32_t* ohc, const double* uo, double* un)
         {
             const Geom& g = *gp;
-            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return nref[w]; },
+            warp_list(wl, lo[LO_REF], lo[LO_REF + g.nlev], warp_id(), warp_count(), [&](long long w) { return nref[w]; },
                       [&](long long w, int b)
                       {
                           const long long e = 32 * w + b;
@@ -649,12 +660,13 @@ namespace sg
         //    operations, same bits) and passed by a shuffle;
         //  - /dx and dt/dx use dx = 2^-l exactly: x / 2^-l == x * 2^l.
         template <int DIM>
-        __global__ void k_upwind(const Geom* __restrict__ gp, const int* wl, long long n, const uint32_t* cells, const double* __restrict__ u,
+        __global__ void k_upwind(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* cells, const double* __restrict__ u,
                                  double* __restrict__ unp1, UpwindArgs p)
         {
-            const Geom& g  = *gp;
-            const int lane = threadIdx.x & 31;
-            for (long long i = warp_id(); i < n; i += warp_count())
+            const Geom& g       = *gp;
+            const int lane      = threadIdx.x & 31;
+            const long long n   = lo[LO_CELLS + g.nlev];
+            for (long long i = lo[LO_CELLS] + warp_id(); i < n; i += warp_count())
             {
                 const long long w  = __ldg(wl + i);
                 const uint32_t v   = __ldg(cells + w);
@@ -723,251 +735,394 @@ namespace sg
         }
 
         // --------------------------------------------------- layout moves
-        __global__ void k_gather(const int* wl, long long n, const uint32_t* ref, const int* rank, const double* dense, double* compact)
+        __global__ void k_gather(const int* wl, const long long* lo, int nlev, const uint32_t* ref, const int* rank, const double* dense, double* compact)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+            warp_list(wl, lo[LO_REF], lo[LO_REF + nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; },
                       [&](long long w, int b) { compact[ref_index(ref, rank, Pos{w, b})] = dense[32 * w + b]; });
         }
 
-        __global__ void k_scatter(const int* wl, long long n, const uint32_t* ref, const int* rank, const double* compact, double* dense)
+        __global__ void k_scatter(const int* wl, const long long* lo, int nlev, const uint32_t* ref, const int* rank, const double* compact, double* dense)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+            warp_list(wl, lo[LO_REF], lo[LO_REF + nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; },
                       [&](long long w, int b) { dense[32 * w + b] = compact[ref_index(ref, rank, Pos{w, b})]; });
         }
 
-        __global__ void k_fill(const int* wl, long long n, const uint32_t* ref, double* dense, double v)
+        __global__ void k_fill(const int* wl, const long long* lo, int nlev, const uint32_t* ref, double* dense, double v)
         {
-            warp_list(wl, 0, n, warp_id(), warp_count(), [&](long long w) { return ref[w]; }, [&](long long w, int b) { dense[32 * w + b] = v; });
+            warp_list(wl, lo[LO_REF], lo[LO_REF + nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; }, [&](long long w, int b) { dense[32 * w + b] = v; });
+        }
+    } // namespace
+
+    namespace
+    {
+        int blocks_words(const Geom& g, int l0, int l1)
+        {
+            if (l1 < l0)
+            {
+                return 1;
+            }
+            return blocks_for_items(g.lv[l1].woff + g.lv[l1].nwords - g.lv[l0].woff);
         }
     } // namespace
 
     int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
     {
-        const long long n = m.lo_ref[c.g.nlev];
-        k_gather<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(m.wl_ref, n, m.ref, m.rank, dense, compact);
+        k_gather<<<blocks_words(c.g, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
         ++c.n_launches;
         return check(c, "gather");
     }
 
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense)
     {
-        const long long n = m.lo_ref[c.g.nlev];
-        k_scatter<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(m.wl_ref, n, m.ref, m.rank, compact, dense);
+        k_scatter<<<blocks_words(c.g, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, compact, dense);
         ++c.n_launches;
         return check(c, "scatter");
     }
 
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value)
     {
-        const long long n = m.lo_ref[c.g.nlev];
-        k_fill<<<blocks_for_items(n), BLOCK, 0, c.stream>>>(m.wl_ref, n, m.ref, dense, value);
+        k_fill<<<blocks_words(c.g, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, dense, value);
         ++c.n_launches;
         return check(c, "fill");
     }
 
-    // update_ghost_mr / update_ghost_mr_aggregated (algorithm/update_ghost_mr.hpp:195-270)
+    // --------------------------------------------------------------- graphs
+    // The launch sequences below depend only on the level geometry and on
+    // the buffers they touch: list sizes and level ranges are read on the
+    // device.  Each is captured once per buffer combination into a CUDA graph
+    // and replayed.
+    template <class F>
+    int run_cached(Ctx& c, unsigned long long k0, unsigned long long k1, unsigned long long k2, unsigned long long k3, F seq)
+    {
+        if (!c.use_graphs || c.timers.enabled)
+        {
+            return seq();
+        }
+        for (auto& e : c.graphs)
+        {
+            if (e.key[0] == k0 && e.key[1] == k1 && e.key[2] == k2 && e.key[3] == k3)
+            {
+                if (cudaGraphLaunch(e.exec, c.stream) != cudaSuccess)
+                {
+                    return check(c, "cudaGraphLaunch");
+                }
+                c.n_launches += e.kernels;
+                return SG_OK;
+            }
+        }
+        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        {
+            return check(c, "cudaStreamBeginCapture");
+        }
+        const int before = c.n_launches;
+        int st           = seq();
+        cudaGraph_t graph = nullptr;
+        cudaError_t e     = cudaStreamEndCapture(c.stream, &graph);
+        if (st || e != cudaSuccess)
+        {
+            if (graph)
+            {
+                cudaGraphDestroy(graph);
+            }
+            if (!st)
+            {
+                c.err = std::string("graph capture: ") + cudaGetErrorString(e);
+                st    = SG_ERR_CUDA;
+            }
+            cudaGetLastError();
+            return st;
+        }
+        cudaGraphExec_t exec = nullptr;
+        e                    = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess)
+        {
+            return check(c, "cudaGraphInstantiate");
+        }
+        if (c.graphs.size() >= 64)
+        {
+            cudaGraphExecDestroy(c.graphs.front().exec);
+            c.graphs.erase(c.graphs.begin());
+        }
+        const int kernels = c.n_launches - before;
+        c.graphs.push_back({{k0, k1, k2, k3}, exec, kernels});
+        if (cudaGraphLaunch(exec, c.stream) != cudaSuccess)
+        {
+            return check(c, "cudaGraphLaunch");
+        }
+        return SG_OK;
+    }
+
+    namespace
+    {
+        unsigned long long bits_of(double v)
+        {
+            unsigned long long b;
+            std::memcpy(&b, &v, sizeof(b));
+            return b;
+        }
+
+        unsigned long long ptr_key(const void* p)
+        {
+            return static_cast<unsigned long long>(reinterpret_cast<uintptr_t>(p));
+        }
+
+        // update_ghost_mr / update_ghost_mr_aggregated (algorithm/update_ghost_mr.hpp:195-270)
+        int seq_ghost(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv)
+        {
+            ScopedTimer timer(c, T_GHOST);
+            const Geom& g   = c.g;
+            const int minl  = c.cfg.min_level;
+            const int maxl  = c.cfg.max_level;
+            const int lmin  = minl >= 2 ? minl - 2 : 0; // no reference cell below min_level-2
+            const int ndiag = (g.dim == 2) ? 4 : 20;
+            for (int l = maxl; l >= lmin; --l)
+            {
+                GhostLevelArgs a{};
+                a.l            = l;
+                a.do_corners   = (l >= minl && l <= maxl) ? 1 : 0;
+                a.do_project   = l < maxl;
+                a.do_dirichlet = (l >= minl) && has_bc;
+                a.do_predict   = (l >= minl && l < maxl);
+                a.value        = bcv;
+                a.nb_corner    = a.do_corners ? ndiag : 0;
+                const int n    = g.lv[l].n;
+                a.nfaces       = (a.do_project || a.do_dirichlet || a.do_predict)
+                                     ? static_cast<long long>(2 * g.dim) * ((g.dim == 2) ? n : static_cast<long long>(n) * n)
+                                     : 0;
+                a.nb_face      = static_cast<int>((a.nfaces + BLOCK - 1) / BLOCK);
+                a.do_proj      = l > lmin;
+                const int nb_proj = a.do_proj ? blocks_words(g, l - 1, l - 1) : 0;
+                const int grid    = a.nb_corner + a.nb_face + nb_proj;
+                if (grid > 0)
+                {
+                    if (g.dim == 2)
+                    {
+                        k_ghost_level<2><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                    }
+                    else
+                    {
+                        k_ghost_level<3><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                    }
+                    ++c.n_launches;
+                }
+            }
+            for (int l = (lmin > 1 ? lmin : 1); l <= maxl; ++l)
+            {
+                if (g.dim == 2)
+                {
+                    k_predict<2><<<blocks_words(g, l, l), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                                                                                 m.ref, u);
+                }
+                else
+                {
+                    k_predict<3><<<blocks_words(g, l, l), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                                                                                 m.ref, u);
+                }
+                ++c.n_launches;
+            }
+            return check(c, "update_ghost_mr");
+        }
+
+        // Adapt::harten up to the fixed-point test (mr/adapt.hpp:276-375):
+        // tags, ghost update, details, criteria, tag finalisation, new cells,
+        // two graduation passes and the comparison with the current cells.
+        // Reads the pass index and thresholds staged in pinned memory; leaves
+        // the flags in pinned memory.  No host synchronisation.
+        int seq_front(Ctx& c, DeviceMesh& m, DeviceMesh& nm, double* u, bool has_bc, double bcv)
+        {
+            const Geom& g  = c.g;
+            const int minl = c.cfg.min_level;
+            const int maxl = c.cfg.max_level;
+            int st;
+            cudaMemcpyAsync(c.d_ite, c.h_ite, sizeof(int), cudaMemcpyHostToDevice, c.stream);
+            cudaMemcpyAsync(c.d_eps, c.h_eps, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+            cudaMemsetAsync(c.d_flags, 0, F_COUNT * sizeof(int), c.stream);
+            k_tag_init<<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
+            ++c.n_launches;
+            if ((st = check(c, "tag_init")) || (st = seq_ghost(c, m, u, has_bc, bcv)))
+            {
+                return st;
+            }
+
+            timer_start(c, T_DETAIL);
+            const int dl0 = minl > 0 ? minl - 1 : 0;
+            const int dl1 = maxl - 1;
+            if (dl1 >= dl0)
+            {
+                if (g.dim == 2)
+                {
+                    k_detail<2><<<blocks_words(g, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                                                                                    m.ref, m.hc, m.hc2, u, c.detail);
+                }
+                else
+                {
+                    k_detail<3><<<blocks_words(g, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                                                                                    m.ref, m.hc, m.hc2, u, c.detail);
+                }
+                ++c.n_launches;
+            }
+            timer_stop(c, T_DETAIL);
+
+            timer_start(c, T_TAG);
+            if (minl >= 1 && maxl >= minl)
+            {
+                if (g.dim == 2)
+                {
+                    k_criteria<2><<<blocks_words(g, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                                                                                                m.ref, m.hc, c.detail, c.tag);
+                }
+                else
+                {
+                    k_criteria<3><<<blocks_words(g, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                                                                                                m.ref, m.hc, c.detail, c.tag);
+                }
+                ++c.n_launches;
+            }
+            timer_stop(c, T_TAG);
+
+            timer_start(c, T_FINALIZE);
+            for (int l = maxl; l > 0; --l)
+            {
+                if (g.dim == 2)
+                {
+                    k_maximum<2><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                }
+                else
+                {
+                    k_maximum<3><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                }
+                ++c.n_launches;
+            }
+            timer_stop(c, T_FINALIZE);
+            if ((st = check(c, "criteria")))
+            {
+                return st;
+            }
+
+            timer_start(c, T_MESH_UPDATE);
+            if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0)) || (st = grad_pass(c, nm.cells, F_GRAD1))
+                || (st = bitmaps_differ(c, nm.cells, m.cells, F_DIFFER)))
+            {
+                return st;
+            }
+            timer_stop(c, T_MESH_UPDATE);
+            cudaMemcpyAsync(c.h_flags, c.d_flags, F_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+            return check(c, "harten front");
+        }
+
+        // new mesh from the new cells and update_fields (mr/adapt.hpp:380-386)
+        int seq_back(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un)
+        {
+            const Geom& g = c.g;
+            int st        = build_mesh(c, nm);
+            if (st)
+            {
+                return st;
+            }
+            ScopedTimer tf(c, T_FIELDS_UPDATE);
+            if (g.dim == 2)
+            {
+                k_update_fields<2><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                                                                                            nm.cells, m.ref, m.cells, m.hc, uo, un);
+            }
+            else
+            {
+                k_update_fields<3><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                                                                                            nm.cells, m.ref, m.cells, m.hc, uo, un);
+            }
+            ++c.n_launches;
+            return check(c, "update_fields");
+        }
+    } // namespace
+
     int update_ghost_mr(Ctx& c, DeviceField& f)
     {
-        ScopedTimer timer(c, T_GHOST);
-        const Geom& g   = c.g;
-        DeviceMesh& m   = c.m();
-        const int minl  = c.cfg.min_level;
-        const int maxl  = c.cfg.max_level;
-        const int lmin  = minl >= 2 ? minl - 2 : 0; // no reference cell below min_level-2
-        double* u       = f.data;
-        const int ndiag = (g.dim == 2) ? 4 : 20;
         if (c.cfg.ghost_width != 1)
         {
             c.err = "update_ghost_mr: only a ghost width of 1 is implemented";
             return SG_ERR_ARG;
         }
-        for (int l = maxl; l >= lmin; --l)
-        {
-            GhostLevelArgs a{};
-            a.l            = l;
-            a.do_corners   = (l >= minl && l <= maxl) ? 1 : 0;
-            a.do_project   = l < maxl;
-            a.do_dirichlet = (l >= minl) && f.has_bc;
-            a.do_predict   = (l >= minl && l < maxl);
-            a.value        = f.bc_value;
-            a.nb_corner    = a.do_corners ? ndiag : 0;
-            const int n    = g.lv[l].n;
-            a.nfaces       = (a.do_project || a.do_dirichlet || a.do_predict)
-                                 ? static_cast<long long>(2 * g.dim) * ((g.dim == 2) ? n : static_cast<long long>(n) * n)
-                                 : 0;
-            a.nb_face      = static_cast<int>((a.nfaces + BLOCK - 1) / BLOCK);
-            if (l > lmin)
-            {
-                a.p_begin = m.lo_ref[l - 1];
-                a.p_end   = m.lo_ref[l];
-            }
-            const long long items = a.p_end - a.p_begin;
-            const int nb_proj     = items > 0 ? blocks_for_items(items) : 0;
-            const int grid        = a.nb_corner + a.nb_face + nb_proj;
-            if (grid > 0)
-            {
-                if (g.dim == 2)
-                {
-                    k_ghost_level<2><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.cells, m.uni, m.proj, m.ref, u);
-                }
-                else
-                {
-                    k_ghost_level<3><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.cells, m.uni, m.proj, m.ref, u);
-                }
-                ++c.n_launches;
-            }
-        }
-        for (int l = (lmin > 1 ? lmin : 1); l <= maxl; ++l)
-        {
-            const long long b = m.lo_ref[l], e = m.lo_ref[l + 1];
-            if (e > b)
-            {
-                if (g.dim == 2)
-                {
-                    k_predict<2><<<blocks_for_items(e - b), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, b, e, m.cells, m.proj, m.ref, u);
-                }
-                else
-                {
-                    k_predict<3><<<blocks_for_items(e - b), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, b, e, m.cells, m.proj, m.ref, u);
-                }
-                ++c.n_launches;
-            }
-        }
-        return check(c, "update_ghost_mr");
+        DeviceMesh& m = c.m();
+        double* u     = f.data;
+        return run_cached(c, 1, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
+                          [&]() { return seq_ghost(c, m, u, f.has_bc, f.bc_value); });
     }
 
     // Adapt::harten (mr/adapt.hpp:276-389) for one field
     int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged)
     {
-        const Geom& g  = c.g;
-        DeviceMesh& m  = c.m();
+        if (c.cfg.ghost_width != 1)
+        {
+            c.err = "harten: only a ghost width of 1 is implemented";
+            return SG_ERR_ARG;
+        }
         const int minl = c.cfg.min_level;
         const int maxl = c.cfg.max_level;
-        const int dim  = g.dim;
-        int st;
-
-        k_tag_init<<<blocks_for_items(m.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.lo_ref[g.nlev], m.ref, m.cells, c.tag, c.detail);
-        ++c.n_launches;
-        if ((st = check(c, "tag_init")))
+        const int dim  = c.g.dim;
+        DeviceMesh& m  = c.m();
+        DeviceMesh& nm = c.spare();
+        // the pinned inputs of the previous pass have been consumed: every
+        // pass ends with a synchronisation
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
-            return st;
+            return check(c, "harten sync");
         }
-        if ((st = update_ghost_mr(c, f)))
+        *c.h_ite = ite;
+        for (int l = 0; l < MAXLEV; ++l)
         {
-            return st;
+            c.h_eps[l] = c.h_eps[MAXLEV + l] = c.h_eps[2 * MAXLEV + l] = 0.;
         }
-
-        const int dl0 = minl > 0 ? minl - 1 : 0;
-        const int dl1 = maxl - ite - 1;
-        timer_start(c, T_DETAIL);
-        if (dl1 >= dl0 && m.lo_ref[dl1 + 1] > m.lo_ref[dl0])
-        {
-            const long long b = m.lo_ref[dl0], e_ = m.lo_ref[dl1 + 1];
-            if (g.dim == 2)
-            {
-                k_detail<2><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, b, e_, m.ref, m.hc, m.hc2, f.data,
-                                                                        c.detail);
-            }
-            else
-            {
-                k_detail<3><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, b, e_, m.ref, m.hc, m.hc2, f.data,
-                                                                        c.detail);
-            }
-            ++c.n_launches;
-        }
-        timer_stop(c, T_DETAIL);
-        timer_start(c, T_TAG);
-        double* e = c.h_eps;
-        cudaStreamSynchronize(c.stream); // h_eps may still feed an earlier copy
         for (int l = minl; l <= maxl - ite; ++l)
         {
-            const int exponent      = dim * (maxl - l);
-            e[l]                    = eps / (1 << exponent);
-            e[MAXLEV + l]           = std::pow(2.0, regularity + dim) * e[l];
-            e[2 * MAXLEV + l]       = e[MAXLEV + l] / (1 << dim);
+            const int exponent        = dim * (maxl - l);
+            c.h_eps[l]                = eps / (1 << exponent);
+            c.h_eps[MAXLEV + l]       = std::pow(2.0, regularity + dim) * c.h_eps[l];
+            c.h_eps[2 * MAXLEV + l]   = c.h_eps[MAXLEV + l] / (1 << dim);
         }
-        cudaMemcpyAsync(c.d_eps, e, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
-        const int cl0 = minl, cl1 = maxl - ite;
-        if (cl1 >= cl0 && cl0 >= 1 && m.lo_ref[cl1] > m.lo_ref[cl0 - 1])
+        double* u = f.data;
+        int st    = run_cached(c, 2, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
+                               [&]() { return seq_front(c, m, nm, u, f.has_bc, f.bc_value); });
+        if (st)
         {
-            const long long b = m.lo_ref[cl0 - 1], e_ = m.lo_ref[cl1];
-            if (g.dim == 2)
-            {
-                k_criteria<2><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, b, e_, m.ref, m.hc, c.detail, c.tag);
-            }
-            else
-            {
-                k_criteria<3><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, b, e_, m.ref, m.hc, c.detail, c.tag);
-            }
-            ++c.n_launches;
+            return st;
         }
-        timer_stop(c, T_TAG);
-        timer_start(c, T_FINALIZE);
-        for (int l = maxl; l > 0; --l)
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
-            const long long b = m.lo_ref[l - 1], e_ = m.lo_ref[l];
-            if (e_ > b)
+            return check(c, "harten front sync");
+        }
+        if (c.h_flags[F_GRAD1])
+        {
+            // graduation still refining after two passes: finish it with
+            // host-tested passes, then compare again
+            if ((st = graduate(c, nm.cells, nullptr)))
             {
-                if (g.dim == 2)
-                {
-                    k_maximum<2><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, b, e_, m.ref, m.hc, c.tag);
-                }
-                else
-                {
-                    k_maximum<3><<<blocks_for_items(e_ - b), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, b, e_, m.ref, m.hc, c.tag);
-                }
-                ++c.n_launches;
+                return st;
+            }
+            cudaMemsetAsync(c.d_flags + F_DIFFER, 0, sizeof(int), c.stream);
+            if ((st = bitmaps_differ(c, nm.cells, m.cells, F_DIFFER)))
+            {
+                return st;
+            }
+            cudaMemcpyAsync(c.h_flags + F_DIFFER, c.d_flags + F_DIFFER, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+            if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+            {
+                return check(c, "harten compare sync");
             }
         }
-        timer_stop(c, T_FINALIZE);
-        if ((st = check(c, "criteria")))
+        if (!c.h_flags[F_DIFFER])
         {
-            return st;
-        }
-
-        timer_start(c, T_MESH_UPDATE);
-        DeviceMesh& nm = c.spare();
-        if ((st = new_cells_from_tags(c, m, nm.cells)))
-        {
-            return st;
-        }
-        if ((st = graduate(c, nm.cells, nullptr)))
-        {
-            return st;
-        }
-        bool same = false;
-        if ((st = bitmaps_equal(c, nm.cells, m.cells, &same)))
-        {
-            return st;
-        }
-        if (same)
-        {
-            timer_stop(c, T_MESH_UPDATE);
             *converged = true;
             return SG_OK;
         }
         *converged = false;
-        if ((st = build_mesh(c, nm)))
+        st         = run_cached(c, 3, static_cast<unsigned long long>(c.cur), ptr_key(u), ptr_key(f.spare),
+                                [&]() { return seq_back(c, m, nm, u, f.spare); });
+        if (st)
         {
             return st;
         }
-        timer_stop(c, T_MESH_UPDATE);
-        ScopedTimer tf(c, T_FIELDS_UPDATE);
-        if (g.dim == 2)
-        {
-            k_update_fields<2><<<blocks_for_items(nm.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.lo_ref[g.nlev], nm.ref,
-                                                                                      nm.cells, m.ref, m.cells, m.hc, f.data, f.spare);
-        }
-        else
-        {
-            k_update_fields<3><<<blocks_for_items(nm.lo_ref[g.nlev]), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.lo_ref[g.nlev], nm.ref,
-                                                                                      nm.cells, m.ref, m.cells, m.hc, f.data, f.spare);
-        }
-        ++c.n_launches;
-        if ((st = check(c, "update_fields")))
-        {
-            return st;
-        }
+        nm.host_valid = false; // a replayed graph refreshed the counters without host code
         std::swap(f.data, f.spare);
         c.cur = 1 - c.cur;
         return SG_OK;
@@ -1006,9 +1161,8 @@ namespace sg
     int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme)
     {
         ScopedTimer timer(c, T_UPWIND);
-        const Geom& g = c.g;
+        const Geom& g       = c.g;
         const DeviceMesh& m = c.m();
-        const long long n   = m.lo_cells[g.nlev];
         UpwindArgs p{};
         for (int d = 0; d < g.dim; ++d)
         {
@@ -1017,13 +1171,14 @@ namespace sg
         }
         p.dt     = dt;
         p.scheme = scheme;
+        const int nb = blocks_words(g, 0, g.nlev - 1);
         if (g.dim == 2)
         {
-            k_upwind<2><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, p);
+            k_upwind<2><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p);
         }
         else
         {
-            k_upwind<3><<<blocks_for_items(n), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, n, m.cells, u.data, unp1.data, p);
+            k_upwind<3><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p);
         }
         ++c.n_launches;
         return check(c, "upwind");

@@ -195,7 +195,7 @@ namespace sg
             }
         }
 
-        __global__ void k_scan_top(long long* sums, long long nb, long long* counts)
+        __global__ void k_scan_top(long long* sums, long long nb, long long* counts, int nlev)
         {
             const long long per = (nb + blockDim.x - 1) / blockDim.x;
             const long long b0  = threadIdx.x * per;
@@ -224,6 +224,14 @@ namespace sg
                 if (threadIdx.x == 0)
                 {
                     counts[k] = tot;
+                    if (k == 1)
+                    {
+                        counts[LO_REF + nlev] = tot;
+                    }
+                    if (k == 3)
+                    {
+                        counts[LO_CELLS + nlev] = tot;
+                    }
                 }
             }
         }
@@ -250,8 +258,8 @@ namespace sg
                 {
                     if (g.lv[l].woff == w)
                     {
-                        counts[4 + l]              = off[1];
-                        counts[4 + (MAXLEV + 1) + l] = off[3];
+                        counts[LO_REF + l]   = off[1];
+                        counts[LO_CELLS + l] = off[3];
                     }
                 }
                 const uint32_t r = ref[w], c = cells[w];
@@ -275,29 +283,28 @@ namespace sg
         const long long n  = c.g.total_words;
         const long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
         k_scan_sums<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, m.cells, n, nb, c.block_sums);
-        k_scan_top<<<1, 1024, 0, c.stream>>>(c.block_sums, nb, c.d_counts);
+        k_scan_top<<<1, 1024, 0, c.stream>>>(c.block_sums, nb, m.d_lo, c.g.nlev);
         k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(c.d_geom, m.ref, m.cells, n, nb, c.block_sums, m.rank, m.wl_ref, m.wl_cells,
-                                                                          c.d_counts);
+                                                                          m.d_lo);
         c.n_launches += 3;
-        int st = check(c, "scan_rank");
-        if (st)
+        cudaMemcpyAsync(m.h_lo, m.d_lo, COUNTS * sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
+        m.host_valid = false;
+        return check(c, "scan_rank");
+    }
+
+    int host_counts(Ctx& c, DeviceMesh& m)
+    {
+        if (m.host_valid)
         {
-            return st;
+            return SG_OK;
         }
-        cudaMemcpyAsync(c.h_counts, c.d_counts, COUNTS * sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
         if (cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
-            return check(c, "scan_rank sync");
+            return check(c, "host_counts");
         }
-        m.nb_ref   = c.h_counts[0];
-        m.nb_cells = c.h_counts[2];
-        for (int l = 0; l < c.g.nlev; ++l)
-        {
-            m.lo_ref[l]   = c.h_counts[4 + l];
-            m.lo_cells[l] = c.h_counts[4 + (MAXLEV + 1) + l];
-        }
-        m.lo_ref[c.g.nlev]   = c.h_counts[1];
-        m.lo_cells[c.g.nlev] = c.h_counts[3];
+        m.nb_ref     = m.h_lo[0];
+        m.nb_cells   = m.h_lo[2];
+        m.host_valid = true;
         if (m.nb_ref >= (1LL << 31))
         {
             c.err = "reference mesh exceeds 2^31 cells";
@@ -549,14 +556,15 @@ namespace sg
                             "new_cells");
     }
 
-    // make_graduation (algorithm/graduation.hpp:573-726, 245-330): the cells
-    // of level l that lie under the (2*grad_width)-expansion of a leaf cell
-    // two or more levels finer are refined, until a fixed point.  The
-    // contiguous-boundary pass (graduation.hpp:121-249) is a no-op for a
-    // max_stencil_radius of 1.
-    int graduate(Ctx& c, uint32_t* nc, int* iterations)
+    // One pass of make_graduation (algorithm/graduation.hpp:573-726,
+    // 245-330): the cells of level l that lie under the
+    // (2*grad_width)-expansion of a leaf cell two or more levels finer are
+    // refined.  flag[slot] is set when the pass refined something.  A pass
+    // that finds nothing leaves the cells unchanged, so extra passes after the
+    // fixed point are no-ops.  The contiguous-boundary pass
+    // (graduation.hpp:121-249) is a no-op for a max_stencil_radius of 1.
+    int grad_pass(Ctx& c, uint32_t* nc, int slot)
     {
-        ScopedTimer timer(c, T_GRADUATION);
         const Geom g   = c.g;
         const int top  = g.nlev - 1;
         const int maxl = c.cfg.max_level;
@@ -565,74 +573,85 @@ namespace sg
         uint32_t* ec1  = c.t1;
         uint32_t* d    = c.t2;
         uint32_t* rr   = c.t3;
-        int* flag      = c.d_flags;
+        int* flag      = c.d_flags + slot;
         const size_t bytes = static_cast<size_t>(g.total_words) * 4;
-        int nit        = 0;
+        int st = launch_words(c, 0, top,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = box_dilate_word(g, nc, l, row, wi, gw2); },
+                              "grad_expand");
+        if (st)
+        {
+            return st;
+        }
+        st = launch_words(c, 0, top,
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                          { ec1[w] = (l + 1 < g.nlev) ? coarsen_word(g, e, l, row, wi) : 0u; },
+                          "grad_coarsen");
+        if (st)
+        {
+            return st;
+        }
+        cudaMemsetAsync(d, 0, bytes, c.stream);
+        cudaMemsetAsync(rr, 0, bytes, c.stream);
+        // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. 0
+        for (int l = maxl - 2; l >= 0; --l)
+        {
+            st = launch_words(c, l, l,
+                              [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
+                              {
+                                  const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | coarsen_word(g, d, ll, row, wi);
+                                  d[w]              = dv;
+                                  const uint32_t rv = nc[w] & dv;
+                                  rr[w]             = rv;
+                                  if (rv)
+                                  {
+                                      atomicOr(flag, 1);
+                                  }
+                              },
+                              "grad_down");
+            if (st)
+            {
+                return st;
+            }
+        }
+        return launch_words(c, 0, top,
+                            [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                            {
+                                const uint32_t r = rr[w];
+                                uint32_t v       = nc[w] & ~r;
+                                if (l >= 1)
+                                {
+                                    v |= refine_word(g, rr, l, row, wi);
+                                }
+                                if (v != nc[w])
+                                {
+                                    nc[w] = v;
+                                }
+                            },
+                            "grad_apply");
+    }
+
+    // make_graduation to the fixed point, with a host test after each pass
+    int graduate(Ctx& c, uint32_t* nc, int* iterations)
+    {
+        ScopedTimer timer(c, T_GRADUATION);
+        int nit = 0;
         for (;;)
         {
             ++nit;
-            int st = launch_words(c, 0, top,
-                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = box_dilate_word(g, nc, l, row, wi, gw2); },
-                                  "grad_expand");
+            cudaMemsetAsync(c.d_flags + F_GRADX, 0, sizeof(int), c.stream);
+            int st = grad_pass(c, nc, F_GRADX);
             if (st)
             {
                 return st;
             }
-            st = launch_words(c, 0, top,
-                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                              { ec1[w] = (l + 1 < g.nlev) ? coarsen_word(g, e, l, row, wi) : 0u; },
-                              "grad_coarsen");
-            if (st)
-            {
-                return st;
-            }
-            cudaMemsetAsync(d, 0, bytes, c.stream);
-            cudaMemsetAsync(rr, 0, bytes, c.stream);
-            cudaMemsetAsync(flag, 0, sizeof(int), c.stream);
-            // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. 0
-            for (int l = maxl - 2; l >= 0; --l)
-            {
-                st = launch_words(c, l, l,
-                                  [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
-                                  {
-                                      const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | coarsen_word(g, d, ll, row, wi);
-                                      d[w]              = dv;
-                                      const uint32_t rv = nc[w] & dv;
-                                      rr[w]             = rv;
-                                      if (rv)
-                                      {
-                                          atomicOr(flag, 1);
-                                      }
-                                  },
-                                  "grad_down");
-                if (st)
-                {
-                    return st;
-                }
-            }
-            cudaMemcpyAsync(c.h_flags, flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+            cudaMemcpyAsync(c.h_flags + F_GRADX, c.d_flags + F_GRADX, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
             if (cudaStreamSynchronize(c.stream) != cudaSuccess)
             {
                 return check(c, "graduate sync");
             }
-            if (!c.h_flags[0])
+            if (!c.h_flags[F_GRADX])
             {
                 break;
-            }
-            st = launch_words(c, 0, top,
-                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                              {
-                                  uint32_t v = nc[w] & ~rr[w];
-                                  if (l >= 1)
-                                  {
-                                      v |= refine_word(g, rr, l, row, wi);
-                                  }
-                                  nc[w] = v;
-                              },
-                              "grad_apply");
-            if (st)
-            {
-                return st;
             }
             if (nit > 64)
             {
@@ -647,29 +666,19 @@ namespace sg
         return SG_OK;
     }
 
-    int bitmaps_equal(Ctx& c, const uint32_t* a, const uint32_t* b, bool* equal)
+    // flag[slot] = (a != b), without synchronisation
+    int bitmaps_differ(Ctx& c, const uint32_t* a, const uint32_t* b, int slot)
     {
-        int* flag = c.d_flags;
-        cudaMemsetAsync(flag, 0, sizeof(int), c.stream);
-        int st = launch_words(c, 0, c.g.nlev - 1,
-                              [=] __device__(const Geom&, int, long long w, long long, int)
-                              {
-                                  if (a[w] != b[w])
-                                  {
-                                      atomicOr(flag, 1);
-                                  }
-                              },
-                              "compare");
-        if (st)
-        {
-            return st;
-        }
-        cudaMemcpyAsync(c.h_flags, flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
-        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
-        {
-            return check(c, "compare sync");
-        }
-        *equal = c.h_flags[0] == 0;
-        return SG_OK;
+        int* flag = c.d_flags + slot;
+        return launch_words(c, 0, c.g.nlev - 1,
+                            [=] __device__(const Geom&, int, long long w, long long, int)
+                            {
+                                if (a[w] != b[w])
+                                {
+                                    atomicOr(flag, 1);
+                                }
+                            },
+                            "compare");
     }
+
 } // namespace sg
