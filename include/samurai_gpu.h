@@ -121,6 +121,14 @@ int sg_upwind(sg_field_t u, sg_field_t unp1, const double* a, double dt, int sch
 int sg_detail_download(sg_field_t u, double* values, long long n);
 int sg_tag_download(sg_field_t u, unsigned char* values, long long n);
 
+/* u.array() to host memory without allocating anything (no counterpart in the reference: samurai has no
+ * C interface).  For callers that cannot let a library allocate device memory, e.g. a process whose device
+ * memory is reserved by another allocator.  Same output as sg_field_download, through a static 16 MiB device
+ * array instead of an allocated staging buffer: meshes beyond 2^21 reference cells are rejected with
+ * SG_ERR_CAPACITY.  The first call on a device sets the array up (make it before any stream capture); calls
+ * share the array, so calls that overlap on the GPU race. */
+int sg_field_download_noalloc(sg_field_t field, double* values, long long n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,7 @@ def lib():
         "sg_field_set_dirichlet": (i, [vp, d]),
         "sg_field_upload": (i, [vp, vp, ll]),
         "sg_field_download": (i, [vp, vp, ll]),
+        "sg_field_download_noalloc": (i, [vp, vp, ll]),
         "sg_field_upload_device": (i, [vp, vp, ll]),
         "sg_field_download_device": (i, [vp, vp, ll]),
         "sg_field_set_cells": (i, [vp, vp, ll]),

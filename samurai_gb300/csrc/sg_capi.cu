@@ -1,4 +1,5 @@
 // C ABI of libsamurai_gpu.so (declared in include/samurai_gpu.h).
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -7,34 +8,38 @@
 #include "../../include/samurai_gpu.h"
 #include "sg_ctx.cuh"
 
-struct sg_mesh_s
-{
-    sg::Ctx ctx;
-    double* staging     = nullptr; // compact host<->device staging (nb_ref doubles)
-    long long staging_n = 0;
-};
-
-struct sg_field_s
-{
-    sg_mesh_s* mesh = nullptr;
-    sg::DeviceField f;
-};
+#include "sg_handles.cuh"
 
 namespace
 {
-    thread_local std::string g_err;
+    // per-thread message of the last failure; a fixed buffer, so that
+    // reporting an error never allocates
+    thread_local char g_err[512] = "";
 
-    int fail(int code, const std::string& msg)
+    int fail(int code, const char* msg, const char* detail = nullptr)
     {
-        g_err = msg;
+        std::snprintf(g_err, sizeof(g_err), "%s%s", msg ? msg : "", detail ? detail : "");
         return code;
     }
 
+} // namespace
+
+namespace sg
+{
+    // the C ABI's error text, for entry points defined in other files
+    void set_last_error(const char* msg, const char* detail)
+    {
+        fail(0, msg, detail);
+    }
+}
+
+namespace
+{
     int from_ctx(sg::Ctx& c, int st)
     {
         if (st != sg::SG_OK)
         {
-            g_err = c.err.empty() ? "error" : c.err;
+            fail(st, c.err.empty() ? "error" : c.err.c_str());
         }
         return st;
     }
@@ -263,7 +268,7 @@ extern "C"
 {
     const char* sg_last_error(void)
     {
-        return g_err.c_str();
+        return g_err;
     }
 
     int sg_version(int* major, int* minor)
@@ -362,7 +367,7 @@ extern "C"
         {
             std::string msg = c.err;
             destroy_ctx(h);
-            return fail(SG_ERR_CUDA, "sg_mesh_create: " + msg);
+            return fail(SG_ERR_CUDA, "sg_mesh_create: ", msg.c_str());
         }
         cudaMemcpyAsync(c.d_geom, &c.g, sizeof(sg::Geom), cudaMemcpyHostToDevice, c.stream);
         for (int k = 0; k < 2; ++k)
@@ -385,7 +390,7 @@ extern "C"
         {
             std::string msg = c.err;
             destroy_ctx(h);
-            return fail(st, "sg_mesh_create: " + msg);
+            return fail(st, "sg_mesh_create: ", msg.c_str());
         }
         *out = h;
         return SG_OK;
@@ -636,7 +641,7 @@ extern "C"
         cudaError_t e = cudaStreamSynchronize(mesh->ctx.stream);
         if (e != cudaSuccess)
         {
-            return fail(SG_ERR_CUDA, std::string("sg_mesh_synchronize: ") + cudaGetErrorString(e));
+            return fail(SG_ERR_CUDA, "sg_mesh_synchronize: ", cudaGetErrorString(e));
         }
         return from_ctx(mesh->ctx, sg::device_error(mesh->ctx));
     }
@@ -689,7 +694,7 @@ extern "C"
         cudaError_t err = cudaGetLastError();
         if (err != cudaSuccess)
         {
-            return fail(SG_ERR_CUDA, std::string("sg_device_fp64_rate: ") + cudaGetErrorString(err));
+            return fail(SG_ERR_CUDA, "sg_device_fp64_rate: ", cudaGetErrorString(err));
         }
         const double ops = 2.0 * 8.0 * iters * static_cast<double>(blocks) * threads;
         *gflops          = ops / (ms * 1e-3) / 1e9;
@@ -756,7 +761,7 @@ extern "C"
         if (dalloc(mesh->ctx, &f->f.data, static_cast<size_t>(mesh->ctx.capacity)))
         {
             delete f;
-            return fail(SG_ERR_CUDA, "sg_field_create: " + mesh->ctx.err);
+            return fail(SG_ERR_CUDA, "sg_field_create: ", mesh->ctx.err.c_str());
         }
         cudaMemsetAsync(f->f.data, 0, static_cast<size_t>(mesh->ctx.capacity) * sizeof(double), mesh->ctx.stream);
         *out = f;

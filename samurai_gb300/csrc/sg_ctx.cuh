@@ -162,6 +162,8 @@ namespace sg
     int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten);
     int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme);
     int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact);
+    cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact); // no error text
+    cudaError_t read_device_error(Ctx& c, int* v);                                                  // reads and clears
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense);
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value);
     int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged);

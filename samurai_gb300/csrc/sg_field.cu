@@ -765,11 +765,37 @@ namespace sg
         }
     } // namespace
 
-    int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
+    cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
     {
         k_gather<<<blocks_words(c.g, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
         ++c.n_launches;
-        return check(c, "gather");
+        return cudaGetLastError();
+    }
+
+    int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
+    {
+        if (launch_gather(c, m, dense, compact) != cudaSuccess)
+        {
+            c.err = "gather: kernel launch failed";
+            return SG_ERR_CUDA;
+        }
+        return SG_OK;
+    }
+
+    cudaError_t read_device_error(Ctx& c, int* v)
+    {
+        *v            = 0;
+        cudaError_t e = cudaMemcpyFromSymbolAsync(v, sg_device_error, sizeof(int), 0, cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess)
+        {
+            e = cudaStreamSynchronize(c.stream);
+        }
+        if (e == cudaSuccess && *v)
+        {
+            const int zero = 0;
+            e              = cudaMemcpyToSymbolAsync(sg_device_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, c.stream);
+        }
+        return e;
     }
 
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense)
