@@ -123,6 +123,7 @@ namespace sg
         int* d_ite          = nullptr; // Harten pass index seen by the detail/criteria kernels
         int* h_ite          = nullptr; // pinned staging
         bool use_graphs     = true;    // replay captured launch sequences
+        int fuse_top        = -1;      // levels 0..fuse_top are small enough for one-block chains
         struct GraphEntry
         {
             unsigned long long key[4];
@@ -190,6 +191,25 @@ namespace sg
             timer_stop(c, id);
         }
     };
+
+    // A level-serial chain (union, reference children, graduation, tag
+    // finalisation, ghost passes) runs its levels of at most FUSE_WORDS words
+    // in a single block that steps through them with __syncthreads(), instead
+    // of one launch per level.
+    constexpr long long FUSE_WORDS = 16384;
+
+    inline int fuse_top_of(const Geom& g)
+    {
+        int t = -1;
+        for (int l = 0; l < g.nlev; ++l)
+        {
+            if (g.lv[l].nwords <= FUSE_WORDS)
+            {
+                t = l;
+            }
+        }
+        return t;
+    }
 
     // blocks of 256 threads (8 warps) for a warp-per-item loop over at most
     // max_items list entries: one wave of resident warps at most

@@ -299,101 +299,83 @@ namespace sg
         //  - projection of the reference cells of level l onto proj_cells[l-1]
         //    (numeric/projection.hpp:15-65).
         template <int DIM>
-        __global__ void k_ghost_level(const Geom* __restrict__ gp, GhostLevelArgs a, const int* wl_ref, const long long* lo, const uint32_t* cells,
-                                      const uint32_t* uni,
-                                      const uint32_t* proj, const uint32_t* ref, double* u)
+        __device__ __forceinline__ void face_work(const Geom& g, const GhostLevelArgs& a, long long t, const uint32_t* cells, const uint32_t* uni,
+                                                  const uint32_t* ref, double* u)
         {
-            const Geom& g = *gp;
-            const int l = a.l;
-            if (static_cast<int>(blockIdx.x) < a.nb_corner)
+            const int l        = a.l;
+            const int n        = g.lv[l].n;
+            const long long nf = (DIM == 2) ? n : static_cast<long long>(n) * n;
+            const int k        = static_cast<int>(t / nf);
+            int in[3], dir[3];
+            face_cell(g, l, k, t - k * nf, in, dir);
+            const Pos pi = pos_of(g, l, in[0], in[1], in[2]);
+            const int gx = in[0] + dir[0], gy = in[1] + dir[1], gz = in[2] + dir[2];
+            if ((a.do_dirichlet || a.do_predict) && test(cells, pi))
             {
-                int d[3];
-                diagonal_dir(DIM, static_cast<int>(blockIdx.x), d);
-                corner_role(g, d, l, cells, ref, u);
-                return;
+                const long long eg = elem_at(g, l, gx, gy, gz);
+                if (a.do_dirichlet)
+                {
+                    u[eg] = 2 * a.value - u[elem(pi)];
+                }
+                if (a.do_predict)
+                {
+                    const double v = u[eg];
+                    for (int sz = 0; sz < (DIM == 3 ? 2 : 1); ++sz)
+                    {
+                        for (int sy = 0; sy < 2; ++sy)
+                        {
+                            for (int sx = 0; sx < 2; ++sx)
+                            {
+                                const Pos pf = pos_of(g, l + 1, 2 * gx + sx, 2 * gy + sy, DIM == 3 ? 2 * gz + sz : 0);
+                                if (test(ref, pf))
+                                {
+                                    u[elem(pf)] = v;
+                                }
+                            }
+                        }
+                    }
+                }
             }
-            if (static_cast<int>(blockIdx.x) < a.nb_corner + a.nb_face)
+            else if (a.do_project && test(uni, pi))
             {
-                const long long t = static_cast<long long>(blockIdx.x - a.nb_corner) * blockDim.x + threadIdx.x;
-                if (t >= a.nfaces)
+                const Pos pg = pos_of(g, l, gx, gy, gz);
+                if (!test(ref, pg))
                 {
                     return;
                 }
-                const int n        = g.lv[l].n;
-                const long long nf = (DIM == 2) ? n : static_cast<long long>(n) * n;
-                const int k        = static_cast<int>(t / nf);
-                int in[3], dir[3];
-                face_cell(g, l, k, t - k * nf, in, dir);
-                const Pos pi = pos_of(g, l, in[0], in[1], in[2]);
-                const int gx = in[0] + dir[0], gy = in[1] + dir[1], gz = in[2] + dir[2];
-                if ((a.do_dirichlet || a.do_predict) && test(cells, pi))
+                double sum = 0.;
+                int nch    = 0;
+                for (int dl = 1; dl <= 2 && nch == 0 && l + dl < g.nlev; ++dl)
                 {
-                    const long long eg = elem_at(g, l, gx, gy, gz);
-                    if (a.do_dirichlet)
+                    const int lc = l + dl;
+                    const int m  = 1 << dl;
+                    for (int sz = 0; sz < (DIM == 3 ? m : 1); ++sz)
                     {
-                        u[eg] = 2 * a.value - u[elem(pi)];
-                    }
-                    if (a.do_predict)
-                    {
-                        const double v = u[eg];
-                        for (int sz = 0; sz < (DIM == 3 ? 2 : 1); ++sz)
+                        for (int sy = 0; sy < m; ++sy)
                         {
-                            for (int sy = 0; sy < 2; ++sy)
+                            for (int sx = 0; sx < m; ++sx)
                             {
-                                for (int sx = 0; sx < 2; ++sx)
+                                const Pos pc = pos_of(g, lc, gx * m + sx, gy * m + sy, DIM == 3 ? gz * m + sz : 0);
+                                if (test(ref, pc))
                                 {
-                                    const Pos pf = pos_of(g, l + 1, 2 * gx + sx, 2 * gy + sy, DIM == 3 ? 2 * gz + sz : 0);
-                                    if (test(ref, pf))
-                                    {
-                                        u[elem(pf)] = v;
-                                    }
+                                    sum = sum + u[elem(pc)];
+                                    ++nch;
                                 }
                             }
                         }
                     }
                 }
-                else if (a.do_project && test(uni, pi))
-                {
-                    const Pos pg = pos_of(g, l, gx, gy, gz);
-                    if (!test(ref, pg))
-                    {
-                        return;
-                    }
-                    double sum = 0.;
-                    int nch    = 0;
-                    for (int dl = 1; dl <= 2 && nch == 0 && l + dl < g.nlev; ++dl)
-                    {
-                        const int lc = l + dl;
-                        const int m  = 1 << dl;
-                        for (int sz = 0; sz < (DIM == 3 ? m : 1); ++sz)
-                        {
-                            for (int sy = 0; sy < m; ++sy)
-                            {
-                                for (int sx = 0; sx < m; ++sx)
-                                {
-                                    const Pos pc = pos_of(g, lc, gx * m + sx, gy * m + sy, DIM == 3 ? gz * m + sz : 0);
-                                    if (test(ref, pc))
-                                    {
-                                        sum = sum + u[elem(pc)];
-                                        ++nch;
-                                    }
-                                }
-                            }
-                        }
-                    }
-                    u[elem(pg)] = nch > 0 ? sum / static_cast<double>(nch) : 0.;
-                }
-                return;
+                u[elem(pg)] = nch > 0 ? sum / static_cast<double>(nch) : 0.;
             }
-            // projection role
-            const int lc              = l - 1;
-            const long long rb        = static_cast<long long>(blockIdx.x - a.nb_corner - a.nb_face);
-            const long long warp0     = (rb * blockDim.x + threadIdx.x) >> 5;
-            const long long nwarps    = (static_cast<long long>(gridDim.x - a.nb_corner - a.nb_face) * blockDim.x) >> 5;
-            if (!a.do_proj)
-            {
-                return;
-            }
+        }
+
+        // projection of the reference cells of level l onto proj_cells[l-1]
+        // (numeric/projection.hpp:15-65), warps warp0, warp0+nwarps, ...
+        template <int DIM>
+        __device__ __forceinline__ void project_level(const Geom& g, int l, const int* wl_ref, const long long* lo, const uint32_t* proj, const uint32_t* ref,
+                                                      double* u, long long warp0, long long nwarps)
+        {
+            const int lc = l - 1;
             warp_list(wl_ref, lo[LO_REF + lc], lo[LO_REF + lc + 1], warp0, nwarps,
                       [&](long long w)
                       {
@@ -410,11 +392,10 @@ namespace sg
         // prediction of the ghosts of level l from level l-1
         // (algorithm/update_ghost_mr.hpp:224-233)
         template <int DIM>
-        __global__ void k_predict(const Geom* __restrict__ gp, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells, const uint32_t* proj,
-                                  const uint32_t* ref, double* u)
+        __device__ __forceinline__ void predict_level(const Geom& g, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
+                                                      const uint32_t* proj, const uint32_t* ref, double* u, long long warp0, long long nwarps)
         {
-            const Geom& g = *gp;
-            warp_list(wl_ref, lo[LO_REF + l], lo[LO_REF + l + 1], warp_id(), warp_count(),
+            warp_list(wl_ref, lo[LO_REF + l], lo[LO_REF + l + 1], warp0, nwarps,
                       [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, l, w);
@@ -425,6 +406,122 @@ namespace sg
                           const Cell c  = cell_of(g, l, w, b);
                           u[32 * w + b] = predict_one(g, u, l, c.x, c.y, c.z, order);
                       });
+        }
+
+        // One launch per level of the top-down pass of update_ghost_mr
+        // (algorithm/update_ghost_mr.hpp:206-222).  Within a level the
+        // reference's operations touch disjoint cells and read only cells
+        // finalised earlier, so they run concurrently as block roles:
+        //  - corners: outer corners and their projection two levels down;
+        //  - faces: per Cartesian direction, the Dirichlet ghost 2v - u
+        //    (bc/dirichlet.hpp:22-29) then predict_bc to level l+1
+        //    (update_outer_ghost.hpp:195-266) by the same thread, or project_bc
+        //    (update_outer_ghost.hpp:20-155) next to union cells;
+        //  - projection of the reference cells of level l onto proj_cells[l-1].
+        template <int DIM>
+        __global__ void k_ghost_level(const Geom* __restrict__ gp, GhostLevelArgs a, const int* wl_ref, const long long* lo, const uint32_t* cells,
+                                      const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, double* u)
+        {
+            const Geom& g = *gp;
+            const int l   = a.l;
+            if (static_cast<int>(blockIdx.x) < a.nb_corner)
+            {
+                int d[3];
+                diagonal_dir(DIM, static_cast<int>(blockIdx.x), d);
+                corner_role(g, d, l, cells, ref, u);
+                return;
+            }
+            if (static_cast<int>(blockIdx.x) < a.nb_corner + a.nb_face)
+            {
+                const long long t = static_cast<long long>(blockIdx.x - a.nb_corner) * blockDim.x + threadIdx.x;
+                if (t < a.nfaces)
+                {
+                    face_work<DIM>(g, a, t, cells, uni, ref, u);
+                }
+                return;
+            }
+            if (!a.do_proj)
+            {
+                return;
+            }
+            const long long rb     = static_cast<long long>(blockIdx.x - a.nb_corner - a.nb_face);
+            const long long warp0  = (rb * blockDim.x + threadIdx.x) >> 5;
+            const long long nwarps = (static_cast<long long>(gridDim.x - a.nb_corner - a.nb_face) * blockDim.x) >> 5;
+            project_level<DIM>(g, l, wl_ref, lo, proj, ref, u, warp0, nwarps);
+        }
+
+        struct GhostChainArgs
+        {
+            int l_hi, l_lo; // levels of the chain, walked from l_hi down to l_lo
+            int lmin;       // lowest level holding reference cells
+            int has_bc;
+            double value;
+        };
+
+        // The small levels of the top-down pass in one block: the roles of
+        // k_ghost_level one level after the other.
+        template <int DIM>
+        __global__ void __launch_bounds__(1024, 1) k_ghost_levels_small(const Geom* __restrict__ gp, GhostChainArgs ca, const int* wl_ref, const long long* lo, const uint32_t* cells,
+                                             const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, double* u)
+        {
+            const Geom& g         = *gp;
+            const int minl        = g.min_level, maxl = g.max_level;
+            const int ndiag       = (DIM == 2) ? 4 : 20;
+            const long long warp0 = threadIdx.x >> 5;
+            const long long nw    = blockDim.x >> 5;
+            for (int l = ca.l_hi; l >= ca.l_lo; --l)
+            {
+                GhostLevelArgs a{};
+                a.l            = l;
+                a.do_project   = l < maxl;
+                a.do_dirichlet = (l >= minl) && ca.has_bc;
+                a.do_predict   = (l >= minl && l < maxl);
+                a.value        = ca.value;
+                if (l >= minl && l <= maxl)
+                {
+                    for (int k = 0; k < ndiag; ++k)
+                    {
+                        int d[3];
+                        diagonal_dir(DIM, k, d);
+                        corner_role(g, d, l, cells, ref, u);
+                    }
+                }
+                if (a.do_project || a.do_dirichlet || a.do_predict)
+                {
+                    const int n              = g.lv[l].n;
+                    const long long nfaces   = static_cast<long long>(2 * DIM) * ((DIM == 2) ? n : static_cast<long long>(n) * n);
+                    for (long long t = threadIdx.x; t < nfaces; t += blockDim.x)
+                    {
+                        face_work<DIM>(g, a, t, cells, uni, ref, u);
+                    }
+                }
+                if (l > ca.lmin)
+                {
+                    project_level<DIM>(g, l, wl_ref, lo, proj, ref, u, warp0, nw);
+                }
+                __syncthreads();
+            }
+        }
+
+        template <int DIM>
+        __global__ void k_predict(const Geom* __restrict__ gp, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
+                                  const uint32_t* proj, const uint32_t* ref, double* u)
+        {
+            predict_level<DIM>(*gp, l, order, wl_ref, lo, cells, proj, ref, u, warp_id(), warp_count());
+        }
+
+        // the small levels of the bottom-up pass in one block
+        template <int DIM>
+        __global__ void __launch_bounds__(1024, 1) k_predict_small(const Geom* __restrict__ gp, int l_lo, int l_hi, int order, const int* wl_ref, const long long* lo,
+                                        const uint32_t* cells, const uint32_t* proj, const uint32_t* ref, double* u)
+        {
+            const long long warp0 = threadIdx.x >> 5;
+            const long long nw    = blockDim.x >> 5;
+            for (int l = l_lo; l <= l_hi; ++l)
+            {
+                predict_level<DIM>(*gp, l, order, wl_ref, lo, cells, proj, ref, u, warp0, nw);
+                __syncthreads();
+            }
         }
 
         // -------------------------------------------------------- details
@@ -556,12 +653,12 @@ namespace sg
 
         // maximum_op (mr/operators.hpp:22-96), children at level l
         template <int DIM>
-        __global__ void k_maximum(const Geom* __restrict__ gp, int l, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
-                                  uint8_t* tag)
+        __device__ __forceinline__ void maximum_level(const Geom& g, int l, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
+                                                      uint8_t* tag, long long warp0, long long nwarps)
         {
-            const Geom& g = *gp;
             const int lc = l - 1;
-            warp_list(wl, lo[LO_REF + lc], lo[LO_REF + l], warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
+            warp_list(wl, lo[LO_REF + lc], lo[LO_REF + l], warp0, nwarps,
+                      [&](long long w) { return ref[w] & hc[w]; },
                       [&](long long w, int b)
                       {
                           const Cell c  = cell_of(g, lc, w, b);
@@ -595,6 +692,27 @@ namespace sg
                               }
                           }
                       });
+        }
+
+        template <int DIM>
+        __global__ void k_maximum(const Geom* __restrict__ gp, int l, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
+                                  uint8_t* tag)
+        {
+            maximum_level<DIM>(*gp, l, wl, lo, ref, hc, tag, warp_id(), warp_count());
+        }
+
+        // the small levels of the tag finalisation in one block, l_hi down to 1
+        template <int DIM>
+        __global__ void __launch_bounds__(1024, 1) k_maximum_small(const Geom* __restrict__ gp, int l_hi, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
+                                        uint8_t* tag)
+        {
+            const long long warp0 = threadIdx.x >> 5;
+            const long long nw    = blockDim.x >> 5;
+            for (int l = l_hi; l >= 1; --l)
+            {
+                maximum_level<DIM>(*gp, l, wl, lo, ref, hc, tag, warp0, nw);
+                __syncthreads();
+            }
         }
 
         // update_fields (algorithm/update_fields.hpp:27-127): copy on
@@ -902,7 +1020,9 @@ namespace sg
             const int maxl  = c.cfg.max_level;
             const int lmin  = minl >= 2 ? minl - 2 : 0; // no reference cell below min_level-2
             const int ndiag = (g.dim == 2) ? 4 : 20;
-            for (int l = maxl; l >= lmin; --l)
+            const int ft = c.fuse_top;
+            int l        = maxl;
+            for (; l >= lmin && l - 1 > ft; --l)
             {
                 GhostLevelArgs a{};
                 a.l            = l;
@@ -933,17 +1053,46 @@ namespace sg
                     ++c.n_launches;
                 }
             }
-            for (int l = (lmin > 1 ? lmin : 1); l <= maxl; ++l)
+            if (l >= lmin)
             {
+                GhostChainArgs ca{l, lmin, lmin, has_bc ? 1 : 0, bcv};
                 if (g.dim == 2)
                 {
-                    k_predict<2><<<blocks_words(g, l, l), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
-                                                                                 m.ref, u);
+                    k_ghost_levels_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                 }
                 else
                 {
-                    k_predict<3><<<blocks_words(g, l, l), BLOCK, 0, c.stream>>>(c.d_geom, l, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
-                                                                                 m.ref, u);
+                    k_ghost_levels_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                }
+                ++c.n_launches;
+            }
+            const int lp0 = lmin > 1 ? lmin : 1;
+            int lp        = lp0;
+            if (lp <= maxl && lp <= ft)
+            {
+                const int e = maxl < ft ? maxl : ft;
+                if (g.dim == 2)
+                {
+                    k_predict_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                }
+                else
+                {
+                    k_predict_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                }
+                ++c.n_launches;
+                lp = e + 1;
+            }
+            for (; lp <= maxl; ++lp)
+            {
+                if (g.dim == 2)
+                {
+                    k_predict<2><<<blocks_words(g, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                                                                                   m.ref, u);
+                }
+                else
+                {
+                    k_predict<3><<<blocks_words(g, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                                                                                   m.ref, u);
                 }
                 ++c.n_launches;
             }
@@ -1008,17 +1157,32 @@ namespace sg
             timer_stop(c, T_TAG);
 
             timer_start(c, T_FINALIZE);
-            for (int l = maxl; l > 0; --l)
             {
-                if (g.dim == 2)
+                int l = maxl;
+                for (; l > 0 && l - 1 > c.fuse_top; --l)
                 {
-                    k_maximum<2><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                    if (g.dim == 2)
+                    {
+                        k_maximum<2><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                    }
+                    else
+                    {
+                        k_maximum<3><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                    }
+                    ++c.n_launches;
                 }
-                else
+                if (l > 0)
                 {
-                    k_maximum<3><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                    if (g.dim == 2)
+                    {
+                        k_maximum_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                    }
+                    else
+                    {
+                        k_maximum_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                    }
+                    ++c.n_launches;
                 }
-                ++c.n_launches;
             }
             timer_stop(c, T_FINALIZE);
             if ((st = check(c, "criteria")))

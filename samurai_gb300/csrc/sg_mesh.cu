@@ -91,6 +91,81 @@ namespace sg
             }
         }
 
+        // one block walks the levels l_first -> l_last (either direction)
+        template <class F>
+        __global__ void __launch_bounds__(1024, 1) k_words_chain(const Geom* __restrict__ gp, int l_first, int l_last, F f)
+        {
+            const Geom& g  = *gp;
+            const int step = l_last >= l_first ? 1 : -1;
+            for (int l = l_first;; l += step)
+            {
+                const LevelGeom& L = g.lv[l];
+                for (long long k = threadIdx.x; k < L.nwords; k += blockDim.x)
+                {
+                    const long long w   = L.woff + k;
+                    const long long row = k / L.W;
+                    f(g, l, w, row, static_cast<int>(k - row * L.W));
+                }
+                __syncthreads();
+                if (l == l_last)
+                {
+                    break;
+                }
+            }
+        }
+
+        template <class F>
+        int launch_words(Ctx& c, int l0, int l1, F f, const char* what);
+
+        // the levels l_first -> l_last one after the other: the large ones by
+        // separate launches, the small ones (<= fuse_top) by one block
+        template <class F>
+        int launch_chain(Ctx& c, int l_first, int l_last, F f, const char* what)
+        {
+            const int ft = c.fuse_top;
+            int st       = SG_OK;
+            if (l_first >= l_last)
+            {
+                int l = l_first;
+                for (; l >= l_last && l > ft; --l)
+                {
+                    if ((st = launch_words(c, l, l, f, what)))
+                    {
+                        return st;
+                    }
+                }
+                if (l >= l_last)
+                {
+                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, l_last, f);
+                    ++c.n_launches;
+                    st = check(c, what);
+                }
+            }
+            else
+            {
+                int l = l_first;
+                if (l <= ft)
+                {
+                    const int e = l_last < ft ? l_last : ft;
+                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, e, f);
+                    ++c.n_launches;
+                    if ((st = check(c, what)))
+                    {
+                        return st;
+                    }
+                    l = e + 1;
+                }
+                for (; l <= l_last; ++l)
+                {
+                    if ((st = launch_words(c, l, l, f, what)))
+                    {
+                        return st;
+                    }
+                }
+            }
+            return st;
+        }
+
         template <class F>
         int launch_words(Ctx& c, int l0, int l1, F f, const char* what)
         {
@@ -356,9 +431,9 @@ namespace sg
 
         // union cells, top-down: union[l] = (cells[l+1] | union[l+1]).on(l)
         cudaMemsetAsync(uni, 0, bytes, c.stream);
-        for (int l = maxl - 1; l >= 0; --l)
+        if (maxl >= 1)
         {
-            st = launch_words(c, l, l,
+            st = launch_chain(c, maxl - 1, 0,
                               [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
                               { uni[w] = hc[w] | coarsen_word(g, uni, ll, row, wi); },
                               "union");
@@ -410,9 +485,9 @@ namespace sg
 
         // children of the projection cells, bottom-up:
         // reference[l+1] |= (reference[l] & union[l]) refined
-        for (int l = 0; l + 1 <= maxl; ++l)
+        if (maxl >= 1)
         {
-            st = launch_words(c, l + 1, l + 1,
+            st = launch_chain(c, 1, maxl,
                               [=] __device__(const Geom& g, int lf, long long w, long long row, int k)
                               {
                                   const LevelGeom& F = g.lv[lf];
@@ -593,9 +668,9 @@ namespace sg
         cudaMemsetAsync(d, 0, bytes, c.stream);
         cudaMemsetAsync(rr, 0, bytes, c.stream);
         // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. 0
-        for (int l = maxl - 2; l >= 0; --l)
+        if (maxl >= 2)
         {
-            st = launch_words(c, l, l,
+            st = launch_chain(c, maxl - 2, 0,
                               [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
                               {
                                   const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | coarsen_word(g, d, ll, row, wi);
