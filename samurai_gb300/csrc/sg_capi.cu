@@ -328,7 +328,8 @@ extern "C"
         c.cfg.ghost_width          = max_stencil_radius > prediction_radius ? max_stencil_radius : prediction_radius;
         c.g                        = sg::make_geom(dim, min_level, max_level);
         c.capacity                 = 32 * c.g.total_words;
-        c.fuse_top                 = sg::fuse_top_of(c.g);
+        c.fuse_top                 = sg::fuse_top_of(c.g, sg::FUSE_WORDS);
+        c.fuse_top_field           = sg::fuse_top_of(c.g, sg::FUSE_WORDS_FIELD);
         if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
         {
             cudaGetLastError();

@@ -123,7 +123,8 @@ namespace sg
         int* d_ite          = nullptr; // Harten pass index seen by the detail/criteria kernels
         int* h_ite          = nullptr; // pinned staging
         bool use_graphs     = true;    // replay captured launch sequences
-        int fuse_top        = -1;      // levels 0..fuse_top are small enough for one-block chains
+        int fuse_top        = -1;      // levels 0..fuse_top are small enough for one-block mesh chains
+        int fuse_top_field  = -1;      // the same for the FP64 field chains
         struct GraphEntry
         {
             unsigned long long key[4];
@@ -196,14 +197,19 @@ namespace sg
     // finalisation, ghost passes) runs its levels of at most FUSE_WORDS words
     // in a single block that steps through them with __syncthreads(), instead
     // of one launch per level.
-    constexpr long long FUSE_WORDS = 16384;
+    // The integer word chains of the mesh construction stay in one block up
+    // to 16K words per level; the FP64 field chains, whose cells wait on
+    // memory, only up to 2K words (a single block cannot hide that latency
+    // on larger levels).
+    constexpr long long FUSE_WORDS       = 16384;
+    constexpr long long FUSE_WORDS_FIELD = 2048;
 
-    inline int fuse_top_of(const Geom& g)
+    inline int fuse_top_of(const Geom& g, long long limit)
     {
         int t = -1;
         for (int l = 0; l < g.nlev; ++l)
         {
-            if (g.lv[l].nwords <= FUSE_WORDS)
+            if (g.lv[l].nwords <= limit)
             {
                 t = l;
             }

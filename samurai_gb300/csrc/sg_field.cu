@@ -1020,7 +1020,7 @@ namespace sg
             const int maxl  = c.cfg.max_level;
             const int lmin  = minl >= 2 ? minl - 2 : 0; // no reference cell below min_level-2
             const int ndiag = (g.dim == 2) ? 4 : 20;
-            const int ft = c.fuse_top;
+            const int ft = c.fuse_top_field;
             int l        = maxl;
             for (; l >= lmin && l - 1 > ft; --l)
             {
@@ -1159,7 +1159,7 @@ namespace sg
             timer_start(c, T_FINALIZE);
             {
                 int l = maxl;
-                for (; l > 0 && l - 1 > c.fuse_top; --l)
+                for (; l > 0 && l - 1 > c.fuse_top_field; --l)
                 {
                     if (g.dim == 2)
                     {
