@@ -616,6 +616,7 @@ extern "C"
             bm[static_cast<size_t>(p.w)] |= 1u << p.b;
         }
         cudaMemcpyAsync(c.m().cells, bm.data(), bm.size() * 4, cudaMemcpyHostToDevice, c.stream);
+        ++c.mesh_version;
         int st = sg::build_mesh(c, c.m());
         if (!st)
         {
@@ -808,6 +809,7 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_field_upload_device: size differs from the reference mesh");
         }
+        field->f.ghosts_valid = false;
         return from_ctx(c, sg::scatter_compact(c, c.m(), dvalues, field->f.data));
     }
 
@@ -850,6 +852,7 @@ extern "C"
             return from_ctx(c, SG_ERR_CUDA);
         }
         cudaMemcpyAsync(h->staging, values, static_cast<size_t>(n) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        field->f.ghosts_valid = false;
         int st = sg::scatter_compact(c, c.m(), h->staging, field->f.data);
         if (!st && cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
@@ -958,6 +961,8 @@ extern "C"
             return fail(SG_ERR_ARG, "sg_field_swap: fields must live on the same mesh");
         }
         std::swap(a->f.data, b->f.data);
+        a->f.ghosts_valid = false;
+        b->f.ghosts_valid = false;
         return SG_OK;
     }
 
@@ -1019,6 +1024,7 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_upwind: the README scheme is two-dimensional");
         }
+        unp1->f.ghosts_valid = false;
         return from_ctx(c, sg::upwind(c, u->f, unp1->f, a, dt, scheme));
     }
 

@@ -123,6 +123,7 @@ namespace sg
         int* d_ite          = nullptr; // Harten pass index seen by the detail/criteria kernels
         int* h_ite          = nullptr; // pinned staging
         bool use_graphs     = true;    // replay captured launch sequences
+        unsigned long long mesh_version = 1; // bumped at every change of the current mesh
         int fuse_top        = -1;      // levels 0..fuse_top are small enough for one-block mesh chains
         int fuse_top_field  = -1;      // the same for the FP64 field chains
         struct GraphEntry
@@ -154,6 +155,11 @@ namespace sg
         bool has_bc    = false;
         double bc_value = 0.;
         std::string name;
+        // update_ghost_mr is idempotent: when neither the leaf values nor the
+        // mesh changed since the last one, a new call would rewrite the same
+        // ghost values, and is skipped
+        bool ghosts_valid          = false;
+        unsigned long long ghost_version = 0;
     };
 
     // kernels and drivers (sg_mesh.cu / sg_field.cu)
@@ -198,11 +204,11 @@ namespace sg
     // in a single block that steps through them with __syncthreads(), instead
     // of one launch per level.
     // The integer word chains of the mesh construction stay in one block up
-    // to 16K words per level; the FP64 field chains, whose cells wait on
-    // memory, only up to 2K words (a single block cannot hide that latency
-    // on larger levels).
+    // to 16K words per level.  The FP64 field chains are not fused: their
+    // cells wait on memory, and one block serialises that latency (measured
+    // slower than one launch per level even at 2K words), so the limit is 0.
     constexpr long long FUSE_WORDS       = 16384;
-    constexpr long long FUSE_WORDS_FIELD = 2048;
+    constexpr long long FUSE_WORDS_FIELD = 0;
 
     inline int fuse_top_of(const Geom& g, long long limit)
     {

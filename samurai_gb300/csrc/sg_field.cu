@@ -1101,7 +1101,7 @@ namespace sg
 
         // Adapt::harten up to the fixed-point test (mr/adapt.hpp:276-375):
         // tags, ghost update, details, criteria, tag finalisation, new cells,
-        // two graduation passes and the comparison with the current cells.
+        // one graduation pass and the comparison with the current cells.
         // Reads the pass index and thresholds staged in pinned memory; leaves
         // the flags in pinned memory.  No host synchronisation.
         int seq_front(Ctx& c, DeviceMesh& m, DeviceMesh& nm, double* u, bool has_bc, double bcv)
@@ -1191,7 +1191,7 @@ namespace sg
             }
 
             timer_start(c, T_MESH_UPDATE);
-            if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0)) || (st = grad_pass(c, nm.cells, F_GRAD1))
+            if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0))
                 || (st = bitmaps_differ(c, nm.cells, m.cells, F_DIFFER)))
             {
                 return st;
@@ -1233,10 +1233,20 @@ namespace sg
             c.err = "update_ghost_mr: only a ghost width of 1 is implemented";
             return SG_ERR_ARG;
         }
+        if (f.ghosts_valid && f.ghost_version == c.mesh_version)
+        {
+            return SG_OK;
+        }
         DeviceMesh& m = c.m();
         double* u     = f.data;
-        return run_cached(c, 1, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
-                          [&]() { return seq_ghost(c, m, u, f.has_bc, f.bc_value); });
+        int st        = run_cached(c, 1, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
+                                   [&]() { return seq_ghost(c, m, u, f.has_bc, f.bc_value); });
+        if (!st)
+        {
+            f.ghosts_valid  = true;
+            f.ghost_version = c.mesh_version;
+        }
+        return st;
     }
 
     // Adapt::harten (mr/adapt.hpp:276-389) for one field
@@ -1281,9 +1291,11 @@ namespace sg
         {
             return check(c, "harten front sync");
         }
-        if (c.h_flags[F_GRAD1])
+        f.ghosts_valid  = true; // the front's ghost update ran on the current mesh
+        f.ghost_version = c.mesh_version;
+        if (c.h_flags[F_GRAD0])
         {
-            // graduation still refining after two passes: finish it with
+            // the graduation pass refined cells: finish the fixed point with
             // host-tested passes, then compare again
             if ((st = graduate(c, nm.cells, nullptr)))
             {
@@ -1315,6 +1327,8 @@ namespace sg
         nm.host_valid = false; // a replayed graph refreshed the counters without host code
         std::swap(f.data, f.spare);
         c.cur = 1 - c.cur;
+        ++c.mesh_version;
+        f.ghosts_valid = false;
         return SG_OK;
     }
 
