@@ -129,6 +129,29 @@ int sg_tag_download(sg_field_t u, unsigned char* values, long long n);
  * share the array, so calls that overlap on the GPU race. */
 int sg_field_download_noalloc(sg_field_t field, double* values, long long n);
 
+/* Batched mode: n independent problems (u[k], unp1[k] on a mesh of their own, meshes may differ in dimension and
+ * levels) advanced together.  samurai has no batched API: the calls below stand for a user's loop over problems
+ * that makes, for each k, the calls of the time loop of demos/FiniteVolume/advection_2d.cpp:140-147.  The
+ * instances run concurrently on their own streams, driven by n_threads host threads (instance k on thread
+ * k mod n_threads); results are those of the serial calls on each instance.  Per-instance arrays: eps[k],
+ * regularity[k], dt[k], a[3k .. 3k+dim-1] (stride 3 whatever the dimension), n_harten[k] (may be NULL). */
+typedef struct sg_batch_s* sg_batch_t;
+int sg_batch_create(int n, const sg_field_t* u, const sg_field_t* unp1, int n_threads, sg_batch_t* out);
+int sg_batch_destroy(sg_batch_t batch);
+int sg_batch_size(sg_batch_t batch, int* n);
+/* MRadaptation_k(eps[k], regularity[k]) for every k (mr/adapt.hpp:147-203) */
+int sg_batch_adapt(sg_batch_t batch, const double* eps, const double* regularity, int* n_harten);
+/* samurai::update_ghost_mr(u[k]) for every k (algorithm/update_ghost_mr.hpp:261-270) */
+int sg_batch_update_ghost_mr(sg_batch_t batch);
+/* unp1[k] = u[k] - dt[k] * samurai::upwind(a_k, u[k]) for every k (stencil_field.hpp:91-179) */
+int sg_batch_upwind(sg_batch_t batch, const double* a, const double* dt, int scheme);
+/* std::swap(u[k].array(), unp1[k].array()) for every k */
+int sg_batch_swap(sg_batch_t batch);
+/* one time step of every instance: adapt, update_ghost_mr, upwind, swap (advection_2d.cpp:140-147) */
+int sg_batch_step(sg_batch_t batch, const double* eps, const double* regularity, const double* a, const double* dt, int scheme,
+                  int* n_harten);
+int sg_batch_synchronize(sg_batch_t batch);
+
 #ifdef __cplusplus
 }
 #endif

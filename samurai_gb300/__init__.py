@@ -83,6 +83,15 @@ def lib():
         "sg_upwind": (i, [vp, vp, vp, d, i]),
         "sg_detail_download": (i, [vp, vp, ll]),
         "sg_tag_download": (i, [vp, vp, ll]),
+        "sg_batch_create": (i, [i, vp, vp, i, ctypes.POINTER(vp)]),
+        "sg_batch_destroy": (i, [vp]),
+        "sg_batch_size": (i, [vp, pi]),
+        "sg_batch_adapt": (i, [vp, vp, vp, vp]),
+        "sg_batch_update_ghost_mr": (i, [vp]),
+        "sg_batch_upwind": (i, [vp, vp, vp, i]),
+        "sg_batch_swap": (i, [vp]),
+        "sg_batch_step": (i, [vp, vp, vp, vp, vp, i, vp]),
+        "sg_batch_synchronize": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -494,3 +503,73 @@ class AdvectionSim:
 
     def set_cells(self, level, coords):
         self.mesh.set_cells(level, coords)
+
+
+# ---------------------------------------------------------------- batched mode
+class Batch:
+    """Independent advection problems advanced together (the sg_batch_* calls).
+
+    ``sims`` are AdvectionSim objects, one mesh each; ``eps``, ``regularity``,
+    ``dt`` hold one value per instance and ``a`` one velocity per instance.
+    Each call does, for every instance, what the serial calls on that
+    instance do, with the instances running side by side on the GPU."""
+
+    def __init__(self, sims, n_threads=8):
+        self.sims = list(sims)
+        n = len(self.sims)
+        self._u = (ctypes.c_void_p * n)(*[s.u.h.value for s in self.sims])
+        self._unp1 = (ctypes.c_void_p * n)(*[s.unp1.h.value for s in self.sims])
+        h = ctypes.c_void_p()
+        _check(lib().sg_batch_create(n, self._u, self._unp1, int(n_threads), ctypes.byref(h)), "sg_batch_create")
+        self._h = h
+        self.n_harten = np.zeros(n, dtype=np.int32)
+
+    def __len__(self):
+        return len(self.sims)
+
+    def _params(self, values):
+        v = np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64), (len(self.sims),)))
+        return v
+
+    def _velocities(self, a):
+        """one velocity for all instances, or one per instance (rows of any length <= 3)"""
+        n = len(self.sims)
+        rows = [a] * n if np.ndim(a[0]) == 0 else list(a)
+        if len(rows) != n:
+            raise SamuraiGpuError("need one velocity per instance")
+        out = np.zeros((n, 3), dtype=np.float64)
+        for k, r in enumerate(rows):
+            out[k, : len(r)] = np.asarray(r, dtype=np.float64)
+        return out
+
+    def adapt(self, eps, regularity):
+        e, r = self._params(eps), self._params(regularity)
+        _check(lib().sg_batch_adapt(self._h, _ptr(e), _ptr(r), _ptr(self.n_harten)), "sg_batch_adapt")
+        return self.n_harten.copy()
+
+    def update_ghost(self):
+        _check(lib().sg_batch_update_ghost_mr(self._h), "sg_batch_update_ghost_mr")
+
+    def upwind(self, a, dt, scheme=UPWIND_OP):
+        av, dv = self._velocities(a), self._params(dt)
+        _check(lib().sg_batch_upwind(self._h, _ptr(av), _ptr(dv), int(scheme)), "sg_batch_upwind")
+        _check(lib().sg_batch_swap(self._h), "sg_batch_swap")
+
+    def step(self, eps, regularity, a, dt, scheme=UPWIND_OP):
+        e, r, av, dv = self._params(eps), self._params(regularity), self._velocities(a), self._params(dt)
+        _check(lib().sg_batch_step(self._h, _ptr(e), _ptr(r), _ptr(av), _ptr(dv), int(scheme), _ptr(self.n_harten)), "sg_batch_step")
+        return self.n_harten
+
+    def synchronize(self):
+        _check(lib().sg_batch_synchronize(self._h), "sg_batch_synchronize")
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            lib().sg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

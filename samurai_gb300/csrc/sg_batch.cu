@@ -1,0 +1,436 @@
+// Batched mode: many independent MR advection problems stepped together.
+//
+// samurai runs one problem per process; a user with many problems (parameter
+// sweeps, ensembles) loops over them, each time step of each problem waiting
+// for its own Harten passes.  Here every instance keeps its own mesh, stream
+// and captured graphs, and the instances advance in lockstep phases: all
+// fronts of Harten pass i are launched before any is waited for, so the GPU
+// runs the instances' small, launch-bound graphs side by side.  Host threads
+// split the instances between them (instance k on thread k mod T); each
+// thread drives its share in the same lockstep order.
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../../include/samurai_gpu.h"
+#include "sg_ctx.cuh"
+#include "sg_handles.cuh"
+
+namespace sg
+{
+    void set_last_error(const char* msg, const char* detail);
+    int ensure_spare(Ctx& c, DeviceField& f);
+}
+
+struct sg_batch_s
+{
+    std::vector<sg_field_t> u, unp1;
+    int n_threads = 1;
+
+    // worker pool: thread t runs job(t) for every new generation
+    std::vector<std::thread> workers;
+    std::mutex mu;
+    std::condition_variable cv_start, cv_done;
+    long long generation = 0;
+    int pending          = 0;
+    bool stop            = false;
+    std::function<void(int)> job;
+
+    // first failure of the current call
+    std::mutex err_mu;
+    std::atomic<int> status{SG_OK};
+    char msg[512] = "";
+
+    void record(int st, const char* text)
+    {
+        std::lock_guard<std::mutex> lk(err_mu);
+        if (status.load() == SG_OK && st != SG_OK)
+        {
+            std::snprintf(msg, sizeof(msg), "%s", text ? text : "error");
+            status.store(st);
+        }
+    }
+
+    void worker(int t)
+    {
+        long long seen = 0;
+        for (;;)
+        {
+            std::function<void(int)> j;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_start.wait(lk, [&] { return stop || generation != seen; });
+                if (stop)
+                {
+                    return;
+                }
+                seen = generation;
+                j    = job;
+            }
+            j(t);
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                if (--pending == 0)
+                {
+                    cv_done.notify_one();
+                }
+            }
+        }
+    }
+
+    // runs f(t) for t = 0 .. n_threads-1 and waits; returns the first status
+    int run(const std::function<void(int)>& f)
+    {
+        status = SG_OK;
+        msg[0] = '\0';
+        if (n_threads == 1)
+        {
+            f(0);
+        }
+        else
+        {
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                job     = f;
+                pending = n_threads;
+                ++generation;
+            }
+            cv_start.notify_all();
+            std::unique_lock<std::mutex> lk(mu);
+            cv_done.wait(lk, [&] { return pending == 0; });
+        }
+        const int st = status.load();
+        if (st != SG_OK)
+        {
+            sg::set_last_error(msg, nullptr);
+        }
+        return st;
+    }
+
+    // instances of thread t
+    template <class F>
+    void for_mine(int t, F&& f)
+    {
+        for (size_t k = static_cast<size_t>(t); k < u.size(); k += static_cast<size_t>(n_threads))
+        {
+            f(k);
+        }
+    }
+
+    ~sg_batch_s()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv_start.notify_all();
+        for (auto& w : workers)
+        {
+            w.join();
+        }
+    }
+};
+
+namespace
+{
+    int bfail(int code, const char* msg)
+    {
+        sg::set_last_error(msg, nullptr);
+        return code;
+    }
+
+    // Adapt::operator() (mr/adapt.hpp:147-195) for the instances of thread t,
+    // pass by pass in lockstep; n_harten[k] as sg_adapt reports it
+    void adapt_share(sg_batch_s& b, int t, const double* eps, const double* regularity, int* n_harten)
+    {
+        std::vector<size_t> live;
+        int max_passes = 0;
+        b.for_mine(t,
+                   [&](size_t k)
+                   {
+                       sg::Ctx& c = b.u[k]->mesh->ctx;
+                       const int n = c.cfg.max_level - c.cfg.min_level;
+                       if (n_harten)
+                       {
+                           n_harten[k] = 0;
+                       }
+                       if (n > 0)
+                       {
+                           live.push_back(k);
+                           max_passes = std::max(max_passes, n);
+                       }
+                   });
+        for (int ite = 0; ite < max_passes && !live.empty(); ++ite)
+        {
+            std::vector<size_t> started;
+            for (size_t k : live)
+            {
+                sg::Ctx& c = b.u[k]->mesh->ctx;
+                if (ite >= c.cfg.max_level - c.cfg.min_level)
+                {
+                    continue;
+                }
+                const int st = sg::harten_begin(c, b.u[k]->f, ite, eps[k], regularity[k]);
+                if (st)
+                {
+                    b.record(st, c.err.c_str());
+                    return;
+                }
+                started.push_back(k);
+            }
+            live.clear();
+            for (size_t k : started)
+            {
+                sg::Ctx& c = b.u[k]->mesh->ctx;
+                bool conv  = false;
+                const int st = sg::harten_end(c, b.u[k]->f, &conv);
+                if (st)
+                {
+                    b.record(st, c.err.c_str());
+                    return;
+                }
+                if (n_harten)
+                {
+                    n_harten[k] = ite + 1;
+                }
+                if (!conv)
+                {
+                    live.push_back(k);
+                }
+            }
+        }
+        b.for_mine(t,
+                   [&](size_t k)
+                   {
+                       sg::Ctx& c = b.u[k]->mesh->ctx;
+                       if (b.status == SG_OK)
+                       {
+                           const int st = sg::device_error(c);
+                           if (st)
+                           {
+                               b.record(st, c.err.c_str());
+                           }
+                       }
+                   });
+    }
+
+    void ghost_share(sg_batch_s& b, int t)
+    {
+        b.for_mine(t,
+                   [&](size_t k)
+                   {
+                       sg::Ctx& c   = b.u[k]->mesh->ctx;
+                       const int st = sg::update_ghost_mr(c, b.u[k]->f);
+                       if (st)
+                       {
+                           b.record(st, c.err.c_str());
+                       }
+                   });
+    }
+
+    void upwind_share(sg_batch_s& b, int t, const double* a, const double* dt, int scheme, bool swap)
+    {
+        b.for_mine(t,
+                   [&](size_t k)
+                   {
+                       sg::Ctx& c = b.u[k]->mesh->ctx;
+                       b.unp1[k]->f.ghosts_valid = false;
+                       const int st = sg::upwind(c, b.u[k]->f, b.unp1[k]->f, a + 3 * k, dt[k], scheme);
+                       if (st)
+                       {
+                           b.record(st, c.err.c_str());
+                           return;
+                       }
+                       if (swap)
+                       {
+                           std::swap(b.u[k]->f.data, b.unp1[k]->f.data);
+                           b.u[k]->f.ghosts_valid    = false;
+                           b.unp1[k]->f.ghosts_valid = false;
+                       }
+                   });
+    }
+
+    int check_upwind_args(sg_batch_s* b, const double* a, const double* dt, int scheme)
+    {
+        if (!a || !dt)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch: null velocity or time-step array");
+        }
+        if (scheme != SG_UPWIND_OP && scheme != SG_README)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch: unknown scheme");
+        }
+        if (scheme == SG_README)
+        {
+            for (auto* f : b->u)
+            {
+                if (f->mesh->ctx.g.dim != 2)
+                {
+                    return bfail(SG_ERR_ARG, "sg_batch: the README scheme is two-dimensional");
+                }
+            }
+        }
+        return SG_OK;
+    }
+} // namespace
+
+extern "C"
+{
+    int sg_batch_create(int n, const sg_field_t* u, const sg_field_t* unp1, int n_threads, sg_batch_t* out)
+    {
+        if (!out || n <= 0 || !u || !unp1 || n_threads <= 0)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_create: need n > 0 field pairs, n_threads > 0 and an output handle");
+        }
+        *out = nullptr;
+        std::vector<sg_mesh_s*> meshes;
+        for (int k = 0; k < n; ++k)
+        {
+            if (!u[k] || !unp1[k] || u[k] == unp1[k] || u[k]->mesh != unp1[k]->mesh)
+            {
+                return bfail(SG_ERR_ARG, "sg_batch_create: each instance needs two distinct fields on one mesh");
+            }
+            meshes.push_back(u[k]->mesh);
+        }
+        std::sort(meshes.begin(), meshes.end());
+        if (std::adjacent_find(meshes.begin(), meshes.end()) != meshes.end())
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_create: two instances share a mesh");
+        }
+        for (int k = 0; k < n; ++k)
+        {
+            sg::Ctx& c = u[k]->mesh->ctx;
+            if (sg::ensure_spare(c, u[k]->f))
+            {
+                return bfail(SG_ERR_CUDA, c.err.c_str());
+            }
+        }
+        auto* b = new (std::nothrow) sg_batch_s();
+        if (!b)
+        {
+            return bfail(SG_ERR_CAPACITY, "sg_batch_create: out of host memory");
+        }
+        b->u.assign(u, u + n);
+        b->unp1.assign(unp1, unp1 + n);
+        b->n_threads = std::min(n_threads, n);
+        if (b->n_threads > 1)
+        {
+            for (int t = 0; t < b->n_threads; ++t)
+            {
+                b->workers.emplace_back([b, t] { b->worker(t); });
+            }
+        }
+        *out = b;
+        return SG_OK;
+    }
+
+    int sg_batch_destroy(sg_batch_t b)
+    {
+        delete b;
+        return SG_OK;
+    }
+
+    int sg_batch_size(sg_batch_t b, int* n)
+    {
+        if (!b || !n)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_size: null argument");
+        }
+        *n = static_cast<int>(b->u.size());
+        return SG_OK;
+    }
+
+    int sg_batch_adapt(sg_batch_t b, const double* eps, const double* regularity, int* n_harten)
+    {
+        if (!b || !eps || !regularity)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_adapt: null argument");
+        }
+        return b->run([&](int t) { adapt_share(*b, t, eps, regularity, n_harten); });
+    }
+
+    int sg_batch_update_ghost_mr(sg_batch_t b)
+    {
+        if (!b)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_update_ghost_mr: null batch");
+        }
+        return b->run([&](int t) { ghost_share(*b, t); });
+    }
+
+    int sg_batch_upwind(sg_batch_t b, const double* a, const double* dt, int scheme)
+    {
+        if (!b)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_upwind: null batch");
+        }
+        if (int st = check_upwind_args(b, a, dt, scheme))
+        {
+            return st;
+        }
+        return b->run([&](int t) { upwind_share(*b, t, a, dt, scheme, false); });
+    }
+
+    int sg_batch_swap(sg_batch_t b)
+    {
+        if (!b)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_swap: null batch");
+        }
+        for (size_t k = 0; k < b->u.size(); ++k)
+        {
+            std::swap(b->u[k]->f.data, b->unp1[k]->f.data);
+            b->u[k]->f.ghosts_valid    = false;
+            b->unp1[k]->f.ghosts_valid = false;
+        }
+        return SG_OK;
+    }
+
+    int sg_batch_step(sg_batch_t b, const double* eps, const double* regularity, const double* a, const double* dt, int scheme,
+                      int* n_harten)
+    {
+        if (!b || !eps || !regularity)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_step: null argument");
+        }
+        if (int st = check_upwind_args(b, a, dt, scheme))
+        {
+            return st;
+        }
+        return b->run(
+            [&](int t)
+            {
+                adapt_share(*b, t, eps, regularity, n_harten);
+                if (b->status != SG_OK)
+                {
+                    return;
+                }
+                ghost_share(*b, t);
+                upwind_share(*b, t, a, dt, scheme, true);
+            });
+    }
+
+    int sg_batch_synchronize(sg_batch_t b)
+    {
+        if (!b)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_synchronize: null batch");
+        }
+        for (auto* f : b->u)
+        {
+            sg::Ctx& c = f->mesh->ctx;
+            if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+            {
+                return bfail(SG_ERR_CUDA, "sg_batch_synchronize: a stream failed");
+            }
+        }
+        return SG_OK;
+    }
+}

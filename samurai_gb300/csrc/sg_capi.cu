@@ -24,14 +24,6 @@ namespace
 
 } // namespace
 
-namespace sg
-{
-    // the C ABI's error text, for entry points defined in other files
-    void set_last_error(const char* msg, const char* detail)
-    {
-        fail(0, msg, detail);
-    }
-}
 
 namespace
 {
@@ -263,6 +255,25 @@ namespace
         }
     }
 } // namespace
+
+namespace sg
+{
+    // the C ABI's error text, for entry points defined in other files
+    void set_last_error(const char* msg, const char* detail)
+    {
+        fail(0, msg, detail);
+    }
+
+    // the spare buffer adaptation swaps into, allocated on first use
+    int ensure_spare(Ctx& c, DeviceField& f)
+    {
+        if (!f.spare && dalloc(c, &f.spare, static_cast<size_t>(c.capacity)))
+        {
+            return SG_ERR_CUDA;
+        }
+        return SG_OK;
+    }
+} // namespace sg
 
 extern "C"
 {

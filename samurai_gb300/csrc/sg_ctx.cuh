@@ -175,6 +175,8 @@ namespace sg
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense);
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value);
     int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged);
+    int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity); // no synchronisation
+    int harten_end(Ctx& c, DeviceField& f, bool* converged);
     int device_error(Ctx& c); // reads and clears the device error word (synchronises)
 
     void timer_start(Ctx& c, int id);

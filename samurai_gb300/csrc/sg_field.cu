@@ -1101,7 +1101,7 @@ namespace sg
 
         // Adapt::harten up to the fixed-point test (mr/adapt.hpp:276-375):
         // tags, ghost update, details, criteria, tag finalisation, new cells,
-        // one graduation pass and the comparison with the current cells.
+        // two graduation passes and the comparison with the current cells.
         // Reads the pass index and thresholds staged in pinned memory; leaves
         // the flags in pinned memory.  No host synchronisation.
         int seq_front(Ctx& c, DeviceMesh& m, DeviceMesh& nm, double* u, bool has_bc, double bcv)
@@ -1191,7 +1191,7 @@ namespace sg
             }
 
             timer_start(c, T_MESH_UPDATE);
-            if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0))
+            if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0)) || (st = grad_pass(c, nm.cells, F_GRAD1))
                 || (st = bitmaps_differ(c, nm.cells, m.cells, F_DIFFER)))
             {
                 return st;
@@ -1249,8 +1249,12 @@ namespace sg
         return st;
     }
 
-    // Adapt::harten (mr/adapt.hpp:276-389) for one field
-    int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged)
+    // Adapt::harten (mr/adapt.hpp:276-389) for one field, in two halves:
+    // harten_begin launches everything up to the fixed-point test without
+    // waiting; harten_end waits for it, finishes the graduation if needed and
+    // launches the new mesh and update_fields.  Between the two halves the
+    // host may launch other meshes' work (batched mode).
+    int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity)
     {
         if (c.cfg.ghost_width != 1)
         {
@@ -1262,12 +1266,8 @@ namespace sg
         const int dim  = c.g.dim;
         DeviceMesh& m  = c.m();
         DeviceMesh& nm = c.spare();
-        // the pinned inputs of the previous pass have been consumed: every
-        // pass ends with a synchronisation
-        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
-        {
-            return check(c, "harten sync");
-        }
+        // the pinned inputs staged here were consumed by the previous pass,
+        // which ended with harten_end's synchronisation
         *c.h_ite = ite;
         for (int l = 0; l < MAXLEV; ++l)
         {
@@ -1275,28 +1275,31 @@ namespace sg
         }
         for (int l = minl; l <= maxl - ite; ++l)
         {
-            const int exponent        = dim * (maxl - l);
-            c.h_eps[l]                = eps / (1 << exponent);
-            c.h_eps[MAXLEV + l]       = std::pow(2.0, regularity + dim) * c.h_eps[l];
-            c.h_eps[2 * MAXLEV + l]   = c.h_eps[MAXLEV + l] / (1 << dim);
+            const int exponent      = dim * (maxl - l);
+            c.h_eps[l]              = eps / (1 << exponent);
+            c.h_eps[MAXLEV + l]     = std::pow(2.0, regularity + dim) * c.h_eps[l];
+            c.h_eps[2 * MAXLEV + l] = c.h_eps[MAXLEV + l] / (1 << dim);
         }
         double* u = f.data;
-        int st    = run_cached(c, 2, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
-                               [&]() { return seq_front(c, m, nm, u, f.has_bc, f.bc_value); });
-        if (st)
-        {
-            return st;
-        }
+        return run_cached(c, 2, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
+                          [&]() { return seq_front(c, m, nm, u, f.has_bc, f.bc_value); });
+    }
+
+    int harten_end(Ctx& c, DeviceField& f, bool* converged)
+    {
+        DeviceMesh& m  = c.m();
+        DeviceMesh& nm = c.spare();
+        int st;
         if (cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
             return check(c, "harten front sync");
         }
         f.ghosts_valid  = true; // the front's ghost update ran on the current mesh
         f.ghost_version = c.mesh_version;
-        if (c.h_flags[F_GRAD0])
+        if (c.h_flags[F_GRAD1])
         {
-            // the graduation pass refined cells: finish the fixed point with
-            // host-tested passes, then compare again
+            // graduation still refining after two passes: finish the fixed
+            // point with host-tested passes, then compare again
             if ((st = graduate(c, nm.cells, nullptr)))
             {
                 return st;
@@ -1318,6 +1321,7 @@ namespace sg
             return SG_OK;
         }
         *converged = false;
+        double* u  = f.data;
         st         = run_cached(c, 3, static_cast<unsigned long long>(c.cur), ptr_key(u), ptr_key(f.spare),
                                 [&]() { return seq_back(c, m, nm, u, f.spare); });
         if (st)
@@ -1330,6 +1334,19 @@ namespace sg
         ++c.mesh_version;
         f.ghosts_valid = false;
         return SG_OK;
+    }
+
+    // No synchronisation before the pass: the pinned thresholds it rewrites
+    // were consumed before the previous pass's harten_end returned, and its
+    // launches queue behind whatever the stream still runs.
+    int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged)
+    {
+        int st = harten_begin(c, f, ite, eps, regularity);
+        if (st)
+        {
+            return st;
+        }
+        return harten_end(c, f, converged);
     }
 
     // Adapt::operator() (mr/adapt.hpp:147-195)

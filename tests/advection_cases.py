@@ -77,6 +77,56 @@ def shapes_2d(seed, n_squares=16, n_gauss=16):
     return f
 
 
+def shape_sum_2d(squares, gaussians):
+    """u0 = sum of indicator squares (side, cx, cy, amp) and Gaussians (sigma, cx, cy, amp)."""
+
+    def f(level, coords):
+        c = centers(level, coords)
+        u = np.zeros(len(c))
+        for side, cx, cy, amp in squares:
+            inside = (np.abs(c[:, 0] - cx) <= 0.5 * side) & (np.abs(c[:, 1] - cy) <= 0.5 * side)
+            u = u + np.where(inside, amp, 0.0)
+        for sig, cx, cy, amp in gaussians:
+            r2 = (c[:, 0] - cx) * (c[:, 0] - cx) + (c[:, 1] - cy) * (c[:, 1] - cy)
+            u = u + amp * np.exp(-r2 / (2.0 * sig * sig))
+        return u
+
+    return f
+
+
+def batch_instances(seed, n, max_levels=(7, 11), min_level=2):
+    """Seeded independent 2D problems for the batched mode: max_level
+    U{7..11}, min_level 2, a U[-1,1]^2, 1-8 shapes (squares or Gaussians with
+    the distributions of shapes_2d), eps in {1e-3, 1e-4}, regularity 2,
+    dt = 0.5 * 2^-max_level (stable for |a_x| + |a_y| <= 2)."""
+    rng = SplitMix64(seed)
+    out = []
+    for _ in range(n):
+        lo, hi = max_levels
+        maxl = lo + min(hi - lo, int(rng.uniform() * (hi - lo + 1)))
+        a = (rng.uniform(-1.0, 1.0), rng.uniform(-1.0, 1.0))
+        n_shapes = 1 + min(7, int(rng.uniform() * 8))
+        squares, gaussians = [], []
+        for _ in range(n_shapes):
+            if rng.uniform() < 0.5:
+                squares.append((rng.uniform(0.02, 0.1), rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8), rng.uniform(0.5, 1.0)))
+            else:
+                gaussians.append((rng.uniform(0.005, 0.03), rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.8), rng.uniform(0.5, 1.0)))
+        eps = 1e-3 if rng.uniform() < 0.5 else 1e-4
+        out.append(
+            dict(
+                min_level=min_level,
+                max_level=maxl,
+                a=a,
+                eps=eps,
+                regularity=2.0,
+                dt=0.5 / (1 << maxl),
+                u0=shape_sum_2d(squares, gaussians),
+            )
+        )
+    return out
+
+
 def ball_3d(seed, n_gauss=8):
     """Seeded ball indicator (radius U[0.1,0.2], centre U[0.3,0.7]^3) plus
     Gaussians (sigma U[0.01,0.05], centre U[0.3,0.7]^3, amplitude U[0.5,1])."""

@@ -53,3 +53,21 @@ def test_minimal_ghost_width_rule():
     cfg = sg.mesh_config(2).min_level(2).max_level(5)
     assert cfg.parse_args() == 2  # mesh_config.hpp:388-393
     assert cfg.max_stencil_size(2).disable_minimal_ghost_width().parse_args() == 1
+
+
+def test_batch_argument_checks():
+    """sg_batch_create validates its arguments before touching a device."""
+    import ctypes
+
+    import samurai_gb300 as sg
+
+    L = sg.lib()
+    h = ctypes.c_void_p()
+    arr = (ctypes.c_void_p * 1)()
+    assert L.sg_batch_create(0, arr, arr, 1, ctypes.byref(h)) == 1
+    assert b"n > 0" in L.sg_last_error()
+    assert L.sg_batch_create(1, arr, arr, 1, ctypes.byref(h)) == 1
+    assert b"two distinct fields" in L.sg_last_error()
+    assert L.sg_batch_create(1, arr, arr, 0, ctypes.byref(h)) == 1
+    assert L.sg_batch_step(None, None, None, None, None, 0, None) == 1
+    assert L.sg_batch_synchronize(None) == 1
