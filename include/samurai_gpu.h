@@ -152,6 +152,30 @@ int sg_batch_step(sg_batch_t batch, const double* eps, const double* regularity,
                   int* n_harten);
 int sg_batch_synchronize(sg_batch_t batch);
 
+/* Discrete adjoint of the time loop (no counterpart in samurai, which has no derivatives).  The loop of
+ * demos/FiniteVolume/advection_2d.cpp:140-147 (MRadaptation(eps, regularity); update_ghost_mr; upwind; swap)
+ * is recorded with its mesh sequence; derivatives are those of the loop on the recorded meshes (adaptation
+ * decisions are piecewise constant).  Fields are leaf values in for_each_cell order (algorithm.hpp:301-363):
+ * u0 on the initial mesh (the leaf cells of u when the adjoint is created), uT on the final mesh.  The dense
+ * field is checkpointed every checkpoint_every steps; the backward pass recomputes each segment from its
+ * checkpoint.  a has dim entries; ga receives dim entries. */
+typedef struct sg_adjoint_s* sg_adjoint_t;
+int sg_adjoint_create(sg_field_t u, int checkpoint_every, sg_adjoint_t* out);
+int sg_adjoint_destroy(sg_adjoint_t adj);
+/* leaf counts of the initial and final meshes and the number of recorded steps */
+int sg_adjoint_counts(sg_adjoint_t adj, long long* n0, long long* nT, int* n_steps);
+/* leaf cells (level, dim coordinates) of the initial (which = 0) or final (which = 1) mesh */
+int sg_adjoint_cells(sg_adjoint_t adj, int which, int* level, int* coords, long long n);
+/* forward with adaptation from u0: n_steps of the loop, recording meshes and checkpoints */
+int sg_adjoint_record(sg_adjoint_t adj, const double* u0, int n_steps, double eps, double regularity, const double* a, double dt, int scheme,
+                      long long* nT);
+/* uT of the last forward (record or replay) */
+int sg_adjoint_final(sg_adjoint_t adj, double* uT, long long nT);
+/* the recorded steps on the recorded meshes from u0 with velocity a; uT may be NULL */
+int sg_adjoint_replay(sg_adjoint_t adj, const double* u0, const double* a, double* uT);
+/* reverse pass at the last forward: gT = dJ/duT gives g0 = dJ/du0 and ga = dJ/da */
+int sg_adjoint_backward(sg_adjoint_t adj, const double* gT, double* g0, double* ga);
+
 #ifdef __cplusplus
 }
 #endif

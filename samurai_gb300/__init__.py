@@ -92,6 +92,14 @@ def lib():
         "sg_batch_swap": (i, [vp]),
         "sg_batch_step": (i, [vp, vp, vp, vp, vp, i, vp]),
         "sg_batch_synchronize": (i, [vp]),
+        "sg_adjoint_create": (i, [vp, i, ctypes.POINTER(vp)]),
+        "sg_adjoint_destroy": (i, [vp]),
+        "sg_adjoint_counts": (i, [vp, pl, pl, pi]),
+        "sg_adjoint_cells": (i, [vp, i, vp, vp, ll]),
+        "sg_adjoint_record": (i, [vp, vp, i, d, d, vp, d, i, pl]),
+        "sg_adjoint_final": (i, [vp, vp, ll]),
+        "sg_adjoint_replay": (i, [vp, vp, vp, vp]),
+        "sg_adjoint_backward": (i, [vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -566,6 +574,84 @@ class Batch:
     def close(self):
         if getattr(self, "_h", None) is not None and _lib is not None:
             lib().sg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- adjoint
+class Adjoint:
+    """Discrete adjoint of the time loop (the sg_adjoint_* calls).
+
+    Created from a field: its current leaf cells are the initial mesh.
+    record() runs the loop with adaptation from leaf values u0 and records
+    the mesh sequence; replay() reruns the recorded steps on the recorded
+    meshes (the frozen-mesh map); backward() gives dJ/du0 and dJ/da at the
+    last forward from dJ/duT.  Leaf values are in for_each_cell order."""
+
+    def __init__(self, u, checkpoint_every=16):
+        self.dim = u.mesh.dim
+        h = ctypes.c_void_p()
+        _check(lib().sg_adjoint_create(u.h, int(checkpoint_every), ctypes.byref(h)), "sg_adjoint_create")
+        self._h = h
+
+    def counts(self):
+        n0, nT, ns = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+        _check(lib().sg_adjoint_counts(self._h, ctypes.byref(n0), ctypes.byref(nT), ctypes.byref(ns)), "sg_adjoint_counts")
+        return n0.value, nT.value, ns.value
+
+    def cells(self, which):
+        """(level, coords) of the initial ("initial") or final ("final") mesh"""
+        w = {"initial": 0, "final": 1}[which]
+        n0, nT, _ = self.counts()
+        n = n0 if w == 0 else nT
+        lev = np.empty(n, np.int32)
+        co = np.empty((n, self.dim), np.int32)
+        _check(lib().sg_adjoint_cells(self._h, w, _ptr(lev), _ptr(co), n), "sg_adjoint_cells")
+        return lev, co
+
+    def _vel(self, a):
+        av = np.zeros(3, np.float64)
+        av[: self.dim] = np.asarray(a, np.float64)[: self.dim]
+        return av
+
+    def record(self, u0, n_steps, eps, regularity, a, dt, scheme=UPWIND_OP):
+        u0 = np.ascontiguousarray(u0, np.float64)
+        nT = ctypes.c_longlong()
+        av = self._vel(a)
+        _check(lib().sg_adjoint_record(self._h, _ptr(u0), int(n_steps), float(eps), float(regularity), _ptr(av), float(dt), int(scheme),
+                                       ctypes.byref(nT)), "sg_adjoint_record")
+        return self.final()
+
+    def final(self):
+        _, nT, _ = self.counts()
+        out = np.empty(nT, np.float64)
+        _check(lib().sg_adjoint_final(self._h, _ptr(out), nT), "sg_adjoint_final")
+        return out
+
+    def replay(self, u0, a):
+        u0 = np.ascontiguousarray(u0, np.float64)
+        _, nT, _ = self.counts()
+        out = np.empty(nT, np.float64)
+        av = self._vel(a)
+        _check(lib().sg_adjoint_replay(self._h, _ptr(u0), _ptr(av), _ptr(out)), "sg_adjoint_replay")
+        return out
+
+    def backward(self, gT):
+        gT = np.ascontiguousarray(gT, np.float64)
+        n0, _, _ = self.counts()
+        g0 = np.empty(n0, np.float64)
+        ga = np.zeros(3, np.float64)
+        _check(lib().sg_adjoint_backward(self._h, _ptr(gT), _ptr(g0), _ptr(ga)), "sg_adjoint_backward")
+        return g0, ga[: self.dim].copy()
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            lib().sg_adjoint_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -1,0 +1,1128 @@
+// Discrete adjoint of the MR advection time loop (sg_adjoint_*).
+//
+// samurai has no adjoint; this extends its time loop
+// (demos/FiniteVolume/advection_2d.cpp:124-156: MRadaptation, update_ghost_mr,
+// upwind, swap) with reverse-mode derivatives.  The adaptation decisions
+// (thresholds on details, graduation) are piecewise constant in the field,
+// so the derivative is that of the loop on its recorded mesh sequence:
+//
+//   record    the forward with adaptation; keeps every mesh the loop visits
+//             (leaf bitmaps) and the dense field every K steps (checkpoints);
+//   replay    the same steps on the recorded meshes from any u0 and velocity:
+//             the frozen-mesh map whose derivative the adjoint computes;
+//   backward  segment by segment from the last: recompute the segment from its
+//             checkpoint on the recorded meshes, recording every ghost-update
+//             and update_fields launch onto a tape (its matrix, see
+//             sg_access.cuh) and keeping the ghosted field of every step; then
+//             walk the segment backwards applying transposes: the upwind step
+//             (and its velocity derivative) by dedicated kernels, the tape
+//             launches by scatter kernels, in reverse launch order.
+//
+// Every operator of a step is linear in the field on a frozen mesh; the
+// Dirichlet value only adds a constant.  The upwind step is bilinear in (a, u);
+// d|a|/da = sign(a), 0 at a = 0.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/samurai_gpu.h"
+#include "sg_access.cuh"
+#include "sg_ctx.cuh"
+#include "sg_handles.cuh"
+
+namespace sg
+{
+    void set_last_error(const char* msg, const char* detail);
+    int ensure_spare(Ctx& c, DeviceField& f);
+
+    namespace
+    {
+        constexpr int ABLOCK = 256;
+
+        __device__ __forceinline__ long long gtid()
+        {
+            return blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+        }
+        __device__ __forceinline__ long long gstride()
+        {
+            return static_cast<long long>(gridDim.x) * blockDim.x;
+        }
+
+        __global__ void k_tape_mark(const long long* count, long long* marks, int p)
+        {
+            marks[p] = *count;
+        }
+
+        // transpose of one recorded launch: lam_j[src] += w * lam_i[dst]
+        __global__ void k_tape_scatter(const int* __restrict__ dst, const int* __restrict__ src, const double* __restrict__ w, long long b,
+                                       long long e, const double* lam_i, double* lam_j)
+        {
+            for (long long r = b + gtid(); r < e; r += gstride())
+            {
+                const int j = src[r];
+                if (j >= 0)
+                {
+                    const double v = w[r] * lam_i[dst[r]];
+                    if (v != 0.)
+                    {
+                        atomicAdd(lam_j + j, v);
+                    }
+                }
+            }
+        }
+
+        // the entries a launch overwrote do not reach back past it
+        __global__ void k_tape_zero(const int* __restrict__ dst, long long b, long long e, double* lam)
+        {
+            for (long long r = b + gtid(); r < e; r += gstride())
+            {
+                lam[dst[r]] = 0.;
+            }
+        }
+
+        __device__ __forceinline__ double pow2d(int l)
+        {
+            return __longlong_as_double(static_cast<long long>(1023 + l) << 52);
+        }
+
+        struct UpwindAdj
+        {
+            double ha[3], hb[3]; // .5 a_d and .5 |a_d|
+            double sgn[3];       // sign(a_d)
+            double dt;
+            int scheme;
+        };
+
+        // the leaf cell of level l at (x, y, z), if any
+        template <int DIM>
+        __device__ __forceinline__ bool leaf_at(const Geom& g, const uint32_t* cells, int l, int x, int y, int z, long long* e)
+        {
+            const Pos p = pos_of(g, l, x, y, z);
+            if (p.w < 0 || !((cells[p.w] >> p.b) & 1u))
+            {
+                return false;
+            }
+            *e = elem(p);
+            return true;
+        }
+
+        // mu = U^T lam for unp1 = u - dt * upwind(a, u) on the leaf cells of
+        // one mesh (the forward is k_upwind); gather form, one thread per
+        // dense element, deterministic.
+        template <int DIM>
+        __global__ void k_upwind_adjoint(const Geom* __restrict__ gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
+                                         double* __restrict__ mu, UpwindAdj p)
+        {
+            const Geom& g       = *gp;
+            const long long tot = 32 * g.total_words;
+            for (long long k = gtid(); k < tot; k += gstride())
+            {
+                const long long w = k >> 5;
+                const int b       = static_cast<int>(k & 31);
+                const int l       = level_of(g, w);
+                const Cell c      = cell_of(g, l, w, b);
+                const double s    = p.dt * pow2d(l);
+                double acc        = 0.;
+                long long e;
+                if ((cells[w] >> b) & 1u)
+                {
+                    double self = 0.;
+                    for (int d = 0; d < DIM; ++d)
+                    {
+                        self += p.scheme == 1 ? 1. : 2. * p.hb[d];
+                    }
+                    acc += lam[k] * (1. - s * self);
+                }
+                for (int d = 0; d < DIM; ++d)
+                {
+                    const int dx = d == 0, dy = d == 1, dz = d == 2;
+                    // cell c - e_d sees k as its right neighbour
+                    if (p.scheme == 0 && leaf_at<DIM>(g, cells, l, c.x - dx, c.y - dy, c.z - dz, &e))
+                    {
+                        acc += lam[e] * (-s * (p.ha[d] - p.hb[d]));
+                    }
+                    // cell c + e_d sees k as its left neighbour
+                    if (leaf_at<DIM>(g, cells, l, c.x + dx, c.y + dy, c.z + dz, &e))
+                    {
+                        acc += lam[e] * (p.scheme == 1 ? s : s * (p.ha[d] + p.hb[d]));
+                    }
+                }
+                mu[k] = acc;
+            }
+        }
+
+        // per-block partial sums of lam . dU/da_d u for the leaf cells
+        template <int DIM>
+        __global__ void k_upwind_da(const Geom* __restrict__ gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
+                                    const double* __restrict__ u, UpwindAdj p, double* partial)
+        {
+            const Geom& g       = *gp;
+            const long long tot = 32 * g.total_words;
+            double acc[3]       = {0., 0., 0.};
+            for (long long k = gtid(); k < tot; k += gstride())
+            {
+                const long long w = k >> 5;
+                const int b       = static_cast<int>(k & 31);
+                if (!((cells[w] >> b) & 1u) || lam[k] == 0.)
+                {
+                    continue;
+                }
+                const int l        = level_of(g, w);
+                const LevelGeom& L = g.lv[l];
+                const double s     = p.dt * pow2d(l);
+                const long long st[3] = {1, 32LL * L.W, 32LL * L.W * L.R};
+                const double uc       = u[k];
+                for (int d = 0; d < DIM; ++d)
+                {
+                    const double ur = u[k + st[d]], ul = u[k - st[d]];
+                    // dF(uL,uR)/da = .5 (uL + uR) + .5 sign(a) (uL - uR)
+                    const double dr = .5 * (uc + ur) + .5 * p.sgn[d] * (uc - ur);
+                    const double dl = .5 * (ul + uc) + .5 * p.sgn[d] * (ul - uc);
+                    acc[d] += lam[k] * (-s * (dr - dl));
+                }
+            }
+            __shared__ double red[3][ABLOCK];
+            for (int d = 0; d < 3; ++d)
+            {
+                red[d][threadIdx.x] = acc[d];
+            }
+            __syncthreads();
+            for (int h = ABLOCK / 2; h > 0; h >>= 1)
+            {
+                if (static_cast<int>(threadIdx.x) < h)
+                {
+                    for (int d = 0; d < 3; ++d)
+                    {
+                        red[d][threadIdx.x] += red[d][threadIdx.x + h];
+                    }
+                }
+                __syncthreads();
+            }
+            if (threadIdx.x == 0)
+            {
+                for (int d = 0; d < 3; ++d)
+                {
+                    partial[3 * blockIdx.x + d] = red[d][0];
+                }
+            }
+        }
+
+        // ga[d] += sum of the partials, in block order (deterministic)
+        __global__ void k_sum_partials(const double* partial, int nb, double* ga)
+        {
+            if (threadIdx.x < 3)
+            {
+                double s = 0.;
+                for (int k = 0; k < nb; ++k)
+                {
+                    s += partial[3 * k + threadIdx.x];
+                }
+                ga[threadIdx.x] += s;
+            }
+        }
+
+        __global__ void k_leaf_scatter(const long long* __restrict__ el, const double* __restrict__ v, long long n, double* dense)
+        {
+            for (long long i = gtid(); i < n; i += gstride())
+            {
+                dense[el[i]] = v[i];
+            }
+        }
+
+        __global__ void k_leaf_gather(const long long* __restrict__ el, const double* __restrict__ dense, long long n, double* v)
+        {
+            for (long long i = gtid(); i < n; i += gstride())
+            {
+                v[i] = dense[el[i]];
+            }
+        }
+
+        int grid_of(long long n)
+        {
+            long long b = (n + ABLOCK - 1) / ABLOCK;
+            b           = std::max(1LL, std::min(b, 152LL * 16));
+            return static_cast<int>(b);
+        }
+    } // namespace
+} // namespace sg
+
+struct sg_adjoint_s
+{
+    sg_mesh_t mesh  = nullptr; // private copy of the initial mesh, then the loop's meshes
+    sg_field_t u    = nullptr;
+    sg_field_t unp1 = nullptr;
+    int K           = 16; // checkpoint interval
+
+    // recorded loop
+    struct Step
+    {
+        int mesh0;   // index in bits of the mesh at the start of the step
+        int n_trans; // meshes bits[mesh0+1 .. mesh0+n_trans] visited by the adaptation
+    };
+    std::vector<uint32_t*> bits; // leaf bitmaps, device
+    std::vector<Step> steps;
+    double a[3] = {0., 0., 0.};
+    double dt = 0., eps = 0., reg = 0.;
+    int scheme = 0;
+    bool have_forward = false;
+    std::vector<double*> ckpt; // dense field at the start of steps 0, K, 2K, ...
+
+    // leaf cells of the initial and the final mesh (for_each_cell order)
+    std::vector<int> lev0, co0, levT, coT;
+    long long* d_el0 = nullptr;
+    long long* d_elT = nullptr;
+    long long n0 = 0, nT = 0, cap0 = 0, capT = 0;
+    double* d_uT     = nullptr; // final leaf values of the last forward
+    long long uT_cap = 0;
+
+    // tape and adjoint buffers
+    sg::TapeDev tape{};
+    long long tape_cap = 0;
+    long long* d_marks = nullptr;
+    long long* h_marks = nullptr;
+    int marks_cap      = 0;
+    double* lam[2]     = {nullptr, nullptr};
+    std::vector<double*> ug; // ghosted field of each step of a segment
+    double* d_partial = nullptr;
+    double* d_ga      = nullptr;
+    double* d_vals    = nullptr; // leaf-value staging
+    long long vals_cap = 0;
+    char err[512]      = "";
+};
+
+namespace
+{
+    using sg::Ctx;
+
+    int afail(int code, const char* msg, const char* detail = nullptr)
+    {
+        sg::set_last_error(msg, detail);
+        return code;
+    }
+
+    Ctx& ctx_of(sg_adjoint_t adj)
+    {
+        return adj->mesh->ctx;
+    }
+
+    int cuda_ok(Ctx& c, const char* what)
+    {
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+        {
+            c.err = std::string(what) + ": " + cudaGetErrorString(e);
+            return SG_ERR_CUDA;
+        }
+        return SG_OK;
+    }
+
+    template <class T>
+    int dmalloc(T** p, size_t n)
+    {
+        if (cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+        {
+            cudaGetLastError();
+            *p = nullptr;
+            return SG_ERR_CUDA;
+        }
+        return SG_OK;
+    }
+
+    template <class T>
+    void dfree(T*& p)
+    {
+        if (p)
+        {
+            cudaFree(p);
+            p = nullptr;
+        }
+    }
+
+    size_t bitmap_bytes(Ctx& c)
+    {
+        return static_cast<size_t>(c.g.total_words) * sizeof(uint32_t);
+    }
+    size_t dense_bytes(Ctx& c)
+    {
+        return static_cast<size_t>(c.capacity) * sizeof(double);
+    }
+
+    // the current mesh becomes the recorded mesh k
+    int load_mesh(sg_adjoint_t adj, int k)
+    {
+        Ctx& c = ctx_of(adj);
+        cudaMemcpyAsync(c.m().cells, adj->bits[static_cast<size_t>(k)], bitmap_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+        int st = sg::build_mesh(c, c.m());
+        c.m().host_valid = false;
+        ++c.mesh_version;
+        adj->u->f.ghosts_valid    = false;
+        adj->unp1->f.ghosts_valid = false;
+        return st;
+    }
+
+    int push_current_bits(sg_adjoint_t adj)
+    {
+        Ctx& c      = ctx_of(adj);
+        uint32_t* b = nullptr;
+        if (dmalloc(&b, static_cast<size_t>(c.g.total_words)))
+        {
+            c.err = "adjoint: out of device memory for the mesh sequence";
+            return SG_ERR_CUDA;
+        }
+        cudaMemcpyAsync(b, c.m().cells, bitmap_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+        adj->bits.push_back(b);
+        return SG_OK;
+    }
+
+    // leaf cells of the current mesh: levels, coordinates and dense elements
+    int current_leaves(sg_adjoint_t adj, std::vector<int>& lev, std::vector<int>& co, long long** d_el, long long* n, long long* cap)
+    {
+        Ctx& c = ctx_of(adj);
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return st;
+        }
+        const long long nc = c.m().nb_cells;
+        const int dim      = c.g.dim;
+        lev.assign(static_cast<size_t>(nc), 0);
+        co.assign(static_cast<size_t>(nc * dim), 0);
+        if (int st = sg_mesh_get_cells(adj->mesh, lev.data(), co.data(), nullptr, nc))
+        {
+            return st;
+        }
+        std::vector<long long> el(static_cast<size_t>(nc));
+        for (long long i = 0; i < nc; ++i)
+        {
+            const int* x = &co[static_cast<size_t>(i * dim)];
+            const sg::Pos p = sg::pos_of(c.g, lev[static_cast<size_t>(i)], x[0], x[1], dim == 3 ? x[2] : 0);
+            el[static_cast<size_t>(i)] = sg::elem(p);
+        }
+        if (nc > *cap)
+        {
+            dfree(*d_el);
+            if (dmalloc(d_el, static_cast<size_t>(nc)))
+            {
+                c.err = "adjoint: out of device memory";
+                return SG_ERR_CUDA;
+            }
+            *cap = nc;
+        }
+        cudaMemcpyAsync(*d_el, el.data(), static_cast<size_t>(nc) * sizeof(long long), cudaMemcpyHostToDevice, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return sg::check(c, "adjoint leaves");
+        }
+        *n = nc;
+        return SG_OK;
+    }
+
+    int stage_vals(sg_adjoint_t adj, long long n)
+    {
+        if (n > adj->vals_cap)
+        {
+            dfree(adj->d_vals);
+            if (dmalloc(&adj->d_vals, static_cast<size_t>(n)))
+            {
+                ctx_of(adj).err = "adjoint: out of device memory";
+                return SG_ERR_CUDA;
+            }
+            adj->vals_cap = n;
+        }
+        return SG_OK;
+    }
+
+    // dense field of the initial mesh from leaf values (host), other entries 0
+    int set_initial_field(sg_adjoint_t adj, const double* u0, double* dense)
+    {
+        Ctx& c = ctx_of(adj);
+        if (int st = stage_vals(adj, adj->n0))
+        {
+            return st;
+        }
+        cudaMemsetAsync(dense, 0, dense_bytes(c), c.stream);
+        cudaMemcpyAsync(adj->d_vals, u0, static_cast<size_t>(adj->n0) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        sg::k_leaf_scatter<<<sg::grid_of(adj->n0), sg::ABLOCK, 0, c.stream>>>(adj->d_el0, adj->d_vals, adj->n0, dense);
+        return cuda_ok(c, "adjoint initial field");
+    }
+
+    int ensure_ckpt(sg_adjoint_t adj, size_t k)
+    {
+        Ctx& c = ctx_of(adj);
+        while (adj->ckpt.size() <= k)
+        {
+            double* p = nullptr;
+            if (dmalloc(&p, static_cast<size_t>(c.capacity)))
+            {
+                c.err = "adjoint: out of device memory for checkpoints";
+                return SG_ERR_CUDA;
+            }
+            adj->ckpt.push_back(p);
+        }
+        return SG_OK;
+    }
+
+    void free_recording(sg_adjoint_t adj)
+    {
+        for (size_t k = 1; k < adj->bits.size(); ++k)
+        {
+            dfree(adj->bits[k]);
+        }
+        if (!adj->bits.empty())
+        {
+            adj->bits.resize(1);
+        }
+        adj->steps.clear();
+        adj->have_forward = false;
+    }
+
+    // the recorded steps [s, e) on their meshes, value mode, from the field
+    // already in u (on the mesh of step s, loaded by the caller).  With a
+    // tape: every ghost/update_fields launch is also recorded (phases
+    // appended to `phases`), and the ghosted field of step n is kept in ug[n-s].
+    enum PhaseKind : int
+    {
+        PH_GHOST    = 0, // in place on the field
+        PH_TRANSFER = 1, // update_fields: new field from the old one
+        PH_UPWIND   = 2  // the upwind step of step `step`
+    };
+    struct Phase
+    {
+        int kind;
+        int step;
+        int mesh; // index in bits of the mesh the upwind ran on
+    };
+
+    int replay_range(sg_adjoint_t adj, int s, int e, bool taped, std::vector<Phase>* phases, bool store_ckpt)
+    {
+        Ctx& c               = ctx_of(adj);
+        sg::DeviceField& u   = adj->u->f;
+        sg::DeviceField& up1 = adj->unp1->f;
+        int st;
+        int np = 0;
+        auto mark = [&]()
+        {
+            sg::k_tape_mark<<<1, 1, 0, c.stream>>>(adj->tape.count, adj->d_marks, np);
+            ++np;
+        };
+        auto room = [&](int extra) { return np + extra < adj->marks_cap; };
+        for (int n = s; n < e; ++n)
+        {
+            const auto& S = adj->steps[static_cast<size_t>(n)];
+            if (store_ckpt && n % adj->K == 0)
+            {
+                if ((st = ensure_ckpt(adj, static_cast<size_t>(n / adj->K))))
+                {
+                    return st;
+                }
+                cudaMemcpyAsync(adj->ckpt[static_cast<size_t>(n / adj->K)], u.data, dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+            }
+            for (int t = 1; t <= S.n_trans; ++t)
+            {
+                if ((st = sg::ghost_value(c, c.m(), u.data, u.has_bc, u.bc_value)))
+                {
+                    return st;
+                }
+                if (taped)
+                {
+                    if (!room(256))
+                    {
+                        c.err = "adjoint: too many launches in one segment";
+                        return SG_ERR_CAPACITY;
+                    }
+                    const int p0 = np;
+                    if ((st = sg::ghost_tape(c, c.m(), adj->tape, u.has_bc, u.bc_value, mark)))
+                    {
+                        return st;
+                    }
+                    for (int p = p0; p < np; ++p)
+                    {
+                        phases->push_back({PH_GHOST, n, -1});
+                    }
+                }
+                sg::DeviceMesh& nm = c.spare();
+                cudaMemcpyAsync(nm.cells, adj->bits[static_cast<size_t>(S.mesh0 + t)], bitmap_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+                if ((st = sg::build_mesh(c, nm)))
+                {
+                    return st;
+                }
+                if ((st = sg::update_fields_value(c, c.m(), nm, u.data, u.spare)))
+                {
+                    return st;
+                }
+                if (taped)
+                {
+                    if ((st = sg::update_fields_tape(c, c.m(), nm, adj->tape)))
+                    {
+                        return st;
+                    }
+                    mark();
+                    phases->push_back({PH_TRANSFER, n, -1});
+                }
+                nm.host_valid = false;
+                std::swap(u.data, u.spare);
+                c.cur = 1 - c.cur;
+                ++c.mesh_version;
+            }
+            if ((st = sg::ghost_value(c, c.m(), u.data, u.has_bc, u.bc_value)))
+            {
+                return st;
+            }
+            if (taped)
+            {
+                if (!room(256))
+                {
+                    c.err = "adjoint: too many launches in one segment";
+                    return SG_ERR_CAPACITY;
+                }
+                const int p0 = np;
+                if ((st = sg::ghost_tape(c, c.m(), adj->tape, u.has_bc, u.bc_value, mark)))
+                {
+                    return st;
+                }
+                for (int p = p0; p < np; ++p)
+                {
+                    phases->push_back({PH_GHOST, n, -1});
+                }
+                cudaMemcpyAsync(adj->ug[static_cast<size_t>(n - s)], u.data, dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+                mark(); // empty phase: keeps marks and phases aligned
+                phases->push_back({PH_UPWIND, n, S.mesh0 + S.n_trans});
+            }
+            u.ghosts_valid = false;
+            if ((st = sg::upwind(c, u, up1, adj->a, adj->dt, adj->scheme)))
+            {
+                return st;
+            }
+            std::swap(u.data, up1.data);
+            up1.ghosts_valid = false;
+        }
+        return cuda_ok(c, "adjoint replay");
+    }
+
+    // leaves of the final mesh and their values (kept for sg_adjoint_final)
+    int final_leaves(sg_adjoint_t adj)
+    {
+        Ctx& c = ctx_of(adj);
+        if (int st = current_leaves(adj, adj->levT, adj->coT, &adj->d_elT, &adj->nT, &adj->capT))
+        {
+            return st;
+        }
+        if (adj->nT > adj->uT_cap)
+        {
+            dfree(adj->d_uT);
+            if (dmalloc(&adj->d_uT, static_cast<size_t>(adj->nT)))
+            {
+                c.err = "adjoint: out of device memory";
+                return SG_ERR_CUDA;
+            }
+            adj->uT_cap = adj->nT;
+        }
+        sg::k_leaf_gather<<<sg::grid_of(adj->nT), sg::ABLOCK, 0, c.stream>>>(adj->d_elT, adj->u->f.data, adj->nT, adj->d_uT);
+        return cuda_ok(c, "adjoint final field");
+    }
+
+    int ensure_tape(sg_adjoint_t adj, long long cap)
+    {
+        Ctx& c = ctx_of(adj);
+        if (cap <= adj->tape_cap)
+        {
+            return SG_OK;
+        }
+        dfree(adj->tape.dst);
+        dfree(adj->tape.src);
+        dfree(adj->tape.w);
+        if (dmalloc(&adj->tape.dst, static_cast<size_t>(cap)) || dmalloc(&adj->tape.src, static_cast<size_t>(cap))
+            || dmalloc(&adj->tape.w, static_cast<size_t>(cap)))
+        {
+            c.err = "adjoint: out of device memory for the tape";
+            adj->tape_cap = 0;
+            return SG_ERR_CUDA;
+        }
+        adj->tape_cap = cap;
+        adj->tape.cap = cap;
+        return SG_OK;
+    }
+
+    sg::UpwindAdj upwind_adj(sg_adjoint_t adj)
+    {
+        sg::UpwindAdj p{};
+        for (int d = 0; d < 3; ++d)
+        {
+            p.ha[d]  = .5 * adj->a[d];
+            p.hb[d]  = .5 * std::fabs(adj->a[d]);
+            p.sgn[d] = adj->a[d] > 0. ? 1. : (adj->a[d] < 0. ? -1. : 0.);
+        }
+        p.dt     = adj->dt;
+        p.scheme = adj->scheme;
+        return p;
+    }
+
+    // reverse pass over one segment whose phases and tape are recorded;
+    // lam[0] holds the adjoint of the field after the segment
+    int reverse_segment(sg_adjoint_t adj, int s, const std::vector<Phase>& phases)
+    {
+        Ctx& c = ctx_of(adj);
+        const long long tot = 32 * c.g.total_words;
+        const sg::UpwindAdj p = upwind_adj(adj);
+        const int nb_da = sg::grid_of(tot);
+        for (int k = static_cast<int>(phases.size()) - 1; k >= 0; --k)
+        {
+            const Phase& ph   = phases[static_cast<size_t>(k)];
+            const long long b = k > 0 ? adj->h_marks[k - 1] : 0;
+            const long long e = adj->h_marks[k];
+            if (ph.kind == PH_UPWIND)
+            {
+                const uint32_t* cells = adj->bits[static_cast<size_t>(ph.mesh)];
+                if (p.scheme == 0)
+                {
+                    if (c.g.dim == 2)
+                    {
+                        sg::k_upwind_da<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->ug[static_cast<size_t>(ph.step - s)], p,
+                                                                              adj->d_partial);
+                    }
+                    else
+                    {
+                        sg::k_upwind_da<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->ug[static_cast<size_t>(ph.step - s)], p,
+                                                                              adj->d_partial);
+                    }
+                    sg::k_sum_partials<<<1, 32, 0, c.stream>>>(adj->d_partial, nb_da, adj->d_ga);
+                }
+                if (c.g.dim == 2)
+                {
+                    sg::k_upwind_adjoint<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->lam[1], p);
+                }
+                else
+                {
+                    sg::k_upwind_adjoint<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->lam[1], p);
+                }
+                std::swap(adj->lam[0], adj->lam[1]);
+            }
+            else if (ph.kind == PH_GHOST)
+            {
+                if (e > b)
+                {
+                    sg::k_tape_scatter<<<sg::grid_of(e - b), sg::ABLOCK, 0, c.stream>>>(adj->tape.dst, adj->tape.src, adj->tape.w, b, e, adj->lam[0],
+                                                                                         adj->lam[0]);
+                    sg::k_tape_zero<<<sg::grid_of(e - b), sg::ABLOCK, 0, c.stream>>>(adj->tape.dst, b, e, adj->lam[0]);
+                }
+            }
+            else
+            {
+                cudaMemsetAsync(adj->lam[1], 0, dense_bytes(c), c.stream);
+                if (e > b)
+                {
+                    sg::k_tape_scatter<<<sg::grid_of(e - b), sg::ABLOCK, 0, c.stream>>>(adj->tape.dst, adj->tape.src, adj->tape.w, b, e, adj->lam[0],
+                                                                                         adj->lam[1]);
+                }
+                std::swap(adj->lam[0], adj->lam[1]);
+            }
+        }
+        return cuda_ok(c, "adjoint reverse");
+    }
+} // namespace
+
+extern "C"
+{
+    int sg_adjoint_create(sg_field_t u, int checkpoint_every, sg_adjoint_t* out)
+    {
+        if (!u || !out || checkpoint_every < 1)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_create: need a field, checkpoint_every >= 1 and an output handle");
+        }
+        *out         = nullptr;
+        sg::Ctx& uc  = u->mesh->ctx;
+        const auto& cfg = uc.cfg;
+        auto* adj    = new (std::nothrow) sg_adjoint_s();
+        if (!adj)
+        {
+            return afail(SG_ERR_CAPACITY, "sg_adjoint_create: out of host memory");
+        }
+        adj->K = checkpoint_every;
+        int st = sg_mesh_create(cfg.dim, cfg.min_level, cfg.max_level, cfg.max_stencil_radius, cfg.prediction_radius, cfg.graduation_width, &adj->mesh);
+        if (st)
+        {
+            delete adj;
+            return st;
+        }
+        // the initial mesh: u's current leaf cells
+        long long nc = 0, nref = 0;
+        if ((st = sg_mesh_counts(u->mesh, &nc, &nref)))
+        {
+            sg_adjoint_destroy(adj);
+            return st;
+        }
+        std::vector<int> lev(static_cast<size_t>(nc)), co(static_cast<size_t>(nc * cfg.dim));
+        if ((st = sg_mesh_get_cells(u->mesh, lev.data(), co.data(), nullptr, nc)) || (st = sg_mesh_set_cells(adj->mesh, nc, lev.data(), co.data()))
+            || (st = sg_field_create(adj->mesh, "u", &adj->u)) || (st = sg_field_create(adj->mesh, "unp1", &adj->unp1)))
+        {
+            sg_adjoint_destroy(adj);
+            return st;
+        }
+        if (u->f.has_bc && (st = sg_field_set_dirichlet(adj->u, u->f.bc_value)))
+        {
+            sg_adjoint_destroy(adj);
+            return st;
+        }
+        Ctx& c = ctx_of(adj);
+        if (c.capacity >= (1LL << 31))
+        {
+            sg_adjoint_destroy(adj);
+            return afail(SG_ERR_CAPACITY, "sg_adjoint_create: the tape indexes elements with 32 bits; this mesh has more");
+        }
+        if (sg::ensure_spare(c, adj->u->f) || push_current_bits(adj)
+            || current_leaves(adj, adj->lev0, adj->co0, &adj->d_el0, &adj->n0, &adj->cap0) != SG_OK)
+        {
+            const int code = SG_ERR_CUDA;
+            sg::set_last_error(c.err.c_str(), nullptr);
+            sg_adjoint_destroy(adj);
+            return code;
+        }
+        adj->marks_cap = 1 << 16;
+        if (dmalloc(&adj->d_marks, static_cast<size_t>(adj->marks_cap)) || cudaMallocHost(reinterpret_cast<void**>(&adj->h_marks), sizeof(long long) * adj->marks_cap) != cudaSuccess
+            || dmalloc(&adj->tape.count, 1) || dmalloc(&adj->tape.overflow, 1) || dmalloc(&adj->lam[0], static_cast<size_t>(c.capacity))
+            || dmalloc(&adj->lam[1], static_cast<size_t>(c.capacity)) || dmalloc(&adj->d_partial, static_cast<size_t>(3 * 152 * 16))
+            || dmalloc(&adj->d_ga, 3))
+        {
+            sg_adjoint_destroy(adj);
+            return afail(SG_ERR_CUDA, "sg_adjoint_create: out of device memory");
+        }
+        *out = adj;
+        return SG_OK;
+    }
+
+    int sg_adjoint_destroy(sg_adjoint_t adj)
+    {
+        if (!adj)
+        {
+            return SG_OK;
+        }
+        if (adj->mesh)
+        {
+            cudaStreamSynchronize(adj->mesh->ctx.stream);
+        }
+        for (auto*& b : adj->bits)
+        {
+            dfree(b);
+        }
+        for (auto*& p : adj->ckpt)
+        {
+            dfree(p);
+        }
+        for (auto*& p : adj->ug)
+        {
+            dfree(p);
+        }
+        dfree(adj->d_el0);
+        dfree(adj->d_elT);
+        dfree(adj->d_uT);
+        dfree(adj->tape.dst);
+        dfree(adj->tape.src);
+        dfree(adj->tape.w);
+        dfree(adj->tape.count);
+        dfree(adj->tape.overflow);
+        dfree(adj->d_marks);
+        if (adj->h_marks)
+        {
+            cudaFreeHost(adj->h_marks);
+        }
+        dfree(adj->lam[0]);
+        dfree(adj->lam[1]);
+        dfree(adj->d_partial);
+        dfree(adj->d_ga);
+        dfree(adj->d_vals);
+        if (adj->u)
+        {
+            sg_field_destroy(adj->u);
+        }
+        if (adj->unp1)
+        {
+            sg_field_destroy(adj->unp1);
+        }
+        if (adj->mesh)
+        {
+            sg_mesh_destroy(adj->mesh);
+        }
+        delete adj;
+        return SG_OK;
+    }
+
+    int sg_adjoint_counts(sg_adjoint_t adj, long long* n0, long long* nT, int* n_steps)
+    {
+        if (!adj)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_counts: null handle");
+        }
+        if (n0)
+        {
+            *n0 = adj->n0;
+        }
+        if (nT)
+        {
+            *nT = adj->have_forward ? adj->nT : 0;
+        }
+        if (n_steps)
+        {
+            *n_steps = static_cast<int>(adj->steps.size());
+        }
+        return SG_OK;
+    }
+
+    int sg_adjoint_cells(sg_adjoint_t adj, int which, int* level, int* coords, long long n)
+    {
+        if (!adj || (which != 0 && which != 1))
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_cells: which is 0 (initial mesh) or 1 (final mesh)");
+        }
+        if (which == 1 && !adj->have_forward)
+        {
+            return afail(SG_ERR_STATE, "sg_adjoint_cells: no forward run yet");
+        }
+        const auto& lev = which ? adj->levT : adj->lev0;
+        const auto& co  = which ? adj->coT : adj->co0;
+        if (n != static_cast<long long>(lev.size()))
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_cells: size differs from the number of cells");
+        }
+        if (level)
+        {
+            std::copy(lev.begin(), lev.end(), level);
+        }
+        if (coords)
+        {
+            std::copy(co.begin(), co.end(), coords);
+        }
+        return SG_OK;
+    }
+
+    int sg_adjoint_record(sg_adjoint_t adj, const double* u0, int n_steps, double eps, double regularity, const double* a, double dt, int scheme,
+                          long long* nT)
+    {
+        if (!adj || !u0 || !a || n_steps < 0 || (scheme != SG_UPWIND_OP && scheme != SG_README))
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_record: invalid argument");
+        }
+        Ctx& c = ctx_of(adj);
+        if (scheme == SG_README && c.g.dim != 2)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_record: the README scheme is two-dimensional");
+        }
+        free_recording(adj);
+        for (int d = 0; d < 3; ++d)
+        {
+            adj->a[d] = d < c.g.dim ? a[d] : 0.;
+        }
+        adj->dt     = dt;
+        adj->eps    = eps;
+        adj->reg    = regularity;
+        adj->scheme = scheme;
+        sg::DeviceField& u   = adj->u->f;
+        sg::DeviceField& up1 = adj->unp1->f;
+        int st;
+        if ((st = load_mesh(adj, 0)) || (st = set_initial_field(adj, u0, u.data)))
+        {
+            return afail(st, c.err.c_str());
+        }
+        const int passes = c.cfg.max_level - c.cfg.min_level;
+        for (int n = 0; n < n_steps; ++n)
+        {
+            if (n % adj->K == 0)
+            {
+                if ((st = ensure_ckpt(adj, static_cast<size_t>(n / adj->K))))
+                {
+                    return afail(st, c.err.c_str());
+                }
+                cudaMemcpyAsync(adj->ckpt[static_cast<size_t>(n / adj->K)], u.data, dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+            }
+            sg_adjoint_s::Step S{static_cast<int>(adj->bits.size()) - 1, 0};
+            for (int i = 0; i < passes; ++i)
+            {
+                bool conv = false;
+                if ((st = sg::harten(c, u, i, eps, regularity, &conv)))
+                {
+                    return afail(st, c.err.c_str());
+                }
+                if (conv)
+                {
+                    break;
+                }
+                if ((st = push_current_bits(adj)))
+                {
+                    return afail(st, c.err.c_str());
+                }
+                ++S.n_trans;
+            }
+            adj->steps.push_back(S);
+            if ((st = sg::update_ghost_mr(c, u)) || (st = sg::upwind(c, u, up1, adj->a, dt, scheme)))
+            {
+                return afail(st, c.err.c_str());
+            }
+            std::swap(u.data, up1.data);
+            u.ghosts_valid   = false;
+            up1.ghosts_valid = false;
+        }
+        if ((st = sg::device_error(c)) || (st = final_leaves(adj)))
+        {
+            return afail(st, c.err.c_str());
+        }
+        adj->have_forward = true;
+        if (nT)
+        {
+            *nT = adj->nT;
+        }
+        return SG_OK;
+    }
+
+    int sg_adjoint_final(sg_adjoint_t adj, double* uT, long long n)
+    {
+        if (!adj || !uT)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_final: null argument");
+        }
+        if (!adj->have_forward || n != adj->nT)
+        {
+            return afail(SG_ERR_STATE, "sg_adjoint_final: no forward run, or n differs from the final number of cells");
+        }
+        Ctx& c = ctx_of(adj);
+        cudaMemcpyAsync(uT, adj->d_uT, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return afail(SG_ERR_CUDA, "sg_adjoint_final: CUDA error");
+        }
+        return SG_OK;
+    }
+
+    int sg_adjoint_replay(sg_adjoint_t adj, const double* u0, const double* a, double* uT)
+    {
+        if (!adj || !u0 || !a)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_replay: null argument");
+        }
+        if (!adj->have_forward)
+        {
+            return afail(SG_ERR_STATE, "sg_adjoint_replay: nothing recorded");
+        }
+        Ctx& c = ctx_of(adj);
+        for (int d = 0; d < 3; ++d)
+        {
+            adj->a[d] = d < c.g.dim ? a[d] : 0.;
+        }
+        int st;
+        if ((st = load_mesh(adj, 0)) || (st = set_initial_field(adj, u0, adj->u->f.data))
+            || (st = replay_range(adj, 0, static_cast<int>(adj->steps.size()), false, nullptr, true)))
+        {
+            return afail(st, c.err.c_str());
+        }
+        if ((st = sg::device_error(c)))
+        {
+            return afail(st, c.err.c_str());
+        }
+        // the final mesh is the recorded one: same leaves as after record
+        sg::k_leaf_gather<<<sg::grid_of(adj->nT), sg::ABLOCK, 0, c.stream>>>(adj->d_elT, adj->u->f.data, adj->nT, adj->d_uT);
+        return uT ? sg_adjoint_final(adj, uT, adj->nT) : SG_OK;
+    }
+
+    int sg_adjoint_backward(sg_adjoint_t adj, const double* gT, double* g0, double* ga)
+    {
+        if (!adj || !gT || !g0)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_backward: null argument");
+        }
+        if (!adj->have_forward)
+        {
+            return afail(SG_ERR_STATE, "sg_adjoint_backward: nothing recorded");
+        }
+        Ctx& c         = ctx_of(adj);
+        const int T    = static_cast<int>(adj->steps.size());
+        const int K    = adj->K;
+        int st;
+        // lam = dJ/du_T on the final leaves, 0 elsewhere
+        if ((st = stage_vals(adj, std::max(adj->nT, adj->n0))))
+        {
+            return afail(st, c.err.c_str());
+        }
+        cudaMemsetAsync(adj->lam[0], 0, dense_bytes(c), c.stream);
+        cudaMemcpyAsync(adj->d_vals, gT, static_cast<size_t>(adj->nT) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        sg::k_leaf_scatter<<<sg::grid_of(adj->nT), sg::ABLOCK, 0, c.stream>>>(adj->d_elT, adj->d_vals, adj->nT, adj->lam[0]);
+        cudaMemsetAsync(adj->d_ga, 0, 3 * sizeof(double), c.stream);
+        while (static_cast<int>(adj->ug.size()) < std::min(K, std::max(T, 1)))
+        {
+            double* p = nullptr;
+            if (dmalloc(&p, static_cast<size_t>(c.capacity)))
+            {
+                return afail(SG_ERR_CUDA, "sg_adjoint_backward: out of device memory");
+            }
+            adj->ug.push_back(p);
+        }
+        if ((st = ensure_tape(adj, std::max(adj->tape_cap, 8 * c.capacity))))
+        {
+            return afail(st, c.err.c_str());
+        }
+        std::vector<Phase> phases;
+        for (int s = ((T - 1) / K) * K; s >= 0 && T > 0; s -= K)
+        {
+            const int e = std::min(T, s + K);
+            for (int attempt = 0;; ++attempt)
+            {
+                phases.clear();
+                cudaMemsetAsync(adj->tape.count, 0, sizeof(long long), c.stream);
+                cudaMemsetAsync(adj->tape.overflow, 0, sizeof(int), c.stream);
+                if ((st = load_mesh(adj, adj->steps[static_cast<size_t>(s)].mesh0)))
+                {
+                    return afail(st, c.err.c_str());
+                }
+                cudaMemcpyAsync(adj->u->f.data, adj->ckpt[static_cast<size_t>(s / K)], dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+                if ((st = replay_range(adj, s, e, true, &phases, false)))
+                {
+                    return afail(st, c.err.c_str());
+                }
+                int overflow    = 0;
+                long long count = 0;
+                cudaMemcpyAsync(&overflow, adj->tape.overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+                cudaMemcpyAsync(&count, adj->tape.count, sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
+                cudaMemcpyAsync(adj->h_marks, adj->d_marks, sizeof(long long) * phases.size(), cudaMemcpyDeviceToHost, c.stream);
+                if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+                {
+                    return afail(SG_ERR_CUDA, "sg_adjoint_backward: CUDA error in the recomputation");
+                }
+                if (overflow & 1)
+                {
+                    return afail(SG_ERR_CAPACITY, "sg_adjoint_backward: a recorded operator has more terms than a form holds");
+                }
+                if (!(overflow & 2))
+                {
+                    break;
+                }
+                if (attempt > 4 || (st = ensure_tape(adj, std::max(2 * adj->tape_cap, count + count / 4))))
+                {
+                    return afail(SG_ERR_CUDA, "sg_adjoint_backward: the tape does not fit in device memory");
+                }
+            }
+            if ((st = reverse_segment(adj, s, phases)))
+            {
+                return afail(st, c.err.c_str());
+            }
+        }
+        if ((st = sg::device_error(c)))
+        {
+            return afail(st, c.err.c_str());
+        }
+        sg::k_leaf_gather<<<sg::grid_of(adj->n0), sg::ABLOCK, 0, c.stream>>>(adj->d_el0, adj->lam[0], adj->n0, adj->d_vals);
+        cudaMemcpyAsync(g0, adj->d_vals, static_cast<size_t>(adj->n0) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        double h_ga[3] = {0., 0., 0.};
+        cudaMemcpyAsync(h_ga, adj->d_ga, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return afail(SG_ERR_CUDA, "sg_adjoint_backward: CUDA error");
+        }
+        if (ga)
+        {
+            for (int d = 0; d < c.g.dim; ++d)
+            {
+                ga[d] = h_ga[d];
+            }
+        }
+        return SG_OK;
+    }
+}

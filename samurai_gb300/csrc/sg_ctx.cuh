@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdio>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -176,6 +177,12 @@ namespace sg
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value);
     int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged);
     int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity); // no synchronisation
+    // one step's linear operators on a frozen mesh (replay and adjoint)
+    struct TapeDev;
+    int ghost_value(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv);
+    int ghost_tape(Ctx& c, DeviceMesh& m, const TapeDev& t, bool has_bc, double bcv, const std::function<void()>& mark);
+    int update_fields_value(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un);
+    int update_fields_tape(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const TapeDev& t);
     int harten_end(Ctx& c, DeviceField& f, bool* converged);
     int device_error(Ctx& c); // reads and clears the device error word (synchronises)
 

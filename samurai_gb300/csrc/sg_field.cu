@@ -5,7 +5,10 @@
 // rounded on its own, in the reference's association order, so that the
 // detail thresholds take the same decisions as the CPU implementation.
 #include <cstring>
+#include <functional>
+#include <type_traits>
 
+#include "sg_access.cuh"
 #include "sg_ctx.cuh"
 
 namespace sg
@@ -95,14 +98,15 @@ namespace sg
         }
 
         // prediction_op<order,false> for one fine cell (numeric/prediction.hpp:286-361)
-        __device__ __forceinline__ double predict_one(const Geom& g, const double* u, int l, int x, int y, int z, int order)
+        template <class A>
+        __device__ __forceinline__ typename A::V predict_one(const Geom& g, const A& u, int l, int x, int y, int z, int order)
         {
             const int px = x >> 1, py = y >> 1, pz = z >> 1;
             if (order == 0)
             {
-                return u[elem_at(g, l - 1, px, py, pz)];
+                return u.get(elem_at(g, l - 1, px, py, pz));
             }
-            double acc  = 0.;
+            typename A::V acc = A::konst(0.);
             const int nz = (g.dim == 3) ? 3 : 1;
             for (int sz = 0; sz < nz; ++sz)
             {
@@ -118,7 +122,7 @@ namespace sg
                         {
                             coeff = coeff * interp1(z & 1, sz);
                         }
-                        acc = acc + u[base + sx] * coeff;
+                        acc = acc + u.get(base + sx) * coeff;
                     }
                 }
             }
@@ -126,16 +130,17 @@ namespace sg
         }
 
         // projection_op_ (numeric/projection.hpp:15-65)
-        __device__ __forceinline__ double project_one(const Geom& g, const double* u, int lf, int x, int y, int z)
+        template <class A>
+        __device__ __forceinline__ typename A::V project_one(const Geom& g, const A& u, int lf, int x, int y, int z)
         {
-            double sum   = 0.;
+            typename A::V sum = A::konst(0.);
             const int nz = (g.dim == 3) ? 2 : 1;
             for (int sz = 0; sz < nz; ++sz)
             {
                 for (int sy = 0; sy < 2; ++sy)
                 {
                     const long long e = elem_at(g, lf, 2 * x, 2 * y + sy, (g.dim == 3) ? 2 * z + sz : 0);
-                    sum               = sum + (u[e] + u[e + 1]);
+                    sum               = sum + (u.get(e) + u.get(e + 1));
                 }
             }
             const double inv = (g.dim == 3) ? 0.125 : 0.25;
@@ -184,8 +189,10 @@ namespace sg
         // update_outer_corners_by_polynomial_extrapolation for a ghost width
         // of 1 (bc/apply_field_bc.hpp:371-505) followed by project_corner_below
         // (algorithm/update_outer_ghost.hpp:268-337), one block per diagonal
-        // direction.
-        __device__ void corner_role(const Geom& g, const int* d, int l, const uint32_t* cells, const uint32_t* ref, double* u)
+        // direction.  parts: 1 the corners, 2 their projection below, 3 both
+        // (the projection reads the corners, after a block barrier).
+        template <class A>
+        __device__ void corner_role(const Geom& g, const int* d, int l, const uint32_t* cells, const uint32_t* ref, const A& u, int parts = 3)
         {
             const int n = g.lv[l].n;
             int nfree   = 0;
@@ -194,7 +201,7 @@ namespace sg
                 nfree += (d[k] == 0);
             }
             const long long npos = (nfree == 0) ? 1 : n; // 3D edges have one free axis
-            for (long long t = threadIdx.x; t < npos; t += blockDim.x)
+            for (long long t = threadIdx.x; (parts & 1) && t < npos; t += blockDim.x)
             {
                 int c[3];
                 for (int k = 0; k < 3; ++k)
@@ -205,10 +212,20 @@ namespace sg
                 if (test(cells, pc))
                 {
                     const long long eg = elem_at(g, l, c[0] + d[0], c[1] + d[1], g.dim == 3 ? c[2] + d[2] : 0);
-                    u[eg]              = u[elem(pc)];
+                    u.put(eg, u.get(elem(pc)));
                 }
             }
-            __syncthreads();
+            if (parts != 3)
+            {
+                if (!(parts & 2))
+                {
+                    return;
+                }
+            }
+            else
+            {
+                __syncthreads();
+            }
             for (int dl = 1; dl <= 2; ++dl)
             {
                 const int pl = l - dl;
@@ -235,7 +252,7 @@ namespace sg
                     const Pos pf = pos_of(g, l, ch[0], ch[1], ch[2]);
                     if (test(ref, pg) && test(ref, pf))
                     {
-                        u[elem(pg)] = u[elem(pf)];
+                        u.put(elem(pg), u.get(elem(pf)));
                     }
                 }
             }
@@ -285,6 +302,7 @@ namespace sg
             int nb_face;      // blocks of the face role
             long long nfaces; // face positions (2*dim directions)
             int do_proj;      // project the reference of level l onto proj_cells[l-1]
+            int corner_parts; // corner_role parts run by the corner blocks
         };
 
         // One launch per level of the top-down pass of update_ghost_mr
@@ -298,9 +316,9 @@ namespace sg
         //    (update_outer_ghost.hpp:20-155) next to union cells;
         //  - projection of the reference cells of level l onto proj_cells[l-1]
         //    (numeric/projection.hpp:15-65).
-        template <int DIM>
+        template <int DIM, class A>
         __device__ __forceinline__ void face_work(const Geom& g, const GhostLevelArgs& a, long long t, const uint32_t* cells, const uint32_t* uni,
-                                                  const uint32_t* ref, double* u)
+                                                  const uint32_t* ref, const A& u)
         {
             const int l        = a.l;
             const int n        = g.lv[l].n;
@@ -313,13 +331,18 @@ namespace sg
             if ((a.do_dirichlet || a.do_predict) && test(cells, pi))
             {
                 const long long eg = elem_at(g, l, gx, gy, gz);
+                typename A::V v;
                 if (a.do_dirichlet)
                 {
-                    u[eg] = 2 * a.value - u[elem(pi)];
+                    v = A::konst(2 * a.value) - u.get(elem(pi));
+                    u.put(eg, v);
+                }
+                else
+                {
+                    v = u.get(eg);
                 }
                 if (a.do_predict)
                 {
-                    const double v = u[eg];
                     for (int sz = 0; sz < (DIM == 3 ? 2 : 1); ++sz)
                     {
                         for (int sy = 0; sy < 2; ++sy)
@@ -329,7 +352,7 @@ namespace sg
                                 const Pos pf = pos_of(g, l + 1, 2 * gx + sx, 2 * gy + sy, DIM == 3 ? 2 * gz + sz : 0);
                                 if (test(ref, pf))
                                 {
-                                    u[elem(pf)] = v;
+                                    u.put(elem(pf), v);
                                 }
                             }
                         }
@@ -343,8 +366,8 @@ namespace sg
                 {
                     return;
                 }
-                double sum = 0.;
-                int nch    = 0;
+                typename A::V sum = A::konst(0.);
+                int nch           = 0;
                 for (int dl = 1; dl <= 2 && nch == 0 && l + dl < g.nlev; ++dl)
                 {
                     const int lc = l + dl;
@@ -358,22 +381,22 @@ namespace sg
                                 const Pos pc = pos_of(g, lc, gx * m + sx, gy * m + sy, DIM == 3 ? gz * m + sz : 0);
                                 if (test(ref, pc))
                                 {
-                                    sum = sum + u[elem(pc)];
+                                    sum = sum + u.get(elem(pc));
                                     ++nch;
                                 }
                             }
                         }
                     }
                 }
-                u[elem(pg)] = nch > 0 ? sum / static_cast<double>(nch) : 0.;
+                u.put(elem(pg), nch > 0 ? sum / static_cast<double>(nch) : A::konst(0.));
             }
         }
 
         // projection of the reference cells of level l onto proj_cells[l-1]
         // (numeric/projection.hpp:15-65), warps warp0, warp0+nwarps, ...
-        template <int DIM>
+        template <int DIM, class A>
         __device__ __forceinline__ void project_level(const Geom& g, int l, const int* wl_ref, const long long* lo, const uint32_t* proj, const uint32_t* ref,
-                                                      double* u, long long warp0, long long nwarps)
+                                                      const A& u, long long warp0, long long nwarps)
         {
             const int lc = l - 1;
             warp_list(wl_ref, lo[LO_REF + lc], lo[LO_REF + lc + 1], warp0, nwarps,
@@ -384,16 +407,16 @@ namespace sg
                       },
                       [&](long long w, int b)
                       {
-                          const Cell c  = cell_of(g, lc, w, b);
-                          u[32 * w + b] = project_one(g, u, l, c.x, c.y, c.z);
+                          const Cell c = cell_of(g, lc, w, b);
+                          u.put(32 * w + b, project_one(g, u, l, c.x, c.y, c.z));
                       });
         }
 
         // prediction of the ghosts of level l from level l-1
         // (algorithm/update_ghost_mr.hpp:224-233)
-        template <int DIM>
+        template <int DIM, class A>
         __device__ __forceinline__ void predict_level(const Geom& g, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
-                                                      const uint32_t* proj, const uint32_t* ref, double* u, long long warp0, long long nwarps)
+                                                      const uint32_t* proj, const uint32_t* ref, const A& u, long long warp0, long long nwarps)
         {
             warp_list(wl_ref, lo[LO_REF + l], lo[LO_REF + l + 1], warp0, nwarps,
                       [&](long long w)
@@ -403,8 +426,8 @@ namespace sg
                       },
                       [&](long long w, int b)
                       {
-                          const Cell c  = cell_of(g, l, w, b);
-                          u[32 * w + b] = predict_one(g, u, l, c.x, c.y, c.z, order);
+                          const Cell c = cell_of(g, l, w, b);
+                          u.put(32 * w + b, predict_one(g, u, l, c.x, c.y, c.z, order));
                       });
         }
 
@@ -418,9 +441,9 @@ namespace sg
         //    (update_outer_ghost.hpp:195-266) by the same thread, or project_bc
         //    (update_outer_ghost.hpp:20-155) next to union cells;
         //  - projection of the reference cells of level l onto proj_cells[l-1].
-        template <int DIM>
+        template <int DIM, class A>
         __global__ void k_ghost_level(const Geom* __restrict__ gp, GhostLevelArgs a, const int* wl_ref, const long long* lo, const uint32_t* cells,
-                                      const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, double* u)
+                                      const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, A u)
         {
             const Geom& g = *gp;
             const int l   = a.l;
@@ -428,7 +451,7 @@ namespace sg
             {
                 int d[3];
                 diagonal_dir(DIM, static_cast<int>(blockIdx.x), d);
-                corner_role(g, d, l, cells, ref, u);
+                corner_role(g, d, l, cells, ref, u, a.corner_parts);
                 return;
             }
             if (static_cast<int>(blockIdx.x) < a.nb_corner + a.nb_face)
@@ -462,7 +485,7 @@ namespace sg
         // k_ghost_level one level after the other.
         template <int DIM>
         __global__ void __launch_bounds__(1024, 1) k_ghost_levels_small(const Geom* __restrict__ gp, GhostChainArgs ca, const int* wl_ref, const long long* lo, const uint32_t* cells,
-                                             const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, double* u)
+                                             const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, ValAcc u)
         {
             const Geom& g         = *gp;
             const int minl        = g.min_level, maxl = g.max_level;
@@ -503,9 +526,9 @@ namespace sg
             }
         }
 
-        template <int DIM>
+        template <int DIM, class A>
         __global__ void k_predict(const Geom* __restrict__ gp, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
-                                  const uint32_t* proj, const uint32_t* ref, double* u)
+                                  const uint32_t* proj, const uint32_t* ref, A u)
         {
             predict_level<DIM>(*gp, l, order, wl_ref, lo, cells, proj, ref, u, warp_id(), warp_count());
         }
@@ -513,7 +536,7 @@ namespace sg
         // the small levels of the bottom-up pass in one block
         template <int DIM>
         __global__ void __launch_bounds__(1024, 1) k_predict_small(const Geom* __restrict__ gp, int l_lo, int l_hi, int order, const int* wl_ref, const long long* lo,
-                                        const uint32_t* cells, const uint32_t* proj, const uint32_t* ref, double* u)
+                                        const uint32_t* cells, const uint32_t* proj, const uint32_t* ref, ValAcc u)
         {
             const long long warp0 = threadIdx.x >> 5;
             const long long nw    = blockDim.x >> 5;
@@ -718,16 +741,16 @@ namespace sg
         // update_fields (algorithm/update_fields.hpp:27-127): copy on
         // reference ∩ new cells, projection on coarsened cells, prediction on
         // refined cells; every other reference entry of the new field is 0.
-        template <int DIM>
+        template <int DIM, class A>
         __global__ void k_update_fields(const Geom* __restrict__ gp, int order, const int* wl, const long long* lo, const uint32_t* nref,
-                                        const uint32_t* ncells, const uint32_t* oref, const uint32_t* ocells, const uint32_t* ohc, const double* uo, double* un)
+                                        const uint32_t* ncells, const uint32_t* oref, const uint32_t* ocells, const uint32_t* ohc, A uo, A un)
         {
             const Geom& g = *gp;
             warp_list(wl, lo[LO_REF], lo[LO_REF + g.nlev], warp_id(), warp_count(), [&](long long w) { return nref[w]; },
                       [&](long long w, int b)
                       {
                           const long long e = 32 * w + b;
-                          double v          = 0.;
+                          typename A::V v   = A::konst(0.);
                           if ((ncells[w] >> b) & 1u)
                           {
                               const int l  = level_of(g, w);
@@ -742,10 +765,10 @@ namespace sg
                               }
                               else if ((oref[w] >> b) & 1u)
                               {
-                                  v = uo[e];
+                                  v = uo.get(e);
                               }
                           }
-                          un[e] = v;
+                          un.put(e, v);
                       });
         }
 
@@ -1012,16 +1035,20 @@ namespace sg
         }
 
         // update_ghost_mr / update_ghost_mr_aggregated (algorithm/update_ghost_mr.hpp:195-270)
-        int seq_ghost(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv)
+        // as a sequence of launches on accessor u.  ft: levels 0..ft run as
+        // one-block chains (value accessor only; -2 for none).  split: the
+        // corner projection of each level gets a launch of its own, so that
+        // no launch reads what it writes (needed to record the operator).
+        // after() runs after every launch.
+        template <class A, class After>
+        int ghost_launches(Ctx& c, DeviceMesh& m, const A& u, bool has_bc, double bcv, int ft, bool split, After after)
         {
-            ScopedTimer timer(c, T_GHOST);
             const Geom& g   = c.g;
             const int minl  = c.cfg.min_level;
             const int maxl  = c.cfg.max_level;
             const int lmin  = minl >= 2 ? minl - 2 : 0; // no reference cell below min_level-2
             const int ndiag = (g.dim == 2) ? 4 : 20;
-            const int ft = c.fuse_top_field;
-            int l        = maxl;
+            int l           = maxl;
             for (; l >= lmin && l - 1 > ft; --l)
             {
                 GhostLevelArgs a{};
@@ -1032,12 +1059,13 @@ namespace sg
                 a.do_predict   = (l >= minl && l < maxl);
                 a.value        = bcv;
                 a.nb_corner    = a.do_corners ? ndiag : 0;
+                a.corner_parts = split ? 1 : 3;
                 const int n    = g.lv[l].n;
                 a.nfaces       = (a.do_project || a.do_dirichlet || a.do_predict)
                                      ? static_cast<long long>(2 * g.dim) * ((g.dim == 2) ? n : static_cast<long long>(n) * n)
                                      : 0;
-                a.nb_face      = static_cast<int>((a.nfaces + BLOCK - 1) / BLOCK);
-                a.do_proj      = l > lmin;
+                a.nb_face         = static_cast<int>((a.nfaces + BLOCK - 1) / BLOCK);
+                a.do_proj         = l > lmin;
                 const int nb_proj = a.do_proj ? blocks_words(g, l - 1, l - 1) : 0;
                 const int grid    = a.nb_corner + a.nb_face + nb_proj;
                 if (grid > 0)
@@ -1051,36 +1079,60 @@ namespace sg
                         k_ghost_level<3><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     ++c.n_launches;
+                    after();
                 }
-            }
-            if (l >= lmin)
-            {
-                GhostChainArgs ca{l, lmin, lmin, has_bc ? 1 : 0, bcv};
-                if (g.dim == 2)
+                if (split && a.nb_corner > 0)
                 {
-                    k_ghost_levels_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                    GhostLevelArgs b = a;
+                    b.corner_parts   = 2;
+                    b.nb_face        = 0;
+                    b.nfaces         = 0;
+                    b.do_proj        = 0;
+                    if (g.dim == 2)
+                    {
+                        k_ghost_level<2><<<b.nb_corner, BLOCK, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                    }
+                    else
+                    {
+                        k_ghost_level<3><<<b.nb_corner, BLOCK, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                    }
+                    ++c.n_launches;
+                    after();
                 }
-                else
-                {
-                    k_ghost_levels_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
-                }
-                ++c.n_launches;
             }
             const int lp0 = lmin > 1 ? lmin : 1;
             int lp        = lp0;
-            if (lp <= maxl && lp <= ft)
+            if constexpr (std::is_same<A, ValAcc>::value)
             {
-                const int e = maxl < ft ? maxl : ft;
-                if (g.dim == 2)
+                if (l >= lmin)
                 {
-                    k_predict_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                    GhostChainArgs ca{l, lmin, lmin, has_bc ? 1 : 0, bcv};
+                    if (g.dim == 2)
+                    {
+                        k_ghost_levels_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                    }
+                    else
+                    {
+                        k_ghost_levels_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                    }
+                    ++c.n_launches;
+                    after();
                 }
-                else
+                if (lp <= maxl && lp <= ft)
                 {
-                    k_predict_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                    const int e = maxl < ft ? maxl : ft;
+                    if (g.dim == 2)
+                    {
+                        k_predict_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                    }
+                    else
+                    {
+                        k_predict_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                    }
+                    ++c.n_launches;
+                    after();
+                    lp = e + 1;
                 }
-                ++c.n_launches;
-                lp = e + 1;
             }
             for (; lp <= maxl; ++lp)
             {
@@ -1095,8 +1147,33 @@ namespace sg
                                                                                    m.ref, u);
                 }
                 ++c.n_launches;
+                after();
             }
             return check(c, "update_ghost_mr");
+        }
+
+        int seq_ghost(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv)
+        {
+            ScopedTimer timer(c, T_GHOST);
+            return ghost_launches(c, m, ValAcc{u}, has_bc, bcv, c.fuse_top_field, false, [] {});
+        }
+
+        // update_fields (algorithm/update_fields.hpp:27-127) from mesh m to nm
+        template <class A>
+        void update_fields_launch(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const A& uo, const A& un)
+        {
+            const Geom& g = c.g;
+            if (g.dim == 2)
+            {
+                k_update_fields<2><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                                                                                            nm.cells, m.ref, m.cells, m.hc, uo, un);
+            }
+            else
+            {
+                k_update_fields<3><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                                                                                            nm.cells, m.ref, m.cells, m.hc, uo, un);
+            }
+            ++c.n_launches;
         }
 
         // Adapt::harten up to the fixed-point test (mr/adapt.hpp:276-375):
@@ -1204,24 +1281,13 @@ namespace sg
         // new mesh from the new cells and update_fields (mr/adapt.hpp:380-386)
         int seq_back(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un)
         {
-            const Geom& g = c.g;
-            int st        = build_mesh(c, nm);
+            int st = build_mesh(c, nm);
             if (st)
             {
                 return st;
             }
             ScopedTimer tf(c, T_FIELDS_UPDATE);
-            if (g.dim == 2)
-            {
-                k_update_fields<2><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
-                                                                                            nm.cells, m.ref, m.cells, m.hc, uo, un);
-            }
-            else
-            {
-                k_update_fields<3><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
-                                                                                            nm.cells, m.ref, m.cells, m.hc, uo, un);
-            }
-            ++c.n_launches;
+            update_fields_launch(c, m, nm, ValAcc{const_cast<double*>(uo)}, ValAcc{un});
             return check(c, "update_fields");
         }
     } // namespace
@@ -1347,6 +1413,43 @@ namespace sg
             return st;
         }
         return harten_end(c, f, converged);
+    }
+
+    // ---------------------------------------------------------------
+    // Operators of one step on a given (frozen) mesh, for the replay and the
+    // adjoint: the ghost update and update_fields either applied (value) or
+    // recorded onto a tape, one tape phase per launch; mark(p) closes a phase.
+    int ghost_value(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv)
+    {
+        return ghost_launches(c, m, ValAcc{u}, has_bc, bcv, c.fuse_top_field, false, [] {});
+    }
+
+    int ghost_tape(Ctx& c, DeviceMesh& m, const TapeDev& t, bool has_bc, double bcv, const std::function<void()>& mark)
+    {
+        if (c.g.dim == 2)
+        {
+            return ghost_launches(c, m, TapeAcc<FormCap<2>::value>{t}, has_bc, bcv, -2, true, mark);
+        }
+        return ghost_launches(c, m, TapeAcc<FormCap<3>::value>{t}, has_bc, bcv, -2, true, mark);
+    }
+
+    int update_fields_value(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un)
+    {
+        update_fields_launch(c, m, nm, ValAcc{const_cast<double*>(uo)}, ValAcc{un});
+        return check(c, "update_fields");
+    }
+
+    int update_fields_tape(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const TapeDev& t)
+    {
+        if (c.g.dim == 2)
+        {
+            update_fields_launch(c, m, nm, TapeAcc<FormCap<2>::value>{t}, TapeAcc<FormCap<2>::value>{t});
+        }
+        else
+        {
+            update_fields_launch(c, m, nm, TapeAcc<FormCap<3>::value>{t}, TapeAcc<FormCap<3>::value>{t});
+        }
+        return check(c, "update_fields (tape)");
     }
 
     // Adapt::operator() (mr/adapt.hpp:147-195)

@@ -168,3 +168,22 @@ def demo_time_loop(sim, dt, Tf, eps, regularity, a, scheme=0):
         sim.upwind(a, dt, scheme)
         nt += 1
     return nt
+
+
+def gaussian_target(seed):
+    """Seeded Gaussian target of the adjoint workload: centre U[0.3,0.7]^2,
+    sigma U[0.05,0.15], amplitude 1."""
+    rng = SplitMix64(seed)
+    cx, cy = rng.uniform(0.3, 0.7), rng.uniform(0.3, 0.7)
+    sig = rng.uniform(0.05, 0.15)
+
+    def f(level, coords):
+        c = centers(level, coords)
+        r2 = (c[:, 0] - cx) * (c[:, 0] - cx) + (c[:, 1] - cy) * (c[:, 1] - cy)
+        return np.exp(-r2 / (2.0 * sig * sig))
+
+    return f
+
+
+def cell_volumes(level, dim=2):
+    return np.ldexp(1.0, -dim * level.astype(np.int64))
