@@ -331,6 +331,7 @@ namespace samurai
         const ScalarField<Mesh>* u;
         std::array<double, Mesh::dim> a;
         double dt;
+        int scheme;
     };
 
     template <class Mesh>
@@ -338,6 +339,7 @@ namespace samurai
     {
         const ScalarField<Mesh>* u;
         std::array<double, Mesh::dim> a;
+        int scheme = SG_UPWIND_OP;
     };
 
     template <class Mesh>
@@ -346,6 +348,7 @@ namespace samurai
       public:
 
         static constexpr std::size_t dim = Mesh::dim;
+        using mesh_t                     = Mesh;
 
         ScalarField(std::string name, Mesh& mesh)
             : m_mesh(&mesh)
@@ -570,7 +573,31 @@ namespace samurai
     template <class Mesh>
     ScaledUpwind<Mesh> operator*(double dt, const UpwindOp<Mesh>& op)
     {
-        return {op.u, op.a, dt};
+        return {op.u, op.a, dt, op.scheme};
+    }
+
+    // VelocityVector<dim> (schemes/fv/operators/convection_lin.hpp:8-9)
+    template <std::size_t dim>
+    using VelocityVector = std::array<double, dim>;
+
+    // make_convection_upwind<Field>(velocity) (schemes/fv/operators/convection_lin.hpp:16-89): the
+    // conservative flux form; conv(u) is evaluated on the device inside unp1 = u - dt * conv(u)
+    template <class Field>
+    struct ConvectionUpwind
+    {
+        VelocityVector<Field::dim> velocity;
+
+        auto operator()(const Field& u) const
+        {
+            UpwindOp<typename Field::mesh_t> op{&u, velocity, SG_CONVECTION};
+            return op;
+        }
+    };
+
+    template <class Field>
+    ConvectionUpwind<Field> make_convection_upwind(const VelocityVector<Field::dim>& velocity)
+    {
+        return {velocity};
     }
 
     template <class Mesh>
@@ -580,7 +607,7 @@ namespace samurai
         {
             throw std::invalid_argument("samurai_gb300: u - dt * upwind(a, v) needs v == u");
         }
-        return {&u, s.a, s.dt, SG_UPWIND_OP};
+        return {&u, s.a, s.dt, s.scheme};
     }
 } // namespace samurai
 

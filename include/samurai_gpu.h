@@ -53,7 +53,10 @@ enum sg_mesh_id
 enum sg_scheme
 {
     SG_UPWIND_OP = 0, /* unp1 = u - dt * samurai::upwind(a, u)  (stencil_field.hpp:91-179, demos/FiniteVolume/advection_2d.cpp:144) */
-    SG_README    = 1  /* the README for_each_interval lambda    (README.md:144-153) */
+    SG_README    = 1, /* the README for_each_interval lambda    (README.md:144-153) */
+    SG_CONVECTION = 2 /* unp1 = u - dt * conv(u), conv = samurai::make_convection_upwind<Field>(a): the conservative flux
+                         form with level-jump interfaces (schemes/fv/operators/convection_lin.hpp:16-89,
+                         schemes/fv/flux_based/explicit_flux_based_scheme__lin_hom.hpp:39-319) */
 };
 
 const char* sg_last_error(void);
@@ -115,7 +118,7 @@ int sg_adapt(sg_field_t u, double eps, double regularity, int* n_harten);
 int sg_harten(sg_field_t u, int ite, double eps, double regularity, int* converged);
 /* samurai::update_ghost_mr(u) (algorithm/update_ghost_mr.hpp:261-270) */
 int sg_update_ghost_mr(sg_field_t u);
-/* unp1 = u - dt * samurai::upwind(a, u) on mesh[cells] (a has dim entries) */
+/* unp1 = u - dt * samurai::upwind(a, u) on mesh[cells] (a has dim entries), or one of the other schemes above */
 int sg_upwind(sg_field_t u, sg_field_t unp1, const double* a, double dt, int scheme);
 /* detail and tag fields of the last Harten pass, reference numbering (n = nb_reference) */
 int sg_detail_download(sg_field_t u, double* values, long long n);

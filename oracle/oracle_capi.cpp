@@ -244,7 +244,7 @@ extern "C"
     }
 
     // u <- u - dt * upwind(a, u) on the cells; ghost storage becomes NaN
-    // (scheme 0: upwind operator, 1: README lambda)
+    // (scheme 0: upwind operator, 1: README lambda, 2: make_convection_upwind)
     int oracle_upwind(void* h, const double* a, double dt, int scheme)
     {
         try

@@ -1829,9 +1829,216 @@ namespace oracle
     // --------------------------------------------------------------- upwind
     enum class Scheme
     {
-        UpwindOp = 0, // unp1 = u - dt * upwind(a, u)   (stencil_field.hpp:38-44, 91-97)
-        Readme   = 1  // README lambda, a = (1,1)        (README.md:144-153)
+        UpwindOp   = 0, // unp1 = u - dt * upwind(a, u)   (stencil_field.hpp:38-44, 91-97)
+        Readme     = 1, // README lambda, a = (1,1)        (README.md:144-153)
+        Convection = 2  // unp1 = u - dt * conv(u), conv = make_convection_upwind<Field>(a)
     };
+
+    // make_convection_upwind(velocity) (schemes/fv/operators/convection_lin.hpp:16-89) applied explicitly:
+    // the output field is filled with 0 (explicit_FV_scheme.hpp:51-56), then direction by direction
+    // (explicit_FV_scheme.hpp:78-101) every interface adds its contributions in the order of
+    // flux_based_scheme__lin_hom.hpp:74-238 with the sequential-context loops of
+    // explicit_flux_based_scheme__lin_hom.hpp:39-110 and the boundary loop of :276-318: same-level
+    // interfaces level by level, then level jumps (direction, then opposite direction) level by level,
+    // then boundary interfaces.  Interfaces come from interface.hpp:36-330 and 440-510.  The upwind flux
+    // in direction d is a_d * u_left when a_d >= 0, a_d * u_right otherwise.
+    template <std::size_t D>
+    Field convection_apply(const Mesh<D>& m, const Field& u, const std::array<double, D>& a)
+    {
+        Field out(m.nb_ref, 0.0);
+        int cmin = MAXL, cmax = -1;
+        for (int l = 0; l < MAXL; ++l)
+        {
+            if (!m.cells[l].empty())
+            {
+                cmin = std::min(cmin, l);
+                cmax = std::max(cmax, l);
+            }
+        }
+        if (cmax < 0)
+        {
+            return out;
+        }
+        const int minl = std::max(m.cfg.min_level, cmin - 1);
+        const int maxl = std::min(m.cfg.max_level, cmax + 1);
+        auto hf        = [](double hface, double hcell) { return std::pow(hface, static_cast<int>(D) - 1) / std::pow(hcell, static_cast<int>(D)); };
+        auto length    = [](int level) { return 1.0 / static_cast<double>(1LL << level); };
+        auto coord     = [](const Key<D>& k, int x)
+        {
+            Coord<D> c;
+            c[0] = x;
+            for (int d = 0; d < static_cast<int>(D) - 1; ++d)
+            {
+                c[d + 1] = k[d];
+            }
+            return c;
+        };
+        auto parent = [](Coord<D> c)
+        {
+            for (auto& v : c)
+            {
+                v >>= 1;
+            }
+            return c;
+        };
+        auto U = [&](int level, const Coord<D>& c) { return u[static_cast<std::size_t>(m.idx(level, c))]; };
+        auto O = [&](int level, const Coord<D>& c) -> double& { return out[static_cast<std::size_t>(m.idx(level, c))]; };
+
+        for (int d = 0; d < static_cast<int>(D); ++d)
+        {
+            Dir<D> e{};
+            e[d]            = 1;
+            const Dir<D> me = scale<D>(e, -1);
+            // FluxStencilCoeffs (left, right) of the upwind flux (convection_lin.hpp:38-76)
+            const double fl = a[d] >= 0 ? a[d] : 0.;
+            const double fr = a[d] >= 0 ? 0. : a[d];
+            const double flux[2] = {fl, fr};
+
+            // same level (flux_based_scheme__lin_hom.hpp:90-111)
+            for (int level = minl; level <= maxl; ++level)
+            {
+                const double h      = length(level);
+                const double factor = hf(h, h);
+                const double lc[2]  = {factor * flux[0], factor * flux[1]};
+                const double rc[2]  = {-lc[0], -lc[1]};
+                const auto I        = inter(m.cells[level], translate(m.cells[level], me));
+                for (const auto& [k, r] : I.rows)
+                {
+                    for (const auto& iv : r)
+                    {
+                        for (int c = 0; c < 2; ++c)
+                        {
+                            for (int x = iv.s; x < iv.e; ++x)
+                            {
+                                const Coord<D> L = coord(k, x);
+                                O(level, L) += lc[c] * U(level, add<D>(L, e, c));
+                            }
+                            for (int x = iv.s; x < iv.e; ++x)
+                            {
+                                const Coord<D> L = coord(k, x);
+                                O(level, add<D>(L, e)) += rc[c] * U(level, add<D>(L, e, c));
+                            }
+                        }
+                    }
+                }
+            }
+
+            // level jumps (flux_based_scheme__lin_hom.hpp:113-169)
+            for (int level = minl; level < maxl; ++level)
+            {
+                const double hl = length(level), hl1 = length(level + 1);
+                {
+                    // coarse left, fine right (interface.hpp:125-219)
+                    const double lf = hf(hl1, hl), rf = hf(hl1, hl1);
+                    const double lc[2] = {lf * flux[0], lf * flux[1]};
+                    const double rc[2] = {-rf * flux[0], -rf * flux[1]};
+                    const auto P       = on(inter(m.cells[level], translate(m.cells[level + 1], me)), level + 1);
+                    for (const auto& [k, r] : P.rows)
+                    {
+                        for (const auto& iv : r)
+                        {
+                            const int n = iv.e - iv.s;
+                            for (int c = 0; c < 2; ++c)
+                            {
+                                if (n == 1)
+                                {
+                                    const Coord<D> p = coord(k, iv.s);
+                                    O(level, parent(p)) += lc[c] * U(level + 1, add<D>(p, e, c));
+                                    O(level + 1, add<D>(p, e)) += rc[c] * U(level + 1, add<D>(p, e, c));
+                                }
+                                else
+                                {
+                                    for (int ii = 0; ii < n / 2; ++ii)
+                                    {
+                                        const Coord<D> p0 = coord(k, iv.s + 2 * ii), p1 = coord(k, iv.s + 2 * ii + 1);
+                                        O(level, parent(p0)) += lc[c] * U(level + 1, add<D>(p0, e, c)) + lc[c] * U(level + 1, add<D>(p1, e, c));
+                                    }
+                                    for (int x = iv.s; x < iv.e; ++x)
+                                    {
+                                        const Coord<D> p = coord(k, x);
+                                        O(level + 1, add<D>(p, e)) += rc[c] * U(level + 1, add<D>(p, e, c));
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                {
+                    // fine left, coarse right (interface.hpp:221-328): stencil {Q - e, Q}
+                    const double lf = hf(hl1, hl1), rf = hf(hl1, hl);
+                    const double lc[2] = {lf * flux[0], lf * flux[1]};
+                    const double rc[2] = {-rf * flux[0], -rf * flux[1]};
+                    const auto Q       = on(inter(m.cells[level], translate(m.cells[level + 1], e)), level + 1);
+                    for (const auto& [k, r] : Q.rows)
+                    {
+                        for (const auto& iv : r)
+                        {
+                            const int n = iv.e - iv.s;
+                            for (int c = 0; c < 2; ++c)
+                            {
+                                if (n == 1)
+                                {
+                                    const Coord<D> q  = coord(k, iv.s);
+                                    const Coord<D> fl_ = add<D>(q, me);
+                                    O(level + 1, fl_) += lc[c] * U(level + 1, add<D>(fl_, e, c));
+                                    O(level, parent(q)) += rc[c] * U(level + 1, add<D>(fl_, e, c));
+                                }
+                                else
+                                {
+                                    for (int x = iv.s; x < iv.e; ++x)
+                                    {
+                                        const Coord<D> fl_ = add<D>(coord(k, x), me);
+                                        O(level + 1, fl_) += lc[c] * U(level + 1, add<D>(fl_, e, c));
+                                    }
+                                    for (int ii = 0; ii < n / 2; ++ii)
+                                    {
+                                        const Coord<D> q0 = coord(k, iv.s + 2 * ii), q1 = coord(k, iv.s + 2 * ii + 1);
+                                        O(level, parent(q0)) += rc[c] * U(level + 1, add<D>(add<D>(q0, me), e, c))
+                                                              + rc[c] * U(level + 1, add<D>(add<D>(q1, me), e, c));
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+
+            // boundary interfaces (flux_based_scheme__lin_hom.hpp:184-226)
+            for (int level = 0; level < MAXL; ++level)
+            {
+                if (m.cells[level].empty())
+                {
+                    continue;
+                }
+                const double h = length(level);
+                double co[2]   = {hf(h, h) * flux[0], hf(h, h) * flux[1]};
+                for (int side = 0; side < 2; ++side)
+                {
+                    const Dir<D> dir = side == 0 ? e : me;
+                    const auto B     = domain_boundary(m, level, dir);
+                    for (const auto& [k, r] : B.rows)
+                    {
+                        for (const auto& iv : r)
+                        {
+                            for (int c = 0; c < 2; ++c)
+                            {
+                                for (int x = iv.s; x < iv.e; ++x)
+                                {
+                                    const Coord<D> X = coord(k, x);
+                                    // stencil {0, e} in the direction, {-e, 0} in the opposite one
+                                    const Coord<D> s = side == 0 ? add<D>(X, e, c) : add<D>(add<D>(X, me), e, c);
+                                    O(level, X) += co[c] * U(level, s);
+                                }
+                            }
+                        }
+                    }
+                    co[0] *= -1;
+                    co[1] *= -1;
+                }
+            }
+        }
+        return out;
+    }
 
     // Returns unp1 on the reference storage; ghost entries are NaN, which
     // is where the reference's resized unp1 holds indeterminate values.
@@ -1839,6 +2046,21 @@ namespace oracle
     Field upwind_step(const Mesh<D>& m, const Field& u, const std::array<double, D>& a, double dt, Scheme scheme)
     {
         Field unp1(m.nb_ref, std::numeric_limits<double>::quiet_NaN());
+        if (scheme == Scheme::Convection)
+        {
+            // unp1 = u - dt * conv(u) on the cells (field expression, field/field_base.hpp:232-242)
+            const Field out = convection_apply<D>(m, u, a);
+            for (int level = 0; level < MAXL; ++level)
+            {
+                m.cells[level].for_each_cell(
+                    [&](const Coord<D>& c)
+                    {
+                        const auto i = static_cast<std::size_t>(m.idx(level, c));
+                        unp1[i]      = u[i] - dt * out[i];
+                    });
+            }
+            return unp1;
+        }
         for (int level = 0; level < MAXL; ++level)
         {
             const double dx = 1.0 / (1 << level); // cell_length with a unit scaling factor (cell.hpp:17-20)

@@ -28,7 +28,7 @@ _lib = None
 
 SG_CELLS, SG_CELLS_AND_GHOSTS, SG_PROJ_CELLS, SG_UNION_CELLS, SG_REFERENCE = range(5)
 MESH_IDS = {"cells": 0, "cells_and_ghosts": 1, "proj_cells": 2, "union_cells": 3, "reference": 4, "all_cells": 4}
-UPWIND_OP, README = 0, 1
+UPWIND_OP, README, CONVECTION = 0, 1, 2
 
 
 class SamuraiGpuError(RuntimeError):

@@ -901,7 +901,7 @@ extern "C"
     {
         if (!adj || !u0 || !a || n_steps < 0 || (scheme != SG_UPWIND_OP && scheme != SG_README))
         {
-            return afail(SG_ERR_ARG, "sg_adjoint_record: invalid argument");
+            return afail(SG_ERR_ARG, "sg_adjoint_record: invalid argument (the adjoint covers the upwind operator and the README scheme)");
         }
         Ctx& c = ctx_of(adj);
         if (scheme == SG_README && c.g.dim != 2)

@@ -263,7 +263,7 @@ namespace
         {
             return bfail(SG_ERR_ARG, "sg_batch: null velocity or time-step array");
         }
-        if (scheme != SG_UPWIND_OP && scheme != SG_README)
+        if (scheme != SG_UPWIND_OP && scheme != SG_README && scheme != SG_CONVECTION)
         {
             return bfail(SG_ERR_ARG, "sg_batch: unknown scheme");
         }

@@ -364,7 +364,7 @@ extern "C"
         st |= dalloc(c, &c.d_flags, 8);
         st |= dalloc(c, &c.d_geom, 1);
         st |= dalloc(c, &c.d_ite, 1);
-        st |= dalloc(c, &c.d_eps, 3 * sg::MAXLEV);
+        st |= dalloc(c, &c.d_eps, sg::EPS_VELOCITY + 3);
         if (!st)
         {
             if (cudaMallocHost(reinterpret_cast<void**>(&c.h_ite), sizeof(int)) != cudaSuccess
@@ -1026,7 +1026,7 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_upwind: need two distinct fields on the same mesh");
         }
-        if (scheme != SG_UPWIND_OP && scheme != SG_README)
+        if (scheme != SG_UPWIND_OP && scheme != SG_README && scheme != SG_CONVECTION)
         {
             return fail(SG_ERR_ARG, "sg_upwind: unknown scheme");
         }

@@ -216,6 +216,9 @@ namespace sg
     // to 16K words per level.  The FP64 field chains are not fused: their
     // cells wait on memory, and one block serialises that latency (measured
     // slower than one launch per level even at 2K words), so the limit is 0.
+    // device thresholds buffer: [eps | fine | coarse] x MAXLEV, then a velocity
+    constexpr int EPS_VELOCITY = 3 * MAXLEV;
+
     constexpr long long FUSE_WORDS       = 16384;
     constexpr long long FUSE_WORDS_FIELD = 0;
 

@@ -875,6 +875,191 @@ namespace sg
             }
         }
 
+
+        // ---------------------------------------------- flux-form convection
+        // unp1 = u - dt * conv(u) with conv = make_convection_upwind<Field>(a)
+        // (schemes/fv/operators/convection_lin.hpp:16-89), explicit application
+        // (explicit_flux_based_scheme__lin_hom.hpp:39-319).  The reference
+        // visits interfaces (same level by level, then level jumps, then the
+        // boundary, direction by direction) and adds each face's contributions
+        // to both cells; one thread per leaf cell here gathers the same terms
+        // in the order they reach that cell:
+        //  same level   d = 0: [+lc0 u_X], [+rc0 u_X-e], [+lc1 u_X+e], [+rc1 u_X]
+        //               (X left / right of a same-level face, one x-interval);
+        //               d > 0: the face below (previous row) first: [+rc0 u_X-e,
+        //               +rc1 u_X] then [+lc0 u_X, +lc1 u_X+e];
+        //  jumps, X fine (iteration level-1): coarse on the left, then coarse on
+        //               the right, neighbour values from the ghosts at X's level;
+        //  jumps, X coarse (iteration level): fine on the right, then on the
+        //               left, row by row; a face along x adds one term per
+        //               fine row, other faces add the pair sum of the two fine
+        //               cells of a row (the i.size()==1 / pair branches);
+        //  boundary:    +(2^l f) terms with the outer ghost.
+        // Coefficients: face length^(dim-1) / cell volume times the upwind flux
+        // coefficients (a, 0) for a >= 0, (0, a) otherwise; every factor is a
+        // power of two.
+        template <int DIM>
+        __global__ void k_convection(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* cells, const double* __restrict__ u,
+                                     double* __restrict__ unp1, UpwindArgs p, const double* __restrict__ av)
+        {
+            const Geom& g     = *gp;
+            const int lane    = threadIdx.x & 31;
+            const long long n = lo[LO_CELLS + g.nlev];
+            for (long long i = lo[LO_CELLS] + warp_id(); i < n; i += warp_count())
+            {
+                const long long w = __ldg(wl + i);
+                if (!((__ldg(cells + w) >> lane) & 1u))
+                {
+                    continue;
+                }
+                const int m        = level_of(g, w);
+                const Cell cc      = cell_of(g, m, w, lane);
+                const int c[3]     = {cc.x, cc.y, cc.z};
+                const long long eX = 32 * w + lane;
+                const double uX    = u[eX];
+                const int nm       = 1 << m;
+                auto leaf = [&](int l, const int* q) { return l >= 0 && l <= g.max_level && test(cells, g, l, q[0], q[1], DIM == 3 ? q[2] : 0); };
+                auto val  = [&](int l, const int* q) { return u[elem_at(g, l, q[0], q[1], DIM == 3 ? q[2] : 0)]; };
+                double acc = 0.;
+                for (int d = 0; d < DIM; ++d)
+                {
+                    const double a  = av[d];
+                    const double fl = a >= 0 ? a : 0.;
+                    const double fr = a >= 0 ? 0. : a;
+                    int xp[3] = {c[0], c[1], c[2]}, xm[3] = {c[0], c[1], c[2]};
+                    ++xp[d];
+                    --xm[d];
+                    const double s2   = pow2(m);
+                    const double lc0 = s2 * fl, lc1 = s2 * fr;
+                    const double rc0 = -lc0, rc1 = -lc1;
+                    const bool rs = leaf(m, xp), ls = leaf(m, xm);
+                    // same level
+                    if (d == 0)
+                    {
+                        if (rs) acc = acc + lc0 * uX;
+                        if (ls) acc = acc + rc0 * val(m, xm);
+                        if (rs) acc = acc + lc1 * val(m, xp);
+                        if (ls) acc = acc + rc1 * uX;
+                    }
+                    else
+                    {
+                        if (ls)
+                        {
+                            acc = acc + rc0 * val(m, xm);
+                            acc = acc + rc1 * uX;
+                        }
+                        if (rs)
+                        {
+                            acc = acc + lc0 * uX;
+                            acc = acc + lc1 * val(m, xp);
+                        }
+                    }
+                    const bool out_r = xp[d] >= nm, out_l = xm[d] < 0;
+                    // level jumps with X the fine cell
+                    int pp[3] = {xp[0] >> 1, xp[1] >> 1, xp[2] >> 1}, pm[3] = {xm[0] >> 1, xm[1] >> 1, xm[2] >> 1};
+                    const bool lcoarse = !ls && !out_l && m >= 1 && leaf(m - 1, pm);
+                    const bool rcoarse = !rs && !out_r && m >= 1 && leaf(m - 1, pp);
+                    if (lcoarse)
+                    {
+                        acc = acc + rc0 * val(m, xm);
+                        acc = acc + rc1 * uX;
+                    }
+                    if (rcoarse)
+                    {
+                        acc = acc + lc0 * uX;
+                        acc = acc + lc1 * val(m, xp);
+                    }
+                    // level jumps with X the coarse cell: its face children at m+1
+                    const double sf = pow2(m - DIM + 1);
+                    int ch[3]       = {2 * c[0], 2 * c[1], 2 * c[2]};
+                    ch[d]           = 2 * c[d] + 2;
+                    const bool rfine = !rs && !rcoarse && !out_r && leaf(m + 1, ch);
+                    ch[d]            = 2 * c[d] - 1;
+                    const bool lfine = !ls && !lcoarse && !out_l && leaf(m + 1, ch);
+                    // fine rows of the face in row order (z outer, y inner); a face
+                    // normal to y or z has the pair of fine cells within each row
+                    const int nrow = (d == 0) ? (DIM == 3 ? 4 : 2) : (DIM == 3 ? 2 : 1);
+                    if (rfine)
+                    {
+                        const double j0 = sf * fl, j1 = sf * fr;
+                        for (int r = 0; r < nrow; ++r)
+                        {
+                            int q[3] = {2 * c[0], 2 * c[1], 2 * c[2]};
+                            q[d]     = 2 * c[d] + 1;
+                            if (d == 0)
+                            {
+                                q[1] += r & 1;
+                                if (DIM == 3)
+                                {
+                                    q[2] += r >> 1;
+                                }
+                                int qe[3] = {q[0] + 1, q[1], q[2]};
+                                acc       = acc + j0 * val(m + 1, q);
+                                acc       = acc + j1 * val(m + 1, qe);
+                            }
+                            else
+                            {
+                                if (DIM == 3)
+                                {
+                                    q[d == 1 ? 2 : 1] += r;
+                                }
+                                int qb[3] = {q[0] + 1, q[1], q[2]};
+                                int qe[3] = {q[0], q[1], q[2]}, qbe[3] = {qb[0], qb[1], qb[2]};
+                                ++qe[d];
+                                ++qbe[d];
+                                acc = acc + (j0 * val(m + 1, q) + j0 * val(m + 1, qb));
+                                acc = acc + (j1 * val(m + 1, qe) + j1 * val(m + 1, qbe));
+                            }
+                        }
+                    }
+                    if (lfine)
+                    {
+                        const double j0 = -sf * fl, j1 = -sf * fr;
+                        for (int r = 0; r < nrow; ++r)
+                        {
+                            int q[3] = {2 * c[0], 2 * c[1], 2 * c[2]}; // Q, inside X on its left face
+                            if (d == 0)
+                            {
+                                q[1] += r & 1;
+                                if (DIM == 3)
+                                {
+                                    q[2] += r >> 1;
+                                }
+                                int qm[3] = {q[0] - 1, q[1], q[2]};
+                                acc       = acc + j0 * val(m + 1, qm);
+                                acc       = acc + j1 * val(m + 1, q);
+                            }
+                            else
+                            {
+                                if (DIM == 3)
+                                {
+                                    q[d == 1 ? 2 : 1] += r;
+                                }
+                                int qb[3] = {q[0] + 1, q[1], q[2]};
+                                int qm[3] = {q[0], q[1], q[2]}, qbm[3] = {qb[0], qb[1], qb[2]};
+                                --qm[d];
+                                --qbm[d];
+                                acc = acc + (j0 * val(m + 1, qm) + j0 * val(m + 1, qbm));
+                                acc = acc + (j1 * val(m + 1, q) + j1 * val(m + 1, qb));
+                            }
+                        }
+                    }
+                    // boundary interfaces
+                    if (out_r)
+                    {
+                        acc = acc + lc0 * uX;
+                        acc = acc + lc1 * val(m, xp);
+                    }
+                    if (out_l)
+                    {
+                        acc = acc + (-lc0) * val(m, xm);
+                        acc = acc + (-lc1) * uX;
+                    }
+                }
+                unp1[eX] = uX - p.dt * acc;
+            }
+        }
+
         // --------------------------------------------------- layout moves
         __global__ void k_gather(const int* wl, const long long* lo, int nlev, const uint32_t* ref, const int* rank, const double* dense, double* compact)
         {
@@ -1496,7 +1681,20 @@ namespace sg
         p.dt     = dt;
         p.scheme = scheme;
         const int nb = blocks_words(g, 0, g.nlev - 1);
-        if (g.dim == 2)
+        if (scheme == 2)
+        {
+            double* av = c.d_eps + EPS_VELOCITY;
+            cudaMemcpyAsync(av, a, g.dim * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+            if (g.dim == 2)
+            {
+                k_convection<2><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p, av);
+            }
+            else
+            {
+                k_convection<3><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p, av);
+            }
+        }
+        else if (g.dim == 2)
         {
             k_upwind<2><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p);
         }

@@ -167,3 +167,22 @@ def test_3d_small(sg):
         g.upwind([1.0, 1.0, 1.0], dt, 0)
         compare_fields(g, o, "3d it %d" % it, cells_only=True)
     compare_meshes(g, o, 5, "3d")
+
+
+@pytest.mark.parametrize("dim,minl,maxl,a", [(2, 2, 7, (1.0, 0.7)), (2, 3, 8, (-0.6, 1.0)), (2, 2, 6, (0.0, -1.0)), (3, 2, 5, (0.8, -0.5, 1.0))])
+def test_convection_flux_form(sg, dim, minl, maxl, a):
+    """make_convection_upwind (flux form, level-jump interfaces) against the
+    oracle: meshes and leaf values bit-identical over several adapted steps."""
+    g, o = pair(sg, dim, minl, maxl)
+    f = shapes_2d(17, 4, 4) if dim == 2 else ball_3d(9)
+    init_both(g, o, f)
+    dt = 0.4 / (1 << maxl)
+    for step in range(4):
+        o.adapt(1e-3, 1.0)
+        g.adapt(1e-3, 1.0)
+        o.update_ghost()
+        g.update_ghost()
+        o.upwind(a, dt, 2)
+        g.upwind(a, dt, sg.CONVECTION)
+        compare_cells(g, o, "convection step %d" % step)
+        compare_fields(g, o, "convection step %d" % step, cells_only=True)
