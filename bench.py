@@ -29,18 +29,26 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
-from advection_cases import shapes_2d  # noqa: E402
+from advection_cases import ball_3d, shapes_2d  # noqa: E402
 
-CFG = dict(dim=2, min_level=4, max_level=12, a=(1.0, 0.5), eps=1e-4, regularity=2.0, seed=2026)
+CFG = dict(dim=2, min_level=4, max_level=12, a=(1.0, 0.5), eps=1e-4, regularity=2.0, seed=2026, cfl=0.5)
+# the 3D workload (--workload advection3d): ball + 8 Gaussians, a = (1,1,1), L3..9
+CFG_3D = dict(dim=3, min_level=3, max_level=9, a=(1.0, 1.0, 1.0), eps=1e-3, regularity=1.0, seed=2026, cfl=0.3)
 METRIC = "active cell-updates/s"
 UNIT = "cell-updates/s"
 L2_BYTES = 129 * 1024 * 1024
+UPWIND_DRAM_BYTES_PER_CELL = 8346368.0 / 536428.0
 
 
 def workload_config(extra=None):
+    if CFG["dim"] == 3:
+        desc = ("3D MR linear advection, min_level 3, max_level 9 (512^3), a=(1,1,1), eps 1e-3, regularity 1, "
+                "ball + 8 Gaussians (seed %d), Dirichlet 0, dt=0.3*dx_min, upwind" % CFG["seed"])
+    else:
+        desc = ("2D MR linear advection, min_level 4, max_level 12 (4096^2), a=(1,0.5), eps 1e-4, regularity 2, "
+                "16 squares + 16 Gaussians (seed %d), Dirichlet 0, dt=0.5*dx_min, upwind" % CFG["seed"])
     c = {
-        "workload": "2D MR linear advection, min_level 4, max_level 12 (4096^2), a=(1,0.5), eps 1e-4, regularity 2, "
-        "16 squares + 16 Gaussians (seed %d), Dirichlet 0, dt=0.5*dx_min, upwind" % CFG["seed"],
+        "workload": desc,
         "min_level": CFG["min_level"],
         "max_level": CFG["max_level"],
         "max_stencil_radius": 1,
@@ -53,6 +61,8 @@ def workload_config(extra=None):
 
 
 def initial_values(level, coords):
+    if CFG["dim"] == 3:
+        return ball_3d(CFG["seed"])(level, coords)
     return shapes_2d(CFG["seed"])(level, coords)
 
 
@@ -123,16 +133,27 @@ class ClockSampler:
 def halo_count(level, coords):
     """Distinct same-level non-leaf neighbours (+-1 along each axis) of the
     leaf cells: the ghost values the upwind stencil reads."""
-    key_bits = 24
+    key_bits = 21
+    dim = coords.shape[1]
     total = 0
     for l in np.unique(level):
         c = coords[level == l].astype(np.int64) + 64
-        keys = c[:, 0] | (c[:, 1] << key_bits)
+
+        def key(x):
+            k = x[:, 0] | (x[:, 1] << key_bits)
+            if dim == 3:
+                k = k | (x[:, 2] << (2 * key_bits))
+            return k
+
+        keys = key(c)
         nb = []
-        for dx, dy in ((1, 0), (-1, 0), (0, 1), (0, -1)):
-            nb.append((c[:, 0] + dx) | ((c[:, 1] + dy) << key_bits))
+        for d in range(dim):
+            for s_ in (1, -1):
+                cc = c.copy()
+                cc[:, d] += s_
+                nb.append(key(cc))
         nb = np.unique(np.concatenate(nb))
-        total += int(np.setdiff1d(nb, keys, assume_unique=True).size)
+        total += int(np.setdiff1d(nb, np.unique(keys), assume_unique=True).size)
     return total
 
 
@@ -153,7 +174,7 @@ def run_gpu(args):
 
     dim, minl, maxl = CFG["dim"], CFG["min_level"], CFG["max_level"]
     a = list(CFG["a"])
-    dt = 0.5 / (1 << maxl)
+    dt = CFG["cfl"] / (1 << maxl)
     sim = sg.AdvectionSim(dim, minl, maxl, 1, 1)
     lv, co, _ = sim.cells()
     sim.set_cell_values(initial_values(lv, co))
@@ -267,17 +288,18 @@ def run_gpu(args):
     achieved = alg_bytes / (upw_ms / 1e3) / 1e9
     # FP64 roof: the upwind formula of the reference costs 5 FP64 operations
     # per face flux plus 5 (2D) to assemble the update: 26 per cell in 2D
-    fp64_ops = 26 * nc
+    # the reference's formula: 5 FP64 operations per face flux (2 dim fluxes),
+    # 2 dim - 1 to combine them, 3 to scale and update: 26 in 2D, 38 in 3D
+    fp64_ops = (10 * dim + 2 * dim - 1 + 3) * nc
     try:
         fp64_peak = sg.device_fp64_rate()
     except Exception:
         fp64_peak = None
-    traffic = None
-    try:
-        traffic_info = json.load(open(os.path.join(ROOT, "profiles", "upwind_traffic.json")))
-        traffic = traffic_info.get("bytes_per_launch")
-    except Exception:
-        pass
+    # DRAM bytes of one k_upwind launch, from the ncu capture summarised in
+    # profiles/k_upwind_2d_L12.md (8 346 368 B read + 0 B written for 536 428
+    # leaf cells), scaled to this launch's leaf cells: the traffic grows with
+    # the cells read and written
+    traffic = UPWIND_DRAM_BYTES_PER_CELL * nc
 
     # ---- samurai's named timers over a few extra steps (per-phase GPU time)
     phase_steps = 10
@@ -307,12 +329,13 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps),
                     "steps": e2e_steps, "api": "sg_field_upload + sg_adapt + sg_update_ghost_mr + sg_upwind + sg_field_swap + sg_field_download"},
             "roofline": {"bound": "hbm", "kernel": "k_upwind", "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": int(alg_bytes), "launch_ms": upw_ms,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": "ncu dram__bytes of a 536 428-cell launch, scaled by leaf cells",
+                         "algorithmic_bytes": int(alg_bytes), "launch_ms": upw_ms,
                          "cells": int(nc), "halo": int(halo),
                          "fp64": {"achieved_gflops": fp64_ops / (upw_ms / 1e3) / 1e9, "peak_gflops": fp64_peak,
                                   "peak_source": "measured in this run (sg_device_fp64_rate probe)",
                                   "frac": (fp64_ops / (upw_ms / 1e3) / 1e9 / fp64_peak) if fp64_peak else None,
-                                  "ops_per_launch": int(fp64_ops), "note": "26 FP64 operations per leaf cell in the reference's formula"}},
+                                  "ops_per_launch": int(fp64_ops), "note": "FP64 operations per leaf cell in the reference's formula: 26 (2D), 38 (3D)"}},
             "gpu_launches": int(launches),
             "launches_per_step": launches / args.steps,
             "phases_ms_per_step": phases,
@@ -358,7 +381,7 @@ def run_reference(args):
     from oracle.pyoracle import OracleSim
 
     dim, minl, maxl = CFG["dim"], CFG["min_level"], CFG["max_level"]
-    dt = 0.5 / (1 << maxl)
+    dt = CFG["cfl"] / (1 << maxl)
     t_setup = time.perf_counter()
     o = OracleSim(dim, minl, maxl, 1, 1)
     lv, co, _ = o.cells()
@@ -594,7 +617,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="advection2d", choices=["advection2d", "batch", "adjoint"],
+    p.add_argument("--workload", default="advection2d", choices=["advection2d", "advection3d", "batch", "adjoint"],
                    help="advection2d: the max_level-12 2D problem (default); batch: independent problems through sg_batch_step; "
                         "adjoint: the discrete adjoint of a max_level-10 loop")
     p.add_argument("--adjoint-steps", type=int, default=256)
@@ -605,6 +628,10 @@ def main():
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    if args.workload == "advection3d":
+        CFG.clear()
+        CFG.update(CFG_3D)
+        args.no_cpu_baseline = True
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
