@@ -1,9 +1,13 @@
 // demos/FiniteVolume/advection_2d.cpp of samurai, written against the
 // GB300 drop-in header: the samurai calls are the demo's own (the output and
 // CLI parts are replaced by printing the final cells).  Usage:
-//   advection_2d <pred 0|1> <out.txt>
+//   advection_2d <pred 0|1> <out.txt> [convection]
+// With "convection" the step is the flux form of
+// demos/FiniteVolume/linear_convection.cpp: unp1 = u - dt * conv(u) with
+// conv = make_convection_upwind<decltype(u)>(a).
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 
 #include <samurai_gb300/samurai.hpp>
 
@@ -32,7 +36,7 @@ void init(Field& u)
 }
 
 template <int pred>
-int run(const char* out_path)
+int run(const char* out_path, bool flux_form)
 {
     constexpr std::size_t dim = 2;
     std::array<double, dim> a{{1, 1}};
@@ -66,7 +70,16 @@ int run(const char* out_path)
         }
         samurai::update_ghost_mr(u);
         unp1.resize();
-        unp1 = u - dt * samurai::upwind(a, u);
+        if (flux_form)
+        {
+            samurai::VelocityVector<dim> velocity = {a[0], a[1]};
+            auto conv                             = samurai::make_convection_upwind<decltype(u)>(velocity);
+            unp1                                  = u - dt * conv(u);
+        }
+        else
+        {
+            unp1 = u - dt * samurai::upwind(a, u);
+        }
         std::swap(u.array(), unp1.array());
         ++nt;
     }
@@ -87,12 +100,13 @@ int main(int argc, char** argv)
 {
     if (argc < 3)
     {
-        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt>\n");
+        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt> [convection]\n");
         return 2;
     }
+    const bool flux_form = argc > 3 && std::string(argv[3]) == "convection";
     try
     {
-        return std::atoi(argv[1]) == 0 ? run<0>(argv[2]) : run<1>(argv[2]);
+        return std::atoi(argv[1]) == 0 ? run<0>(argv[2], flux_form) : run<1>(argv[2], flux_form);
     }
     catch (const std::exception& e)
     {

@@ -42,3 +42,27 @@ def test_demo_matches_golden(tmp_path, pred):
     assert np.array_equal(rows[:, 0].astype(int), g["level"])
     assert np.array_equal(rows[:, 1].astype(int), g["i"]) and np.array_equal(rows[:, 2].astype(int), g["j"])
     np.testing.assert_allclose(rows[:, 3], g["u"], rtol=1e-14, atol=1e-7)
+
+
+@pytest.mark.gpu
+def test_demo_flux_form_matches_oracle(tmp_path):
+    """The demo with unp1 = u - dt * conv(u), conv = make_convection_upwind,
+    against the oracle running the same loop: identical cells and values."""
+    from advection_cases import demo_time_loop, disc
+    from oracle.pyoracle import OracleSim
+
+    exe = compile_demo(tmp_path)
+    out = os.path.join(str(tmp_path), "out.txt")
+    subprocess.check_call([exe, "1", out, "convection"])
+    lines = open(out).read().split("\n")
+    rows = np.array([[float(v) for v in l.split()] for l in lines[1:] if l.strip()])
+    o = OracleSim(2, 4, 10, 1, 1)
+    lv, co, _ = o.cells()
+    o.set_cell_values(disc(lv, co))
+    o.adapt(2e-4, 1.0)
+    nt = demo_time_loop(o, 0.5 / 1024, 0.01, 2e-4, 1.0, (1.0, 1.0), scheme=2)
+    assert int(lines[0]) == nt
+    lv, co, _ = o.cells()
+    assert np.array_equal(rows[:, 0].astype(int), lv)
+    assert np.array_equal(rows[:, 1:3].astype(int), co)
+    assert np.array_equal(rows[:, 3], o.cell_values())
