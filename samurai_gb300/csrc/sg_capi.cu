@@ -1,5 +1,6 @@
 // C ABI of libsamurai_gpu.so (declared in include/samurai_gpu.h).
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -27,6 +28,20 @@ namespace
 
 namespace
 {
+    // launch-shape tuning: a positive integer in the environment overrides a
+    // default threshold (read when a mesh is created)
+    long long tuned(const char* name, long long dflt)
+    {
+        const char* v = std::getenv(name);
+        if (!v || !*v)
+        {
+            return dflt;
+        }
+        char* end          = nullptr;
+        const long long x  = std::strtoll(v, &end, 10);
+        return (end && *end == '\0' && x >= 0) ? x : dflt;
+    }
+
     int from_ctx(sg::Ctx& c, int st)
     {
         if (st != sg::SG_OK)
@@ -339,8 +354,9 @@ extern "C"
         c.cfg.ghost_width          = max_stencil_radius > prediction_radius ? max_stencil_radius : prediction_radius;
         c.g                        = sg::make_geom(dim, min_level, max_level);
         c.capacity                 = 32 * c.g.total_words;
-        c.fuse_top                 = sg::fuse_top_of(c.g, sg::FUSE_WORDS);
-        c.fuse_top_field           = sg::fuse_top_of(c.g, sg::FUSE_WORDS_FIELD);
+        c.fuse_top                 = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS", sg::FUSE_WORDS));
+        c.fuse_top_field           = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS_FIELD", sg::FUSE_WORDS_FIELD));
+        c.fuse_top_max             = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS_MAX", sg::FUSE_WORDS_MAX));
         if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
         {
             cudaGetLastError();

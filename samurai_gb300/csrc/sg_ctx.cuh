@@ -127,6 +127,7 @@ namespace sg
         unsigned long long mesh_version = 1; // bumped at every change of the current mesh
         int fuse_top        = -1;      // levels 0..fuse_top are small enough for one-block mesh chains
         int fuse_top_field  = -1;      // the same for the FP64 field chains
+        int fuse_top_max    = -1;      // the same for the tag-finalisation chain
         struct GraphEntry
         {
             unsigned long long key[4];
@@ -221,6 +222,7 @@ namespace sg
 
     constexpr long long FUSE_WORDS       = 16384;
     constexpr long long FUSE_WORDS_FIELD = 0;
+    constexpr long long FUSE_WORDS_MAX   = 0;
 
     inline int fuse_top_of(const Geom& g, long long limit)
     {

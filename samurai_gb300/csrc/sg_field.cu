@@ -1421,7 +1421,7 @@ namespace sg
             timer_start(c, T_FINALIZE);
             {
                 int l = maxl;
-                for (; l > 0 && l - 1 > c.fuse_top_field; --l)
+                for (; l > 0 && l - 1 > c.fuse_top_max; --l)
                 {
                     if (g.dim == 2)
                     {
