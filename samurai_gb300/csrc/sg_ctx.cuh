@@ -214,13 +214,15 @@ namespace sg
     // in a single block that steps through them with __syncthreads(), instead
     // of one launch per level.
     // The integer word chains of the mesh construction stay in one block up
-    // to 16K words per level.  The FP64 field chains are not fused: their
-    // cells wait on memory, and one block serialises that latency (measured
-    // slower than one launch per level even at 2K words), so the limit is 0.
+    // to 1K words per level (on the 2D max_level-12 step: 1.14 ms/step at 1K,
+    // 1.16 at 4K, 1.25 at 16K, 1.20 without fusion).  The FP64 field chains
+    // and the tag finalisation are not fused: their cells wait on memory, and
+    // one block serialises that latency (measured slower than one launch per
+    // level even at 1K-2K words), so their limit is 0.
     // device thresholds buffer: [eps | fine | coarse] x MAXLEV, then a velocity
     constexpr int EPS_VELOCITY = 3 * MAXLEV;
 
-    constexpr long long FUSE_WORDS       = 16384;
+    constexpr long long FUSE_WORDS       = 1024;
     constexpr long long FUSE_WORDS_FIELD = 0;
     constexpr long long FUSE_WORDS_MAX   = 0;
 
