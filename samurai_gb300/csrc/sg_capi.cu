@@ -180,8 +180,8 @@ namespace
         const sg::LevelGeom& L = g.lv[l];
         for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < L.nwords; w += static_cast<long long>(gridDim.x) * blockDim.x)
         {
-            const long long row = w / L.W;
-            const int wi        = static_cast<int>(w - row * L.W);
+            const unsigned row = sg::fastdiv(static_cast<unsigned>(w), L.mW, L.sW);
+            const int wi       = static_cast<int>(static_cast<unsigned>(w) - row * static_cast<unsigned>(L.W));
             cells[L.woff + w]   = sg::box_mask(g, l, row, wi, 0, 0);
         }
     }

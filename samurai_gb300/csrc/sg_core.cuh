@@ -28,14 +28,53 @@ namespace sg
 
     struct LevelGeom
     {
-        int n;   // 2^l cells per axis inside the unit box
-        int W;   // 32-bit words per row
-        int R;   // rows per axis: n + 2*PY
+        int n;       // 2^l cells per axis inside the unit box
+        int W;       // 32-bit words per row
+        int R;       // rows per axis: n + 2*PY
+        int sW;      // division by W: shift
+        unsigned mW; // division by W: multiplier
+        unsigned mR; // division by R: multiplier
+        int sR;      // division by R: shift
         int pad_;
         long long nrows;  // R^(dim-1)
         long long woff;   // first word of the level
         long long nwords; // nrows * W
     };
+
+    // Unsigned 32-bit division by a run-time constant d >= 2 as a multiply-high
+    // and shifts (the round-up method of Granlund and Montgomery, "Division by
+    // invariant integers using multiplication", 1994): with s = ceil(log2 d)
+    // and m = floor(2^32 (2^s - d) / d) + 1, n / d = (t + ((n - t) >> 1)) >> (s - 1)
+    // where t = (m n) >> 32, exact for every 32-bit n.
+    inline void fastdiv_init(unsigned d, unsigned* m, int* s)
+    {
+        int l = 0;
+        while ((1ull << l) < d)
+        {
+            ++l;
+        }
+        *s = l;
+        *m = static_cast<unsigned>(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+
+    __host__ __device__ __forceinline__ unsigned fastdiv(unsigned n, unsigned m, int s)
+    {
+#ifdef __CUDA_ARCH__
+        const unsigned t = __umulhi(m, n);
+#else
+        const unsigned t = static_cast<unsigned>((static_cast<unsigned long long>(m) * n) >> 32);
+#endif
+        return (t + ((n - t) >> 1)) >> (s - 1);
+    }
+
+    // row -> (y row, z row) of a level (3D rows are z-major)
+    __host__ __device__ __forceinline__ void split_row(const LevelGeom& L, long long row, int* ry, int* rz)
+    {
+        const unsigned r = static_cast<unsigned>(row);
+        const unsigned z = fastdiv(r, L.mR, L.sR);
+        *rz              = static_cast<int>(z);
+        *ry              = static_cast<int>(r - z * static_cast<unsigned>(L.R));
+    }
 
     struct Geom
     {
@@ -64,6 +103,8 @@ namespace sg
             L.nrows      = (dim == 2) ? L.R : static_cast<long long>(L.R) * L.R;
             L.woff       = off;
             L.nwords     = L.nrows * L.W;
+            fastdiv_init(static_cast<unsigned>(L.W), &L.mW, &L.sW);
+            fastdiv_init(static_cast<unsigned>(L.R), &L.mR, &L.sR);
             off += L.nwords;
         }
         g.total_words = off;
@@ -115,9 +156,9 @@ namespace sg
     __host__ __device__ __forceinline__ Cell cell_of(const Geom& g, int l, long long w, int b)
     {
         const LevelGeom& L = g.lv[l];
-        const long long loc = w - L.woff;
-        const long long row = loc / L.W;
-        const int wi        = static_cast<int>(loc - row * L.W);
+        const unsigned loc = static_cast<unsigned>(w - L.woff);
+        const unsigned row = fastdiv(loc, L.mW, L.sW);
+        const int wi       = static_cast<int>(loc - row * static_cast<unsigned>(L.W));
         Cell c;
         c.x = wi * 32 + b - PX;
         if (g.dim == 2)
@@ -127,8 +168,10 @@ namespace sg
         }
         else
         {
-            c.y = static_cast<int>(row % L.R) - PY;
-            c.z = static_cast<int>(row / L.R) - PY;
+            int ry, rz;
+            split_row(L, row, &ry, &rz);
+            c.y = ry - PY;
+            c.z = rz - PY;
         }
         return c;
     }
@@ -202,8 +245,9 @@ namespace sg
         }
         else
         {
-            yc = static_cast<int>(row % C.R) - PY;
-            zc = static_cast<int>(row / C.R) - PY;
+            split_row(C, row, &yc, &zc);
+            yc -= PY;
+            zc -= PY;
         }
         uint32_t out = 0;
         const int nz = (g.dim == 3) ? 2 : 1;
@@ -243,8 +287,9 @@ namespace sg
         }
         else
         {
-            yf = static_cast<int>(row % F.R) - PY;
-            zf = static_cast<int>(row / F.R) - PY;
+            split_row(F, row, &yf, &zf);
+            yf -= PY;
+            zf -= PY;
         }
         const int ry = (yf >> 1) + PY;
         const int rz = (zf >> 1) + PY;
@@ -285,8 +330,7 @@ namespace sg
         }
         else
         {
-            ry = static_cast<int>(row % L.R);
-            rz = static_cast<int>(row / L.R);
+            split_row(L, row, &ry, &rz);
         }
         uint32_t out = 0;
         const int zlo = (g.dim == 3) ? -r : 0, zhi = (g.dim == 3) ? r : 0;
@@ -327,8 +371,9 @@ namespace sg
         }
         else
         {
-            y = static_cast<int>(row % L.R) - PY;
-            z = static_cast<int>(row / L.R) - PY;
+            split_row(L, row, &y, &z);
+            y -= PY;
+            z -= PY;
         }
         const int a = -lo, b = L.n + hi; // allowed range [a, b)
         if (y < a || y >= b || (g.dim == 3 && (z < a || z >= b)))
@@ -365,9 +410,9 @@ namespace sg
     __host__ __device__ __forceinline__ WordLoc word_loc(const Geom& g, int l, long long w)
     {
         const LevelGeom& L = g.lv[l];
-        const long long loc = w - L.woff;
-        const long long row = loc / L.W;
-        return {row, static_cast<int>(loc - row * L.W)};
+        const unsigned loc = static_cast<unsigned>(w - L.woff);
+        const unsigned row = fastdiv(loc, L.mW, L.sW);
+        return {static_cast<long long>(row), static_cast<int>(loc - row * static_cast<unsigned>(L.W))};
     }
 
     // status word shared with the host

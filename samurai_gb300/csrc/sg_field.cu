@@ -75,12 +75,10 @@ namespace sg
         }
 
 
-        // interp_coeffs<3> (numeric/prediction.hpp:32-36), parity 0: even
-        __device__ __forceinline__ double interp1(int parity, int k)
-        {
-            const double sign = parity ? -1. : 1.;
-            return k == 0 ? sign / 8. : (k == 1 ? 1. : -sign / 8.);
-        }
+        // The prediction coefficients interp_coeffs<3> (numeric/prediction.hpp:32-36)
+        // of tap t in {0,1,2} for a child of parity q are 1 at t = 1 and
+        // +-1/8 at t = 0, 2 (negative at t = 0 for odd children, at t = 2 for
+        // even ones); products over the axes are +-8^-k, k = off-centre taps.
 
         // Element of a cell that the reference algorithm guarantees to be in
         // the stored box.  A position outside it (a bug or an invalid mesh)
@@ -106,8 +104,12 @@ namespace sg
             {
                 return u.get(elem_at(g, l - 1, px, py, pz));
             }
+            // acc + u * coeff with coeff = ((1 * cx) * cy) * cz = +-8^-k (k = axes
+            // with an off-centre tap): u * coeff is +-(u * 8^-k) bit for bit
+            // (power-of-two scaling is exact) and acc + (-m) is acc - m
             typename A::V acc = A::konst(0.);
-            const int nz = (g.dim == 3) ? 3 : 1;
+            const int nz      = (g.dim == 3) ? 3 : 1;
+            const int qx = x & 1, qy = y & 1, qz = z & 1;
             for (int sz = 0; sz < nz; ++sz)
             {
                 for (int sy = 0; sy < 3; ++sy)
@@ -115,14 +117,12 @@ namespace sg
                     const long long base = elem_at(g, l - 1, px - 1, py + sy - 1, (g.dim == 3) ? pz + sz - 1 : 0);
                     for (int sx = 0; sx < 3; ++sx)
                     {
-                        double coeff = 1.;
-                        coeff        = coeff * interp1(x & 1, sx);
-                        coeff        = coeff * interp1(y & 1, sy);
-                        if (g.dim == 3)
-                        {
-                            coeff = coeff * interp1(z & 1, sz);
-                        }
-                        acc = acc + u.get(base + sx) * coeff;
+                        const int k      = (sx != 1) + (sy != 1) + (g.dim == 3 && sz != 1);
+                        const bool neg   = ((sx == 0 && qx) || (sx == 2 && !qx)) ^ ((sy == 0 && qy) || (sy == 2 && !qy))
+                                         ^ (g.dim == 3 && ((sz == 0 && qz) || (sz == 2 && !qz)));
+                        const typename A::V v = u.get(base + sx);
+                        const typename A::V m = k == 0 ? v : v * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
+                        acc                   = neg ? acc - m : acc + m;
                     }
                 }
             }
@@ -585,6 +585,10 @@ namespace sg
                           {
                               d[ch] = u[ce[ch]];
                           }
+                          // d -= cf * src with cf = prod interp1 = +-8^-k (k = axes with
+                          // an off-centre tap): cf * src is +-(src * 8^-k) bit for bit
+                          // (power-of-two scaling is exact), and d - (-m) is d + m, so
+                          // one product per source serves all children
                           const int nz = (DIM == 3) ? 3 : 1;
                           for (int sz = 0; sz < nz; ++sz)
                           {
@@ -594,14 +598,15 @@ namespace sg
                                   for (int sx = 0; sx < 3; ++sx)
                                   {
                                       const double src = u[base + sx];
+                                      const int k      = (sx != 1) + (sy != 1) + (DIM == 3 && sz != 1);
+                                      const double m   = k == 0 ? src : src * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
                                       for (int ch = 0; ch < (1 << DIM); ++ch)
                                       {
-                                          double cf = interp1(ch & 1, sx) * interp1((ch >> 1) & 1, sy);
-                                          if (DIM == 3)
-                                          {
-                                              cf = cf * interp1((ch >> 2) & 1, sz);
-                                          }
-                                          d[ch] = d[ch] - cf * src;
+                                          // interp1(parity, t) < 0: t == 0 on odd children, t == 2 on even ones
+                                          const int px = ch & 1, py = (ch >> 1) & 1, pz = (ch >> 2) & 1;
+                                          const bool neg = ((sx == 0 && px) || (sx == 2 && !px)) ^ ((sy == 0 && py) || (sy == 2 && !py))
+                                                           ^ (DIM == 3 && ((sz == 0 && pz) || (sz == 2 && !pz)));
+                                          d[ch]          = neg ? d[ch] + m : d[ch] - m;
                                       }
                                   }
                               }

@@ -103,8 +103,8 @@ namespace sg
                 for (long long k = threadIdx.x; k < L.nwords; k += blockDim.x)
                 {
                     const long long w   = L.woff + k;
-                    const long long row = k / L.W;
-                    f(g, l, w, row, static_cast<int>(k - row * L.W));
+                    const unsigned row = fastdiv(static_cast<unsigned>(k), L.mW, L.sW);
+                    f(g, l, w, static_cast<long long>(row), static_cast<int>(static_cast<unsigned>(k) - row * static_cast<unsigned>(L.W)));
                 }
                 __syncthreads();
                 if (l == l_last)
@@ -500,8 +500,9 @@ namespace sg
                                   }
                                   else
                                   {
-                                      yf = static_cast<int>(row % F.R) - PY;
-                                      zf = static_cast<int>(row / F.R) - PY;
+                                      split_row(F, row, &yf, &zf);
+                                      yf -= PY;
+                                      zf -= PY;
                                   }
                                   const int ry = (yf >> 1) + PY, rz = (zf >> 1) + PY;
                                   const int wc = (k + 1) >> 1;
@@ -612,8 +613,9 @@ namespace sg
                                         }
                                         else
                                         {
-                                            yc = static_cast<int>(row % C.R) - PY;
-                                            zc = static_cast<int>(row / C.R) - PY;
+                                            split_row(C, row, &yc, &zc);
+                                            yc -= PY;
+                                            zc -= PY;
                                         }
                                         const int ry = 2 * yc + PY, rz = 2 * zc + PY;
                                         if (ry >= 0 && ry < F.R && (g.dim == 2 || (rz >= 0 && rz < F.R)))
@@ -649,7 +651,6 @@ namespace sg
         uint32_t* d    = c.t2;
         uint32_t* rr   = c.t3;
         int* flag      = c.d_flags + slot;
-        const size_t bytes = static_cast<size_t>(g.total_words) * 4;
         int st = launch_words(c, 0, top,
                               [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = box_dilate_word(g, nc, l, row, wi, gw2); },
                               "grad_expand");
@@ -665,15 +666,15 @@ namespace sg
         {
             return st;
         }
-        cudaMemsetAsync(d, 0, bytes, c.stream);
-        cudaMemsetAsync(rr, 0, bytes, c.stream);
-        // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. 0
+        // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. 0; d and rr are
+        // written on every word of those levels and read as 0 above them
+        const int dtop = maxl - 2;
         if (maxl >= 2)
         {
             st = launch_chain(c, maxl - 2, 0,
                               [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
                               {
-                                  const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | coarsen_word(g, d, ll, row, wi);
+                                  const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | (ll + 1 <= dtop ? coarsen_word(g, d, ll, row, wi) : 0u);
                                   d[w]              = dv;
                                   const uint32_t rv = nc[w] & dv;
                                   rr[w]             = rv;
@@ -691,9 +692,9 @@ namespace sg
         return launch_words(c, 0, top,
                             [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                             {
-                                const uint32_t r = rr[w];
+                                const uint32_t r = l <= dtop ? rr[w] : 0u;
                                 uint32_t v       = nc[w] & ~r;
-                                if (l >= 1)
+                                if (l >= 1 && l - 1 <= dtop)
                                 {
                                     v |= refine_word(g, rr, l, row, wi);
                                 }
