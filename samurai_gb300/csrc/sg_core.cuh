@@ -318,8 +318,10 @@ namespace sg
         return out;
     }
 
-    // box dilation by r of bitmap `src` at level l, word (row, wi)
-    __device__ __forceinline__ uint32_t box_dilate_word(const Geom& g, const uint32_t* src, int l, long long row, int wi, int r)
+    // Box dilation split by axes: dilate_xy_word dilates along x and y within
+    // a z plane (the whole box dilation in 2D), dilate_z_word along z; in 3D
+    // box = z o xy reads 5 + 15 words instead of 75 for r = 2.
+    __device__ __forceinline__ uint32_t dilate_xy_word(const Geom& g, const uint32_t* src, int l, long long row, int wi, int r)
     {
         const LevelGeom& L = g.lv[l];
         int ry, rz;
@@ -333,27 +335,36 @@ namespace sg
             split_row(L, row, &ry, &rz);
         }
         uint32_t out = 0;
-        const int zlo = (g.dim == 3) ? -r : 0, zhi = (g.dim == 3) ? r : 0;
-        for (int dz = zlo; dz <= zhi; ++dz)
+        for (int dy = -r; dy <= r; ++dy)
         {
-            const int z2 = rz + dz;
-            if (g.dim == 3 && (z2 < 0 || z2 >= L.R))
+            const int y2 = ry + dy;
+            if (y2 < 0 || y2 >= L.R)
             {
                 continue;
             }
-            for (int dy = -r; dy <= r; ++dy)
+            const long long base = L.woff + ((g.dim == 2) ? y2 : static_cast<long long>(rz) * L.R + y2) * L.W;
+            const uint32_t mid   = __ldg(src + base + wi);
+            const uint32_t left  = wi > 0 ? __ldg(src + base + wi - 1) : 0u;
+            const uint32_t right = wi + 1 < L.W ? __ldg(src + base + wi + 1) : 0u;
+            out |= dilate_x(left, mid, right, r);
+        }
+        return out;
+    }
+
+    __device__ __forceinline__ uint32_t dilate_z_word(const Geom& g, const uint32_t* src, int l, long long row, int wi, int r)
+    {
+        const LevelGeom& L = g.lv[l];
+        int ry, rz;
+        split_row(L, row, &ry, &rz);
+        uint32_t out = 0;
+        for (int dz = -r; dz <= r; ++dz)
+        {
+            const int z2 = rz + dz;
+            if (z2 < 0 || z2 >= L.R)
             {
-                const int y2 = ry + dy;
-                if (y2 < 0 || y2 >= L.R)
-                {
-                    continue;
-                }
-                const long long base = L.woff + ((g.dim == 2) ? y2 : static_cast<long long>(z2) * L.R + y2) * L.W;
-                const uint32_t mid   = __ldg(src + base + wi);
-                const uint32_t left  = wi > 0 ? __ldg(src + base + wi - 1) : 0u;
-                const uint32_t right = wi + 1 < L.W ? __ldg(src + base + wi + 1) : 0u;
-                out |= dilate_x(left, mid, right, r);
+                continue;
             }
+            out |= __ldg(src + L.woff + (static_cast<long long>(z2) * L.R + ry) * L.W + wi);
         }
         return out;
     }

@@ -96,7 +96,7 @@ namespace sg
         }
 
         // prediction_op<order,false> for one fine cell (numeric/prediction.hpp:286-361)
-        template <class A>
+        template <int DIM, class A>
         __device__ __forceinline__ typename A::V predict_one(const Geom& g, const A& u, int l, int x, int y, int z, int order)
         {
             const int px = x >> 1, py = y >> 1, pz = z >> 1;
@@ -108,18 +108,20 @@ namespace sg
             // with an off-centre tap): u * coeff is +-(u * 8^-k) bit for bit
             // (power-of-two scaling is exact) and acc + (-m) is acc - m
             typename A::V acc = A::konst(0.);
-            const int nz      = (g.dim == 3) ? 3 : 1;
             const int qx = x & 1, qy = y & 1, qz = z & 1;
-            for (int sz = 0; sz < nz; ++sz)
+#pragma unroll
+            for (int sz = 0; sz < (DIM == 3 ? 3 : 1); ++sz)
             {
+#pragma unroll
                 for (int sy = 0; sy < 3; ++sy)
                 {
-                    const long long base = elem_at(g, l - 1, px - 1, py + sy - 1, (g.dim == 3) ? pz + sz - 1 : 0);
+                    const long long base = elem_at(g, l - 1, px - 1, py + sy - 1, (DIM == 3) ? pz + sz - 1 : 0);
+#pragma unroll
                     for (int sx = 0; sx < 3; ++sx)
                     {
-                        const int k      = (sx != 1) + (sy != 1) + (g.dim == 3 && sz != 1);
+                        const int k      = (sx != 1) + (sy != 1) + (DIM == 3 && sz != 1);
                         const bool neg   = ((sx == 0 && qx) || (sx == 2 && !qx)) ^ ((sy == 0 && qy) || (sy == 2 && !qy))
-                                         ^ (g.dim == 3 && ((sz == 0 && qz) || (sz == 2 && !qz)));
+                                         ^ (DIM == 3 && ((sz == 0 && qz) || (sz == 2 && !qz)));
                         const typename A::V v = u.get(base + sx);
                         const typename A::V m = k == 0 ? v : v * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
                         acc                   = neg ? acc - m : acc + m;
@@ -427,7 +429,7 @@ namespace sg
                       [&](long long w, int b)
                       {
                           const Cell c = cell_of(g, l, w, b);
-                          u.put(32 * w + b, predict_one(g, u, l, c.x, c.y, c.z, order));
+                          u.put(32 * w + b, predict_one<DIM>(g, u, l, c.x, c.y, c.z, order));
                       });
         }
 
@@ -766,7 +768,7 @@ namespace sg
                               }
                               else if (l >= 1 && test(ocells, g, l - 1, c.x >> 1, c.y >> 1, c.z >> 1))
                               {
-                                  v = predict_one(g, uo, l, c.x, c.y, c.z, order);
+                                  v = predict_one<DIM>(g, uo, l, c.x, c.y, c.z, order);
                               }
                               else if ((oref[w] >> b) & 1u)
                               {

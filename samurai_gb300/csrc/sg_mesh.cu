@@ -444,9 +444,25 @@ namespace sg
         }
 
         // cells_and_ghosts: box expansion of the cells by max_stencil_radius
-        st = launch_words(c, 0, top,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = box_dilate_word(g, cells, l, row, wi, r); },
-                          "cag");
+        if (g.dim == 2)
+        {
+            st = launch_words(c, 0, top,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = dilate_xy_word(g, cells, l, row, wi, r); },
+                              "cag");
+        }
+        else
+        {
+            uint32_t* t0 = c.t0;
+            st           = launch_words(c, 0, top,
+                                        [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { t0[w] = dilate_xy_word(g, cells, l, row, wi, r); },
+                                        "cag_xy");
+            if (!st)
+            {
+                st = launch_words(c, 0, top,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = dilate_z_word(g, t0, l, row, wi, r); },
+                                  "cag_z");
+            }
+        }
         if (st)
         {
             return st;
@@ -469,15 +485,42 @@ namespace sg
         {
             return st;
         }
-        st = launch_words(c, 0, top,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                          {
-                              uint32_t v = cag[w];
-                              v |= box_dilate_word(g, t1, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
-                              v |= box_dilate_word(g, hc2, l, row, wi, p);
-                              ref[w] = v;
-                          },
-                          "ref0");
+        if (g.dim == 2)
+        {
+            st = launch_words(c, 0, top,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                              {
+                                  uint32_t v = cag[w];
+                                  v |= dilate_xy_word(g, t1, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
+                                  v |= dilate_xy_word(g, hc2, l, row, wi, p);
+                                  ref[w] = v;
+                              },
+                              "ref0");
+        }
+        else
+        {
+            uint32_t* t2 = c.t2;
+            uint32_t* t3 = c.t3;
+            st           = launch_words(c, 0, top,
+                                        [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                        {
+                                            t2[w] = dilate_xy_word(g, t1, l, row, wi, p);
+                                            t3[w] = dilate_xy_word(g, hc2, l, row, wi, p);
+                                        },
+                                        "ref0_xy");
+            if (!st)
+            {
+                st = launch_words(c, 0, top,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                  {
+                                      uint32_t v = cag[w];
+                                      v |= dilate_z_word(g, t2, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
+                                      v |= dilate_z_word(g, t3, l, row, wi, p);
+                                      ref[w] = v;
+                                  },
+                                  "ref0_z");
+            }
+        }
         if (st)
         {
             return st;
@@ -651,9 +694,26 @@ namespace sg
         uint32_t* d    = c.t2;
         uint32_t* rr   = c.t3;
         int* flag      = c.d_flags + slot;
-        int st = launch_words(c, 0, top,
-                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = box_dilate_word(g, nc, l, row, wi, gw2); },
+        int st;
+        if (g.dim == 2)
+        {
+            st = launch_words(c, 0, top,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = dilate_xy_word(g, nc, l, row, wi, gw2); },
                               "grad_expand");
+        }
+        else
+        {
+            // xy into ec1 (free until the coarsening below), then z
+            st = launch_words(c, 0, top,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { ec1[w] = dilate_xy_word(g, nc, l, row, wi, gw2); },
+                              "grad_expand_xy");
+            if (!st)
+            {
+                st = launch_words(c, 0, top,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = dilate_z_word(g, ec1, l, row, wi, gw2); },
+                                  "grad_expand_z");
+            }
+        }
         if (st)
         {
             return st;
