@@ -128,6 +128,7 @@ namespace sg
         int fuse_top        = -1;      // levels 0..fuse_top are small enough for one-block mesh chains
         int fuse_top_field  = -1;      // the same for the FP64 field chains
         int fuse_top_max    = -1;      // the same for the tag-finalisation chain
+        const int* guard    = nullptr; // device flag: word launches do nothing while it is 0
         struct GraphEntry
         {
             unsigned long long key[4];

@@ -36,7 +36,7 @@ namespace sg
 
     int new_cells_from_tags(Ctx& c, const DeviceMesh& m, uint32_t* nc);
     int graduate(Ctx& c, uint32_t* nc, int* iterations);
-    int grad_pass(Ctx& c, uint32_t* nc, int slot);
+    int grad_pass(Ctx& c, uint32_t* nc, int slot, const int* guard);
     int bitmaps_differ(Ctx& c, const uint32_t* a, const uint32_t* b, int slot);
 
     namespace
@@ -1460,7 +1460,9 @@ namespace sg
             }
 
             timer_start(c, T_MESH_UPDATE);
-            if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0)) || (st = grad_pass(c, nm.cells, F_GRAD1))
+            // the second pass runs on the device only if the first one refined
+            if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0, nullptr))
+                || (st = grad_pass(c, nm.cells, F_GRAD1, c.d_flags + F_GRAD0))
                 || (st = bitmaps_differ(c, nm.cells, m.cells, F_DIFFER)))
             {
                 return st;

@@ -72,9 +72,14 @@ namespace sg
     namespace
     {
         // ------------------------------------------------------------- words
+        // guard: when not null, the launch does nothing unless *guard != 0
         template <class F>
-        __global__ void k_words(const Geom* __restrict__ gp, int l0, int l1, F f)
+        __global__ void k_words(const Geom* __restrict__ gp, int l0, int l1, F f, const int* guard)
         {
+            if (guard && *guard == 0)
+            {
+                return;
+            }
             const Geom& g         = *gp;
             const long long begin = g.lv[l0].woff;
             const long long end   = g.lv[l1].woff + g.lv[l1].nwords;
@@ -93,8 +98,12 @@ namespace sg
 
         // one block walks the levels l_first -> l_last (either direction)
         template <class F>
-        __global__ void __launch_bounds__(1024, 1) k_words_chain(const Geom* __restrict__ gp, int l_first, int l_last, F f)
+        __global__ void __launch_bounds__(1024, 1) k_words_chain(const Geom* __restrict__ gp, int l_first, int l_last, F f, const int* guard)
         {
+            if (guard && *guard == 0)
+            {
+                return;
+            }
             const Geom& g  = *gp;
             const int step = l_last >= l_first ? 1 : -1;
             for (int l = l_first;; l += step)
@@ -136,7 +145,7 @@ namespace sg
                 }
                 if (l >= l_last)
                 {
-                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, l_last, f);
+                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, l_last, f, c.guard);
                     ++c.n_launches;
                     st = check(c, what);
                 }
@@ -147,7 +156,7 @@ namespace sg
                 if (l <= ft)
                 {
                     const int e = l_last < ft ? l_last : ft;
-                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, e, f);
+                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, e, f, c.guard);
                     ++c.n_launches;
                     if ((st = check(c, what)))
                     {
@@ -174,7 +183,7 @@ namespace sg
                 return SG_OK;
             }
             const long long n = c.g.lv[l1].woff + c.g.lv[l1].nwords - c.g.lv[l0].woff;
-            k_words<<<grid_for(n), 256, 0, c.stream>>>(c.d_geom, l0, l1, f);
+            k_words<<<grid_for(n), 256, 0, c.stream>>>(c.d_geom, l0, l1, f, c.guard);
             ++c.n_launches;
             return check(c, what);
         }
@@ -683,8 +692,24 @@ namespace sg
     // that finds nothing leaves the cells unchanged, so extra passes after the
     // fixed point are no-ops.  The contiguous-boundary pass
     // (graduation.hpp:121-249) is a no-op for a max_stencil_radius of 1.
-    int grad_pass(Ctx& c, uint32_t* nc, int slot)
+    int grad_pass(Ctx& c, uint32_t* nc, int slot, const int* guard)
     {
+        // every launch of the pass is skipped on the device when *guard == 0
+        struct GuardScope
+        {
+            Ctx& c;
+            const int* saved;
+            GuardScope(Ctx& cc, const int* gd)
+                : c(cc)
+                , saved(cc.guard)
+            {
+                c.guard = gd;
+            }
+            ~GuardScope()
+            {
+                c.guard = saved;
+            }
+        } scope(c, guard);
         const Geom g   = c.g;
         const int top  = g.nlev - 1;
         const int maxl = c.cfg.max_level;
@@ -775,7 +800,7 @@ namespace sg
         {
             ++nit;
             cudaMemsetAsync(c.d_flags + F_GRADX, 0, sizeof(int), c.stream);
-            int st = grad_pass(c, nc, F_GRADX);
+            int st = grad_pass(c, nc, F_GRADX, nullptr);
             if (st)
             {
                 return st;
