@@ -30,6 +30,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 from advection_cases import ball_3d, shapes_2d  # noqa: E402
+from samurai_gb300.replicas import reduce_over_ranks, shard_instances  # noqa: E402
 
 CFG = dict(dim=2, min_level=4, max_level=12, a=(1.0, 0.5), eps=1e-4, regularity=2.0, seed=2026, cfl=0.5)
 # the 3D workload (--workload advection3d): ball + 8 Gaussians, a = (1,1,1), L3..9
@@ -221,14 +222,7 @@ def run_gpu(args):
     barrier()
     clocks = sampler.stop() if sampler else None
     ms = total_ms / args.steps
-    if world > 1:
-        t = torch.tensor([total_ms, float(cell_updates)], dtype=torch.float64, device="cuda")
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        total_ms_max, cell_updates_all = float(tmax[0]), float(t[1])
-    else:
-        total_ms_max, cell_updates_all = total_ms, float(cell_updates)
+    total_ms_max, cell_updates_all = reduce_over_ranks(total_ms, cell_updates, world, device="cuda")
     value = cell_updates_all / (total_ms_max / 1e3)
 
     # ---- end-to-end through the C ABI with host buffers
@@ -441,8 +435,16 @@ def run_batch(args):
     import samurai_gb300 as sg
     from advection_cases import batch_instances
 
-    torch.cuda.set_device(0)
-    probs = batch_instances(2027, args.instances)
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    all_probs = batch_instances(2027, args.instances)
+    # N GPUs: each rank advances its shard of the instances (no exchange)
+    mine = shard_instances([4.0 ** p["max_level"] for p in all_probs], rank, world)
+    probs = [all_probs[i] for i in mine]
     sims = []
     for p in probs:
         s = sg.AdvectionSim(2, p["min_level"], p["max_level"])
@@ -460,22 +462,29 @@ def run_batch(args):
     batch.synchronize()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
 
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
     def timed(fn, steps):
         total, updates = 0.0, 0
         for _ in range(steps):
             n = sum(s.nb_cells() for s in sims)
             flush.fill_(1)
-            torch.cuda.synchronize()
+            barrier()
             t0 = time.perf_counter()
             fn()
-            torch.cuda.synchronize()
+            barrier()
             total += time.perf_counter() - t0
             updates += n
         return total, updates
 
-    sampler = ClockSampler(0, os.path.join(ROOT, "gpurun_out", "clocks_batch.csv"))
+    sampler = ClockSampler(local, os.path.join(ROOT, "gpurun_out", "clocks_batch.csv")) if rank == 0 else None
     b_s, b_updates = timed(lambda: (batch.step(eps, reg, a, dt), batch.synchronize()), args.steps)
-    clocks = sampler.stop()
+    clocks = sampler.stop() if sampler else None
+    b_ms, b_updates = reduce_over_ranks(1e3 * b_s, b_updates, world, device="cuda")
+    b_s = b_ms / 1e3
 
     def serial_step():
         for p, s in zip(probs, sims):
@@ -485,23 +494,29 @@ def run_batch(args):
 
     serial_steps = max(1, min(args.steps, 10))
     s_s, s_updates = timed(serial_step, serial_steps)
+    s_ms, s_updates = reduce_over_ranks(1e3 * s_s, s_updates, world, device="cuda")
+    s_s = s_ms / 1e3
     cells = [s.nb_cells() for s in sims]
+    if rank != 0:
+        batch.close()
+        return
     line = {
         "metric": METRIC,
         "value": b_updates / b_s,
         "unit": UNIT,
-        "n_gpus": 1,
+        "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": 1e3 * b_s / args.steps,
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong",  # a fixed set of instances shared by the ranks
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: seeded shapes per instance (no dataset involved)",
         "config": {"workload": "%d independent 2D MR advection problems: max_level U{7..11}, min_level 2, a U[-1,1]^2, 1-8 shapes, "
-                               "eps 1e-3 or 1e-4, regularity 2, dt=0.5*dx_min (seed 2027)" % len(sims),
-                   "host_threads": args.batch_threads, "cells_final_total": int(sum(cells)),
+                               "eps 1e-3 or 1e-4, regularity 2, dt=0.5*dx_min (seed 2027)" % len(all_probs),
+                   "parallelism": "instances sharded over %d GPU(s), no exchange" % world,
+                   "host_threads": args.batch_threads, "cells_final_total_rank0": int(sum(cells)),
                    "cells_final_max": int(max(cells)), "cells_final_min": int(min(cells)),
                    "timing": "wall clock between device synchronisations, L2 flushed (256 MiB write) before every step"},
         "serial": {"value": s_updates / s_s, "unit": UNIT, "steps": serial_steps, "ms_per_step": 1e3 * s_s / serial_steps,
