@@ -367,6 +367,33 @@ def cpu_baseline(sim, a, dt, budget_s=15.0):
             "sample": "%d steps of the same workload from the GPU run's final mesh and values (%.1f s)" % (n, el)}
 
 
+def batch_cpu_baseline(probs, sims, budget_s=15.0):
+    """The CPU oracle stepping the batched instances one after the other (as a
+    samurai user would), each from the GPU run's current mesh and values, for
+    about budget_s seconds; 1 thread."""
+    from oracle.pyoracle import OracleSim
+
+    t_run = 0.0
+    updates = 0
+    n = 0
+    for p, sim in zip(probs, sims):
+        lv, co, _ = sim.cells()
+        o = OracleSim(2, p["min_level"], p["max_level"], 1, 1)
+        o.set_cells(lv, co)
+        o.set_cell_values(sim.cell_values())
+        t0 = time.perf_counter()
+        updates += o.nb_cells()
+        o.adapt(p["eps"], p["regularity"])
+        o.update_ghost()
+        o.upwind(list(p["a"]), p["dt"], 0)
+        t_run += time.perf_counter() - t0
+        n += 1
+        if t_run > budget_s:
+            break
+    return {"value": updates / t_run, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_info(),
+            "sample": "one time step of each of the first %d instances, from the GPU run's meshes and values (%.1f s)" % (n, t_run)}
+
+
 # --------------------------------------------------------- reference arm
 def run_reference(args):
     rank, world, local = dist_env()
@@ -500,6 +527,7 @@ def run_batch(args):
     if rank != 0:
         batch.close()
         return
+    cpu = None if args.no_cpu_baseline else batch_cpu_baseline(probs, sims)
     line = {
         "metric": METRIC,
         "value": b_updates / b_s,
@@ -523,6 +551,7 @@ def run_batch(args):
                    "api": "sg_adapt + sg_update_ghost_mr + sg_upwind + sg_field_swap per instance, one after the other"},
         "speedup_vs_serial": (b_updates / b_s) / (s_updates / s_s),
         "clocks": clocks,
+        "cpu_baseline": cpu,
     }
     print(json.dumps(line))
     batch.close()
@@ -646,7 +675,6 @@ def main():
     if args.workload == "advection3d":
         CFG.clear()
         CFG.update(CFG_3D)
-        args.no_cpu_baseline = True
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
