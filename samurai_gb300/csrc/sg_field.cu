@@ -95,6 +95,28 @@ namespace sg
             return elem(p);
         }
 
+        // A box of cells [x0, x0+n) x [y0, y0+n) x [z0, z0+n) at level l as a base
+        // element and strides: both corners are checked against the stored
+        // box (a violation is recorded and every access goes to element 0)
+        struct Box3
+        {
+            long long base, sy, sz;
+        };
+
+        template <int DIM>
+        __device__ __forceinline__ Box3 box_at(const Geom& g, int l, int x0, int y0, int z0, int n)
+        {
+            const Pos lo = pos_of(g, l, x0, y0, DIM == 3 ? z0 : 0);
+            const Pos hi = pos_of(g, l, x0 + n - 1, y0 + n - 1, DIM == 3 ? z0 + n - 1 : 0);
+            if (lo.w < 0 || hi.w < 0)
+            {
+                atomicOr(&sg_device_error, 1);
+                return {0, 0, 0};
+            }
+            const LevelGeom& L = g.lv[l];
+            return {elem(lo), 32LL * L.W, 32LL * L.W * L.R};
+        }
+
         // prediction_op<order,false> for one fine cell (numeric/prediction.hpp:286-361)
         template <int DIM, class A>
         __device__ __forceinline__ typename A::V predict_one(const Geom& g, const A& u, int l, int x, int y, int z, int order)
@@ -109,13 +131,14 @@ namespace sg
             // (power-of-two scaling is exact) and acc + (-m) is acc - m
             typename A::V acc = A::konst(0.);
             const int qx = x & 1, qy = y & 1, qz = z & 1;
+            const Box3 bx     = box_at<DIM>(g, l - 1, px - 1, py - 1, pz - 1, 3);
 #pragma unroll
             for (int sz = 0; sz < (DIM == 3 ? 3 : 1); ++sz)
             {
 #pragma unroll
                 for (int sy = 0; sy < 3; ++sy)
                 {
-                    const long long base = elem_at(g, l - 1, px - 1, py + sy - 1, (DIM == 3) ? pz + sz - 1 : 0);
+                    const long long base = bx.base + sy * bx.sy + sz * bx.sz;
 #pragma unroll
                     for (int sx = 0; sx < 3; ++sx)
                     {
@@ -132,20 +155,22 @@ namespace sg
         }
 
         // projection_op_ (numeric/projection.hpp:15-65)
-        template <class A>
+        template <int DIM, class A>
         __device__ __forceinline__ typename A::V project_one(const Geom& g, const A& u, int lf, int x, int y, int z)
         {
             typename A::V sum = A::konst(0.);
-            const int nz = (g.dim == 3) ? 2 : 1;
-            for (int sz = 0; sz < nz; ++sz)
+            const Box3 bx     = box_at<DIM>(g, lf, 2 * x, 2 * y, 2 * z, 2);
+#pragma unroll
+            for (int sz = 0; sz < (DIM == 3 ? 2 : 1); ++sz)
             {
+#pragma unroll
                 for (int sy = 0; sy < 2; ++sy)
                 {
-                    const long long e = elem_at(g, lf, 2 * x, 2 * y + sy, (g.dim == 3) ? 2 * z + sz : 0);
+                    const long long e = bx.base + sy * bx.sy + sz * bx.sz;
                     sum               = sum + (u.get(e) + u.get(e + 1));
                 }
             }
-            const double inv = (g.dim == 3) ? 0.125 : 0.25;
+            const double inv = (DIM == 3) ? 0.125 : 0.25;
             return sum * inv;
         }
 
@@ -410,7 +435,7 @@ namespace sg
                       [&](long long w, int b)
                       {
                           const Cell c = cell_of(g, lc, w, b);
-                          u.put(32 * w + b, project_one(g, u, l, c.x, c.y, c.z));
+                          u.put(32 * w + b, project_one<DIM>(g, u, l, c.x, c.y, c.z));
                       });
         }
 
@@ -569,9 +594,10 @@ namespace sg
                           const int l    = level_of(g, w);
                           const Cell c   = cell_of(g, l, w, b);
                           long long ce[8];
+                          const Box3 cb = box_at<DIM>(g, l + 1, 2 * c.x, 2 * c.y, 2 * c.z, 2);
                           for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
-                              ce[ch] = elem_at(g, l + 1, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), DIM == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
+                              ce[ch] = cb.base + (ch & 1) + ((ch >> 1) & 1) * cb.sy + ((ch >> 2) & 1) * cb.sz;
                           }
                           if (order == 0)
                           {
@@ -591,12 +617,15 @@ namespace sg
                           // an off-centre tap): cf * src is +-(src * 8^-k) bit for bit
                           // (power-of-two scaling is exact), and d - (-m) is d + m, so
                           // one product per source serves all children
-                          const int nz = (DIM == 3) ? 3 : 1;
+                          const int nz  = (DIM == 3) ? 3 : 1;
+                          const Box3 sb = box_at<DIM>(g, l, c.x - 1, c.y - 1, c.z - 1, 3);
+#pragma unroll
                           for (int sz = 0; sz < nz; ++sz)
                           {
+#pragma unroll
                               for (int sy = 0; sy < 3; ++sy)
                               {
-                                  const long long base = elem_at(g, l, c.x - 1, c.y + sy - 1, DIM == 3 ? c.z + sz - 1 : 0);
+                                  const long long base = sb.base + sy * sb.sy + sz * sb.sz;
                                   for (int sx = 0; sx < 3; ++sx)
                                   {
                                       const double src = u[base + sx];
@@ -641,9 +670,10 @@ namespace sg
                           const int lf  = lc + 1;
                           const Cell c  = cell_of(g, lc, w, b);
                           long long fo[8];
+                          const Box3 fb = box_at<DIM>(g, lf, 2 * c.x, 2 * c.y, 2 * c.z, 2);
                           for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
-                              fo[ch] = elem_at(g, lf, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), DIM == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
+                              fo[ch] = fb.base + (ch & 1) + ((ch >> 1) & 1) * fb.sy + ((ch >> 2) & 1) * fb.sz;
                           }
                           if (lf > g.min_level)
                           {
@@ -694,9 +724,10 @@ namespace sg
                           const Cell c  = cell_of(g, lc, w, b);
                           long long fo[8];
                           uint8_t keep = 0, coarsen = 2;
+                          const Box3 fb = box_at<DIM>(g, l, 2 * c.x, 2 * c.y, 2 * c.z, 2);
                           for (int ch = 0; ch < (1 << DIM); ++ch)
                           {
-                              fo[ch] = elem_at(g, l, 2 * c.x + (ch & 1), 2 * c.y + ((ch >> 1) & 1), DIM == 3 ? 2 * c.z + ((ch >> 2) & 1) : 0);
+                              fo[ch] = fb.base + (ch & 1) + ((ch >> 1) & 1) * fb.sy + ((ch >> 2) & 1) * fb.sz;
                               const uint8_t t = tag[fo[ch]];
                               keep |= t & 1;
                               coarsen &= t & 2;
@@ -764,7 +795,7 @@ namespace sg
                               const Cell c = cell_of(g, l, w, b);
                               if ((ohc[w] >> b) & 1u)
                               {
-                                  v = project_one(g, uo, l + 1, c.x, c.y, c.z);
+                                  v = project_one<DIM>(g, uo, l + 1, c.x, c.y, c.z);
                               }
                               else if (l >= 1 && test(ocells, g, l - 1, c.x >> 1, c.y >> 1, c.z >> 1))
                               {
