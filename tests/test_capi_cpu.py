@@ -71,3 +71,41 @@ def test_batch_argument_checks():
     assert L.sg_batch_create(1, arr, arr, 0, ctypes.byref(h)) == 1
     assert L.sg_batch_step(None, None, None, None, None, 0, None) == 1
     assert L.sg_batch_synchronize(None) == 1
+
+
+def test_mesh_create_rejects_unsupported_configurations():
+    """sg_mesh_create checks its configuration before touching a device:
+    dimension 2 or 3, 1 <= min_level <= max_level <= 23, stencil radius 1,
+    prediction radius 0 or 1 (include/samurai_gpu.h)."""
+    import ctypes
+
+    import samurai_gb300 as sg
+
+    L = sg.lib()
+    h = ctypes.c_void_p()
+    bad = [
+        (1, 2, 5, 1, 1, 1),   # dimension
+        (4, 2, 5, 1, 1, 1),
+        (2, 0, 5, 1, 1, 1),   # min_level >= 1
+        (2, 6, 5, 1, 1, 1),   # min_level <= max_level
+        (2, 2, 24, 1, 1, 1),  # max_level <= 23
+        (2, 2, 5, 2, 1, 1),   # stencil radius 1 only
+        (2, 2, 5, 1, 2, 1),   # prediction radius 0 or 1
+    ]
+    for args in bad:
+        assert L.sg_mesh_create(*args, ctypes.byref(h)) == 1, args
+        assert L.sg_last_error()
+    assert L.sg_mesh_create(2, 2, 5, 1, 1, 1, None) == 1
+
+
+def test_adjoint_argument_checks():
+    import ctypes
+
+    import samurai_gb300 as sg
+
+    L = sg.lib()
+    h = ctypes.c_void_p()
+    assert L.sg_adjoint_create(None, 16, ctypes.byref(h)) == 1
+    assert L.sg_adjoint_backward(None, None, None, None) == 1
+    assert L.sg_adjoint_replay(None, None, None, None) == 1
+    assert L.sg_adjoint_destroy(None) == 0

@@ -186,3 +186,51 @@ def test_convection_flux_form(sg, dim, minl, maxl, a):
         g.upwind(a, dt, sg.CONVECTION)
         compare_cells(g, o, "convection step %d" % step)
         compare_fields(g, o, "convection step %d" % step, cells_only=True)
+
+
+@pytest.mark.parametrize("dim,minl,maxl,bc", [(2, 2, 7, 0.25), (3, 2, 5, -0.5)])
+def test_nonzero_dirichlet(sg, dim, minl, maxl, bc):
+    """Dirichlet<1> with a non-zero value: outer ghosts 2v - u, their
+    projections and predictions, through adapted steps of both schemes."""
+    g = sg.AdvectionSim(dim, minl, maxl, 1, 1, 1, bc)
+    o = OracleSim(dim, minl, maxl, 1, 1, 1, bc)
+    init_both(g, o, shapes_2d(5, 3, 3) if dim == 2 else ball_3d(4))
+    a = (0.75, -1.0) if dim == 2 else (0.5, -0.75, 1.0)
+    dt = 0.4 / (1 << maxl)
+    for step in range(3):
+        for s in (g, o):
+            s.adapt(1e-3, 1.0)
+            s.update_ghost()
+        compare_fields(g, o, "ghosts, step %d" % step)
+        scheme = 2 if step == 1 else 0
+        o.upwind(a, dt, scheme)
+        g.upwind(a, dt, scheme)
+        compare_meshes(g, o, maxl, "step %d" % step)
+        compare_fields(g, o, "step %d" % step, cells_only=True)
+
+
+def test_single_level_mesh(sg):
+    """min_level == max_level: the adaptation has no pass, the mesh stays
+    uniform, and the ghost update and upwind still match."""
+    g, o = pair(sg, 2, 5, 5)
+    init_both(g, o, readme_square)
+    for _ in range(2):
+        assert g.adapt(1e-4, 2.0) == 0
+        o.adapt(1e-4, 2.0)
+        g.update_ghost()
+        o.update_ghost()
+        g.upwind((1.0, 0.5), 0.5 / 32)
+        o.upwind((1.0, 0.5), 0.5 / 32)
+    compare_meshes(g, o, 5, "single level")
+    compare_fields(g, o, "single level", cells_only=True)
+
+
+def test_zero_field_coarsens_to_min_level(sg):
+    """u = 0: every detail vanishes, the mesh coarsens to min_level."""
+    g, o = pair(sg, 2, 3, 8)
+    init_both(g, o, lambda lv, co: np.zeros(len(lv)))
+    g.adapt(1e-4, 2.0)
+    o.adapt(1e-4, 2.0)
+    lv, _, _ = g.cells()
+    assert np.all(lv == 3)
+    compare_meshes(g, o, 8, "zero field")
