@@ -47,43 +47,20 @@ namespace sg
         // non-empty words of a superset (reference or leaf cells) in
         // ascending order; word_of(w) narrows it to the subset a kernel acts
         // on.  Consecutive cells of a word are consecutive doubles, so every
-        // field access of a warp is one 256-byte segment.  The next word's
-        // index and subset word are loaded before the current word's cells
-        // run, so those two dependent loads overlap the cell work.
+        // field access of a warp is one 256-byte segment.
         template <class WordF, class CellF>
         __device__ __forceinline__ void warp_list(const int* list, long long begin, long long end, long long warp0, long long nwarps, WordF word_of,
                                                   CellF cell)
         {
             const int lane = threadIdx.x & 31;
-            long long i    = begin + warp0;
-            if (i >= end)
+            for (long long i = begin + warp0; i < end; i += nwarps)
             {
-                return;
-            }
-            long long w = __ldg(list + i);
-            uint32_t v  = word_of(w);
-            for (;;)
-            {
-                const long long inext = i + nwarps;
-                const bool more       = inext < end;
-                long long wn          = 0;
-                uint32_t vn           = 0;
-                if (more)
-                {
-                    wn = __ldg(list + inext);
-                    vn = word_of(wn);
-                }
+                const long long w = __ldg(list + i);
+                const uint32_t v  = word_of(w);
                 if ((v >> lane) & 1u)
                 {
                     cell(w, lane);
                 }
-                if (!more)
-                {
-                    break;
-                }
-                i = inext;
-                w = wn;
-                v = vn;
             }
         }
 
