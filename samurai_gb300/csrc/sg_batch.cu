@@ -27,6 +27,7 @@ namespace sg
 {
     void set_last_error(const char* msg, const char* detail);
     int ensure_spare(Ctx& c, DeviceField& f);
+    void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words);
 }
 
 struct sg_batch_s
@@ -311,6 +312,7 @@ extern "C"
             {
                 return bfail(SG_ERR_CUDA, c.err.c_str());
             }
+            sg::set_fusion(c, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS);
         }
         auto* b = new (std::nothrow) sg_batch_s();
         if (!b)

@@ -279,6 +279,21 @@ namespace sg
         fail(0, msg, detail);
     }
 
+    // one-block chain limits of a mesh; the captured launch sequences are
+    // dropped, since they were recorded with the previous limits
+    void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words)
+    {
+        cudaStreamSynchronize(c.stream);
+        c.fuse_top       = fuse_top_of(c.g, mesh_words);
+        c.fuse_top_field = fuse_top_of(c.g, field_words);
+        c.fuse_top_max   = fuse_top_of(c.g, max_words);
+        for (auto& ge : c.graphs)
+        {
+            cudaGraphExecDestroy(ge.exec);
+        }
+        c.graphs.clear();
+    }
+
     // the spare buffer adaptation swaps into, allocated on first use
     int ensure_spare(Ctx& c, DeviceField& f)
     {
