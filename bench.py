@@ -43,11 +43,11 @@ UPWIND_DRAM_BYTES_PER_CELL = 8346368.0 / 536428.0
 
 def workload_config(extra=None):
     if CFG["dim"] == 3:
-        desc = ("3D MR linear advection, min_level 3, max_level 9 (512^3), a=(1,1,1), eps 1e-3, regularity 1, "
-                "ball + 8 Gaussians (seed %d), Dirichlet 0, dt=0.3*dx_min, upwind" % CFG["seed"])
+        desc = ("3D MR linear advection, min_level 3, max_level %d, a=(1,1,1), eps 1e-3, regularity 1, "
+                "ball + 8 Gaussians (seed %d), Dirichlet 0, dt=0.3*dx_min, upwind" % (CFG["max_level"], CFG["seed"]))
     else:
-        desc = ("2D MR linear advection, min_level 4, max_level 12 (4096^2), a=(1,0.5), eps 1e-4, regularity 2, "
-                "16 squares + 16 Gaussians (seed %d), Dirichlet 0, dt=0.5*dx_min, upwind" % CFG["seed"])
+        desc = ("2D MR linear advection, min_level 4, max_level %d, a=(1,0.5), eps 1e-4, regularity 2, "
+                "16 squares + 16 Gaussians (seed %d), Dirichlet 0, dt=0.5*dx_min, upwind" % (CFG["max_level"], CFG["seed"]))
     c = {
         "workload": desc,
         "min_level": CFG["min_level"],
@@ -519,13 +519,14 @@ def run_batch(args):
             s.update_ghost()
             s.upwind(p["a"], p["dt"])
 
+    # the serial calls with the instances' own launch shapes (the batch sets its own)
+    batch.close()
     serial_steps = max(1, min(args.steps, 10))
     s_s, s_updates = timed(serial_step, serial_steps)
     s_ms, s_updates = reduce_over_ranks(1e3 * s_s, s_updates, world, device="cuda")
     s_s = s_ms / 1e3
     cells = [s.nb_cells() for s in sims]
     if rank != 0:
-        batch.close()
         return
     cpu = None if args.no_cpu_baseline else batch_cpu_baseline(probs, sims)
     line = {
@@ -664,6 +665,7 @@ def main():
     p.add_argument("--workload", default="advection2d", choices=["advection2d", "advection3d", "batch", "adjoint"],
                    help="advection2d: the max_level-12 2D problem (default); batch: independent problems through sg_batch_step; "
                         "adjoint: the discrete adjoint of a max_level-10 loop")
+    p.add_argument("--max-level", type=int, default=None, help="a smaller max_level for the advection workloads (profiling captures)")
     p.add_argument("--adjoint-steps", type=int, default=256)
     p.add_argument("--fd-directions", type=int, default=64)
     p.add_argument("--instances", type=int, default=256)
@@ -675,6 +677,8 @@ def main():
     if args.workload == "advection3d":
         CFG.clear()
         CFG.update(CFG_3D)
+    if args.max_level is not None:
+        CFG["max_level"] = args.max_level
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":

@@ -28,12 +28,14 @@ namespace sg
     void set_last_error(const char* msg, const char* detail);
     int ensure_spare(Ctx& c, DeviceField& f);
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words);
+    void set_fusion_tops(Ctx& c, int mesh_top, int field_top, int max_top);
 }
 
 struct sg_batch_s
 {
     std::vector<sg_field_t> u, unp1;
     int n_threads = 1;
+    std::vector<int> saved_tops; // the instances' own one-block chain limits, restored on destroy
 
     // worker pool: thread t runs job(t) for every new generation
     std::vector<std::thread> workers;
@@ -312,7 +314,6 @@ extern "C"
             {
                 return bfail(SG_ERR_CUDA, c.err.c_str());
             }
-            sg::set_fusion(c, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS);
         }
         auto* b = new (std::nothrow) sg_batch_s();
         if (!b)
@@ -321,6 +322,12 @@ extern "C"
         }
         b->u.assign(u, u + n);
         b->unp1.assign(unp1, unp1 + n);
+        for (int k = 0; k < n; ++k)
+        {
+            sg::Ctx& c = u[k]->mesh->ctx;
+            b->saved_tops.insert(b->saved_tops.end(), {c.fuse_top, c.fuse_top_field, c.fuse_top_max});
+            sg::set_fusion(c, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS);
+        }
         b->n_threads = std::min(n_threads, n);
         if (b->n_threads > 1)
         {
@@ -335,6 +342,13 @@ extern "C"
 
     int sg_batch_destroy(sg_batch_t b)
     {
+        if (b)
+        {
+            for (size_t k = 0; k < b->u.size(); ++k)
+            {
+                sg::set_fusion_tops(b->u[k]->mesh->ctx, b->saved_tops[3 * k], b->saved_tops[3 * k + 1], b->saved_tops[3 * k + 2]);
+            }
+        }
         delete b;
         return SG_OK;
     }

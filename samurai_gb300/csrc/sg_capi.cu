@@ -281,17 +281,22 @@ namespace sg
 
     // one-block chain limits of a mesh; the captured launch sequences are
     // dropped, since they were recorded with the previous limits
-    void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words)
+    void set_fusion_tops(Ctx& c, int mesh_top, int field_top, int max_top)
     {
         cudaStreamSynchronize(c.stream);
-        c.fuse_top       = fuse_top_of(c.g, mesh_words);
-        c.fuse_top_field = fuse_top_of(c.g, field_words);
-        c.fuse_top_max   = fuse_top_of(c.g, max_words);
+        c.fuse_top       = mesh_top;
+        c.fuse_top_field = field_top;
+        c.fuse_top_max   = max_top;
         for (auto& ge : c.graphs)
         {
             cudaGraphExecDestroy(ge.exec);
         }
         c.graphs.clear();
+    }
+
+    void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words)
+    {
+        set_fusion_tops(c, fuse_top_of(c.g, mesh_words), fuse_top_of(c.g, field_words), fuse_top_of(c.g, max_words));
     }
 
     // the spare buffer adaptation swaps into, allocated on first use
