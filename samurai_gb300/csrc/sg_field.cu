@@ -95,6 +95,43 @@ namespace sg
             return elem(p);
         }
 
+        // x * 8^-k, exactly, without the FP64 pipe when it can: for a normal x
+        // whose product stays normal the product is x with its exponent
+        // lowered by 3k (what the multiplication would round to, since it is
+        // exact); zeros keep their bits; other values take the multiplication.
+        __device__ __forceinline__ double scale8(double x, int k)
+        {
+            const long long b = __double_as_longlong(x);
+            const int e       = static_cast<int>((b >> 52) & 0x7FF);
+            if (e > 3 * k && e < 0x7FF)
+            {
+                return __longlong_as_double(b - (static_cast<long long>(3 * k) << 52));
+            }
+            if ((static_cast<unsigned long long>(b) << 1) == 0)
+            {
+                return x;
+            }
+            return x * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
+        }
+
+        // -x when neg, by the sign bit (exact, no FP64 operation)
+        __device__ __forceinline__ double negate_if(bool neg, double x)
+        {
+            return __longlong_as_double(__double_as_longlong(x) ^ (static_cast<long long>(neg) << 63));
+        }
+
+        template <int CAP>
+        __device__ __forceinline__ LinForm<CAP> scale8(const LinForm<CAP>& x, int k)
+        {
+            return x * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
+        }
+
+        template <int CAP>
+        __device__ __forceinline__ LinForm<CAP> negate_if(bool neg, const LinForm<CAP>& x)
+        {
+            return neg ? -x : x;
+        }
+
         // A box of cells [x0, x0+n) x [y0, y0+n) x [z0, z0+n) at level l as a base
         // element and strides: both corners are checked against the stored
         // box (a violation is recorded and every access goes to element 0)
@@ -146,8 +183,9 @@ namespace sg
                         const bool neg   = ((sx == 0 && qx) || (sx == 2 && !qx)) ^ ((sy == 0 && qy) || (sy == 2 && !qy))
                                          ^ (DIM == 3 && ((sz == 0 && qz) || (sz == 2 && !qz)));
                         const typename A::V v = u.get(base + sx);
-                        const typename A::V m = k == 0 ? v : v * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
-                        acc                   = neg ? acc - m : acc + m;
+                        // acc + u * coeff == acc + (+-m): one FP64 addition per tap
+                        const typename A::V m = k == 0 ? v : scale8(v, k);
+                        acc                   = acc + negate_if(neg, m);
                     }
                 }
             }
@@ -630,7 +668,7 @@ namespace sg
                                   {
                                       const double src = u[base + sx];
                                       const int k      = (sx != 1) + (sy != 1) + (DIM == 3 && sz != 1);
-                                      const double m   = k == 0 ? src : src * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
+                                      const double m   = k == 0 ? src : scale8(src, k);
                                       for (int ch = 0; ch < (1 << DIM); ++ch)
                                       {
                                           // interp1(parity, t) < 0: t == 0 on odd children, t == 2 on even ones
