@@ -95,23 +95,35 @@ namespace sg
             return elem(p);
         }
 
-        // x * 8^-k, exactly, without the FP64 pipe when it can: for a normal x
-        // whose product stays normal the product is x with its exponent
-        // lowered by 3k (what the multiplication would round to, since it is
+        // x * 2^-s (0 < s < 64), exactly, without the FP64 pipe when it can: for
+        // a normal x whose product stays normal the product is x with its
+        // exponent lowered by s (what the multiplication rounds to, since it is
         // exact); zeros keep their bits; other values take the multiplication.
-        __device__ __forceinline__ double scale8(double x, int k)
+        __device__ __forceinline__ double scale_down(double x, int s)
         {
             const long long b = __double_as_longlong(x);
             const int e       = static_cast<int>((b >> 52) & 0x7FF);
-            if (e > 3 * k && e < 0x7FF)
+            if (e > s && e < 0x7FF)
             {
-                return __longlong_as_double(b - (static_cast<long long>(3 * k) << 52));
+                return __longlong_as_double(b - (static_cast<long long>(s) << 52));
             }
             if ((static_cast<unsigned long long>(b) << 1) == 0)
             {
                 return x;
             }
-            return x * (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125));
+            return x * __longlong_as_double(static_cast<long long>(1023 - s) << 52);
+        }
+
+        // x * 8^-k: the prediction coefficients' magnitudes
+        __device__ __forceinline__ double scale8(double x, int k)
+        {
+            return scale_down(x, 3 * k);
+        }
+
+        template <int CAP>
+        __device__ __forceinline__ LinForm<CAP> scale_down(const LinForm<CAP>& x, int s)
+        {
+            return x * (1.0 / static_cast<double>(1LL << s));
         }
 
         // -x when neg, by the sign bit (exact, no FP64 operation)
@@ -208,8 +220,8 @@ namespace sg
                     sum               = sum + (u.get(e) + u.get(e + 1));
                 }
             }
-            const double inv = (DIM == 3) ? 0.125 : 0.25;
-            return sum * inv;
+            // sum * (1 / 2^dim)
+            return scale_down(sum, DIM);
         }
 
         // ----------------------------------------------------------- tags
@@ -859,6 +871,24 @@ namespace sg
             return __longlong_as_double(static_cast<long long>(1023 + l) << 52);
         }
 
+        // x * 2^l (l >= 0), exactly, by raising the exponent when x and the
+        // product are normal numbers; zeros keep their bits; otherwise the
+        // multiplication
+        __device__ __forceinline__ double scale2(double x, int l)
+        {
+            const long long b = __double_as_longlong(x);
+            const int e       = static_cast<int>((b >> 52) & 0x7FF);
+            if (e > 0 && e + l < 0x7FF)
+            {
+                return __longlong_as_double(b + (static_cast<long long>(l) << 52));
+            }
+            if ((static_cast<unsigned long long>(b) << 1) == 0)
+            {
+                return x;
+            }
+            return x * pow2(l);
+        }
+
         struct UpwindArgs
         {
             double ha[3]; // .5 * a_d, as the reference's flux forms it
@@ -946,7 +976,7 @@ namespace sg
                     s                = s + -ff;
                     s                = s + bf;
                 }
-                const double up = s * pow2(l);
+                const double up = scale2(s, l); // s / dx with dx = 2^-l
                 unp1[e]         = uc - p.dt * up;
             }
         }
