@@ -129,6 +129,7 @@ namespace sg
         int fuse_top_field  = -1;      // the same for the FP64 field chains
         int fuse_top_max    = -1;      // the same for the tag-finalisation chain
         const int* guard    = nullptr; // device flag: word launches do nothing while it is 0
+        long long max_blocks = 152LL * 8; // grid limit of the one-warp-per-word launches (x4 for one thread per word)
         struct GraphEntry
         {
             unsigned long long key[4];

@@ -1187,19 +1187,22 @@ namespace sg
 
     namespace
     {
-        int blocks_words(const Geom& g, int l0, int l1)
+        // one warp per word of levels l0..l1, at most the mesh's block limit
+        int blocks_words(const Ctx& c, int l0, int l1)
         {
             if (l1 < l0)
             {
                 return 1;
             }
-            return blocks_for_items(g.lv[l1].woff + g.lv[l1].nwords - g.lv[l0].woff);
+            const Geom& g      = c.g;
+            const long long nb = (g.lv[l1].woff + g.lv[l1].nwords - g.lv[l0].woff + 7) / 8;
+            return static_cast<int>(nb < 1 ? 1 : (nb > c.max_blocks ? c.max_blocks : nb));
         }
     } // namespace
 
     cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
     {
-        k_gather<<<blocks_words(c.g, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
+        k_gather<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
         ++c.n_launches;
         return cudaGetLastError();
     }
@@ -1232,14 +1235,14 @@ namespace sg
 
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense)
     {
-        k_scatter<<<blocks_words(c.g, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, compact, dense);
+        k_scatter<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, compact, dense);
         ++c.n_launches;
         return check(c, "scatter");
     }
 
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value)
     {
-        k_fill<<<blocks_words(c.g, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, dense, value);
+        k_fill<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, dense, value);
         ++c.n_launches;
         return check(c, "fill");
     }
@@ -1357,7 +1360,7 @@ namespace sg
                                      : 0;
                 a.nb_face         = static_cast<int>((a.nfaces + BLOCK - 1) / BLOCK);
                 a.do_proj         = l > lmin;
-                const int nb_proj = a.do_proj ? blocks_words(g, l - 1, l - 1) : 0;
+                const int nb_proj = a.do_proj ? blocks_words(c, l - 1, l - 1) : 0;
                 const int grid    = a.nb_corner + a.nb_face + nb_proj;
                 if (grid > 0)
                 {
@@ -1429,12 +1432,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_predict<2><<<blocks_words(g, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<2><<<blocks_words(c, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 else
                 {
-                    k_predict<3><<<blocks_words(g, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<3><<<blocks_words(c, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 ++c.n_launches;
@@ -1456,12 +1459,12 @@ namespace sg
             const Geom& g = c.g;
             if (g.dim == 2)
             {
-                k_update_fields<2><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                k_update_fields<2><<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
                                                                                             nm.cells, m.ref, m.cells, m.hc, uo, un);
             }
             else
             {
-                k_update_fields<3><<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                k_update_fields<3><<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
                                                                                             nm.cells, m.ref, m.cells, m.hc, uo, un);
             }
             ++c.n_launches;
@@ -1481,7 +1484,7 @@ namespace sg
             cudaMemcpyAsync(c.d_ite, c.h_ite, sizeof(int), cudaMemcpyHostToDevice, c.stream);
             cudaMemcpyAsync(c.d_eps, c.h_eps, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
             cudaMemsetAsync(c.d_flags, 0, F_COUNT * sizeof(int), c.stream);
-            k_tag_init<<<blocks_words(g, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
+            k_tag_init<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
             ++c.n_launches;
             if ((st = check(c, "tag_init")) || (st = seq_ghost(c, m, u, has_bc, bcv)))
             {
@@ -1495,12 +1498,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_detail<2><<<blocks_words(g, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                    k_detail<2><<<blocks_words(c, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
                                                                                     m.ref, m.hc, m.hc2, u, c.detail);
                 }
                 else
                 {
-                    k_detail<3><<<blocks_words(g, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                    k_detail<3><<<blocks_words(c, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
                                                                                     m.ref, m.hc, m.hc2, u, c.detail);
                 }
                 ++c.n_launches;
@@ -1512,12 +1515,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_criteria<2><<<blocks_words(g, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                    k_criteria<2><<<blocks_words(c, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
                                                                                                 m.ref, m.hc, c.detail, c.tag);
                 }
                 else
                 {
-                    k_criteria<3><<<blocks_words(g, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                    k_criteria<3><<<blocks_words(c, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
                                                                                                 m.ref, m.hc, c.detail, c.tag);
                 }
                 ++c.n_launches;
@@ -1531,11 +1534,11 @@ namespace sg
                 {
                     if (g.dim == 2)
                     {
-                        k_maximum<2><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<2><<<blocks_words(c, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     else
                     {
-                        k_maximum<3><<<blocks_words(g, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<3><<<blocks_words(c, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     ++c.n_launches;
                 }
@@ -1788,7 +1791,7 @@ namespace sg
         }
         p.dt     = dt;
         p.scheme = scheme;
-        const int nb = blocks_words(g, 0, g.nlev - 1);
+        const int nb = blocks_words(c, 0, g.nlev - 1);
         if (scheme == 2)
         {
             double* av = c.d_eps + EPS_VELOCITY;

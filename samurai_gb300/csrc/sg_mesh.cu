@@ -183,7 +183,7 @@ namespace sg
                 return SG_OK;
             }
             const long long n = c.g.lv[l1].woff + c.g.lv[l1].nwords - c.g.lv[l0].woff;
-            k_words<<<grid_for(n), 256, 0, c.stream>>>(c.d_geom, l0, l1, f, c.guard);
+            k_words<<<grid_for(n, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.d_geom, l0, l1, f, c.guard);
             ++c.n_launches;
             return check(c, what);
         }
@@ -630,7 +630,7 @@ namespace sg
     int new_cells_from_tags(Ctx& c, const DeviceMesh& m, uint32_t* nc)
     {
         const Geom g = c.g;
-        k_tag_flags<<<grid_for(g.total_words), 256, 0, c.stream>>>(c.d_geom, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
+        k_tag_flags<<<grid_for(g.total_words, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.d_geom, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
         ++c.n_launches;
         int st = check(c, "tag_flags");
         if (st)
