@@ -4,6 +4,7 @@
 // first-order upwind step.  Built with --fmad=false: every FP64 operation is
 // rounded on its own, in the reference's association order, so that the
 // detail thresholds take the same decisions as the CPU implementation.
+#include <algorithm>
 #include <cstring>
 #include <functional>
 #include <type_traits>
@@ -812,14 +813,14 @@ namespace sg
             maximum_level<DIM>(*gp, l, wl, lo, ref, hc, tag, warp_id(), warp_count());
         }
 
-        // the small levels of the tag finalisation in one block, l_hi down to 1
+        // the small levels of the tag finalisation in one block, l_hi down to l_lo
         template <int DIM>
-        __global__ void __launch_bounds__(1024, 1) k_maximum_small(const Geom* __restrict__ gp, int l_hi, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
-                                        uint8_t* tag)
+        __global__ void __launch_bounds__(1024, 1) k_maximum_small(const Geom* __restrict__ gp, int l_hi, int l_lo, const int* wl, const long long* lo,
+                                                                   const uint32_t* ref, const uint32_t* hc, uint8_t* tag)
         {
             const long long warp0 = threadIdx.x >> 5;
             const long long nw    = blockDim.x >> 5;
-            for (int l = l_hi; l >= 1; --l)
+            for (int l = l_hi; l >= l_lo; --l)
             {
                 maximum_level<DIM>(*gp, l, wl, lo, ref, hc, tag, warp0, nw);
                 __syncthreads();
@@ -1529,8 +1530,11 @@ namespace sg
 
             timer_start(c, T_FINALIZE);
             {
-                int l = maxl;
-                for (; l > 0 && l - 1 > c.fuse_top_max; --l)
+                // children at levels maxl .. min_level: below min_level no parent
+                // has a leaf child, so the operator has nothing to do there
+                const int lstop = std::max(1, c.cfg.min_level);
+                int l           = maxl;
+                for (; l >= lstop && l - 1 > c.fuse_top_max; --l)
                 {
                     if (g.dim == 2)
                     {
@@ -1542,15 +1546,15 @@ namespace sg
                     }
                     ++c.n_launches;
                 }
-                if (l > 0)
+                if (l >= lstop)
                 {
                     if (g.dim == 2)
                     {
-                        k_maximum_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     else
                     {
-                        k_maximum_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     ++c.n_launches;
                 }

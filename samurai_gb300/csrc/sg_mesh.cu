@@ -1,3 +1,4 @@
+#include <algorithm>
 // Mesh construction on the device: the MRMesh ids from a leaf-cell bitmap,
 // and the integer kernels of the adaptation (tags -> new cells, graduation).
 //
@@ -536,10 +537,12 @@ namespace sg
         }
 
         // children of the projection cells, bottom-up:
-        // reference[l+1] |= (reference[l] & union[l]) refined
-        if (maxl >= 1)
+        // reference[l+1] |= (reference[l] & union[l]) refined; the reference
+        // starts at min_level - 2, so the first level with a source is above it
+        const int ref_lo = std::max(1, std::max(c.cfg.min_level - 2, 0) + 1);
+        if (maxl >= ref_lo)
         {
-            st = launch_chain(c, 1, maxl,
+            st = launch_chain(c, ref_lo, maxl,
                               [=] __device__(const Geom& g, int lf, long long w, long long row, int k)
                               {
                                   const LevelGeom& F = g.lv[lf];
@@ -751,12 +754,14 @@ namespace sg
         {
             return st;
         }
-        // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. 0; d and rr are
-        // written on every word of those levels and read as 0 above them
+        // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. min_level (below
+        // min_level there is no cell to refine); d and rr are written on every
+        // word of those levels and read as 0 outside them
         const int dtop = maxl - 2;
-        if (maxl >= 2)
+        const int dlo  = c.cfg.min_level;
+        if (dtop >= dlo)
         {
-            st = launch_chain(c, maxl - 2, 0,
+            st = launch_chain(c, dtop, dlo,
                               [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
                               {
                                   const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | (ll + 1 <= dtop ? coarsen_word(g, d, ll, row, wi) : 0u);
@@ -777,9 +782,9 @@ namespace sg
         return launch_words(c, 0, top,
                             [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                             {
-                                const uint32_t r = l <= dtop ? rr[w] : 0u;
+                                const uint32_t r = (l >= dlo && l <= dtop) ? rr[w] : 0u;
                                 uint32_t v       = nc[w] & ~r;
-                                if (l >= 1 && l - 1 <= dtop)
+                                if (l - 1 >= dlo && l - 1 <= dtop)
                                 {
                                     v |= refine_word(g, rr, l, row, wi);
                                 }
