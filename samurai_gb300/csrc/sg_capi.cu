@@ -421,9 +421,15 @@ extern "C"
             return fail(SG_ERR_CUDA, "sg_mesh_create: ", msg.c_str());
         }
         cudaMemcpyAsync(c.d_geom, &c.g, sizeof(sg::Geom), cudaMemcpyHostToDevice, c.stream);
+        // every bitmap starts empty: the mesh construction writes only the
+        // levels where a set can be non-empty and relies on zeros elsewhere
         for (int k = 0; k < 2; ++k)
         {
-            cudaMemsetAsync(c.mesh[k].cells, 0, nw * 4, c.stream);
+            sg::DeviceMesh& mk = c.mesh[k];
+            for (uint32_t* bm : {mk.cells, mk.cag, mk.proj, mk.uni, mk.ref, mk.hc, mk.hc2})
+            {
+                cudaMemsetAsync(bm, 0, nw * 4, c.stream);
+            }
         }
         cudaMemsetAsync(c.detail, 0, static_cast<size_t>(c.capacity) * sizeof(double), c.stream);
         cudaMemsetAsync(c.tag, 0, static_cast<size_t>(c.capacity), c.stream);

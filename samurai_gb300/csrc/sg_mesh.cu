@@ -405,7 +405,6 @@ namespace sg
     {
         ScopedTimer timer(c, T_CONSTRUCTION);
         const Geom g       = c.g;
-        const int top      = g.nlev - 1;
         const int maxl     = c.cfg.max_level;
         const int r        = c.cfg.max_stencil_radius;
         const int p        = c.cfg.prediction_radius;
@@ -421,18 +420,23 @@ namespace sg
         const size_t bytes = static_cast<size_t>(g.total_words) * 4;
         int st;
 
-        // cells with a leaf child / grandchild
-        st = launch_words(c, 0, top,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                          { hc[w] = (l + 1 < g.nlev) ? coarsen_word(g, cells, l, row, wi) : 0u; },
+        // Leaf cells lie in levels min_level .. max_level, so each set below
+        // can be non-empty only on a known range of levels; it is computed on
+        // that range, and its other levels keep the zeros they were created
+        // with (no pass ever writes them).
+        const int minl = c.cfg.min_level;
+        const int lmin = minl >= 2 ? minl - 2 : 0; // lowest level of the reference
+
+        // cells with a leaf child (levels min-1 .. max-1) / grandchild (min-2 .. max-2)
+        st = launch_words(c, std::max(minl - 1, 0), maxl - 1,
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { hc[w] = coarsen_word(g, cells, l, row, wi); },
                           "hc");
         if (st)
         {
             return st;
         }
-        st = launch_words(c, 0, top,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                          { hc2[w] = (l + 1 < g.nlev) ? coarsen_word(g, hc, l, row, wi) : 0u; },
+        st = launch_words(c, std::max(minl - 2, 0), maxl - 2,
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { hc2[w] = coarsen_word(g, hc, l, row, wi); },
                           "hc2");
         if (st)
         {
@@ -456,19 +460,19 @@ namespace sg
         // cells_and_ghosts: box expansion of the cells by max_stencil_radius
         if (g.dim == 2)
         {
-            st = launch_words(c, 0, top,
+            st = launch_words(c, minl, maxl,
                               [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = dilate_xy_word(g, cells, l, row, wi, r); },
                               "cag");
         }
         else
         {
             uint32_t* t0 = c.t0;
-            st           = launch_words(c, 0, top,
+            st           = launch_words(c, minl, maxl,
                                         [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { t0[w] = dilate_xy_word(g, cells, l, row, wi, r); },
                                         "cag_xy");
             if (!st)
             {
-                st = launch_words(c, 0, top,
+                st = launch_words(c, minl, maxl,
                                   [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = dilate_z_word(g, t0, l, row, wi, r); },
                                   "cag_z");
             }
@@ -487,21 +491,28 @@ namespace sg
 
         // prediction ghosts: cag[l+1].on(l) expanded by p within the expanded
         // domain, and cells[l+2].on(l) expanded by p
-        st = launch_words(c, 0, top,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                          { t1[w] = (l + 1 < g.nlev) ? coarsen_word(g, cag, l, row, wi) : 0u; },
+        // t1 = cag[l+1].on(l) on levels min-1 .. max-1; the other levels of the
+        // scratch bitmap are not read below
+        const int t1lo = std::max(minl - 1, 0), t1hi = maxl - 1;
+        st = launch_words(c, t1lo, t1hi,
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { t1[w] = coarsen_word(g, cag, l, row, wi); },
                           "cag_on");
         if (st)
         {
             return st;
         }
+        // the reference starts at level min-2: cag (min .. max), t1 (min-1 ..
+        // max-1) and hc2 (min-2 .. max-2)
         if (g.dim == 2)
         {
-            st = launch_words(c, 0, top,
+            st = launch_words(c, lmin, maxl,
                               [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                               {
                                   uint32_t v = cag[w];
-                                  v |= dilate_xy_word(g, t1, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
+                                  if (l >= t1lo && l <= t1hi)
+                                  {
+                                      v |= dilate_xy_word(g, t1, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
+                                  }
                                   v |= dilate_xy_word(g, hc2, l, row, wi, p);
                                   ref[w] = v;
                               },
@@ -511,16 +522,16 @@ namespace sg
         {
             uint32_t* t2 = c.t2;
             uint32_t* t3 = c.t3;
-            st           = launch_words(c, 0, top,
+            st           = launch_words(c, lmin, maxl,
                                         [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                                         {
-                                            t2[w] = dilate_xy_word(g, t1, l, row, wi, p);
+                                            t2[w] = (l >= t1lo && l <= t1hi) ? dilate_xy_word(g, t1, l, row, wi, p) : 0u;
                                             t3[w] = dilate_xy_word(g, hc2, l, row, wi, p);
                                         },
                                         "ref0_xy");
             if (!st)
             {
-                st = launch_words(c, 0, top,
+                st = launch_words(c, lmin, maxl,
                                   [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                                   {
                                       uint32_t v = cag[w];
@@ -579,7 +590,7 @@ namespace sg
                 return st;
             }
         }
-        st = launch_words(c, 0, top, [=] __device__(const Geom&, int, long long w, long long, int) { proj[w] = ref[w] & uni[w]; }, "proj");
+        st = launch_words(c, lmin, maxl, [=] __device__(const Geom&, int, long long w, long long, int) { proj[w] = ref[w] & uni[w]; }, "proj");
         if (st)
         {
             return st;
@@ -714,31 +725,51 @@ namespace sg
             }
         } scope(c, guard);
         const Geom g   = c.g;
-        const int top  = g.nlev - 1;
         const int maxl = c.cfg.max_level;
-        const int gw2  = 2 * c.cfg.graduation_width;
-        uint32_t* e    = c.t0;
+        const int gw   = c.cfg.graduation_width;
+        uint32_t* hcn  = c.t0;
         uint32_t* ec1  = c.t1;
         uint32_t* d    = c.t2;
         uint32_t* rr   = c.t3;
         int* flag      = c.d_flags + slot;
-        int st;
+        // A cell of level l must be refined when a cell of level l+2 or finer
+        // lies within 2 gw cells of it at that finer level: d[l] collects, on
+        // level l, the finer cells dilated by 2 gw (graduation.hpp:628-723).
+        // Levels min_level .. max_level-2 can hold such cells.
+        const int dtop = maxl - 2;
+        const int dlo  = c.cfg.min_level;
+        if (dtop < dlo)
+        {
+            return SG_OK;
+        }
+        // ec1[l] = dilate_2gw(cells[l+1]).on(l), computed as
+        // dilate_gw(cells[l+1].on(l)): per axis the parents of [a - 2gw, b + 2gw]
+        // are [a/2 - gw, b/2 + gw], so both give the same set, and the
+        // dilation then runs on the coarser level
+        const int elo = dlo + 1, ehi = dtop + 1;
+        int st        = launch_words(c, elo, ehi,
+                                     [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { hcn[w] = coarsen_word(g, nc, l, row, wi); },
+                                     "grad_coarsen");
+        if (st)
+        {
+            return st;
+        }
         if (g.dim == 2)
         {
-            st = launch_words(c, 0, top,
-                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = dilate_xy_word(g, nc, l, row, wi, gw2); },
+            st = launch_words(c, elo, ehi,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { ec1[w] = dilate_xy_word(g, hcn, l, row, wi, gw); },
                               "grad_expand");
         }
         else
         {
-            // xy into ec1 (free until the coarsening below), then z
-            st = launch_words(c, 0, top,
-                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { ec1[w] = dilate_xy_word(g, nc, l, row, wi, gw2); },
+            // xy into d (written by the chain only after this), then z
+            st = launch_words(c, elo, ehi,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { d[w] = dilate_xy_word(g, hcn, l, row, wi, gw); },
                               "grad_expand_xy");
             if (!st)
             {
-                st = launch_words(c, 0, top,
-                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { e[w] = dilate_z_word(g, ec1, l, row, wi, gw2); },
+                st = launch_words(c, elo, ehi,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { ec1[w] = dilate_z_word(g, d, l, row, wi, gw); },
                                   "grad_expand_z");
             }
         }
@@ -746,45 +777,32 @@ namespace sg
         {
             return st;
         }
-        st = launch_words(c, 0, top,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                          { ec1[w] = (l + 1 < g.nlev) ? coarsen_word(g, e, l, row, wi) : 0u; },
-                          "grad_coarsen");
+        // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. min_level; d and rr
+        // are written on every word of those levels and read as 0 outside them
+        st = launch_chain(c, dtop, dlo,
+                          [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
+                          {
+                              const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | (ll + 1 <= dtop ? coarsen_word(g, d, ll, row, wi) : 0u);
+                              d[w]              = dv;
+                              const uint32_t rv = nc[w] & dv;
+                              rr[w]             = rv;
+                              if (rv)
+                              {
+                                  atomicOr(flag, 1);
+                              }
+                          },
+                          "grad_down");
         if (st)
         {
             return st;
         }
-        // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. min_level (below
-        // min_level there is no cell to refine); d and rr are written on every
-        // word of those levels and read as 0 outside them
-        const int dtop = maxl - 2;
-        const int dlo  = c.cfg.min_level;
-        if (dtop >= dlo)
-        {
-            st = launch_chain(c, dtop, dlo,
-                              [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
-                              {
-                                  const uint32_t dv = coarsen_word(g, ec1, ll, row, wi) | (ll + 1 <= dtop ? coarsen_word(g, d, ll, row, wi) : 0u);
-                                  d[w]              = dv;
-                                  const uint32_t rv = nc[w] & dv;
-                                  rr[w]             = rv;
-                                  if (rv)
-                                  {
-                                      atomicOr(flag, 1);
-                                  }
-                              },
-                              "grad_down");
-            if (st)
-            {
-                return st;
-            }
-        }
-        return launch_words(c, 0, top,
+        // refine the flagged cells: levels min_level .. max_level-1 change
+        return launch_words(c, dlo, dtop + 1,
                             [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                             {
-                                const uint32_t r = (l >= dlo && l <= dtop) ? rr[w] : 0u;
+                                const uint32_t r = l <= dtop ? rr[w] : 0u;
                                 uint32_t v       = nc[w] & ~r;
-                                if (l - 1 >= dlo && l - 1 <= dtop)
+                                if (l - 1 >= dlo)
                                 {
                                     v |= refine_word(g, rr, l, row, wi);
                                 }
