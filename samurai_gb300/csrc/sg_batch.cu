@@ -34,6 +34,7 @@ namespace sg
 struct sg_batch_s
 {
     std::vector<sg_field_t> u, unp1;
+    std::vector<size_t> order; // instances by decreasing size: the largest are launched first
     int n_threads = 1;
     std::vector<int> saved_tops; // the instances' own one-block chain limits, restored on destroy
 
@@ -117,13 +118,13 @@ struct sg_batch_s
         return st;
     }
 
-    // instances of thread t
+    // instances of thread t, the largest first
     template <class F>
     void for_mine(int t, F&& f)
     {
-        for (size_t k = static_cast<size_t>(t); k < u.size(); k += static_cast<size_t>(n_threads))
+        for (size_t j = static_cast<size_t>(t); j < order.size(); j += static_cast<size_t>(n_threads))
         {
-            f(k);
+            f(order[j]);
         }
     }
 
@@ -322,6 +323,21 @@ extern "C"
         }
         b->u.assign(u, u + n);
         b->unp1.assign(unp1, unp1 + n);
+        // the largest problems have the longest chains of launches: they start
+        // first within each phase, and every host thread gets a share of them
+        std::vector<long long> size(static_cast<size_t>(n));
+        for (int k = 0; k < n; ++k)
+        {
+            sg::Ctx& c = u[k]->mesh->ctx;
+            if (sg::host_counts(c, c.m()))
+            {
+                delete b;
+                return bfail(SG_ERR_CUDA, c.err.c_str());
+            }
+            size[static_cast<size_t>(k)] = c.m().nb_ref;
+            b->order.push_back(static_cast<size_t>(k));
+        }
+        std::stable_sort(b->order.begin(), b->order.end(), [&](size_t x, size_t y) { return size[x] > size[y]; });
         for (int k = 0; k < n; ++k)
         {
             sg::Ctx& c = u[k]->mesh->ctx;
