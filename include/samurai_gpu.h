@@ -136,9 +136,7 @@ int sg_field_download_noalloc(sg_field_t field, double* values, long long n);
  * levels) advanced together.  samurai has no batched API: the calls below stand for a user's loop over problems
  * that makes, for each k, the calls of the time loop of demos/FiniteVolume/advection_2d.cpp:140-147.  The
  * instances run concurrently on their own streams, driven by n_threads host threads (instance k on thread
- * k mod n_threads); results are those of the serial calls on each instance.  While a batch exists its meshes run
- * with batch launch shapes and the streams of the largest quarter of them are given a higher priority (a mesh's
- * stream handle changes: query sg_mesh_stream again after sg_batch_create / sg_batch_destroy).  Per-instance arrays: eps[k],
+ * k mod n_threads); results are those of the serial calls on each instance.  Per-instance arrays: eps[k],
  * regularity[k], dt[k], a[3k .. 3k+dim-1] (stride 3 whatever the dimension), n_harten[k] (may be NULL). */
 typedef struct sg_batch_s* sg_batch_t;
 int sg_batch_create(int n, const sg_field_t* u, const sg_field_t* unp1, int n_threads, sg_batch_t* out);

@@ -29,7 +29,6 @@ namespace sg
     int ensure_spare(Ctx& c, DeviceField& f);
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words);
     void set_fusion_tops(Ctx& c, int mesh_top, int field_top, int max_top);
-    int set_stream_priority(Ctx& c, int priority);
 }
 
 struct sg_batch_s
@@ -339,21 +338,6 @@ extern "C"
             b->order.push_back(static_cast<size_t>(k));
         }
         std::stable_sort(b->order.begin(), b->order.end(), [&](size_t x, size_t y) { return size[x] > size[y]; });
-        // the largest quarter of the problems sets the batched step's critical
-        // path: their streams get the highest priority, the next quarter the
-        // middle one, so the small problems fill the GPU around them
-        int least = 0, greatest = 0;
-        cudaDeviceGetStreamPriorityRange(&least, &greatest);
-        for (size_t j = 0; j < b->order.size(); ++j)
-        {
-            const size_t q = (4 * j) / b->order.size();
-            const int prio = q == 0 ? greatest : (q == 1 ? (least + greatest) / 2 : least);
-            if (prio != least && sg::set_stream_priority(u[b->order[j]]->mesh->ctx, prio))
-            {
-                delete b;
-                return bfail(SG_ERR_CUDA, "sg_batch_create: cannot create prioritised streams");
-            }
-        }
         for (int k = 0; k < n; ++k)
         {
             sg::Ctx& c = u[k]->mesh->ctx;
@@ -376,12 +360,9 @@ extern "C"
     {
         if (b)
         {
-            int least = 0, greatest = 0;
-            cudaDeviceGetStreamPriorityRange(&least, &greatest);
             for (size_t k = 0; k < b->u.size(); ++k)
             {
                 sg::set_fusion_tops(b->u[k]->mesh->ctx, b->saved_tops[3 * k], b->saved_tops[3 * k + 1], b->saved_tops[3 * k + 2]);
-                sg::set_stream_priority(b->u[k]->mesh->ctx, least);
             }
         }
         delete b;

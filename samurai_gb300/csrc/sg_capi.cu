@@ -295,23 +295,6 @@ namespace sg
         c.graphs.clear();
     }
 
-    // the mesh's stream replaced by one of the given priority (0 = default;
-    // more negative = served first); the captured graphs stay valid, since
-    // they are launched into whatever stream the mesh has
-    int set_stream_priority(Ctx& c, int priority)
-    {
-        cudaStream_t s = nullptr;
-        if (cudaStreamSynchronize(c.stream) != cudaSuccess || cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, priority) != cudaSuccess)
-        {
-            cudaGetLastError();
-            c.err = "cannot create a stream with the requested priority";
-            return SG_ERR_CUDA;
-        }
-        cudaStreamDestroy(c.stream);
-        c.stream = s;
-        return SG_OK;
-    }
-
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words)
     {
         set_fusion_tops(c, fuse_top_of(c.g, mesh_words), fuse_top_of(c.g, field_words), fuse_top_of(c.g, max_words));
