@@ -500,18 +500,22 @@ namespace samurai
             return m_reg;
         }
 
+        // details divided by max |u| over the leaf cells (mr/rel_detail.hpp)
         mra_config& relative_detail(bool r)
         {
-            if (r)
-            {
-                throw std::invalid_argument("samurai_gb300: relative detail is not implemented");
-            }
+            m_rel = r;
             return *this;
+        }
+
+        bool relative_detail() const
+        {
+            return m_rel;
         }
 
       private:
 
         double m_eps = 1e-4, m_reg = 1.;
+        bool m_rel   = false;
     };
 
     template <class Field>
@@ -527,7 +531,7 @@ namespace samurai
         void operator()(const mra_config& cfg)
         {
             m_u->sync_to_device();
-            detail::check(sg_adapt(m_u->handle(), cfg.epsilon(), cfg.regularity(), &m_last), "MRadaptation");
+            detail::check(sg_adapt_ex(m_u->handle(), cfg.epsilon(), cfg.regularity(), cfg.relative_detail() ? 1 : 0, &m_last), "MRadaptation");
         }
 
         void operator()(double eps, double regularity)

@@ -116,6 +116,10 @@ int sg_field_swap(sg_field_t a, sg_field_t b);
 int sg_adapt(sg_field_t u, double eps, double regularity, int* n_harten);
 /* one Harten pass (mr/adapt.hpp:276-389); converged = 1 at the fixed point */
 int sg_harten(sg_field_t u, int ite, double eps, double regularity, int* converged);
+/* the same with mra_config().relative_detail(relative_detail): details divided by max |u| over the leaf cells
+   (mr/adapt.hpp:319-322, mr/rel_detail.hpp:75-111) */
+int sg_adapt_ex(sg_field_t u, double eps, double regularity, int relative_detail, int* n_harten);
+int sg_harten_ex(sg_field_t u, int ite, double eps, double regularity, int relative_detail, int* converged);
 /* samurai::update_ghost_mr(u) (algorithm/update_ghost_mr.hpp:261-270) */
 int sg_update_ghost_mr(sg_field_t u);
 /* unp1 = u - dt * samurai::upwind(a, u) on mesh[cells] (a has dim entries), or one of the other schemes above */

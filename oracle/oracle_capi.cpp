@@ -181,14 +181,22 @@ extern "C"
     }
 
     // MRadaptation(eps, regularity): returns the number of harten passes, -1 on error
+    int oracle_adapt_rel(void* h, double eps, double regularity, int relative_detail);
+
     int oracle_adapt(void* h, double eps, double regularity)
+    {
+        return oracle_adapt_rel(h, eps, regularity, 0);
+    }
+
+    // the same with mra_config().relative_detail(relative_detail)
+    int oracle_adapt_rel(void* h, double eps, double regularity, int relative_detail)
     {
         try
         {
             int it = 0;
             DISPATCH(h,
                      {
-                         oracle::MRConfig mr{eps, regularity};
+                         oracle::MRConfig mr{eps, regularity, relative_detail != 0};
                          const int minl = s->mesh.cfg.min_level, maxl = s->mesh.cfg.max_level;
                          if (minl != maxl)
                          {

@@ -33,6 +33,8 @@ def lib():
         L.oracle_get_tag.argtypes = [vp, vp]
         L.oracle_adapt.restype = i
         L.oracle_adapt.argtypes = [vp, d, d]
+        L.oracle_adapt_rel.restype = i
+        L.oracle_adapt_rel.argtypes = [vp, d, d, i]
         L.oracle_harten.restype = i
         L.oracle_harten.argtypes = [vp, i, d, d]
         L.oracle_update_ghost.restype = i
@@ -116,8 +118,8 @@ class OracleSim:
         lib().oracle_get_tag(self.h, _ptr(out))
         return out
 
-    def adapt(self, eps, regularity):
-        r = lib().oracle_adapt(self.h, eps, regularity)
+    def adapt(self, eps, regularity, relative_detail=False):
+        r = lib().oracle_adapt_rel(self.h, eps, regularity, 1 if relative_detail else 0)
         if r < 0:
             raise RuntimeError("oracle adapt failed")
         return r

@@ -1550,9 +1550,32 @@ namespace oracle
 
     struct MRConfig
     {
-        double epsilon    = 1e-4; // mr/config.hpp:63-65
-        double regularity = 1.;
+        double epsilon       = 1e-4; // mr/config.hpp:63-65
+        double regularity    = 1.;
+        bool relative_detail = false; // mr/config.hpp, mr/rel_detail.hpp
     };
+
+    // compute_relative_detail (mr/rel_detail.hpp:75-111) for one scalar field:
+    // the details divided by max |u| over the leaf cells (1 when that maximum is
+    // below the machine epsilon), as a multiplication by its inverse
+    template <std::size_t D>
+    void relative_detail(const Mesh<D>& m, const Field& u, Field& det)
+    {
+        double mx = std::numeric_limits<double>::min();
+        for (int l = 0; l < MAXL; ++l)
+        {
+            m.cells[l].for_each_cell([&](const Coord<D>& c) { mx = std::max(mx, std::abs(u[static_cast<std::size_t>(m.idx(l, c))])); });
+        }
+        if (mx < std::numeric_limits<double>::epsilon())
+        {
+            mx = 1.0;
+        }
+        const double inv = 1. / mx;
+        for (auto& v : det)
+        {
+            v *= inv;
+        }
+    }
 
     // update_fields (algorithm/update_fields.hpp:27-127)
     template <std::size_t D>
@@ -1609,6 +1632,10 @@ namespace oracle
         {
             auto gbc = on(inter(m.ref[level], uni(m.cells[level + 1], m.cells[level + 2])), level);
             gbc.for_each_cell([&](const Coord<D>& c) { detail_one<D>(m, u, det, level, c, m.cfg.prediction_radius); });
+        }
+        if (mr.relative_detail)
+        {
+            relative_detail<D>(m, u, det);
         }
 
         for (int level = minl; level <= maxl - ite; ++level)

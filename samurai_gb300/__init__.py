@@ -79,6 +79,8 @@ def lib():
         "sg_field_swap": (i, [vp, vp]),
         "sg_adapt": (i, [vp, d, d, pi]),
         "sg_harten": (i, [vp, i, d, d, pi]),
+        "sg_adapt_ex": (i, [vp, d, d, i, pi]),
+        "sg_harten_ex": (i, [vp, i, d, d, i, pi]),
         "sg_update_ghost_mr": (i, [vp]),
         "sg_upwind": (i, [vp, vp, vp, d, i]),
         "sg_detail_download": (i, [vp, vp, ll]),
@@ -203,8 +205,7 @@ class mra_config:
     def relative_detail(self, v=None):
         if v is None:
             return self._relative_detail
-        if v:
-            raise SamuraiGpuError("relative detail is not implemented")
+        self._relative_detail = bool(v)
         return self
 
 
@@ -433,19 +434,19 @@ class Adapt:
         self.field = field
         self.last_harten = 0
 
-    def __call__(self, cfg_or_eps, regularity=None):
+    def __call__(self, cfg_or_eps, regularity=None, relative_detail=False):
         if isinstance(cfg_or_eps, mra_config):
-            eps, reg = cfg_or_eps.epsilon(), cfg_or_eps.regularity()
+            eps, reg, rel = cfg_or_eps.epsilon(), cfg_or_eps.regularity(), cfg_or_eps.relative_detail()
         else:
-            eps, reg = float(cfg_or_eps), float(regularity)
+            eps, reg, rel = float(cfg_or_eps), float(regularity), bool(relative_detail)
         n = ctypes.c_int()
-        _check(lib().sg_adapt(self.field.h, eps, reg, ctypes.byref(n)), "sg_adapt")
+        _check(lib().sg_adapt_ex(self.field.h, eps, reg, 1 if rel else 0, ctypes.byref(n)), "sg_adapt")
         self.last_harten = n.value
         return n.value
 
-    def harten(self, ite, eps, reg):
+    def harten(self, ite, eps, reg, relative_detail=False):
         conv = ctypes.c_int()
-        _check(lib().sg_harten(self.field.h, ite, eps, reg, ctypes.byref(conv)), "sg_harten")
+        _check(lib().sg_harten_ex(self.field.h, ite, eps, reg, 1 if relative_detail else 0, ctypes.byref(conv)), "sg_harten")
         return bool(conv.value)
 
 
@@ -487,8 +488,8 @@ class AdvectionSim:
     def set_field(self, values):
         self.u.set_array(values)
 
-    def adapt(self, eps, regularity):
-        return self.adaptation(eps, regularity)
+    def adapt(self, eps, regularity, relative_detail=False):
+        return self.adaptation(eps, regularity, relative_detail)
 
     def harten(self, ite, eps, regularity):
         return self.adaptation.harten(ite, eps, regularity)

@@ -155,6 +155,7 @@ namespace
         dfree(c.d_flags);
         dfree(c.d_geom);
         dfree(c.d_eps);
+        dfree(c.d_absmax);
         if (c.h_eps)
         {
             cudaFreeHost(c.h_eps);
@@ -403,6 +404,7 @@ extern "C"
         st |= dalloc(c, &c.d_geom, 1);
         st |= dalloc(c, &c.d_ite, 1);
         st |= dalloc(c, &c.d_eps, sg::EPS_VELOCITY + 3);
+        st |= dalloc(c, &c.d_absmax, 1);
         if (!st)
         {
             if (cudaMallocHost(reinterpret_cast<void**>(&c.h_ite), sizeof(int)) != cudaSuccess
@@ -1023,6 +1025,11 @@ extern "C"
 
     int sg_adapt(sg_field_t u, double eps, double regularity, int* n_harten)
     {
+        return sg_adapt_ex(u, eps, regularity, 0, n_harten);
+    }
+
+    int sg_adapt_ex(sg_field_t u, double eps, double regularity, int relative_detail, int* n_harten)
+    {
         if (!u)
         {
             return fail(SG_ERR_ARG, "sg_adapt: null field");
@@ -1032,10 +1039,15 @@ extern "C"
         {
             return from_ctx(c, SG_ERR_CUDA);
         }
-        return from_ctx(c, sg::adapt(c, u->f, eps, regularity, n_harten));
+        return from_ctx(c, sg::adapt(c, u->f, eps, regularity, n_harten, relative_detail != 0));
     }
 
     int sg_harten(sg_field_t u, int ite, double eps, double regularity, int* converged)
+    {
+        return sg_harten_ex(u, ite, eps, regularity, 0, converged);
+    }
+
+    int sg_harten_ex(sg_field_t u, int ite, double eps, double regularity, int relative_detail, int* converged)
     {
         if (!u)
         {
@@ -1047,7 +1059,7 @@ extern "C"
             return from_ctx(c, SG_ERR_CUDA);
         }
         bool conv = false;
-        int st    = sg::harten(c, u->f, ite, eps, regularity, &conv);
+        int st    = sg::harten(c, u->f, ite, eps, regularity, &conv, relative_detail != 0);
         if (converged)
         {
             *converged = conv ? 1 : 0;

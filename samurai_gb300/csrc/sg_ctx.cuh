@@ -98,6 +98,8 @@ namespace sg
         Geom g{};                // host copy
         Geom* d_geom = nullptr;  // device copy: kernels read the geometry through this pointer
         double* d_eps = nullptr; // per-level thresholds of the criteria (3 x MAXLEV)
+        unsigned long long* d_absmax = nullptr; // bits of max |u| over the leaf cells (relative details)
+        bool rel_detail = false;                // the Harten pass in flight divides the details by max |u|
         double* h_eps = nullptr; // pinned staging of d_eps
         cudaStream_t stream = nullptr;
         DeviceMesh mesh[2];
@@ -171,15 +173,15 @@ namespace sg
     int scan_rank(Ctx& c, DeviceMesh& m);            // rank, word lists, counters; asynchronous
     int host_counts(Ctx& c, DeviceMesh& m);          // synchronises and refreshes nb_ref / nb_cells
     int update_ghost_mr(Ctx& c, DeviceField& f);     // update_ghost_mr(u)
-    int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten);
+    int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten, bool relative_detail = false);
     int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme);
     int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact);
     cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact); // no error text
     cudaError_t read_device_error(Ctx& c, int* v);                                                  // reads and clears
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense);
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value);
-    int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged);
-    int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity); // no synchronisation
+    int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged, bool relative_detail = false);
+    int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool relative_detail = false); // no synchronisation
     // one step's linear operators on a frozen mesh (replay and adjoint)
     struct TapeDev;
     int ghost_value(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv);

@@ -762,6 +762,52 @@ namespace sg
                       });
         }
 
+        // compute_relative_detail (mr/rel_detail.hpp:75-111), for a scalar
+        // field: max |u| over the leaf cells (the bits of non-negative doubles
+        // order like the doubles, so an integer atomic max is exact and
+        // independent of the order), then every reference detail times
+        // 1 / max (1 when max is below the machine epsilon)
+        __global__ void k_absmax_init(unsigned long long* m)
+        {
+            *m = static_cast<unsigned long long>(__double_as_longlong(2.2250738585072014e-308)); // numeric_limits<double>::min()
+        }
+
+        __global__ void k_absmax(const int* wl, const long long* lo, int nlev, const uint32_t* cells, const double* u, unsigned long long* m)
+        {
+            const int lane    = threadIdx.x & 31;
+            unsigned long long best = 0;
+            for (long long i = lo[LO_CELLS] + warp_id(); i < lo[LO_CELLS + nlev]; i += warp_count())
+            {
+                const long long w = __ldg(wl + i);
+                if ((__ldg(cells + w) >> lane) & 1u)
+                {
+                    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(fabs(u[32 * w + lane])));
+                    best                       = b > best ? b : best;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+                best                       = x > best ? x : best;
+            }
+            if (lane == 0 && best)
+            {
+                atomicMax(m, best);
+            }
+        }
+
+        __global__ void k_rel_scale(const int* wl, const long long* lo, int nlev, const uint32_t* ref, const unsigned long long* m, double* det)
+        {
+            double mx = __longlong_as_double(static_cast<long long>(*m));
+            if (mx < 2.220446049250313e-16) // numeric_limits<double>::epsilon()
+            {
+                mx = 1.0;
+            }
+            const double inv = 1. / mx;
+            warp_list(wl, lo[LO_REF], lo[LO_REF + nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+                      [&](long long w, int b) { det[32 * w + b] *= inv; });
+        }
+
         // maximum_op (mr/operators.hpp:22-96), children at level l
         template <int DIM>
         __device__ __forceinline__ void maximum_level(const Geom& g, int l, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
@@ -1509,6 +1555,13 @@ namespace sg
                 }
                 ++c.n_launches;
             }
+            if (c.rel_detail)
+            {
+                k_absmax_init<<<1, 1, 0, c.stream>>>(c.d_absmax);
+                k_absmax<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_cells, m.d_lo, g.nlev, m.cells, u, c.d_absmax);
+                k_rel_scale<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.d_absmax, c.detail);
+                c.n_launches += 3;
+            }
             timer_stop(c, T_DETAIL);
 
             timer_start(c, T_TAG);
@@ -1620,7 +1673,7 @@ namespace sg
     // waiting; harten_end waits for it, finishes the graduation if needed and
     // launches the new mesh and update_fields.  Between the two halves the
     // host may launch other meshes' work (batched mode).
-    int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity)
+    int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool relative_detail)
     {
         if (c.cfg.ghost_width != 1)
         {
@@ -1647,7 +1700,9 @@ namespace sg
             c.h_eps[2 * MAXLEV + l] = c.h_eps[MAXLEV + l] / (1 << dim);
         }
         double* u = f.data;
-        return run_cached(c, 2, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
+        // the captured front differs with relative details: its own key
+        c.rel_detail = relative_detail;
+        return run_cached(c, relative_detail ? 4 : 2, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
                           [&]() { return seq_front(c, m, nm, u, f.has_bc, f.bc_value); });
     }
 
@@ -1705,9 +1760,9 @@ namespace sg
     // No synchronisation before the pass: the pinned thresholds it rewrites
     // were consumed before the previous pass's harten_end returned, and its
     // launches queue behind whatever the stream still runs.
-    int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged)
+    int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged, bool relative_detail)
     {
-        int st = harten_begin(c, f, ite, eps, regularity);
+        int st = harten_begin(c, f, ite, eps, regularity, relative_detail);
         if (st)
         {
             return st;
@@ -1753,7 +1808,7 @@ namespace sg
     }
 
     // Adapt::operator() (mr/adapt.hpp:147-195)
-    int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten)
+    int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten, bool relative_detail)
     {
         ScopedTimer timer(c, T_ADAPT);
         const int minl = c.cfg.min_level, maxl = c.cfg.max_level;
@@ -1764,7 +1819,7 @@ namespace sg
             {
                 ++it;
                 bool conv = false;
-                int st    = harten(c, f, i, eps, regularity, &conv);
+                int st    = harten(c, f, i, eps, regularity, &conv, relative_detail);
                 if (st)
                 {
                     return st;

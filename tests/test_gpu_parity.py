@@ -234,3 +234,22 @@ def test_zero_field_coarsens_to_min_level(sg):
     lv, _, _ = g.cells()
     assert np.all(lv == 3)
     compare_meshes(g, o, 8, "zero field")
+
+
+@pytest.mark.parametrize("dim,minl,maxl,amp", [(2, 2, 8, 1.0), (2, 3, 7, 1e-3), (3, 2, 5, 5.0)])
+def test_relative_detail(sg, dim, minl, maxl, amp):
+    """mra_config().relative_detail(true): details divided by max |u| over the
+    leaf cells before the criteria (mr/rel_detail.hpp), bit for bit."""
+    g, o = pair(sg, dim, minl, maxl)
+    f = shapes_2d(8, 3, 3) if dim == 2 else ball_3d(6)
+    init_both(g, o, lambda lv, co: amp * f(lv, co))
+    a = (1.0, -0.5) if dim == 2 else (0.5, 1.0, -0.75)
+    dt = 0.4 / (1 << maxl)
+    for step in range(3):
+        assert g.adapt(1e-3, 1.0, relative_detail=True) == o.adapt(1e-3, 1.0, relative_detail=True)
+        compare_meshes(g, o, maxl, "relative detail, step %d" % step)
+        for s in (g, o):
+            s.update_ghost()
+        o.upwind(a, dt)
+        g.upwind(a, dt)
+        compare_fields(g, o, "relative detail, step %d" % step, cells_only=True)
