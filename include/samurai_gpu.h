@@ -120,6 +120,15 @@ int sg_harten(sg_field_t u, int ite, double eps, double regularity, int* converg
    (mr/adapt.hpp:319-322, mr/rel_detail.hpp:75-111) */
 int sg_adapt_ex(sg_field_t u, double eps, double regularity, int relative_detail, int* n_harten);
 int sg_harten_ex(sg_field_t u, int ite, double eps, double regularity, int relative_detail, int* converged);
+/* auto MRadaptation = samurai::make_MRAdapt(f_0, .., f_{n-1}); MRadaptation(mra_config, o_0, .., o_{n_other-1})
+   (mr/adapt.hpp:96-203): the details of the n fields (one component each) decide the mesh, a cell being coarsened
+   when every component is small and refined when one is large (mr/criteria.hpp:45-107); the n fields and the
+   n_other fields are carried to the new mesh (update_ghost_mr of the others first, mr/adapt.hpp:383-385).
+   All fields live on one mesh. */
+int sg_adapt_fields(int n, const sg_field_t* fields, int n_other, const sg_field_t* others, double eps, double regularity,
+                    int relative_detail, int* n_harten);
+/* samurai::update_ghost_mr(f_0, .., f_{n-1}) (algorithm/update_ghost_mr.hpp:261-270) */
+int sg_update_ghost_mr_fields(int n, const sg_field_t* fields);
 /* samurai::update_ghost_mr(u) (algorithm/update_ghost_mr.hpp:261-270) */
 int sg_update_ghost_mr(sg_field_t u);
 /* unp1 = u - dt * samurai::upwind(a, u) on mesh[cells] (a has dim entries), or one of the other schemes above */

@@ -20,6 +20,9 @@ namespace
         oracle::Mesh<D> mesh;
         oracle::Field u;
         oracle::BcConfig bc;
+        // more fields on the same mesh (field k >= 1 is extra[k-1])
+        std::vector<oracle::Field> extra;
+        std::vector<oracle::BcConfig> extra_bc;
         oracle::Field last_detail;
         std::vector<std::uint8_t> last_tag;
     };
@@ -46,6 +49,18 @@ namespace
             case 3: return m.uni;
             default: return m.ref;
         }
+    }
+
+    // field k of the state: 0 is u, k >= 1 the fields added by oracle_add_field
+    template <std::size_t D>
+    oracle::Field& field_k(Sim<D>* s, int k)
+    {
+        return k == 0 ? s->u : s->extra[static_cast<std::size_t>(k - 1)];
+    }
+    template <std::size_t D>
+    oracle::BcConfig& bc_k(Sim<D>* s, int k)
+    {
+        return k == 0 ? s->bc : s->extra_bc[static_cast<std::size_t>(k - 1)];
     }
 
 #define DISPATCH(h, ...)                 \
@@ -168,6 +183,84 @@ extern "C"
     void oracle_set_field(void* h, const double* in)
     {
         DISPATCH(h, std::memcpy(s->u.data(), in, s->u.size() * sizeof(double)));
+    }
+
+    // a new field on the current mesh (values NaN until set), with make_bc<Dirichlet<1>>(f, value)
+    int oracle_add_field(void* h, double dirichlet)
+    {
+        int k = -1;
+        DISPATCH(h,
+                 {
+                     s->extra.emplace_back(s->mesh.nb_ref, std::numeric_limits<double>::quiet_NaN());
+                     oracle::BcConfig b;
+                     b.dirichlet_value = dirichlet;
+                     s->extra_bc.push_back(b);
+                     k = static_cast<int>(s->extra.size());
+                 });
+        return k;
+    }
+
+    void oracle_get_field_k(void* h, int k, double* out)
+    {
+        DISPATCH(h, { auto& f = field_k(s, k); std::memcpy(out, f.data(), f.size() * sizeof(double)); });
+    }
+
+    void oracle_set_field_k(void* h, int k, const double* in)
+    {
+        DISPATCH(h, { auto& f = field_k(s, k); std::memcpy(f.data(), in, f.size() * sizeof(double)); });
+    }
+
+    int oracle_update_ghost_k(void* h, int k)
+    {
+        try
+        {
+            DISPATCH(h, oracle::update_ghost_mr(s->mesh, field_k(s, k), bc_k(s, k)));
+            return 0;
+        }
+        catch (...)
+        {
+            return -1;
+        }
+    }
+
+    // make_MRAdapt(f_0 .. f_{n_crit-1})(mra_config, f_{n_crit} .. f_{n_crit+n_other-1}): the first fields drive the
+    // adaptation, the others follow the mesh; returns the number of Harten passes
+    int oracle_adapt_fields(void* h, double eps, double regularity, int relative_detail, int n_crit, int n_other)
+    {
+        try
+        {
+            int it = 0;
+            DISPATCH(h,
+                     {
+                         std::vector<oracle::Field*> fs, os;
+                         std::vector<const oracle::BcConfig*> bs, obs;
+                         for (int k = 0; k < n_crit; ++k)
+                         {
+                             fs.push_back(&field_k(s, k));
+                             bs.push_back(&bc_k(s, k));
+                         }
+                         for (int k = n_crit; k < n_crit + n_other; ++k)
+                         {
+                             os.push_back(&field_k(s, k));
+                             obs.push_back(&bc_k(s, k));
+                         }
+                         oracle::MRConfig mr{eps, regularity, relative_detail != 0};
+                         const int minl = s->mesh.cfg.min_level, maxl = s->mesh.cfg.max_level;
+                         for (int i = 0; minl != maxl && i < maxl - minl; ++i)
+                         {
+                             ++it;
+                             if (oracle::harten_fields(s->mesh, fs, bs, i, mr, os, obs, &s->last_detail, &s->last_tag))
+                             {
+                                 break;
+                             }
+                         }
+                     });
+            return it;
+        }
+        catch (...)
+        {
+            return -1;
+        }
     }
 
     void oracle_get_detail(void* h, double* out)

@@ -35,6 +35,14 @@ def lib():
         L.oracle_adapt.argtypes = [vp, d, d]
         L.oracle_adapt_rel.restype = i
         L.oracle_adapt_rel.argtypes = [vp, d, d, i]
+        L.oracle_add_field.restype = i
+        L.oracle_add_field.argtypes = [vp, d]
+        L.oracle_get_field_k.argtypes = [vp, i, vp]
+        L.oracle_set_field_k.argtypes = [vp, i, vp]
+        L.oracle_update_ghost_k.restype = i
+        L.oracle_update_ghost_k.argtypes = [vp, i]
+        L.oracle_adapt_fields.restype = i
+        L.oracle_adapt_fields.argtypes = [vp, d, d, i, i, i]
         L.oracle_harten.restype = i
         L.oracle_harten.argtypes = [vp, i, d, d]
         L.oracle_update_ghost.restype = i
@@ -151,3 +159,34 @@ class OracleSim:
         coords = np.ascontiguousarray(coords, np.int32)
         if lib().oracle_set_cells(self.h, len(level), _ptr(level), _ptr(coords)) != 0:
             raise RuntimeError("oracle set_cells failed")
+
+    # ---- more fields on the same mesh (field 0 is the one above)
+    def add_field(self, dirichlet=0.0):
+        """a new field (values undefined until set), with Dirichlet<1> value"""
+        return lib().oracle_add_field(self.h, dirichlet)
+
+    def field_k(self, k):
+        out = np.empty(self.nb_ref(), np.float64)
+        lib().oracle_get_field_k(self.h, k, _ptr(out))
+        return out
+
+    def set_cell_values_k(self, k, values):
+        _, _, index = self.cells()
+        u = np.full(self.nb_ref(), np.nan)
+        u[index] = values
+        lib().oracle_set_field_k(self.h, k, _ptr(np.ascontiguousarray(u)))
+
+    def cell_values_k(self, k):
+        _, _, index = self.cells()
+        return self.field_k(k)[index]
+
+    def update_ghost_k(self, k):
+        if lib().oracle_update_ghost_k(self.h, k) != 0:
+            raise RuntimeError("oracle update_ghost failed")
+
+    def adapt_fields(self, eps, regularity, n_crit, n_other=0, relative_detail=False):
+        """make_MRAdapt(f_0..f_{n_crit-1})(mra_config, others): returns the Harten passes"""
+        r = lib().oracle_adapt_fields(self.h, eps, regularity, 1 if relative_detail else 0, n_crit, n_other)
+        if r < 0:
+            raise RuntimeError("oracle adapt failed")
+        return r

@@ -1614,29 +1614,60 @@ namespace oracle
         return nu;
     }
 
-    // Adapt::harten (mr/adapt.hpp:276-389); returns true at the fixed point.
+    // Adapt<Fields...>::harten (mr/adapt.hpp:276-389), true at the fixed point, with the fields `fs`
+    // driving the criteria (one detail component each: a cell is coarsened
+    // when every component is small, refined when one is large,
+    // mr/criteria.hpp:45-107) and the fields `others` carried to the new mesh
+    // (ghost update, then update_fields: mr/adapt.hpp:383-385).
     template <std::size_t D>
-    bool harten(Mesh<D>& m, Field& u, int ite, const MRConfig& mr, const BcConfig& bc, Field* det_out = nullptr,
-                std::vector<std::uint8_t>* tag_out = nullptr, int* grad_iters = nullptr)
+    bool harten_fields(Mesh<D>& m, const std::vector<Field*>& fs, const std::vector<const BcConfig*>& bcs, int ite, const MRConfig& mr,
+                       const std::vector<Field*>& others, const std::vector<const BcConfig*>& other_bcs, Field* det_out = nullptr,
+                       std::vector<std::uint8_t>* tag_out = nullptr, int* grad_iters = nullptr)
     {
         const int minl = m.cfg.min_level, maxl = m.cfg.max_level;
-        Field det(m.nb_ref, 0.);
+        const std::size_t nf = fs.size();
+        std::vector<Field> dets(nf, Field(m.nb_ref, 0.));
         std::vector<std::uint8_t> tag(m.nb_ref, 0);
         for (int l = 0; l < MAXL; ++l)
         {
             m.cells[l].for_each_cell([&](const Coord<D>& c) { tag[static_cast<std::size_t>(m.idx(l, c))] = FLAG_KEEP; });
         }
-        update_ghost_mr<D>(m, u, bc);
+        for (std::size_t k = 0; k < nf; ++k)
+        {
+            update_ghost_mr<D>(m, *fs[k], *bcs[k]);
+        }
 
         for (int level = (minl > 0 ? minl - 1 : 0); level < maxl - ite; ++level)
         {
             auto gbc = on(inter(m.ref[level], uni(m.cells[level + 1], m.cells[level + 2])), level);
-            gbc.for_each_cell([&](const Coord<D>& c) { detail_one<D>(m, u, det, level, c, m.cfg.prediction_radius); });
+            gbc.for_each_cell(
+                [&](const Coord<D>& c)
+                {
+                    for (std::size_t k = 0; k < nf; ++k)
+                    {
+                        detail_one<D>(m, *fs[k], dets[k], level, c, m.cfg.prediction_radius);
+                    }
+                });
         }
         if (mr.relative_detail)
         {
-            relative_detail<D>(m, u, det);
+            for (std::size_t k = 0; k < nf; ++k)
+            {
+                relative_detail<D>(m, *fs[k], dets[k]);
+            }
         }
+        // |detail| over the components
+        auto above = [&](std::size_t o, double thr)
+        {
+            for (std::size_t k = 0; k < nf; ++k)
+            {
+                if (std::abs(dets[k][o]) > thr)
+                {
+                    return true;
+                }
+            }
+            return false;
+        };
 
         for (int level = minl; level <= maxl - ite; ++level)
         {
@@ -1663,13 +1694,13 @@ namespace oracle
                     }
                     if (fine_level > minl)
                     {
-                        bool cond = std::abs(det[static_cast<std::size_t>(m.idx(level - 1, c))]) > coarse_eps;
+                        bool cond = above(static_cast<std::size_t>(m.idx(level - 1, c)), coarse_eps);
                         if (!cond)
                         {
                             bool ok = true;
                             for (auto o : fo)
                             {
-                                if (std::abs(det[o]) > eps_l)
+                                if (above(o, eps_l))
                                 {
                                     ok = false;
                                     break;
@@ -1688,7 +1719,7 @@ namespace oracle
                     {
                         for (auto o : fo)
                         {
-                            tag[o] |= static_cast<std::uint8_t>((std::abs(det[o]) > fine_eps) * FLAG_REFINE);
+                            tag[o] |= static_cast<std::uint8_t>(above(o, fine_eps) * FLAG_REFINE);
                         }
                     }
                 });
@@ -1747,7 +1778,7 @@ namespace oracle
         }
         if (det_out)
         {
-            *det_out = det;
+            *det_out = dets[0];
         }
         if (tag_out)
         {
@@ -1826,10 +1857,37 @@ namespace oracle
             return true;
         }
         Mesh<D> nm = make_mesh_from_cells<D>(m.cfg, nca);
-        Field nu   = update_fields<D>(m, nm, u);
-        m          = std::move(nm);
-        u          = std::move(nu);
+        for (std::size_t k = 0; k < others.size(); ++k)
+        {
+            update_ghost_mr<D>(m, *others[k], *other_bcs[k]);
+        }
+        std::vector<Field> nus;
+        for (auto* f : fs)
+        {
+            nus.push_back(update_fields<D>(m, nm, *f));
+        }
+        for (auto* f : others)
+        {
+            nus.push_back(update_fields<D>(m, nm, *f));
+        }
+        m = std::move(nm);
+        for (std::size_t k = 0; k < fs.size(); ++k)
+        {
+            *fs[k] = std::move(nus[k]);
+        }
+        for (std::size_t k = 0; k < others.size(); ++k)
+        {
+            *others[k] = std::move(nus[fs.size() + k]);
+        }
         return false;
+    }
+
+    // Adapt<Field>::harten for one field
+    template <std::size_t D>
+    bool harten(Mesh<D>& m, Field& u, int ite, const MRConfig& mr, const BcConfig& bc, Field* det_out = nullptr,
+                std::vector<std::uint8_t>* tag_out = nullptr, int* grad_iters = nullptr)
+    {
+        return harten_fields<D>(m, {&u}, {&bc}, ite, mr, {}, {}, det_out, tag_out, grad_iters);
     }
 
     // Adapt::operator() (mr/adapt.hpp:147-195)

@@ -81,6 +81,8 @@ def lib():
         "sg_harten": (i, [vp, i, d, d, pi]),
         "sg_adapt_ex": (i, [vp, d, d, i, pi]),
         "sg_harten_ex": (i, [vp, i, d, d, i, pi]),
+        "sg_adapt_fields": (i, [i, vp, i, vp, d, d, i, pi]),
+        "sg_update_ghost_mr_fields": (i, [i, vp]),
         "sg_update_ghost_mr": (i, [vp]),
         "sg_upwind": (i, [vp, vp, vp, d, i]),
         "sg_detail_download": (i, [vp, vp, ll]),
@@ -423,35 +425,55 @@ def swap(a, b):
     _check(lib().sg_field_swap(a.h, b.h), "sg_field_swap")
 
 
-def update_ghost_mr(u):
-    _check(lib().sg_update_ghost_mr(u.h), "sg_update_ghost_mr")
+def update_ghost_mr(*fields):
+    """samurai::update_ghost_mr(u, ...) (algorithm/update_ghost_mr.hpp:261-270)"""
+    if len(fields) == 1:
+        _check(lib().sg_update_ghost_mr(fields[0].h), "sg_update_ghost_mr")
+        return
+    hs = (ctypes.c_void_p * len(fields))(*[f.h.value for f in fields])
+    _check(lib().sg_update_ghost_mr_fields(len(fields), hs), "sg_update_ghost_mr_fields")
 
 
 class Adapt:
-    """samurai::Adapt for one field (mr/adapt.hpp:96-203)"""
+    """samurai::Adapt (mr/adapt.hpp:96-203): make_MRAdapt(u, v, ...) adapts the
+    mesh to the details of all its fields; a call may carry other fields along:
+    MRadaptation(mra_config, w, ...) or MRadaptation(eps, regularity, w, ...)."""
 
-    def __init__(self, field):
-        self.field = field
+    def __init__(self, *fields):
+        if not fields:
+            raise SamuraiGpuError("make_MRAdapt needs at least one field")
+        self.fields = fields
+        self.field = fields[0]
         self.last_harten = 0
 
-    def __call__(self, cfg_or_eps, regularity=None, relative_detail=False):
+    def __call__(self, cfg_or_eps, *args, relative_detail=False):
         if isinstance(cfg_or_eps, mra_config):
             eps, reg, rel = cfg_or_eps.epsilon(), cfg_or_eps.regularity(), cfg_or_eps.relative_detail()
+            others = args
         else:
-            eps, reg, rel = float(cfg_or_eps), float(regularity), bool(relative_detail)
+            eps, reg, rel = float(cfg_or_eps), float(args[0]), bool(relative_detail)
+            others = args[1:]
         n = ctypes.c_int()
-        _check(lib().sg_adapt_ex(self.field.h, eps, reg, 1 if rel else 0, ctypes.byref(n)), "sg_adapt")
+        if len(self.fields) == 1 and not others:
+            _check(lib().sg_adapt_ex(self.field.h, eps, reg, 1 if rel else 0, ctypes.byref(n)), "sg_adapt")
+        else:
+            fs = (ctypes.c_void_p * len(self.fields))(*[f.h.value for f in self.fields])
+            os_ = (ctypes.c_void_p * max(1, len(others)))(*[f.h.value for f in others])
+            _check(lib().sg_adapt_fields(len(self.fields), fs, len(others), os_, eps, reg, 1 if rel else 0, ctypes.byref(n)),
+                   "sg_adapt_fields")
         self.last_harten = n.value
         return n.value
 
     def harten(self, ite, eps, reg, relative_detail=False):
+        if len(self.fields) != 1:
+            raise SamuraiGpuError("single Harten passes are exposed for one field")
         conv = ctypes.c_int()
         _check(lib().sg_harten_ex(self.field.h, ite, eps, reg, 1 if relative_detail else 0, ctypes.byref(conv)), "sg_harten")
         return bool(conv.value)
 
 
-def make_MRAdapt(field):
-    return Adapt(field)
+def make_MRAdapt(*fields):
+    return Adapt(*fields)
 
 
 class AdvectionSim:

@@ -1047,6 +1047,80 @@ extern "C"
         return sg_harten_ex(u, ite, eps, regularity, 0, converged);
     }
 
+    int sg_adapt_fields(int n, const sg_field_t* fields, int n_other, const sg_field_t* others, double eps, double regularity,
+                        int relative_detail, int* n_harten)
+    {
+        if (n < 1 || !fields || n_other < 0 || (n_other > 0 && !others) || !fields[0])
+        {
+            return fail(SG_ERR_ARG, "sg_adapt_fields: need n >= 1 fields (and n_other >= 0 others)");
+        }
+        sg_mesh_s* mesh = fields[0]->mesh;
+        sg::Ctx& c      = mesh->ctx;
+        std::vector<sg::DeviceField*> fs, os;
+        for (int k = 0; k < n + n_other; ++k)
+        {
+            sg_field_t f = k < n ? fields[k] : others[k - n];
+            if (!f || f->mesh != mesh)
+            {
+                return fail(SG_ERR_ARG, "sg_adapt_fields: every field must live on the first field's mesh");
+            }
+            for (auto* g : fs)
+            {
+                if (g == &f->f)
+                {
+                    return fail(SG_ERR_ARG, "sg_adapt_fields: a field is listed twice");
+                }
+            }
+            for (auto* g : os)
+            {
+                if (g == &f->f)
+                {
+                    return fail(SG_ERR_ARG, "sg_adapt_fields: a field is listed twice");
+                }
+            }
+            if (!f->f.spare && dalloc(c, &f->f.spare, static_cast<size_t>(c.capacity)))
+            {
+                return from_ctx(c, SG_ERR_CUDA);
+            }
+            (k < n ? fs : os).push_back(&f->f);
+        }
+        if (n > c.detail_comps)
+        {
+            // one dense detail slab per adapted field; the contents are rebuilt by every pass
+            cudaStreamSynchronize(c.stream);
+            dfree(c.detail);
+            if (dalloc(c, &c.detail, static_cast<size_t>(c.capacity) * static_cast<size_t>(n)))
+            {
+                c.detail_comps = 0;
+                return from_ctx(c, SG_ERR_CUDA);
+            }
+            cudaMemsetAsync(c.detail, 0, static_cast<size_t>(c.capacity) * n * sizeof(double), c.stream);
+            c.detail_comps = n;
+            for (auto& ge : c.graphs)
+            {
+                cudaGraphExecDestroy(ge.exec); // they hold the old detail buffer
+            }
+            c.graphs.clear();
+        }
+        return from_ctx(c, sg::adapt_fields(c, fs, os, eps, regularity, relative_detail != 0, n_harten));
+    }
+
+    int sg_update_ghost_mr_fields(int n, const sg_field_t* fields)
+    {
+        if (n < 0 || (n > 0 && !fields))
+        {
+            return fail(SG_ERR_ARG, "sg_update_ghost_mr_fields: null field list");
+        }
+        for (int k = 0; k < n; ++k)
+        {
+            if (int st = sg_update_ghost_mr(fields[k]))
+            {
+                return st;
+            }
+        }
+        return SG_OK;
+    }
+
     int sg_harten_ex(sg_field_t u, int ite, double eps, double regularity, int relative_detail, int* converged)
     {
         if (!u)

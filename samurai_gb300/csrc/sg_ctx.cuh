@@ -99,6 +99,7 @@ namespace sg
         Geom* d_geom = nullptr;  // device copy: kernels read the geometry through this pointer
         double* d_eps = nullptr; // per-level thresholds of the criteria (3 x MAXLEV)
         unsigned long long* d_absmax = nullptr; // bits of max |u| over the leaf cells (relative details)
+        int detail_comps             = 1;       // dense detail slabs allocated (one per adapted field)
         bool rel_detail = false;                // the Harten pass in flight divides the details by max |u|
         double* h_eps = nullptr; // pinned staging of d_eps
         cudaStream_t stream = nullptr;
@@ -189,6 +190,11 @@ namespace sg
     int update_fields_value(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un);
     int update_fields_tape(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const TapeDev& t);
     int harten_end(Ctx& c, DeviceField& f, bool* converged);
+    // the same for the fields fs driving the criteria and the fields os carried along
+    int harten_begin_fields(Ctx& c, const std::vector<DeviceField*>& fs, int ite, double eps, double regularity, bool relative_detail);
+    int harten_end_fields(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, bool* converged);
+    int adapt_fields(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
+                     bool relative_detail, int* n_harten);
     int device_error(Ctx& c); // reads and clears the device error word (synchronises)
 
     void timer_start(Ctx& c, int id);

@@ -704,8 +704,22 @@ namespace sg
         // intersection(cells[l], all_cells[l-1]).on(l-1), fine levels l0..l1
         template <int DIM>
         __global__ void k_criteria(const Geom* __restrict__ gp, const double* __restrict__ eps, const int* wl, const long long* lo, int l0, int l1,
-                                   const int* d_ite, const uint32_t* ref, const uint32_t* hc, const double* det, uint8_t* tag)
+                                   const int* d_ite, const uint32_t* ref, const uint32_t* hc, const double* det, uint8_t* tag, int ncomp,
+                                   long long cstride)
         {
+            // |detail| above a threshold in one of the components (one per
+            // adapted field, mr/criteria.hpp:45-107)
+            auto above = [&](long long e, double thr)
+            {
+                for (int k = 0; k < ncomp; ++k)
+                {
+                    if (fabs(det[k * cstride + e]) > thr)
+                    {
+                        return true;
+                    }
+                }
+                return false;
+            };
             const Geom& g = *gp;
             // fine levels l0 .. min(l1, max_level - ite) (mr/adapt.hpp:325-339); the
             // operator runs on their parents
@@ -728,13 +742,13 @@ namespace sg
                           }
                           if (lf > g.min_level)
                           {
-                              const bool cond = fabs(det[32 * w + b]) > eps[2 * MAXLEV + lf];
+                              const bool cond = above(32 * w + b, eps[2 * MAXLEV + lf]);
                               if (!cond)
                               {
                                   bool ok = true;
                                   for (int ch = 0; ch < (1 << DIM); ++ch)
                                   {
-                                      if (fabs(det[fo[ch]]) > eps[lf])
+                                      if (above(fo[ch], eps[lf]))
                                       {
                                           ok = false;
                                           break;
@@ -753,7 +767,7 @@ namespace sg
                           {
                               for (int ch = 0; ch < (1 << DIM); ++ch)
                               {
-                                  if (fabs(det[fo[ch]]) > eps[MAXLEV + lf])
+                                  if (above(fo[ch], eps[MAXLEV + lf]))
                                   {
                                       tag[fo[ch]] |= 4;
                                   }
@@ -1522,44 +1536,61 @@ namespace sg
         // two graduation passes and the comparison with the current cells.
         // Reads the pass index and thresholds staged in pinned memory; leaves
         // the flags in pinned memory.  No host synchronisation.
-        int seq_front(Ctx& c, DeviceMesh& m, DeviceMesh& nm, double* u, bool has_bc, double bcv)
+        // The fields fs drive the criteria, one detail component each, the
+        // components stored one dense slab after the other.
+        int seq_front(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const std::vector<DeviceField*>& fs)
         {
             const Geom& g  = c.g;
             const int minl = c.cfg.min_level;
             const int maxl = c.cfg.max_level;
+            const int nf   = static_cast<int>(fs.size());
             int st;
             cudaMemcpyAsync(c.d_ite, c.h_ite, sizeof(int), cudaMemcpyHostToDevice, c.stream);
             cudaMemcpyAsync(c.d_eps, c.h_eps, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
             cudaMemsetAsync(c.d_flags, 0, F_COUNT * sizeof(int), c.stream);
             k_tag_init<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
             ++c.n_launches;
-            if ((st = check(c, "tag_init")) || (st = seq_ghost(c, m, u, has_bc, bcv)))
+            for (int k = 1; k < nf; ++k)
+            {
+                k_fill<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.detail + k * c.capacity, 0.);
+                ++c.n_launches;
+            }
+            if ((st = check(c, "tag_init")))
             {
                 return st;
+            }
+            for (DeviceField* f : fs)
+            {
+                if ((st = seq_ghost(c, m, f->data, f->has_bc, f->bc_value)))
+                {
+                    return st;
+                }
             }
 
             timer_start(c, T_DETAIL);
             const int dl0 = minl > 0 ? minl - 1 : 0;
             const int dl1 = maxl - 1;
-            if (dl1 >= dl0)
+            for (int k = 0; k < nf && dl1 >= dl0; ++k)
             {
+                const double* u = fs[k]->data;
+                double* det     = c.detail + k * c.capacity;
                 if (g.dim == 2)
                 {
                     k_detail<2><<<blocks_words(c, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
-                                                                                    m.ref, m.hc, m.hc2, u, c.detail);
+                                                                                    m.ref, m.hc, m.hc2, u, det);
                 }
                 else
                 {
                     k_detail<3><<<blocks_words(c, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
-                                                                                    m.ref, m.hc, m.hc2, u, c.detail);
+                                                                                    m.ref, m.hc, m.hc2, u, det);
                 }
                 ++c.n_launches;
             }
-            if (c.rel_detail)
+            for (int k = 0; k < nf && c.rel_detail; ++k)
             {
                 k_absmax_init<<<1, 1, 0, c.stream>>>(c.d_absmax);
-                k_absmax<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_cells, m.d_lo, g.nlev, m.cells, u, c.d_absmax);
-                k_rel_scale<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.d_absmax, c.detail);
+                k_absmax<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_cells, m.d_lo, g.nlev, m.cells, fs[k]->data, c.d_absmax);
+                k_rel_scale<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.d_absmax, c.detail + k * c.capacity);
                 c.n_launches += 3;
             }
             timer_stop(c, T_DETAIL);
@@ -1570,12 +1601,12 @@ namespace sg
                 if (g.dim == 2)
                 {
                     k_criteria<2><<<blocks_words(c, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
-                                                                                                m.ref, m.hc, c.detail, c.tag);
+                                                                                                m.ref, m.hc, c.detail, c.tag, nf, c.capacity);
                 }
                 else
                 {
                     k_criteria<3><<<blocks_words(c, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
-                                                                                                m.ref, m.hc, c.detail, c.tag);
+                                                                                                m.ref, m.hc, c.detail, c.tag, nf, c.capacity);
                 }
                 ++c.n_launches;
             }
@@ -1632,16 +1663,48 @@ namespace sg
         }
 
         // new mesh from the new cells and update_fields (mr/adapt.hpp:380-386)
-        int seq_back(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un)
+        // for the adapted fields fs and the fields os carried along (their
+        // ghosts are updated first, mr/adapt.hpp:383)
+        int seq_back(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os)
         {
-            int st = build_mesh(c, nm);
-            if (st)
+            int st;
+            for (DeviceField* f : os)
+            {
+                if ((st = seq_ghost(c, m, f->data, f->has_bc, f->bc_value)))
+                {
+                    return st;
+                }
+            }
+            if ((st = build_mesh(c, nm)))
             {
                 return st;
             }
             ScopedTimer tf(c, T_FIELDS_UPDATE);
-            update_fields_launch(c, m, nm, ValAcc{const_cast<double*>(uo)}, ValAcc{un});
+            for (const auto* list : {&fs, &os})
+            {
+                for (DeviceField* f : *list)
+                {
+                    update_fields_launch(c, m, nm, ValAcc{f->data}, ValAcc{f->spare});
+                }
+            }
             return check(c, "update_fields");
+        }
+
+        // graph-cache key of a list of fields: their buffers and boundary values
+        unsigned long long fields_key(const std::vector<DeviceField*>& fs, bool spares)
+        {
+            unsigned long long h = 1469598103934665603ull;
+            auto mix             = [&](unsigned long long v)
+            {
+                h ^= v;
+                h *= 1099511628211ull;
+            };
+            for (const DeviceField* f : fs)
+            {
+                mix(ptr_key(spares ? f->spare : f->data));
+                mix(f->has_bc ? bits_of(f->bc_value) : 1ull);
+            }
+            return h;
         }
     } // namespace
 
@@ -1675,6 +1738,11 @@ namespace sg
     // host may launch other meshes' work (batched mode).
     int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool relative_detail)
     {
+        return harten_begin_fields(c, {&f}, ite, eps, regularity, relative_detail);
+    }
+
+    int harten_begin_fields(Ctx& c, const std::vector<DeviceField*>& fs, int ite, double eps, double regularity, bool relative_detail)
+    {
         if (c.cfg.ghost_width != 1)
         {
             c.err = "harten: only a ghost width of 1 is implemented";
@@ -1699,14 +1767,25 @@ namespace sg
             c.h_eps[MAXLEV + l]     = std::pow(2.0, regularity + dim) * c.h_eps[l];
             c.h_eps[2 * MAXLEV + l] = c.h_eps[MAXLEV + l] / (1 << dim);
         }
-        double* u = f.data;
-        // the captured front differs with relative details: its own key
+        // the captured front differs with relative details and with the
+        // number of fields: keys of their own
         c.rel_detail = relative_detail;
-        return run_cached(c, relative_detail ? 4 : 2, static_cast<unsigned long long>(c.cur), ptr_key(u), f.has_bc ? bits_of(f.bc_value) : 1ull,
-                          [&]() { return seq_front(c, m, nm, u, f.has_bc, f.bc_value); });
+        if (fs.size() == 1)
+        {
+            DeviceField& f = *fs[0];
+            return run_cached(c, relative_detail ? 4 : 2, static_cast<unsigned long long>(c.cur), ptr_key(f.data), f.has_bc ? bits_of(f.bc_value) : 1ull,
+                              [&]() { return seq_front(c, m, nm, fs); });
+        }
+        return run_cached(c, relative_detail ? 6 : 5, static_cast<unsigned long long>(c.cur), fields_key(fs, false), fs.size(),
+                          [&]() { return seq_front(c, m, nm, fs); });
     }
 
     int harten_end(Ctx& c, DeviceField& f, bool* converged)
+    {
+        return harten_end_fields(c, {&f}, {}, converged);
+    }
+
+    int harten_end_fields(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, bool* converged)
     {
         DeviceMesh& m  = c.m();
         DeviceMesh& nm = c.spare();
@@ -1715,8 +1794,11 @@ namespace sg
         {
             return check(c, "harten front sync");
         }
-        f.ghosts_valid  = true; // the front's ghost update ran on the current mesh
-        f.ghost_version = c.mesh_version;
+        for (DeviceField* f : fs)
+        {
+            f->ghosts_valid  = true; // the front's ghost update ran on the current mesh
+            f->ghost_version = c.mesh_version;
+        }
         if (c.h_flags[F_GRAD1])
         {
             // graduation still refining after two passes: finish the fixed
@@ -1742,18 +1824,34 @@ namespace sg
             return SG_OK;
         }
         *converged = false;
-        double* u  = f.data;
-        st         = run_cached(c, 3, static_cast<unsigned long long>(c.cur), ptr_key(u), ptr_key(f.spare),
-                                [&]() { return seq_back(c, m, nm, u, f.spare); });
+        if (fs.size() == 1 && os.empty())
+        {
+            DeviceField& f = *fs[0];
+            st             = run_cached(c, 3, static_cast<unsigned long long>(c.cur), ptr_key(f.data), ptr_key(f.spare),
+                                        [&]() { return seq_back(c, m, nm, fs, os); });
+        }
+        else
+        {
+            std::vector<DeviceField*> all(fs);
+            all.insert(all.end(), os.begin(), os.end());
+            st = run_cached(c, 7 + 16 * fs.size(), static_cast<unsigned long long>(c.cur), fields_key(all, false), fields_key(all, true),
+                            [&]() { return seq_back(c, m, nm, fs, os); });
+        }
         if (st)
         {
             return st;
         }
         nm.host_valid = false; // a replayed graph refreshed the counters without host code
-        std::swap(f.data, f.spare);
+        for (const auto* list : {&fs, &os})
+        {
+            for (DeviceField* f : *list)
+            {
+                std::swap(f->data, f->spare);
+                f->ghosts_valid = false;
+            }
+        }
         c.cur = 1 - c.cur;
         ++c.mesh_version;
-        f.ghosts_valid = false;
         return SG_OK;
     }
 
@@ -1805,6 +1903,38 @@ namespace sg
             update_fields_launch(c, m, nm, TapeAcc<FormCap<3>::value>{t}, TapeAcc<FormCap<3>::value>{t});
         }
         return check(c, "update_fields (tape)");
+    }
+
+    // Adapt<Fields...>::operator()(mra_config, other_fields...) (mr/adapt.hpp:147-195)
+    int adapt_fields(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
+                     bool relative_detail, int* n_harten)
+    {
+        ScopedTimer timer(c, T_ADAPT);
+        const int minl = c.cfg.min_level, maxl = c.cfg.max_level;
+        int it         = 0;
+        for (int i = 0; minl != maxl && i < maxl - minl; ++i)
+        {
+            ++it;
+            bool conv = false;
+            int st    = harten_begin_fields(c, fs, i, eps, regularity, relative_detail);
+            if (!st)
+            {
+                st = harten_end_fields(c, fs, os, &conv);
+            }
+            if (st)
+            {
+                return st;
+            }
+            if (conv)
+            {
+                break;
+            }
+        }
+        if (n_harten)
+        {
+            *n_harten = it;
+        }
+        return device_error(c);
     }
 
     // Adapt::operator() (mr/adapt.hpp:147-195)

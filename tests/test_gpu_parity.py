@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from advection_cases import demo_time_loop, disc, readme_square, shapes_2d, ball_3d
+from advection_cases import ball_3d, centers, demo_time_loop, disc, readme_square, shapes_2d
 from gpu_util import compare_cells, compare_fields, compare_meshes
 from oracle.pyoracle import OracleSim
 
@@ -253,3 +253,43 @@ def test_relative_detail(sg, dim, minl, maxl, amp):
         o.upwind(a, dt)
         g.upwind(a, dt)
         compare_fields(g, o, "relative detail, step %d" % step, cells_only=True)
+
+
+@pytest.mark.parametrize("dim,minl,maxl", [(2, 2, 7), (3, 2, 5)])
+def test_several_fields(sg, dim, minl, maxl):
+    """make_MRAdapt(u, v)(mra_config, w): the details of u and v together
+    decide the mesh (any component large refines, all small coarsens), u, v
+    and the carried field w move to every new mesh; against the oracle,
+    meshes and the three fields bit for bit, with a few upwind steps of u."""
+    mesh = sg.MRMesh(dim, minl, maxl, 1, 1)
+    u, v, w, unp1 = (sg.make_scalar_field(n, mesh) for n in ("u", "v", "w", "unp1"))
+    for f, bc in ((u, 0.0), (v, 0.5), (w, -1.0)):
+        sg.make_bc(sg.Dirichlet(1), f, bc)
+    o = OracleSim(dim, minl, maxl, 1, 1, 1, 0.0)
+    kv, kw = o.add_field(0.5), o.add_field(-1.0)
+    lv, co, _ = o.cells()
+    fu = shapes_2d(3, 2, 2) if dim == 2 else ball_3d(2)
+    fv = (lambda l, c: shapes_2d(4, 1, 3)(l, c) * 0.5) if dim == 2 else (lambda l, c: 0.5 * ball_3d(7)(l, c))
+    fw = lambda l, c: np.cos(3.0 * centers(l, c)[:, 0])
+    for f, k, fun in ((u, 0, fu), (v, kv, fv), (w, kw, fw)):
+        vals = fun(lv, co)
+        f.set_cells(vals)
+        o.set_cell_values_k(k, vals)
+    adapt = sg.make_MRAdapt(u, v)
+    cfg = sg.mra_config().epsilon(1e-3).regularity(1.0)
+    a = (1.0, 0.5) if dim == 2 else (1.0, 0.5, -0.25)
+    dt = 0.4 / (1 << maxl)
+    for step in range(3):
+        assert adapt(cfg, w) == o.adapt_fields(1e-3, 1.0, 2, 1)
+        lg, cg, ig = mesh.cells()
+        lo_, co_, io_ = o.cells()
+        assert np.array_equal(lg, lo_) and np.array_equal(cg, co_) and np.array_equal(ig, io_), "step %d: cells" % step
+        for f, k in ((u, 0), (v, kv), (w, kw)):
+            got, ref = f.cell_values(), o.cell_values_k(k)
+            assert np.array_equal(got, ref), "step %d: field %d differs" % (step, k)
+        sg.update_ghost_mr(u, v, w)
+        for k in (0, kv, kw):
+            o.update_ghost_k(k)
+        unp1.assign_upwind(u, a, dt)
+        sg.swap(u, unp1)
+        o.upwind(a, dt)
