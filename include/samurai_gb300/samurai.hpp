@@ -518,25 +518,46 @@ namespace samurai
         bool m_rel   = false;
     };
 
-    template <class Field>
+    // make_MRAdapt(u, v, ...) (mr/adapt.hpp:96-203, 391-420): the details of all
+    // its fields decide the mesh; a call may carry other fields along
+    template <class Field, class... Fields>
     class Adapt
     {
       public:
 
-        explicit Adapt(Field& u)
-            : m_u(&u)
+        explicit Adapt(Field& u, Fields&... fields)
+            : m_fields{&u, &fields...}
         {
         }
 
-        void operator()(const mra_config& cfg)
+        template <class... Others>
+        void operator()(const mra_config& cfg, Others&... others)
         {
-            m_u->sync_to_device();
-            detail::check(sg_adapt_ex(m_u->handle(), cfg.epsilon(), cfg.regularity(), cfg.relative_detail() ? 1 : 0, &m_last), "MRadaptation");
+            std::vector<sg_field_t> fs, os;
+            for (auto* f : m_fields)
+            {
+                f->sync_to_device();
+                fs.push_back(f->handle());
+            }
+            (others.sync_to_device(), ...);
+            (os.push_back(others.handle()), ...);
+            const int rel = cfg.relative_detail() ? 1 : 0;
+            if (fs.size() == 1 && os.empty())
+            {
+                detail::check(sg_adapt_ex(fs[0], cfg.epsilon(), cfg.regularity(), rel, &m_last), "MRadaptation");
+            }
+            else
+            {
+                detail::check(sg_adapt_fields(static_cast<int>(fs.size()), fs.data(), static_cast<int>(os.size()), os.data(), cfg.epsilon(),
+                                              cfg.regularity(), rel, &m_last),
+                              "MRadaptation");
+            }
         }
 
-        void operator()(double eps, double regularity)
+        template <class... Others>
+        void operator()(double eps, double regularity, Others&... others)
         {
-            (*this)(mra_config().epsilon(eps).regularity(regularity));
+            (*this)(mra_config().epsilon(eps).regularity(regularity), others...);
         }
 
         int last_harten_passes() const
@@ -546,21 +567,22 @@ namespace samurai
 
       private:
 
-        Field* m_u;
+        std::vector<Field*> m_fields;
         int m_last = 0;
     };
 
-    template <class Field>
-    auto make_MRAdapt(Field& u)
+    template <class Field, class... Fields>
+    auto make_MRAdapt(Field& u, Fields&... fields)
     {
-        return Adapt<Field>(u);
+        return Adapt<Field, Fields...>(u, fields...);
     }
 
-    template <class Field>
-    void update_ghost_mr(Field& u)
+    template <class Field, class... Fields>
+    void update_ghost_mr(Field& u, Fields&... fields)
     {
         u.sync_to_device();
         detail::check(sg_update_ghost_mr(u.handle()), "update_ghost_mr");
+        (update_ghost_mr(fields), ...);
     }
 
     template <class Mesh, class A>

@@ -511,7 +511,7 @@ class AdvectionSim:
         self.u.set_array(values)
 
     def adapt(self, eps, regularity, relative_detail=False):
-        return self.adaptation(eps, regularity, relative_detail)
+        return self.adaptation(eps, regularity, relative_detail=relative_detail)
 
     def harten(self, ite, eps, regularity):
         return self.adaptation.harten(ite, eps, regularity)
