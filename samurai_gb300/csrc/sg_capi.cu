@@ -156,6 +156,7 @@ namespace
         dfree(c.d_geom);
         dfree(c.d_eps);
         dfree(c.d_absmax);
+        dfree(c.g.err);
         if (c.h_eps)
         {
             cudaFreeHost(c.h_eps);
@@ -405,6 +406,7 @@ extern "C"
         st |= dalloc(c, &c.d_ite, 1);
         st |= dalloc(c, &c.d_eps, sg::EPS_VELOCITY + 3);
         st |= dalloc(c, &c.d_absmax, 1);
+        st |= dalloc(c, &c.g.err, 1);
         if (!st)
         {
             if (cudaMallocHost(reinterpret_cast<void**>(&c.h_ite), sizeof(int)) != cudaSuccess
@@ -422,6 +424,7 @@ extern "C"
             destroy_ctx(h);
             return fail(SG_ERR_CUDA, "sg_mesh_create: ", msg.c_str());
         }
+        cudaMemsetAsync(c.g.err, 0, sizeof(int), c.stream);
         cudaMemcpyAsync(c.d_geom, &c.g, sizeof(sg::Geom), cudaMemcpyHostToDevice, c.stream);
         // every bitmap starts empty: the mesh construction writes only the
         // levels where a set can be non-empty and relies on zeros elsewhere

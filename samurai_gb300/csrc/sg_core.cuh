@@ -83,6 +83,7 @@ namespace sg
         int min_level;
         int max_level;
         long long total_words;
+        int* err; // device word of the mesh: set by kernels that met a position outside the stored box
         LevelGeom lv[MAXLEV];
     };
 

@@ -14,21 +14,16 @@
 
 namespace sg
 {
-    // set by kernels that met a position outside the stored box
-    __device__ int sg_device_error = 0;
-
+    // the mesh's device error word (Geom::err), read and cleared
     int device_error(Ctx& c)
     {
         int v = 0;
-        if (cudaMemcpyFromSymbolAsync(&v, sg_device_error, sizeof(int), 0, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess
-            || cudaStreamSynchronize(c.stream) != cudaSuccess)
+        if (read_device_error(c, &v) != cudaSuccess)
         {
             return check(c, "device_error");
         }
         if (v)
         {
-            const int zero = 0;
-            cudaMemcpyToSymbolAsync(sg_device_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, c.stream);
             c.err = "a kernel addressed a cell outside the stored level box (invalid mesh)";
             return SG_ERR_STATE;
         }
@@ -90,7 +85,7 @@ namespace sg
             const Pos p = pos_of(g, l, x, y, z);
             if (p.w < 0)
             {
-                atomicOr(&sg_device_error, 1);
+                atomicOr(g.err, 1);
                 return 0;
             }
             return elem(p);
@@ -160,7 +155,7 @@ namespace sg
             const Pos hi = pos_of(g, l, x0 + n - 1, y0 + n - 1, DIM == 3 ? z0 + n - 1 : 0);
             if (lo.w < 0 || hi.w < 0)
             {
-                atomicOr(&sg_device_error, 1);
+                atomicOr(g.err, 1);
                 return {0, 0, 0};
             }
             const LevelGeom& L = g.lv[l];
@@ -1281,15 +1276,14 @@ namespace sg
     cudaError_t read_device_error(Ctx& c, int* v)
     {
         *v            = 0;
-        cudaError_t e = cudaMemcpyFromSymbolAsync(v, sg_device_error, sizeof(int), 0, cudaMemcpyDeviceToHost, c.stream);
+        cudaError_t e = cudaMemcpyAsync(v, c.g.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
         if (e == cudaSuccess)
         {
             e = cudaStreamSynchronize(c.stream);
         }
         if (e == cudaSuccess && *v)
         {
-            const int zero = 0;
-            e              = cudaMemcpyToSymbolAsync(sg_device_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, c.stream);
+            e = cudaMemsetAsync(c.g.err, 0, sizeof(int), c.stream);
         }
         return e;
     }
