@@ -26,6 +26,8 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <tuple>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -316,30 +318,32 @@ namespace samurai
         bool dirty = false;
     };
 
-    template <class Mesh>
-    struct UpwindExpr // u - dt * upwind(a, u)
-    {
-        const ScalarField<Mesh>* u;
-        std::array<double, Mesh::dim> a;
-        double dt;
-        int scheme;
-    };
-
-    template <class Mesh>
-    struct ScaledUpwind
-    {
-        const ScalarField<Mesh>* u;
-        std::array<double, Mesh::dim> a;
-        double dt;
-        int scheme;
-    };
-
-    template <class Mesh>
+    // unp1 = u - dt * op(u): op is upwind(a, u) or a make_convection_upwind operator; Field is a
+    // scalar or a vector field, evaluated on the device when assigned to unp1
+    template <class Field>
     struct UpwindOp
     {
-        const ScalarField<Mesh>* u;
-        std::array<double, Mesh::dim> a;
+        const Field* u;
+        std::array<double, Field::dim> a;
         int scheme = SG_UPWIND_OP;
+    };
+
+    template <class Field>
+    struct ScaledUpwind
+    {
+        const Field* u;
+        std::array<double, Field::dim> a;
+        double dt;
+        int scheme;
+    };
+
+    template <class Field>
+    struct UpwindExpr // u - dt * upwind(a, u)
+    {
+        const Field* u;
+        std::array<double, Field::dim> a;
+        double dt;
+        int scheme;
     };
 
     template <class Mesh>
@@ -347,8 +351,9 @@ namespace samurai
     {
       public:
 
-        static constexpr std::size_t dim = Mesh::dim;
-        using mesh_t                     = Mesh;
+        static constexpr std::size_t dim    = Mesh::dim;
+        static constexpr std::size_t n_comp = 1;
+        using mesh_t                        = Mesh;
 
         ScalarField(std::string name, Mesh& mesh)
             : m_mesh(&mesh)
@@ -404,12 +409,33 @@ namespace samurai
             m_host.valid = false;
         }
 
-        ScalarField& operator=(const UpwindExpr<Mesh>& e)
+        ScalarField& operator=(const UpwindExpr<ScalarField>& e)
         {
-            const_cast<ScalarField<Mesh>*>(e.u)->sync_to_device();
+            const_cast<ScalarField*>(e.u)->sync_to_device();
             detail::check(sg_upwind(e.u->handle(), handle(), e.a.data(), e.dt, e.scheme), "upwind");
             m_host.valid = false;
             return *this;
+        }
+
+        // the scalar fields a call of the C ABI takes for this field
+        void append_handles(std::vector<sg_field_t>& out) const
+        {
+            out.push_back(handle());
+        }
+
+        void set_dirichlet(const std::vector<double>& values)
+        {
+            if (values.size() > 1)
+            {
+                throw std::invalid_argument("make_bc: the number of constant values should be equal to the number of components");
+            }
+            detail::check(sg_field_set_dirichlet(handle(), values.empty() ? 0. : values[0]), "make_bc");
+        }
+
+        void update_ghost()
+        {
+            sync_to_device();
+            detail::check(sg_update_ghost_mr(handle()), "update_ghost_mr");
         }
 
         friend void swap(ScalarField& a, ScalarField& b)
@@ -445,12 +471,209 @@ namespace samurai
         return ScalarField<Mesh>(name, mesh);
     }
 
-    // README spelling make_field<double, 1>(name, mesh)
+    // VectorField<Mesh, double, n_comp> (field/vector_field.hpp:134-216): n_comp scalar
+    // component fields on the device; the host mirror keeps samurai's layout, the values of a
+    // cell side by side (storage shape {size, n_comp})
+    template <class Mesh, std::size_t n_comp_>
+    class VectorField
+    {
+      public:
+
+        static constexpr std::size_t dim    = Mesh::dim;
+        static constexpr std::size_t n_comp = n_comp_;
+        using mesh_t                        = Mesh;
+
+        // v[cell]: the n_comp values of one cell in the host mirror
+        class CellValues
+        {
+          public:
+
+            explicit CellValues(double* p)
+                : m_p(p)
+            {
+            }
+
+            double& operator[](std::size_t c) const
+            {
+                return m_p[c];
+            }
+
+            double& operator()(std::size_t c) const
+            {
+                return m_p[c];
+            }
+
+            const CellValues& operator=(const std::array<double, n_comp>& v) const
+            {
+                for (std::size_t c = 0; c < n_comp; ++c)
+                {
+                    m_p[c] = v[c];
+                }
+                return *this;
+            }
+
+            const CellValues& operator=(double v) const
+            {
+                for (std::size_t c = 0; c < n_comp; ++c)
+                {
+                    m_p[c] = v;
+                }
+                return *this;
+            }
+
+          private:
+
+            double* m_p;
+        };
+
+        VectorField(std::string name, Mesh& mesh)
+            : m_mesh(&mesh)
+            , m_name(std::move(name))
+        {
+            static_assert(n_comp >= 1 && n_comp <= SG_MAX_COMPONENTS, "samurai_gb300: 1 <= n_comp <= SG_MAX_COMPONENTS");
+            sg_vfield_t h = nullptr;
+            detail::check(sg_vector_field_create(mesh.handle(), m_name.c_str(), static_cast<int>(n_comp), &h), "make_vector_field");
+            m_h = std::shared_ptr<sg_vfield_s>(h, [](sg_vfield_t p) { sg_vector_field_destroy(p); });
+        }
+
+        sg_vfield_t handle() const
+        {
+            return m_h.get();
+        }
+
+        Mesh& mesh() const
+        {
+            return *m_mesh;
+        }
+
+        CellValues operator[](const Cell<dim>& cell)
+        {
+            pull();
+            m_host.dirty = true;
+            return CellValues(m_host.values.data() + static_cast<std::size_t>(cell.index) * n_comp);
+        }
+
+        std::array<double, n_comp> operator[](const Cell<dim>& cell) const
+        {
+            const_cast<VectorField*>(this)->pull();
+            std::array<double, n_comp> r;
+            for (std::size_t c = 0; c < n_comp; ++c)
+            {
+                r[c] = m_host.values[static_cast<std::size_t>(cell.index) * n_comp + c];
+            }
+            return r;
+        }
+
+        void resize()
+        {
+        }
+
+        VectorField& array()
+        {
+            return *this;
+        }
+
+        void sync_to_device()
+        {
+            if (m_host.dirty)
+            {
+                detail::check(sg_vector_field_upload(handle(), m_host.values.data(), static_cast<long long>(m_host.values.size())), "upload");
+                m_host.dirty = false;
+            }
+            m_host.valid = false;
+        }
+
+        void append_handles(std::vector<sg_field_t>& out) const
+        {
+            for (std::size_t c = 0; c < n_comp; ++c)
+            {
+                sg_field_t f = nullptr;
+                detail::check(sg_vector_field_component(handle(), static_cast<int>(c), &f), "component");
+                out.push_back(f);
+            }
+        }
+
+        void set_dirichlet(const std::vector<double>& values)
+        {
+            if (!values.empty() && values.size() != n_comp)
+            {
+                throw std::invalid_argument("make_bc: the number of constant values should be equal to the number of components");
+            }
+            std::array<double, n_comp> v{};
+            for (std::size_t c = 0; c < values.size(); ++c)
+            {
+                v[c] = values[c];
+            }
+            detail::check(sg_vector_field_set_dirichlet(handle(), v.data()), "make_bc");
+        }
+
+        void update_ghost()
+        {
+            sync_to_device();
+            detail::check(sg_vector_update_ghost_mr(handle()), "update_ghost_mr");
+        }
+
+        VectorField& operator=(const UpwindExpr<VectorField>& e)
+        {
+            const_cast<VectorField*>(e.u)->sync_to_device();
+            detail::check(sg_vector_upwind(e.u->handle(), handle(), e.a.data(), e.dt, e.scheme), "upwind");
+            m_host.valid = false;
+            return *this;
+        }
+
+        friend void swap(VectorField& a, VectorField& b)
+        {
+            a.sync_to_device();
+            b.sync_to_device();
+            detail::check(sg_vector_field_swap(a.handle(), b.handle()), "swap");
+        }
+
+      private:
+
+        void pull()
+        {
+            if (m_host.valid)
+            {
+                return;
+            }
+            m_host.values.resize(m_mesh->nb_cells() * n_comp);
+            detail::check(sg_vector_field_download(handle(), m_host.values.data(), static_cast<long long>(m_host.values.size())), "download");
+            m_host.valid = true;
+        }
+
+        Mesh* m_mesh;
+        std::string m_name;
+        std::shared_ptr<sg_vfield_s> m_h;
+        FieldArray m_host;
+    };
+
+    // make_vector_field<double, n_comp>(name, mesh) and make_vector_field<n_comp>(name, mesh)
+    // (field/vector_field.hpp:232-237, 278-283)
+    template <class value_t, std::size_t n_comp, class Mesh>
+    auto make_vector_field(const std::string& name, Mesh& mesh)
+    {
+        static_assert(std::is_same_v<value_t, double>, "samurai_gb300 fields are FP64");
+        return VectorField<Mesh, n_comp>(name, mesh);
+    }
+
+    template <std::size_t n_comp, class Mesh>
+    auto make_vector_field(const std::string& name, Mesh& mesh)
+    {
+        return VectorField<Mesh, n_comp>(name, mesh);
+    }
+
+    // README spelling make_field<double, n_comp>(name, mesh)
     template <class value_t, std::size_t n_comp, class Mesh>
     auto make_field(const std::string& name, Mesh& mesh)
     {
-        static_assert(n_comp == 1, "samurai_gb300: vector fields are not implemented");
-        return make_scalar_field<value_t>(name, mesh);
+        if constexpr (n_comp == 1)
+        {
+            return make_scalar_field<value_t>(name, mesh);
+        }
+        else
+        {
+            return make_vector_field<value_t, n_comp>(name, mesh);
+        }
     }
 
     template <std::size_t order = 1>
@@ -459,10 +682,12 @@ namespace samurai
         static_assert(order == 1, "samurai_gb300 implements Dirichlet<1>");
     };
 
-    template <class Bc, class Field>
-    void make_bc(Field& u, double value = 0.)
+    // make_bc<Dirichlet<1>>(u, v_0, .., v_{n_comp-1}) (bc/bc.hpp:752-800): one constant per component,
+    // none for zeros
+    template <class Bc, class Field, class... T>
+    void make_bc(Field& u, T... values)
     {
-        detail::check(sg_field_set_dirichlet(u.handle(), value), "make_bc");
+        u.set_dirichlet(std::vector<double>{static_cast<double>(values)...});
     }
 
     template <class Mesh, class F>
@@ -519,14 +744,15 @@ namespace samurai
     };
 
     // make_MRAdapt(u, v, ...) (mr/adapt.hpp:96-203, 391-420): the details of all
-    // its fields decide the mesh; a call may carry other fields along
+    // its fields decide the mesh (a vector field contributes its components, in
+    // order); a call may carry other fields along
     template <class Field, class... Fields>
     class Adapt
     {
       public:
 
         explicit Adapt(Field& u, Fields&... fields)
-            : m_fields{&u, &fields...}
+            : m_fields(&u, &fields...)
         {
         }
 
@@ -534,13 +760,13 @@ namespace samurai
         void operator()(const mra_config& cfg, Others&... others)
         {
             std::vector<sg_field_t> fs, os;
-            for (auto* f : m_fields)
-            {
-                f->sync_to_device();
-                fs.push_back(f->handle());
-            }
-            (others.sync_to_device(), ...);
-            (os.push_back(others.handle()), ...);
+            std::apply(
+                [&](auto*... f)
+                {
+                    ((f->sync_to_device(), f->append_handles(fs)), ...);
+                },
+                m_fields);
+            ((others.sync_to_device(), others.append_handles(os)), ...);
             const int rel = cfg.relative_detail() ? 1 : 0;
             if (fs.size() == 1 && os.empty())
             {
@@ -567,7 +793,7 @@ namespace samurai
 
       private:
 
-        std::vector<Field*> m_fields;
+        std::tuple<Field*, Fields*...> m_fields;
         int m_last = 0;
     };
 
@@ -580,24 +806,23 @@ namespace samurai
     template <class Field, class... Fields>
     void update_ghost_mr(Field& u, Fields&... fields)
     {
-        u.sync_to_device();
-        detail::check(sg_update_ghost_mr(u.handle()), "update_ghost_mr");
-        (update_ghost_mr(fields), ...);
+        u.update_ghost();
+        (fields.update_ghost(), ...);
     }
 
-    template <class Mesh, class A>
-    auto upwind(const A& a, const ScalarField<Mesh>& u)
+    template <class Field, class A>
+    auto upwind(const A& a, const Field& u)
     {
-        UpwindOp<Mesh> op{&u, {}};
-        for (std::size_t d = 0; d < Mesh::dim; ++d)
+        UpwindOp<Field> op{&u, {}};
+        for (std::size_t d = 0; d < Field::dim; ++d)
         {
             op.a[d] = a[d];
         }
         return op;
     }
 
-    template <class Mesh>
-    ScaledUpwind<Mesh> operator*(double dt, const UpwindOp<Mesh>& op)
+    template <class Field>
+    ScaledUpwind<Field> operator*(double dt, const UpwindOp<Field>& op)
     {
         return {op.u, op.a, dt, op.scheme};
     }
@@ -615,7 +840,7 @@ namespace samurai
 
         auto operator()(const Field& u) const
         {
-            UpwindOp<typename Field::mesh_t> op{&u, velocity, SG_CONVECTION};
+            UpwindOp<Field> op{&u, velocity, SG_CONVECTION};
             return op;
         }
     };
@@ -626,8 +851,8 @@ namespace samurai
         return {velocity};
     }
 
-    template <class Mesh>
-    UpwindExpr<Mesh> operator-(const ScalarField<Mesh>& u, const ScaledUpwind<Mesh>& s)
+    template <class Field>
+    UpwindExpr<Field> operator-(const Field& u, const ScaledUpwind<Field>& s)
     {
         if (&u != s.u)
         {
@@ -642,6 +867,12 @@ namespace std
     // std::swap(u.array(), unp1.array())
     template <class Mesh>
     void swap(samurai::ScalarField<Mesh>& a, samurai::ScalarField<Mesh>& b)
+    {
+        swap(a, b);
+    }
+
+    template <class Mesh, std::size_t n_comp>
+    void swap(samurai::VectorField<Mesh, n_comp>& a, samurai::VectorField<Mesh, n_comp>& b)
     {
         swap(a, b);
     }

@@ -137,6 +137,38 @@ int sg_upwind(sg_field_t u, sg_field_t unp1, const double* a, double dt, int sch
 int sg_detail_download(sg_field_t u, double* values, long long n);
 int sg_tag_download(sg_field_t u, unsigned char* values, long long n);
 
+/* VectorField<mesh, double, n_comp>: samurai::make_vector_field<double, n_comp>(name, mesh)
+ * (field/vector_field.hpp:134-237).  Held on the device as n_comp scalar component fields of the mesh; every scalar
+ * call accepts a component (sg_vector_field_component), so make_MRAdapt(v, u)(cfg) is sg_adapt_fields over v's
+ * components followed by u (the detail of several fields lists their components in order, mr/adapt.hpp:74-95).
+ * Host arrays keep samurai's layout, the values of a cell side by side: element (k, c) at k * n_comp + c
+ * (storage shape {size, n_comp}, field/vector_field.hpp:38).  1 <= n_comp <= SG_MAX_COMPONENTS. */
+enum
+{
+    SG_MAX_COMPONENTS = 16
+};
+typedef struct sg_vfield_s* sg_vfield_t;
+int sg_vector_field_create(sg_mesh_t mesh, const char* name, int n_comp, sg_vfield_t* out);
+int sg_vector_field_destroy(sg_vfield_t v);
+int sg_vector_field_n_comp(sg_vfield_t v, int* n_comp);
+int sg_vector_field_component(sg_vfield_t v, int c, sg_field_t* out);
+/* samurai::make_bc<samurai::Dirichlet<1>>(v, values[0], .., values[n_comp-1]) (bc/bc.hpp:752-800) */
+int sg_vector_field_set_dirichlet(sg_vfield_t v, const double* values);
+/* v.array() in the reference numbering (n = n_comp * nb_reference) */
+int sg_vector_field_upload(sg_vfield_t v, const double* values, long long n);
+int sg_vector_field_download(sg_vfield_t v, double* values, long long n);
+/* v[cell] for the leaf cells in for_each_cell order (n = n_comp * nb_cells) */
+int sg_vector_field_set_cells(sg_vfield_t v, const double* values, long long n);
+int sg_vector_field_get_cells(sg_vfield_t v, double* values, long long n);
+/* std::swap(v.array(), vnp1.array()) */
+int sg_vector_field_swap(sg_vfield_t a, sg_vfield_t b);
+/* make_MRAdapt(v)(mra_config().epsilon(eps).regularity(reg).relative_detail(relative_detail)) (mr/adapt.hpp:147-203) */
+int sg_vector_adapt(sg_vfield_t v, double eps, double regularity, int relative_detail, int* n_harten);
+/* samurai::update_ghost_mr(v) (algorithm/update_ghost_mr.hpp:261-270) */
+int sg_vector_update_ghost_mr(sg_vfield_t v);
+/* unp1 = u - dt * samurai::upwind(a, u) component by component (stencil_field.hpp:91-179), or another scheme */
+int sg_vector_upwind(sg_vfield_t u, sg_vfield_t unp1, const double* a, double dt, int scheme);
+
 /* u.array() to host memory without allocating anything (no counterpart in the reference: samurai has no
  * C interface).  For callers that cannot let a library allocate device memory, e.g. a process whose device
  * memory is reserved by another allocator.  Same output as sg_field_download, through a static 16 MiB device

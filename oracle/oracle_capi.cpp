@@ -344,21 +344,31 @@ extern "C"
         }
     }
 
+    int oracle_upwind_k(void* h, int k, const double* a, double dt, int scheme);
+
     // u <- u - dt * upwind(a, u) on the cells; ghost storage becomes NaN
     // (scheme 0: upwind operator, 1: README lambda, 2: make_convection_upwind)
     int oracle_upwind(void* h, const double* a, double dt, int scheme)
+    {
+        return oracle_upwind_k(h, 0, a, dt, scheme);
+    }
+
+    // the same on field k (a component of a vector field is upwinded alone, stencil_field.hpp:91-179)
+    int oracle_upwind_k(void* h, int k, const double* a, double dt, int scheme)
     {
         try
         {
             if (dim_of(h) == 2)
             {
                 auto* s = as<2>(h);
-                s->u    = oracle::upwind_step<2>(s->mesh, s->u, {a[0], a[1]}, dt, static_cast<oracle::Scheme>(scheme));
+                auto& f = field_k(s, k);
+                f       = oracle::upwind_step<2>(s->mesh, f, {a[0], a[1]}, dt, static_cast<oracle::Scheme>(scheme));
             }
             else
             {
                 auto* s = as<3>(h);
-                s->u    = oracle::upwind_step<3>(s->mesh, s->u, {a[0], a[1], a[2]}, dt, static_cast<oracle::Scheme>(scheme));
+                auto& f = field_k(s, k);
+                f       = oracle::upwind_step<3>(s->mesh, f, {a[0], a[1], a[2]}, dt, static_cast<oracle::Scheme>(scheme));
             }
             return 0;
         }

@@ -49,6 +49,8 @@ def lib():
         L.oracle_update_ghost.argtypes = [vp]
         L.oracle_upwind.restype = i
         L.oracle_upwind.argtypes = [vp, vp, d, i]
+        L.oracle_upwind_k.restype = i
+        L.oracle_upwind_k.argtypes = [vp, i, vp, d, i]
         L.oracle_count_intervals.restype = ll
         L.oracle_count_intervals.argtypes = [vp, i, i]
         L.oracle_get_intervals.argtypes = [vp, i, i, vp]
@@ -183,6 +185,11 @@ class OracleSim:
     def update_ghost_k(self, k):
         if lib().oracle_update_ghost_k(self.h, k) != 0:
             raise RuntimeError("oracle update_ghost failed")
+
+    def upwind_k(self, k, a, dt, scheme=0):
+        a = np.ascontiguousarray(a, np.float64)
+        if lib().oracle_upwind_k(self.h, k, _ptr(a), dt, scheme) != 0:
+            raise RuntimeError("oracle upwind failed")
 
     def adapt_fields(self, eps, regularity, n_crit, n_other=0, relative_detail=False):
         """make_MRAdapt(f_0..f_{n_crit-1})(mra_config, others): returns the Harten passes"""

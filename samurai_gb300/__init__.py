@@ -104,6 +104,19 @@ def lib():
         "sg_adjoint_final": (i, [vp, vp, ll]),
         "sg_adjoint_replay": (i, [vp, vp, vp, vp]),
         "sg_adjoint_backward": (i, [vp, vp, vp, vp]),
+        "sg_vector_field_create": (i, [vp, ctypes.c_char_p, i, ctypes.POINTER(vp)]),
+        "sg_vector_field_destroy": (i, [vp]),
+        "sg_vector_field_n_comp": (i, [vp, pi]),
+        "sg_vector_field_component": (i, [vp, i, ctypes.POINTER(vp)]),
+        "sg_vector_field_set_dirichlet": (i, [vp, vp]),
+        "sg_vector_field_upload": (i, [vp, vp, ll]),
+        "sg_vector_field_download": (i, [vp, vp, ll]),
+        "sg_vector_field_set_cells": (i, [vp, vp, ll]),
+        "sg_vector_field_get_cells": (i, [vp, vp, ll]),
+        "sg_vector_field_swap": (i, [vp, vp]),
+        "sg_vector_adapt": (i, [vp, d, d, i, pi]),
+        "sg_vector_update_ghost_mr": (i, [vp]),
+        "sg_vector_upwind": (i, [vp, vp, vp, d, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -328,15 +341,24 @@ class mra:
 class ScalarField:
     """samurai::ScalarField<MRMesh, double> (field/scalar_field.hpp:77-216)."""
 
-    def __init__(self, name, mesh):
+    n_comp = 1
+
+    def __init__(self, name, mesh, _handle=None):
         self.name = name
         self.mesh = mesh
-        h = ctypes.c_void_p()
-        _check(lib().sg_field_create(mesh.h, name.encode(), ctypes.byref(h)), "sg_field_create")
+        self._owner = _handle is None
+        if _handle is None:
+            h = ctypes.c_void_p()
+            _check(lib().sg_field_create(mesh.h, name.encode(), ctypes.byref(h)), "sg_field_create")
+        else:
+            h = _handle  # a component of a vector field, owned by it
         self.h = h
 
+    def components(self):
+        return [self]
+
     def __del__(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "_owner", False):
             try:
                 lib().sg_field_destroy(self.h)
             except Exception:
@@ -400,6 +422,83 @@ def make_scalar_field(name, mesh):
     return ScalarField(name, mesh)
 
 
+class VectorField:
+    """samurai::VectorField<MRMesh, double, n_comp> (field/vector_field.hpp:134-216).
+
+    Device storage: one scalar component field per component (component-major
+    slabs); host arrays keep samurai's layout, the n_comp values of a cell side
+    by side (storage shape {size, n_comp}).  Every call that takes fields
+    accepts a vector field and acts on its components in order, which is
+    samurai's semantics: make_MRAdapt(v) tests the n_comp details together
+    (mr/criteria.hpp:45-107), ghosts and upwind act component by component."""
+
+    def __init__(self, name, mesh, n_comp):
+        self.name = name
+        self.mesh = mesh
+        self.n_comp = int(n_comp)
+        h = ctypes.c_void_p()
+        _check(lib().sg_vector_field_create(mesh.h, name.encode(), self.n_comp, ctypes.byref(h)), "sg_vector_field_create")
+        self.h = h
+        self._comps = []
+        for c in range(self.n_comp):
+            ch = ctypes.c_void_p()
+            _check(lib().sg_vector_field_component(h, c, ctypes.byref(ch)), "sg_vector_field_component")
+            self._comps.append(ScalarField("%s_%d" % (name, c), mesh, _handle=ch))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().sg_vector_field_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    def components(self):
+        return list(self._comps)
+
+    def component(self, c):
+        return self._comps[c]
+
+    def array(self):
+        """v.array(): shape (nb_reference, n_comp), samurai's reference numbering"""
+        n = self.mesh.nb_cells("reference")
+        out = np.empty((n, self.n_comp), np.float64)
+        _check(lib().sg_vector_field_download(self.h, _ptr(out), out.size), "sg_vector_field_download")
+        return out
+
+    def set_array(self, values):
+        values = np.ascontiguousarray(values, np.float64)
+        _check(lib().sg_vector_field_upload(self.h, _ptr(values), values.size), "sg_vector_field_upload")
+
+    def set_cells(self, values):
+        """v[cell] = values[k] (n_comp values) for every leaf cell, in for_each_cell order"""
+        values = np.ascontiguousarray(values, np.float64)
+        _check(lib().sg_vector_field_set_cells(self.h, _ptr(values), values.size), "sg_vector_field_set_cells")
+
+    def cell_values(self):
+        n = self.mesh.nb_cells("cells")
+        out = np.empty((n, self.n_comp), np.float64)
+        _check(lib().sg_vector_field_get_cells(self.h, _ptr(out), out.size), "sg_vector_field_get_cells")
+        return out
+
+    def assign_upwind(self, u, a, dt, scheme=UPWIND_OP):
+        """self = u - dt * upwind(a, u) on mesh[cells], component by component"""
+        a = np.ascontiguousarray(a, np.float64)
+        _check(lib().sg_vector_upwind(u.h, self.h, _ptr(a), dt, scheme), "sg_vector_upwind")
+
+
+def make_vector_field(name, mesh, n_comp):
+    """samurai::make_vector_field<double, n_comp>(name, mesh) (field/vector_field.hpp:232-237)"""
+    return VectorField(name, mesh, n_comp)
+
+
+def _components(fields):
+    out = []
+    for f in fields:
+        out.extend(f.components())
+    return out
+
+
 make_field = make_scalar_field  # the README's make_field<double, 1>
 
 
@@ -412,21 +511,32 @@ class Dirichlet:
         self.order = order
 
 
-def make_bc(bc, field, value=0.0):
-    """samurai::make_bc<Dirichlet<1>>(u, value)"""
+def make_bc(bc, field, *values):
+    """samurai::make_bc<Dirichlet<1>>(u, value) and make_bc<Dirichlet<1>>(v, v_0, .., v_{n-1})
+    (bc/bc.hpp:752-800); no value means 0 for every component"""
     if not isinstance(bc, Dirichlet):
         raise SamuraiGpuError("only Dirichlet boundary conditions are implemented")
-    _check(lib().sg_field_set_dirichlet(field.h, float(value)), "sg_field_set_dirichlet")
+    comps = field.components()
+    if not values:
+        values = (0.0,) * len(comps)
+    if len(values) != len(comps):
+        raise SamuraiGpuError("make_bc: the number of constant values must equal the number of components")
+    for f, v in zip(comps, values):
+        _check(lib().sg_field_set_dirichlet(f.h, float(v)), "sg_field_set_dirichlet")
     return bc
 
 
 def swap(a, b):
     """std::swap(u.array(), unp1.array())"""
+    if isinstance(a, VectorField) or isinstance(b, VectorField):
+        _check(lib().sg_vector_field_swap(a.h, b.h), "sg_vector_field_swap")
+        return
     _check(lib().sg_field_swap(a.h, b.h), "sg_field_swap")
 
 
 def update_ghost_mr(*fields):
     """samurai::update_ghost_mr(u, ...) (algorithm/update_ghost_mr.hpp:261-270)"""
+    fields = _components(fields)
     if len(fields) == 1:
         _check(lib().sg_update_ghost_mr(fields[0].h), "sg_update_ghost_mr")
         return
@@ -442,8 +552,9 @@ class Adapt:
     def __init__(self, *fields):
         if not fields:
             raise SamuraiGpuError("make_MRAdapt needs at least one field")
-        self.fields = fields
-        self.field = fields[0]
+        # a vector field contributes its components, in order (mr/adapt.hpp:74-95)
+        self.fields = _components(fields)
+        self.field = self.fields[0]
         self.last_harten = 0
 
     def __call__(self, cfg_or_eps, *args, relative_detail=False):
@@ -453,6 +564,7 @@ class Adapt:
         else:
             eps, reg, rel = float(cfg_or_eps), float(args[0]), bool(relative_detail)
             others = args[1:]
+        others = _components(others)
         n = ctypes.c_int()
         if len(self.fields) == 1 and not others:
             _check(lib().sg_adapt_ex(self.field.h, eps, reg, 1 if rel else 0, ctypes.byref(n)), "sg_adapt")

@@ -16,3 +16,11 @@ struct sg_field_s
     sg_mesh_s* mesh = nullptr;
     sg::DeviceField f;
 };
+
+// VectorField<mesh, double, n_comp> (field/vector_field.hpp:134-216): n_comp
+// scalar component fields on one mesh
+struct sg_vfield_s
+{
+    sg_mesh_s* mesh = nullptr;
+    std::vector<sg_field_s*> comp;
+};

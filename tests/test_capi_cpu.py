@@ -109,3 +109,24 @@ def test_adjoint_argument_checks():
     assert L.sg_adjoint_backward(None, None, None, None) == 1
     assert L.sg_adjoint_replay(None, None, None, None) == 1
     assert L.sg_adjoint_destroy(None) == 0
+
+
+def test_vector_field_argument_checks():
+    """make_vector_field / make_bc / make_MRAdapt on vector handles: malformed
+    calls are rejected with SG_ERR_ARG before any device work."""
+    import ctypes
+
+    import samurai_gb300 as sg
+
+    L = sg.lib()
+    h = ctypes.c_void_p()
+    assert L.sg_vector_field_create(None, b"v", 2, ctypes.byref(h)) == 1
+    assert b"n_comp" in L.sg_last_error()
+    assert L.sg_vector_field_component(None, 0, ctypes.byref(h)) == 1
+    assert L.sg_vector_field_set_dirichlet(None, None) == 1
+    assert L.sg_vector_field_swap(None, None) == 1
+    assert L.sg_vector_adapt(None, 1e-3, 1.0, 0, None) == 1
+    assert L.sg_vector_update_ghost_mr(None) == 1
+    assert L.sg_vector_upwind(None, None, None, 0.1, 0) == 1
+    assert L.sg_vector_field_download(None, None, 0) == 1
+    assert L.sg_vector_field_destroy(None) == 0

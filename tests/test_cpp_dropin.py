@@ -10,15 +10,16 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "advection_2d.cpp")
+VSRC = os.path.join(ROOT, "tests", "cpp", "vector_advection_2d.cpp")
 GOLD = os.path.join(ROOT, "tests", "golden")
 
 
-def compile_demo(tmp_path):
+def compile_demo(tmp_path, src=SRC):
     from samurai_gb300 import build
 
     lib = build.build()
-    exe = os.path.join(str(tmp_path), "advection_2d")
-    cmd = ["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), SRC, "-L" + os.path.dirname(lib), "-lsamurai_gpu",
+    exe = os.path.join(str(tmp_path), os.path.splitext(os.path.basename(src))[0])
+    cmd = ["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), src, "-L" + os.path.dirname(lib), "-lsamurai_gpu",
            "-Wl,-rpath," + os.path.dirname(lib), "-o", exe]
     subprocess.check_call(cmd)
     return exe
@@ -26,6 +27,11 @@ def compile_demo(tmp_path):
 
 def test_demo_compiles(tmp_path):
     exe = compile_demo(tmp_path)
+    assert os.path.exists(exe)
+
+
+def test_vector_demo_compiles(tmp_path):
+    exe = compile_demo(tmp_path, VSRC)
     assert os.path.exists(exe)
 
 
@@ -66,3 +72,38 @@ def test_demo_flux_form_matches_oracle(tmp_path):
     assert np.array_equal(rows[:, 0].astype(int), lv)
     assert np.array_equal(rows[:, 1:3].astype(int), co)
     assert np.array_equal(rows[:, 3], o.cell_values())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("relative", [False, True])
+def test_vector_demo_matches_oracle(tmp_path, relative):
+    """make_vector_field<double, 2> through the C++ header: adaptation to both
+    details, per-component Dirichlet values, upwind on the vector field;
+    against the oracle's two-field restatement, bit for bit."""
+    from advection_cases import centers
+    from oracle.pyoracle import OracleSim
+
+    exe = compile_demo(tmp_path, VSRC)
+    out = os.path.join(str(tmp_path), "out.txt")
+    subprocess.check_call([exe, out] + (["relative"] if relative else []))
+    lines = open(out).read().split("\n")
+    rows = np.array([[float(v) for v in l.split()] for l in lines[1:] if l.strip()])
+    o = OracleSim(2, 3, 8, 1, 1, 1, 0.0)
+    k1 = o.add_field(0.25)
+    lv, co, _ = o.cells()
+    c = centers(lv, co)
+    x, y = c[:, 0], c[:, 1]
+    o.set_cell_values(np.where((x - 0.3) * (x - 0.3) + (y - 0.3) * (y - 0.3) <= 0.2 * 0.2, 1.0, 0.0))
+    o.set_cell_values_k(k1, np.where((x >= 0.5) & (x <= 0.7) & (y >= 0.4) & (y <= 0.6), 0.5, 0.0))
+    dt = 0.5 / 256
+    for _ in range(int(lines[0])):
+        o.adapt_fields(1e-3, 1.0, 2, 0, relative_detail=relative)
+        o.update_ghost_k(0)
+        o.update_ghost_k(k1)
+        o.upwind_k(0, (1.0, 0.5), dt)
+        o.upwind_k(k1, (1.0, 0.5), dt)
+    lv, co, _ = o.cells()
+    assert np.array_equal(rows[:, 0].astype(int), lv)
+    assert np.array_equal(rows[:, 1:3].astype(int), co)
+    assert np.array_equal(rows[:, 3], o.cell_values())
+    assert np.array_equal(rows[:, 4], o.cell_values_k(k1))

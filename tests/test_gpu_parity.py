@@ -293,3 +293,60 @@ def test_several_fields(sg, dim, minl, maxl):
         unp1.assign_upwind(u, a, dt)
         sg.swap(u, unp1)
         o.upwind(a, dt)
+
+
+@pytest.mark.parametrize("dim,minl,maxl,rel", [(2, 2, 7, False), (2, 3, 8, True), (3, 2, 5, False)])
+def test_vector_field(sg, dim, minl, maxl, rel):
+    """make_vector_field<double, 3>: make_MRAdapt(v) tests the three detail
+    components together (mr/criteria.hpp:45-107; per-component maxima with
+    relative details), make_bc gives each component its value, ghosts and
+    upwind act component by component, and v.array() keeps samurai's layout
+    (the values of a cell side by side).  Against the oracle's several-field
+    restatement, bit for bit, with upwind steps."""
+    mesh = sg.MRMesh(dim, minl, maxl, 1, 1)
+    v = sg.make_vector_field("v", mesh, 3)
+    vnp1 = sg.make_vector_field("vnp1", mesh, 3)
+    bcs = (0.0, 0.25, -0.5)
+    sg.make_bc(sg.Dirichlet(1), v, *bcs)
+    sg.make_bc(sg.Dirichlet(1), vnp1, *bcs)
+    o = OracleSim(dim, minl, maxl, 1, 1, 1, bcs[0])
+    ks = [0, o.add_field(bcs[1]), o.add_field(bcs[2])]
+    lv, co, _ = o.cells()
+    f0 = shapes_2d(5, 2, 2) if dim == 2 else ball_3d(3)
+    f1 = (lambda l, c: 0.5 * shapes_2d(6, 2, 1)(l, c)) if dim == 2 else (lambda l, c: 0.5 * ball_3d(8)(l, c))
+    f2 = lambda l, c: 0.1 * np.sin(4.0 * centers(l, c)[:, 1])
+    vals = np.stack([f(lv, co) for f in (f0, f1, f2)], axis=1)
+    v.set_cells(vals)
+    for c, k in enumerate(ks):
+        o.set_cell_values_k(k, vals[:, c])
+    adapt = sg.make_MRAdapt(v)
+    cfg = sg.mra_config().epsilon(1e-3).regularity(1.0).relative_detail(rel)
+    a = (1.0, 0.5) if dim == 2 else (1.0, 0.5, -0.25)
+    dt = 0.4 / (1 << maxl)
+    for step in range(3):
+        assert adapt(cfg) == o.adapt_fields(1e-3, 1.0, 3, 0, relative_detail=rel)
+        lg, cg, ig = mesh.cells()
+        lo_, co_, io_ = o.cells()
+        assert np.array_equal(lg, lo_) and np.array_equal(cg, co_) and np.array_equal(ig, io_), "step %d: cells" % step
+        got = v.cell_values()
+        assert got.shape == (len(lg), 3)
+        for c, k in enumerate(ks):
+            assert np.array_equal(got[:, c], o.cell_values_k(k)), "step %d: component %d" % (step, c)
+        sg.update_ghost_mr(v)
+        for k in ks:
+            o.update_ghost_k(k)
+        full = v.array()
+        cells = ig
+        for c, k in enumerate(ks):
+            ref = o.field_k(k)
+            # the reference array holds leaves and ghosts: compare every entry the oracle defines
+            m = ~np.isnan(ref)
+            assert np.array_equal(full[m, c], ref[m]), "step %d: ghosts of component %d" % (step, c)
+        assert np.array_equal(full.reshape(-1)[cells * 3 + 1], got[:, 1])
+        vnp1.assign_upwind(v, a, dt)
+        sg.swap(v, vnp1)
+        for k in ks:
+            o.upwind_k(k, a, dt)
+    got = v.cell_values()
+    for c, k in enumerate(ks):
+        assert np.array_equal(got[:, c], o.cell_values_k(k)), "final component %d" % c
