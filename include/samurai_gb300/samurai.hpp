@@ -23,6 +23,7 @@
 
 #include <array>
 #include <cstddef>
+#include <filesystem>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -860,7 +861,96 @@ namespace samurai
         }
         return {&u, s.a, s.dt, s.scheme};
     }
+    // save / dump / load (io/hdf5.hpp:1331-1350, io/restart.hpp:188-227, 425-495): HDF5 files written and
+    // read by the library without libhdf5; load needs a mesh with the file's dimension and levels
+    namespace detail
+    {
+        class IoList
+        {
+          public:
+
+            IoList()
+            {
+                check(sg_io_create(&m_h), "io");
+            }
+
+            ~IoList()
+            {
+                sg_io_destroy(m_h);
+            }
+
+            IoList(const IoList&)            = delete;
+            IoList& operator=(const IoList&) = delete;
+
+            template <class Mesh>
+            void add(ScalarField<Mesh>& f)
+            {
+                f.sync_to_device();
+                check(sg_io_add_field(m_h, f.handle()), "io");
+            }
+
+            template <class Mesh, std::size_t n>
+            void add(VectorField<Mesh, n>& f)
+            {
+                f.sync_to_device();
+                check(sg_io_add_vector_field(m_h, f.handle()), "io");
+            }
+
+            sg_io_t handle() const
+            {
+                return m_h;
+            }
+
+          private:
+
+            sg_io_t m_h = nullptr;
+        };
+    }
+
+    template <class Cfg, class... T>
+    void save(const std::filesystem::path& path, const std::string& filename, const MRMesh<Cfg>& mesh, const T&... fields)
+    {
+        detail::IoList l;
+        (l.add(const_cast<T&>(fields)), ...);
+        detail::check(sg_save(path.string().c_str(), filename.c_str(), mesh.handle(), l.handle()), "save");
+    }
+
+    template <class Cfg, class... T>
+    void save(const std::string& filename, const MRMesh<Cfg>& mesh, const T&... fields)
+    {
+        save(std::filesystem::current_path(), filename, mesh, fields...);
+    }
+
+    template <class Cfg, class... T>
+    void dump(const std::filesystem::path& path, const std::string& filename, const MRMesh<Cfg>& mesh, const T&... fields)
+    {
+        detail::IoList l;
+        (l.add(const_cast<T&>(fields)), ...);
+        detail::check(sg_dump(path.string().c_str(), filename.c_str(), mesh.handle(), l.handle()), "dump");
+    }
+
+    template <class Cfg, class... T>
+    void dump(const std::string& filename, const MRMesh<Cfg>& mesh, const T&... fields)
+    {
+        dump(std::filesystem::current_path(), filename, mesh, fields...);
+    }
+
+    template <class Cfg, class... T>
+    void load(const std::filesystem::path& path, const std::string& filename, MRMesh<Cfg>& mesh, T&... fields)
+    {
+        detail::IoList l;
+        (l.add(fields), ...);
+        detail::check(sg_load(path.string().c_str(), filename.c_str(), mesh.handle(), l.handle()), "load");
+        (fields.sync_to_device(), ...); // the host mirrors are stale
+    }
+
+    template <class Cfg, class... T>
+    void load(const std::string& filename, MRMesh<Cfg>& mesh, T&... fields)
+    {
+        load(std::filesystem::current_path(), filename, mesh, fields...);
+    }
 } // namespace samurai
+
 
 namespace std
 {

@@ -169,6 +169,27 @@ int sg_vector_update_ghost_mr(sg_vfield_t v);
 /* unp1 = u - dt * samurai::upwind(a, u) component by component (stencil_field.hpp:91-179), or another scheme */
 int sg_vector_upwind(sg_vfield_t u, sg_vfield_t unp1, const double* a, double dt, int scheme);
 
+/* Output and restart files (io/hdf5.hpp, io/restart.hpp), written and read without libhdf5.  A field list
+ * (sg_io_t) names the fields of a call in order, as the variadic fields... of samurai's functions. */
+typedef struct sg_io_s* sg_io_t;
+int sg_io_create(sg_io_t* out);
+int sg_io_destroy(sg_io_t io);
+int sg_io_add_field(sg_io_t io, sg_field_t field);
+int sg_io_add_vector_field(sg_io_t io, sg_vfield_t field);
+/* samurai::save(path, filename, mesh, fields...) (io/hdf5.hpp:1331-1336): <path>/<filename>.h5 holding
+ * /mesh/points, /mesh/connectivity (corner ids in order of first appearance over for_each_cell, io/hdf5.hpp:85-144)
+ * and /mesh/fields/<name> (<name>_<c> per component of a vector field), and <path>/<filename>.xdmf.
+ * fields may be NULL; path NULL or "" is the current directory. */
+int sg_save(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields);
+/* samurai::dump(path, filename, mesh, fields...) (io/restart.hpp:188-201): the leaf CellArray and the fields */
+int sg_dump(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields);
+/* dimension and levels of a restart file, to create the mesh that sg_load fills */
+int sg_restart_levels(const char* path, const char* filename, int* dim, int* min_level, int* max_level);
+/* samurai::load(path, filename, mesh, fields...) (io/restart.hpp:425-463): the mesh becomes the file's leaf cells
+ * (MRMesh(ca, cfg)) and each field gets its leaf values; the mesh must have the file's dimension and levels
+ * (samurai recreates it with them). */
+int sg_load(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields);
+
 /* u.array() to host memory without allocating anything (no counterpart in the reference: samurai has no
  * C interface).  For callers that cannot let a library allocate device memory, e.g. a process whose device
  * memory is reserved by another allocator.  Same output as sg_field_download, through a static 16 MiB device

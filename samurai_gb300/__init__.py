@@ -117,6 +117,14 @@ def lib():
         "sg_vector_adapt": (i, [vp, d, d, i, pi]),
         "sg_vector_update_ghost_mr": (i, [vp]),
         "sg_vector_upwind": (i, [vp, vp, vp, d, i]),
+        "sg_io_create": (i, [ctypes.POINTER(vp)]),
+        "sg_io_destroy": (i, [vp]),
+        "sg_io_add_field": (i, [vp, vp]),
+        "sg_io_add_vector_field": (i, [vp, vp]),
+        "sg_save": (i, [ctypes.c_char_p, ctypes.c_char_p, vp, vp]),
+        "sg_dump": (i, [ctypes.c_char_p, ctypes.c_char_p, vp, vp]),
+        "sg_restart_levels": (i, [ctypes.c_char_p, ctypes.c_char_p, pi, pi, pi]),
+        "sg_load": (i, [ctypes.c_char_p, ctypes.c_char_p, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -524,6 +532,66 @@ def make_bc(bc, field, *values):
     for f, v in zip(comps, values):
         _check(lib().sg_field_set_dirichlet(f.h, float(v)), "sg_field_set_dirichlet")
     return bc
+
+
+class _FieldList:
+    """the fields... of samurai's save / dump / load, in order (an sg_io_t)"""
+
+    def __init__(self, fields):
+        h = ctypes.c_void_p()
+        _check(lib().sg_io_create(ctypes.byref(h)), "sg_io_create")
+        self.h = h
+        for f in fields:
+            if isinstance(f, VectorField):
+                _check(lib().sg_io_add_vector_field(h, f.h), "sg_io_add_vector_field")
+            else:
+                _check(lib().sg_io_add_field(h, f.h), "sg_io_add_field")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().sg_io_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+def _io_args(args):
+    """(path, filename, mesh, fields) from samurai's (path, filename, mesh, fields...)
+    or (filename, mesh, fields...) forms"""
+    if isinstance(args[1], MRMesh):
+        return "", str(args[0]), args[1], args[2:]
+    return str(args[0]), str(args[1]), args[2], args[3:]
+
+
+def save(*args):
+    """samurai::save(path, filename, mesh, fields...) (io/hdf5.hpp:1331-1350): <path>/<filename>.h5 and .xdmf"""
+    path, filename, mesh, fields = _io_args(args)
+    fl = _FieldList(fields)
+    _check(lib().sg_save(path.encode(), filename.encode(), mesh.h, fl.h), "sg_save")
+
+
+def dump(*args):
+    """samurai::dump(path, filename, mesh, fields...) (io/restart.hpp:188-227): a restart file"""
+    path, filename, mesh, fields = _io_args(args)
+    fl = _FieldList(fields)
+    _check(lib().sg_dump(path.encode(), filename.encode(), mesh.h, fl.h), "sg_dump")
+
+
+def restart_levels(path, filename):
+    """(dim, min_level, max_level) of a restart file"""
+    d, lo, hi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(lib().sg_restart_levels(path.encode(), filename.encode(), ctypes.byref(d), ctypes.byref(lo), ctypes.byref(hi)),
+           "sg_restart_levels")
+    return d.value, lo.value, hi.value
+
+
+def load(*args):
+    """samurai::load(path, filename, mesh, fields...) (io/restart.hpp:425-495): the mesh takes the file's leaf
+    cells and the fields their leaf values (create the mesh with restart_levels' dimension and levels)"""
+    path, filename, mesh, fields = _io_args(args)
+    fl = _FieldList(fields)
+    _check(lib().sg_load(path.encode(), filename.encode(), mesh.h, fl.h), "sg_load")
 
 
 def swap(a, b):

@@ -22,5 +22,6 @@ struct sg_field_s
 struct sg_vfield_s
 {
     sg_mesh_s* mesh = nullptr;
+    std::string name;
     std::vector<sg_field_s*> comp;
 };

@@ -120,6 +120,7 @@ extern "C"
             return SG_ERR_CAPACITY;
         }
         v->mesh = mesh;
+        v->name = name ? name : "";
         for (int c = 0; c < n_comp; ++c)
         {
             char nm[256];

@@ -187,3 +187,76 @@ def gaussian_target(seed):
 
 def cell_volumes(level, dim=2):
     return np.ldexp(1.0, -dim * level.astype(np.int64))
+
+
+def save_mesh_arrays(level, coords, max_level):
+    """Points and connectivity of samurai::save for leaf cells in for_each_cell
+    order (io/hdf5.hpp:85-144, extract_coords_and_connectivity): the corners of
+    each cell in the element order of get_element (hdf5.hpp:64-83) receive ids
+    in order of first appearance; points are (x, y, z) with z = 0 in 2D."""
+    level = np.asarray(level).astype(np.int64)
+    coords = np.asarray(coords).astype(np.int64)
+    dim = coords.shape[1]
+    if dim == 2:
+        elem = [(0, 0), (1, 0), (1, 1), (0, 1)]
+    else:
+        elem = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    shift = (max_level - level)[:, None]
+    keys = np.stack([(coords + np.array(e, np.int64)) << shift for e in elem], axis=1).reshape(-1, dim)
+    span = (1 << max_level) + 1
+    scalar = keys[:, 0] + span * keys[:, 1] + (span * span * keys[:, 2] if dim == 3 else 0)
+    _, first, inverse = np.unique(scalar, return_index=True, return_inverse=True)
+    order = np.argsort(first)
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    connectivity = rank[inverse.reshape(-1)].reshape(len(level), len(elem)).astype(np.uint64)
+    points = np.zeros((len(order), 3))
+    points[:, :dim] = np.ldexp(keys[first[order]].astype(np.float64), -max_level)
+    return points, connectivity
+
+
+def level_cell_array(rows, dim):
+    """LevelCellArray layout of one level (level_cell_array.hpp:1005-1077,
+    init_from_level_cell_list) from its x-intervals given row by row in
+    for_each_interval order as records (start, end, y[, z], index).  Returns
+    (intervals, offsets): intervals[d] lists (start, end, index) along
+    dimension d, offsets[d - 1] the offsets of dimension d >= 1.  A direct
+    restatement of the recursion: along dimension N >= 1 each coordinate of a
+    non-empty sub-grid continues the working interval when it is adjacent, or
+    starts one with index = len(offsets) - coordinate; offsets record the
+    size of the dimension below before the sub-grid is added, and a final
+    entry closes each offsets list."""
+    intervals = [[] for _ in range(dim)]
+    offsets = [[] for _ in range(dim - 1)]
+    # nested grid: coordinate -> sub-grid, the innermost holding x-intervals
+    grid = {}
+    for r in rows:
+        key = (int(r[3]), int(r[2])) if dim == 3 else (int(r[2]),)
+        node = grid
+        for k in key[:-1]:
+            node = node.setdefault(k, {})
+        node.setdefault(key[-1], []).append((int(r[0]), int(r[1]), int(r[dim + 1])))
+
+    def build(node, n):
+        cur = None
+        for coord in sorted(node):
+            prev = len(intervals[n - 1])
+            if n - 1 == 0:
+                intervals[0].extend(node[coord])
+            else:
+                build(node[coord], n - 1)
+            if cur is not None and coord == cur[1]:
+                cur[1] += 1
+            else:
+                if cur is not None:
+                    intervals[n].append(tuple(cur))
+                cur = [coord, coord + 1, len(offsets[n - 1]) - coord]
+            offsets[n - 1].append(prev)
+        if cur is not None:
+            intervals[n].append(tuple(cur))
+
+    if rows is not None and len(rows):
+        build(grid, dim - 1)
+        for d in range(dim - 1):
+            offsets[d].append(len(intervals[d]))
+    return intervals, offsets

@@ -1,10 +1,13 @@
 // demos/FiniteVolume/advection_2d.cpp of samurai, written against the
 // GB300 drop-in header: the samurai calls are the demo's own (the output and
 // CLI parts are replaced by printing the final cells).  Usage:
-//   advection_2d <pred 0|1> <out.txt> [convection]
+//   advection_2d <pred 0|1> <out.txt> [upwind|convection [<dir> <name>]]
 // With "convection" the step is the flux form of
 // demos/FiniteVolume/linear_convection.cpp: unp1 = u - dt * conv(u) with
-// conv = make_convection_upwind<decltype(u)>(a).
+// conv = make_convection_upwind<decltype(u)>(a).  With <dir> <name> the final
+// state is also written as the demo's save() does (samurai::save(path,
+// filename, mesh, u), advection_2d.cpp:46-66) and as a restart file
+// (samurai::dump), then read back with samurai::load.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -36,7 +39,7 @@ void init(Field& u)
 }
 
 template <int pred>
-int run(const char* out_path, bool flux_form)
+int run(const char* out_path, bool flux_form, const char* save_dir, const char* save_name)
 {
     constexpr std::size_t dim = 2;
     std::array<double, dim> a{{1, 1}};
@@ -84,6 +87,31 @@ int run(const char* out_path, bool flux_form)
         ++nt;
     }
 
+    if (save_dir)
+    {
+        samurai::save(save_dir, save_name, mesh, u);
+        samurai::dump(save_dir, std::string(save_name) + "_restart", mesh, u);
+        auto mesh2 = samurai::mra::make_mesh(box, config);
+        auto u2    = samurai::make_scalar_field<double>("u", mesh2);
+        samurai::load(save_dir, std::string(save_name) + "_restart", mesh2, u2);
+        std::size_t n1 = 0, n2 = 0, same = 0;
+        samurai::for_each_cell(mesh, [&](auto&) { ++n1; });
+        auto c1         = mesh.cells();
+        auto c2         = mesh2.cells();
+        const auto& cu  = u;
+        const auto& cu2 = u2;
+        n2              = c2.size();
+        for (std::size_t k = 0; k < n1 && k < n2; ++k)
+        {
+            same += (c1[k].level == c2[k].level && c1[k].indices == c2[k].indices && cu[c1[k]] == cu2[c2[k]]) ? 1 : 0;
+        }
+        if (n1 != n2 || same != n1)
+        {
+            std::fprintf(stderr, "restart differs: %zu cells, %zu loaded, %zu equal\n", n1, n2, same);
+            return 1;
+        }
+    }
+
     FILE* f = std::fopen(out_path, "w");
     if (!f)
     {
@@ -100,13 +128,15 @@ int main(int argc, char** argv)
 {
     if (argc < 3)
     {
-        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt> [convection]\n");
+        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt> [upwind|convection [<dir> <name>]]\n");
         return 2;
     }
     const bool flux_form = argc > 3 && std::string(argv[3]) == "convection";
+    const char* save_dir  = argc > 5 ? argv[4] : nullptr;
+    const char* save_name = argc > 5 ? argv[5] : nullptr;
     try
     {
-        return std::atoi(argv[1]) == 0 ? run<0>(argv[2], flux_form) : run<1>(argv[2], flux_form);
+        return std::atoi(argv[1]) == 0 ? run<0>(argv[2], flux_form, save_dir, save_name) : run<1>(argv[2], flux_form, save_dir, save_name);
     }
     catch (const std::exception& e)
     {
