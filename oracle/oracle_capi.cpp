@@ -81,9 +81,23 @@ namespace
 
 extern "C"
 {
+    void* oracle_create_periodic(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width,
+                                 double dirichlet, int periodic_mask);
+
     void* oracle_create(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width, double dirichlet)
     {
+        return oracle_create_periodic(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, dirichlet, 0);
+    }
+
+    // mesh_config<dim>().periodic({bit 0, bit 1, bit 2 of periodic_mask})
+    void* oracle_create_periodic(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width,
+                                 double dirichlet, int periodic_mask)
+    {
         oracle::MeshConfig cfg;
+        for (int d = 0; d < 3; ++d)
+        {
+            cfg.periodic[static_cast<std::size_t>(d)] = ((periodic_mask >> d) & 1) != 0;
+        }
         cfg.min_level          = min_level;
         cfg.max_level          = max_level;
         cfg.max_stencil_radius = max_stencil_radius;

@@ -21,6 +21,8 @@ def lib():
         vp, i, d, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
         L.oracle_create.restype = vp
         L.oracle_create.argtypes = [i, i, i, i, i, i, d]
+        L.oracle_create_periodic.restype = vp
+        L.oracle_create_periodic.argtypes = [i, i, i, i, i, i, d, i]
         L.oracle_destroy.argtypes = [vp]
         L.oracle_nb_cells.restype = ll
         L.oracle_nb_cells.argtypes = [vp]
@@ -70,11 +72,15 @@ MESH_IDS = {"cells": 0, "cells_and_ghosts": 1, "proj_cells": 2, "union_cells": 3
 class OracleSim:
     """One MR advection problem on the unit box, driven step by step."""
 
-    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1, dirichlet=0.0):
+    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1, dirichlet=0.0,
+                 periodic=(False, False, False)):
+        """periodic: one flag per axis (mesh_config::periodic)"""
         self.dim = dim
         self.min_level = min_level
         self.max_level = max_level
-        self.h = lib().oracle_create(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, dirichlet)
+        mask = sum(1 << d for d, p in enumerate(periodic) if p)
+        self.h = lib().oracle_create_periodic(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, dirichlet,
+                                              mask)
         if not self.h:
             raise RuntimeError("oracle_create failed")
 

@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdint>
 #include <limits>
+#include <functional>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -691,7 +692,44 @@ namespace oracle
         int graduation_width   = 1;
         int prediction_radius  = 1; // config_t::prediction_stencil_radius
         int ghost_width        = 1; // max(max_stencil_radius, prediction_radius) after parse_args
+        std::array<bool, 3> periodic{false, false, false}; // mesh_config::periodic (mesh_config.hpp)
+
+        bool any_periodic() const
+        {
+            return periodic[0] || periodic[1] || periodic[2];
+        }
     };
+
+    // detail::get_periodic_directions (mesh.hpp:44-80, graduation.hpp:37-76):
+    // every combination of {-n, +n, 0} over the periodic axes but the zero
+    // one, n = 2^level the number of cells of the unit box per axis
+    template <std::size_t D>
+    std::vector<Coord<D>> periodic_shifts(const MeshConfig& cfg, int level)
+    {
+        std::vector<Coord<D>> out;
+        const int n = 1 << level;
+        Coord<D> cur{};
+        std::function<void(int)> rec = [&](int d)
+        {
+            if (d == static_cast<int>(D))
+            {
+                out.push_back(cur);
+                return;
+            }
+            if (cfg.periodic[d])
+            {
+                cur[d] = -n;
+                rec(d + 1);
+                cur[d] = n;
+                rec(d + 1);
+            }
+            cur[d] = 0;
+            rec(d + 1);
+        };
+        rec(0);
+        out.pop_back(); // the zero shift
+        return out;
+    }
 
     constexpr int MAXL = 22; // levels 0..MAXL-1 stored (samurai's default max_level is 20)
 
@@ -764,9 +802,9 @@ namespace oracle
         }
     }
 
-    // Mesh_base::finalize_mesh (mesh.hpp:426-438) for the serial, non-periodic,
-    // unit-box case: construct_union, update_sub_mesh_impl, construct_corners,
-    // renumbering.
+    // Mesh_base::finalize_mesh (mesh.hpp:426-438) for the serial unit-box
+    // case: construct_union, update_sub_mesh_impl (with its periodic parts),
+    // construct_corners, renumbering.
     template <std::size_t D>
     void finalize_mesh(Mesh<D>& m)
     {
@@ -796,6 +834,23 @@ namespace oracle
             }
         }
         m.cag = cl;
+        // periodicity (mr/mesh.hpp:276-319): the cells translated across the
+        // periodic axes, expanded by the stencil radius, within the expanded
+        // domain -- added to the reference, not to cells_and_ghosts
+        if (cfg.any_periodic())
+        {
+            for (int level = 0; level < MAXL; ++level)
+            {
+                if (m.cells[level].empty())
+                {
+                    continue;
+                }
+                for (const auto& t : periodic_shifts<D>(cfg, level))
+                {
+                    cl[level] = uni(cl[level], inter(expand(translate(m.cells[level], t), r), expand(m.domain(level), r)));
+                }
+            }
+        }
         if (cfg.max_level != cfg.min_level)
         {
             for (int level = 0; level < MAXL; ++level)
@@ -813,6 +868,24 @@ namespace oracle
                 {
                     auto sub_cells = expand(on(m.cells[level], level - 2), p);
                     cl[level - 2]  = uni(cl[level - 2], sub_cells);
+                }
+                // periodic part (mr/mesh.hpp:356-368): translated, projected,
+                // expanded by the prediction radius, within the domain
+                if (cfg.any_periodic())
+                {
+                    for (const auto& t : periodic_shifts<D>(cfg, level))
+                    {
+                        if (level >= 1)
+                        {
+                            auto pc = inter(expand(on(translate(m.cag[level], t), level - 1), p), m.domain(level - 1));
+                            cl[level - 1] = uni(cl[level - 1], pc);
+                        }
+                        if (level - 1 > 0)
+                        {
+                            auto pc = inter(expand(on(translate(m.cells[level], t), level - 2), p), m.domain(level - 2));
+                            cl[level - 2] = uni(cl[level - 2], pc);
+                        }
+                    }
                 }
             }
             m.ref = cl;
@@ -1305,6 +1378,21 @@ namespace oracle
         }
     }
 
+    // a direction with a non-zero component along a periodic axis has no
+    // boundary (update_outer_ghost.hpp:355-366, 379, 426; apply_field_bc.hpp:74-83)
+    template <std::size_t D>
+    bool crosses_periodic(const MeshConfig& cfg, const Dir<D>& d)
+    {
+        for (int i = 0; i < static_cast<int>(D); ++i)
+        {
+            if (d[i] != 0 && cfg.periodic[i])
+            {
+                return true;
+            }
+        }
+        return false;
+    }
+
     // update_outer_ghosts(level, field) (algorithm/update_outer_ghost.hpp:339-437)
     template <std::size_t D>
     void outer_ghosts(const Mesh<D>& m, Field& u, int level, const BcConfig& bc)
@@ -1314,12 +1402,20 @@ namespace oracle
         {
             for (const auto& d : diagonal_directions<D>())
             {
+                if (crosses_periodic<D>(m.cfg, d))
+                {
+                    continue;
+                }
                 outer_corners<D>(m, u, level, d);
                 corner_below<D>(m, u, level, d);
             }
         }
         for (const auto& d : cartesian_directions<D>())
         {
+            if (crosses_periodic<D>(m.cfg, d))
+            {
+                continue;
+            }
             if (level < maxl)
             {
                 int nbc = bc.bc_stencil_size / 2;
@@ -1342,19 +1438,116 @@ namespace oracle
         {
             for (const auto& d : cartesian_directions<D>())
             {
-                further_ghosts<D>(m, u, level, d, bc);
+                if (!crosses_periodic<D>(m.cfg, d))
+                {
+                    further_ghosts<D>(m, u, level, d, bc);
+                }
             }
         }
     }
 
-    // update_ghost_mr (algorithm/update_ghost_mr.hpp:195-237)
+    // [lo[d], hi[d]) per axis at a level
+    template <std::size_t D>
+    LSet<D> box_axes(int level, const Coord<D>& lo, const Coord<D>& hi)
+    {
+        LSet<D> out(level);
+        if constexpr (D == 2)
+        {
+            for (int y = lo[1]; y < hi[1]; ++y)
+            {
+                out.rows[Key<D>{y}] = Row{{lo[0], hi[0]}};
+            }
+        }
+        else
+        {
+            for (int z = lo[2]; z < hi[2]; ++z)
+            {
+                for (int y = lo[1]; y < hi[1]; ++y)
+                {
+                    out.rows[Key<D>{y, z}] = Row{{lo[0], hi[0]}};
+                }
+            }
+        }
+        return out;
+    }
+
+    // iterate_over_periodic_ghosts (algorithm/update_periodic.hpp:27-140), axis
+    // by axis: the ghosts of [n, n + g) pair with [0, g) (shift -n) and then
+    // those of [-g, 0) with [n - g, n) (shift +n), wherever both are
+    // reference cells; the other axes span [-g, n + g).  f(ghost, inner).
+    template <std::size_t D, class F>
+    void periodic_pairs(const Mesh<D>& m, int level, F&& f)
+    {
+        const int g = m.cfg.ghost_width, n = 1 << level;
+        for (int d = 0; d < static_cast<int>(D); ++d)
+        {
+            if (!m.cfg.periodic[d])
+            {
+                continue;
+            }
+            Coord<D> lo, hi;
+            for (int k = 0; k < static_cast<int>(D); ++k)
+            {
+                lo[k] = -g;
+                hi[k] = n + g;
+            }
+            for (int side = 0; side < 2; ++side)
+            {
+                lo[d]       = side == 0 ? n : -g;
+                hi[d]       = side == 0 ? n + g : 0;
+                const int t = side == 0 ? -n : n;
+                inter(m.ref[level], box_axes<D>(level, lo, hi))
+                    .for_each_cell(
+                        [&](const Coord<D>& c)
+                        {
+                            Coord<D> q = c;
+                            q[d] += t;
+                            const long long iq = m.index(level, q);
+                            if (iq >= 0)
+                            {
+                                f(static_cast<std::size_t>(m.idx(level, c)), static_cast<std::size_t>(iq));
+                            }
+                        });
+            }
+        }
+    }
+
+    // update_ghost_periodic(level, field) (algorithm/update_periodic.hpp:19-25)
+    template <std::size_t D>
+    void update_ghost_periodic(const Mesh<D>& m, Field& u, int level)
+    {
+        if (m.cfg.any_periodic())
+        {
+            periodic_pairs<D>(m, level, [&](std::size_t gi, std::size_t ii) { u[gi] = u[ii]; });
+        }
+    }
+
+    // update_tag_periodic(level, tag) (algorithm/update_periodic.hpp:178-300)
+    template <std::size_t D>
+    void update_tag_periodic(const Mesh<D>& m, std::vector<std::uint8_t>& tag, int level)
+    {
+        if (m.cfg.any_periodic())
+        {
+            periodic_pairs<D>(m, level,
+                              [&](std::size_t gi, std::size_t ii)
+                              {
+                                  tag[gi] |= tag[ii];
+                                  tag[ii] |= tag[gi];
+                              });
+        }
+    }
+
+    // update_ghost_mr (algorithm/update_ghost_mr.hpp:195-237), serial: the
+    // subdomain exchanges are empty
     template <std::size_t D>
     void update_ghost_mr(const Mesh<D>& m, Field& u, const BcConfig& bc)
     {
         const int maxl = m.cfg.max_level;
         for (int level = maxl; level >= 0; --level)
         {
+            update_ghost_periodic<D>(m, u, level);
             outer_ghosts<D>(m, u, level, bc);
+            update_ghost_periodic<D>(m, u, level);
             if (level > 0)
             {
                 auto set = on(inter(m.ref[level], m.proj[level - 1]), level - 1);
@@ -1368,6 +1561,7 @@ namespace oracle
             auto expr        = on(inter(pred_ghosts, m.domain(level), m.ref[level - 1]), level);
             expr.for_each_cell([&](const Coord<D>& c)
                                { u[static_cast<std::size_t>(m.idx(level, c))] = predict_one<D>(m, u, level, c, m.cfg.prediction_radius); });
+            update_ghost_periodic<D>(m, u, level);
         }
     }
 
@@ -1463,12 +1657,12 @@ namespace oracle
         int graduation_iterations = 0;
     };
 
-    // make_graduation for the serial, non-periodic case with
-    // max_stencil_radius == 1 (algorithm/graduation.hpp:573-726, 245-330);
+    // make_graduation for the serial case with max_stencil_radius == 1
+    // (algorithm/graduation.hpp:573-726, 245-330);
     // the contiguous-boundary pass is a no-op for a radius of 1
     // (algorithm/graduation.hpp:378-381).
     template <std::size_t D>
-    int make_graduation(std::vector<LSet<D>>& ca, int grad_width, int max_stencil_radius)
+    int make_graduation(std::vector<LSet<D>>& ca, int grad_width, int max_stencil_radius, const MeshConfig* periodic_cfg = nullptr)
     {
         if (max_stencil_radius != 1)
         {
@@ -1498,7 +1692,17 @@ namespace oracle
                     {
                         continue;
                     }
-                    LSet<D> proj = on(expand(ca[fine], 2 * grad_width), fine - 2);
+                    // with periodic axes the fine cells also act through their translates
+                    // (graduation.hpp:309-318): the expansion and projection distribute over the union
+                    LSet<D> src = ca[fine];
+                    if (periodic_cfg && periodic_cfg->any_periodic())
+                    {
+                        for (const auto& t : periodic_shifts<D>(*periodic_cfg, fine))
+                        {
+                            src = uni(src, translate(ca[fine], t));
+                        }
+                    }
+                    LSet<D> proj = on(expand(src, 2 * grad_width), fine - 2);
                     for (int cl = fine - 2;; --cl)
                     {
                         if (!proj.empty())
@@ -1725,9 +1929,10 @@ namespace oracle
                 });
         }
 
-        // tag finalization: maximum_op (mr/operators.hpp:22-96)
+        // tag finalization: update_tag_periodic, then maximum_op (mr/adapt.hpp:348-357, mr/operators.hpp:22-96)
         for (int level = maxl; level > 0; --level)
         {
+            update_tag_periodic<D>(m, tag, level);
             auto ks = on(inter(m.cells[level], m.ref[level - 1]), level - 1);
             ks.for_each_cell(
                 [&](const Coord<D>& c)
@@ -1839,7 +2044,7 @@ namespace oracle
             nca[level] = diff(uni(uni(m.cells[level], add_m[level]), add_p[level]), uni(rem_m[level], rem_p[level]));
             nca[level].level = level;
         }
-        int gi = make_graduation<D>(nca, m.cfg.graduation_width, m.cfg.max_stencil_radius);
+        int gi = make_graduation<D>(nca, m.cfg.graduation_width, m.cfg.max_stencil_radius, &m.cfg);
         if (grad_iters)
         {
             *grad_iters = gi;
