@@ -135,6 +135,29 @@ namespace samurai
             return m_grad;
         }
 
+        // periodicity (mesh_config.hpp:279-331): one flag for every axis, or one per axis
+        auto& periodic(bool p)
+        {
+            m_periodic.fill(p);
+            return *this;
+        }
+
+        auto& periodic(const std::array<bool, dim>& p)
+        {
+            m_periodic = p;
+            return *this;
+        }
+
+        const std::array<bool, dim>& periodic() const
+        {
+            return m_periodic;
+        }
+
+        bool periodic(std::size_t i) const
+        {
+            return m_periodic[i];
+        }
+
         // mesh_config::parse_args (mesh_config.hpp:358-396), without CLI overrides
         int parsed_stencil_radius() const
         {
@@ -150,6 +173,7 @@ namespace samurai
         std::size_t m_min = 0, m_max = 6, m_grad = 1;
         int m_r           = 1;
         bool m_no_min_gw  = false;
+        std::array<bool, dim> m_periodic{};
     };
 
     // deprecated MRConfig<dim> used by the README (mr/mesh.hpp:45-72)
@@ -209,12 +233,19 @@ namespace samurai
 
         MRMesh() = default;
 
-        MRMesh(int min_level, int max_level, int stencil_radius, int prediction_radius, int graduation_width)
+        MRMesh(int min_level, int max_level, int stencil_radius, int prediction_radius, int graduation_width,
+               const std::array<bool, dim>& periodic = {})
             : m_min(min_level)
             , m_max(max_level)
         {
+            int per[3] = {0, 0, 0};
+            for (std::size_t d = 0; d < dim; ++d)
+            {
+                per[d] = periodic[d] ? 1 : 0;
+            }
             sg_mesh_t h = nullptr;
-            detail::check(sg_mesh_create(static_cast<int>(dim), min_level, max_level, stencil_radius, prediction_radius, graduation_width, &h),
+            detail::check(sg_mesh_create_periodic(static_cast<int>(dim), min_level, max_level, stencil_radius, prediction_radius, graduation_width,
+                                                  per, &h),
                           "MRMesh");
             m_h = std::shared_ptr<sg_mesh_s>(h, [](sg_mesh_t p) { sg_mesh_destroy(p); });
         }
@@ -302,7 +333,7 @@ namespace samurai
         auto make_mesh(const Box<double, Cfg::dim>&, const Cfg& cfg)
         {
             return MRMesh<Cfg>(static_cast<int>(cfg.min_level()), static_cast<int>(cfg.max_level()), cfg.parsed_stencil_radius(),
-                               Cfg::prediction_stencil_radius, static_cast<int>(cfg.graduation_width()));
+                               Cfg::prediction_stencil_radius, static_cast<int>(cfg.graduation_width()), cfg.periodic());
         }
     }
 

@@ -67,6 +67,12 @@ int sg_version(int* major, int* minor);
  * also the deprecated MRMesh<MRConfig<dim>>(box, min_level, max_level) (mr/mesh.hpp:166-181). */
 int sg_mesh_create(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width,
                    sg_mesh_t* out);
+/* the same with mesh_config<dim>().periodic({periodic[0], .., periodic[dim-1]}) (mesh_config.hpp): periodic axes have no
+ * boundary; the mesh wraps around them (mr/mesh.hpp:276-368) and the ghost update copies across them
+ * (algorithm/update_periodic.hpp).  periodic may be NULL (no periodic axis).  The flux form (SG_CONVECTION) and the
+ * adjoint are not available on meshes with a periodic axis. */
+int sg_mesh_create_periodic(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width,
+                            const int* periodic, sg_mesh_t* out);
 int sg_mesh_destroy(sg_mesh_t mesh);
 /* mesh.nb_cells(mesh_id_t::cells) and mesh.nb_cells() (= reference size) (mesh.hpp:530-550) */
 int sg_mesh_counts(sg_mesh_t mesh, long long* nb_cells, long long* nb_reference);

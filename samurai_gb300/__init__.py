@@ -53,6 +53,7 @@ def lib():
         "sg_last_error": (ctypes.c_char_p, []),
         "sg_version": (i, [pi, pi]),
         "sg_mesh_create": (i, [i, i, i, i, i, i, ctypes.POINTER(vp)]),
+        "sg_mesh_create_periodic": (i, [i, i, i, i, i, i, vp, ctypes.POINTER(vp)]),
         "sg_mesh_destroy": (i, [vp]),
         "sg_mesh_counts": (i, [vp, pl, pl]),
         "sg_mesh_get_cells": (i, [vp, vp, vp, vp, ll]),
@@ -170,6 +171,20 @@ class mesh_config:
         self._max_stencil_radius = 1
         self._graduation_width = 1
         self._disable_minimal_ghost_width = False
+        self._periodic = [False] * dim
+
+    def periodic(self, p=None):
+        """periodic(bool) fills every axis, periodic([..]) sets them one by one, periodic() reads them
+        (mesh_config.hpp:279-331)"""
+        if p is None:
+            return list(self._periodic)
+        if isinstance(p, (bool, int)):
+            self._periodic = [bool(p)] * self.dim
+        else:
+            if len(p) != self.dim:
+                raise ValueError("one periodicity flag per axis")
+            self._periodic = [bool(v) for v in p]
+        return self
 
     def min_level(self, l):
         self._min_level = l
@@ -236,16 +251,18 @@ class mra_config:
 class MRMesh:
     """samurai::MRMesh on the unit box (mr/mesh.hpp:74-211), device resident."""
 
-    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1):
+    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1, periodic=None):
         self.dim = dim
         self._min_level = min_level
         self._max_level = max_level
         self.max_stencil_radius = max_stencil_radius
         self.prediction_radius = prediction_radius
         self.graduation_width = graduation_width
+        self.periodic = [bool(p) for p in periodic][:dim] if periodic is not None else [False] * dim
         h = ctypes.c_void_p()
-        _check(lib().sg_mesh_create(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, ctypes.byref(h)),
-               "sg_mesh_create")
+        per = (ctypes.c_int * 3)(*([int(p) for p in self.periodic] + [0] * (3 - dim)))
+        _check(lib().sg_mesh_create_periodic(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, per,
+                                             ctypes.byref(h)), "sg_mesh_create")
         self.h = h
 
     @classmethod
@@ -342,7 +359,8 @@ class mra:
         if box.dim != cfg.dim:
             raise ValueError("box and config dimensions differ")
         r = cfg.parse_args()
-        return MRMesh(cfg.dim, cfg._min_level, cfg._max_level, r, cfg.prediction_stencil_radius, cfg._graduation_width)
+        return MRMesh(cfg.dim, cfg._min_level, cfg._max_level, r, cfg.prediction_stencil_radius, cfg._graduation_width,
+                      periodic=cfg._periodic)
 
 
 # ----------------------------------------------------------------- fields
@@ -661,9 +679,10 @@ class AdvectionSim:
     structure (adapt, update_ghost_mr, upwind, swap), used by the tests and
     the benchmark; mirrors the oracle's driver interface."""
 
-    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1, dirichlet=0.0):
+    def __init__(self, dim, min_level, max_level, max_stencil_radius=1, prediction_radius=1, graduation_width=1, dirichlet=0.0,
+                 periodic=None):
         self.dim = dim
-        self.mesh = MRMesh(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width)
+        self.mesh = MRMesh(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, periodic=periodic)
         self.u = make_scalar_field("u", self.mesh)
         self.unp1 = make_scalar_field("unp1", self.mesh)
         make_bc(Dirichlet(1), self.u, dirichlet)

@@ -734,6 +734,10 @@ extern "C"
         *out         = nullptr;
         sg::Ctx& uc  = u->mesh->ctx;
         const auto& cfg = uc.cfg;
+        if (uc.g.periodic)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_create: the adjoint is not available on a mesh with a periodic axis");
+        }
         auto* adj    = new (std::nothrow) sg_adjoint_s();
         if (!adj)
         {

@@ -335,6 +335,12 @@ extern "C"
 
     int sg_mesh_create(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width, sg_mesh_t* out)
     {
+        return sg_mesh_create_periodic(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, nullptr, out);
+    }
+
+    int sg_mesh_create_periodic(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width,
+                                const int* periodic, sg_mesh_t* out)
+    {
         if (!out)
         {
             return fail(SG_ERR_ARG, "sg_mesh_create: null output");
@@ -376,6 +382,12 @@ extern "C"
         c.cfg.graduation_width     = graduation_width;
         c.cfg.ghost_width          = max_stencil_radius > prediction_radius ? max_stencil_radius : prediction_radius;
         c.g                        = sg::make_geom(dim, min_level, max_level);
+        c.g.ghost_width            = c.cfg.ghost_width;
+        c.g.periodic               = 0;
+        for (int d = 0; periodic && d < dim; ++d)
+        {
+            c.g.periodic |= periodic[d] ? (1 << d) : 0;
+        }
         c.capacity                 = 32 * c.g.total_words;
         c.fuse_top                 = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS", sg::FUSE_WORDS));
         c.fuse_top_field           = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS_FIELD", sg::FUSE_WORDS_FIELD));
@@ -1167,6 +1179,10 @@ extern "C"
         if (scheme == SG_README && c.g.dim != 2)
         {
             return fail(SG_ERR_ARG, "sg_upwind: the README scheme is two-dimensional");
+        }
+        if (scheme == SG_CONVECTION && c.g.periodic)
+        {
+            return fail(SG_ERR_ARG, "sg_upwind: the flux form is not available on a mesh with a periodic axis");
         }
         unp1->f.ghosts_valid = false;
         return from_ctx(c, sg::upwind(c, u->f, unp1->f, a, dt, scheme));

@@ -83,7 +83,9 @@ namespace sg
         int min_level;
         int max_level;
         long long total_words;
-        int* err; // device word of the mesh: set by kernels that met a position outside the stored box
+        int* err;      // device word of the mesh: set by kernels that met a position outside the stored box
+        int periodic;  // bit d set: axis d is periodic (mesh_config::periodic)
+        int ghost_width; // max(max_stencil_radius, prediction_radius)
         LevelGeom lv[MAXLEV];
     };
 
@@ -437,4 +439,75 @@ namespace sg
         SG_ERR_STATE    = 4,
         SG_ERR_NOTFOUND = 5
     };
+    // ------------------------------------------------------- periodic axes
+    // A direction with a non-zero component along a periodic axis has no
+    // boundary: its boundary conditions, corners included, are skipped
+    // (algorithm/update_outer_ghost.hpp:355-366, 379, 426).
+    __host__ __device__ __forceinline__ bool crosses_periodic(const Geom& g, const int* d)
+    {
+        for (int k = 0; k < g.dim; ++k)
+        {
+            if (d[k] != 0 && ((g.periodic >> k) & 1))
+            {
+                return true;
+            }
+        }
+        return false;
+    }
+
+    // The 32 bits of bitmap `bm` (level l) at the positions of word (row, wi)
+    // moved by -t: bit b answers "is p - t in bm" for the position p of bit b.
+    // Zero where p - t leaves the stored box.
+    __device__ __forceinline__ uint32_t shifted_word(const Geom& g, const uint32_t* bm, int l, long long row, int wi, int tx, int ty, int tz)
+    {
+        const LevelGeom& L = g.lv[l];
+        long long srow;
+        if (g.dim == 2)
+        {
+            srow = row - ty;
+            if (srow < 0 || srow >= L.R)
+            {
+                return 0u;
+            }
+        }
+        else
+        {
+            int ry, rz;
+            split_row(L, row, &ry, &rz);
+            const int sy = ry - ty, sz = rz - tz;
+            if (sy < 0 || sy >= L.R || sz < 0 || sz >= L.R)
+            {
+                return 0u;
+            }
+            srow = static_cast<long long>(sz) * L.R + sy;
+        }
+        const uint32_t* rp = bm + L.woff + srow * L.W;
+        const long long o  = 32LL * wi - tx; // source bit of bit 0
+        const long long lw = o >> 5;         // floor division
+        const int sh       = static_cast<int>(o & 31);
+        const uint32_t a   = (lw >= 0 && lw < L.W) ? rp[lw] : 0u;
+        const uint32_t b   = (lw + 1 >= 0 && lw + 1 < L.W) ? rp[lw + 1] : 0u;
+        return sh ? ((a >> sh) | (b << (32 - sh))) : a;
+    }
+
+    // The union of the translates of bm by every periodic shift t (each
+    // periodic axis moved by -n, 0 or +n cells, n = 2^l, not all zero:
+    // detail::get_periodic_directions, mesh.hpp:44-80), on word (row, wi).
+    __device__ __forceinline__ uint32_t periodic_translates(const Geom& g, const uint32_t* bm, int l, long long row, int wi)
+    {
+        const int n  = g.lv[l].n;
+        uint32_t acc = 0u;
+        for (int code = 0; code < 27; ++code)
+        {
+            const int c0 = code % 3 - 1, c1 = (code / 3) % 3 - 1, c2 = code / 9 - 1;
+            if ((c0 == 0 && c1 == 0 && c2 == 0) || (g.dim == 2 && c2 != 0) || (c0 && !(g.periodic & 1)) || (c1 && !(g.periodic & 2))
+                || (c2 && !(g.periodic & 4)))
+            {
+                continue;
+            }
+            acc |= shifted_word(g, bm, l, row, wi, c0 * n, c1 * n, c2 * n);
+        }
+        return acc;
+    }
+
 } // namespace sg

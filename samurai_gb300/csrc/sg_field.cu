@@ -267,6 +267,10 @@ namespace sg
         template <class A>
         __device__ void corner_role(const Geom& g, const int* d, int l, const uint32_t* cells, const uint32_t* ref, const A& u, int parts = 3)
         {
+            if (crosses_periodic(g, d))
+            {
+                return; // no corner across a periodic axis (the test is uniform over the block)
+            }
             const int n = g.lv[l].n;
             int nfree   = 0;
             for (int k = 0; k < g.dim; ++k)
@@ -399,6 +403,10 @@ namespace sg
             const int k        = static_cast<int>(t / nf);
             int in[3], dir[3];
             face_cell(g, l, k, t - k * nf, in, dir);
+            if (crosses_periodic(g, dir))
+            {
+                return; // a periodic axis has no boundary
+            }
             const Pos pi = pos_of(g, l, in[0], in[1], in[2]);
             const int gx = in[0] + dir[0], gy = in[1] + dir[1], gz = in[2] + dir[2];
             if ((a.do_dirichlet || a.do_predict) && test(cells, pi))
@@ -544,6 +552,123 @@ namespace sg
             const long long warp0  = (rb * blockDim.x + threadIdx.x) >> 5;
             const long long nwarps = (static_cast<long long>(gridDim.x - a.nb_corner - a.nb_face) * blockDim.x) >> 5;
             project_level<DIM>(g, l, wl_ref, lo, proj, ref, u, warp0, nwarps);
+        }
+
+        // iterate_over_periodic_ghosts (algorithm/update_periodic.hpp:27-140) on
+        // axis d, one side: side 0 pairs the ghosts of [n, n + gw) with [0, gw),
+        // side 1 those of [-gw, 0) with [n - gw, n); the other axes span
+        // [-gw, n + gw).  Only pairs of two reference cells count.  Work item t
+        // of the side: gw * (n + 2 gw)^(dim-1) of them.
+        __device__ __forceinline__ bool periodic_pair(const Geom& g, int l, int d, int side, long long t, const uint32_t* ref, long long* eg,
+                                                      long long* ei)
+        {
+            const int n = g.lv[l].n, gw = g.ghost_width, span = n + 2 * gw;
+            int c[3]    = {0, 0, 0};
+            c[d]        = (side == 0 ? n : -gw) + static_cast<int>(t % gw);
+            long long r = t / gw;
+            for (int k = 0; k < g.dim; ++k)
+            {
+                if (k != d)
+                {
+                    c[k] = -gw + static_cast<int>(r % span);
+                    r /= span;
+                }
+            }
+            int q[3] = {c[0], c[1], c[2]};
+            q[d] += side == 0 ? -n : n;
+            const Pos pg = pos_of(g, l, c[0], c[1], c[2]);
+            const Pos pi = pos_of(g, l, q[0], q[1], q[2]);
+            if (!test(ref, pg) || !test(ref, pi))
+            {
+                return false;
+            }
+            *eg = elem(pg);
+            *ei = elem(pi);
+            return true;
+        }
+
+        inline long long periodic_side_items(const Geom& g, int l)
+        {
+            const long long span = g.lv[l].n + 2 * g.ghost_width;
+            return g.ghost_width * (g.dim == 2 ? span : span * span);
+        }
+
+        // update_ghost_periodic(level, field) (algorithm/update_periodic.hpp:19-25)
+        // on one axis: both sides at once (they read inner cells and write
+        // outer ghosts, so no item reads what another writes)
+        __global__ void k_periodic_copy(const Geom* __restrict__ gp, int l, int d, long long per_side, const uint32_t* ref, double* u)
+        {
+            const Geom& g     = *gp;
+            const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+            if (t >= 2 * per_side)
+            {
+                return;
+            }
+            const int side = t >= per_side ? 1 : 0;
+            long long eg, ei;
+            if (periodic_pair(g, l, d, side, t - side * per_side, ref, &eg, &ei))
+            {
+                u[eg] = u[ei];
+            }
+        }
+
+        // update_tag_periodic(level, tag) (algorithm/update_periodic.hpp:178-300)
+        // on one axis and side: both cells of a pair take the union of their tags
+        __global__ void k_periodic_tag(const Geom* __restrict__ gp, int l, int d, int side, long long per_side, const uint32_t* ref, uint8_t* tag)
+        {
+            const Geom& g     = *gp;
+            const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+            if (t >= per_side)
+            {
+                return;
+            }
+            long long eg, ei;
+            if (periodic_pair(g, l, d, side, t, ref, &eg, &ei))
+            {
+                tag[eg] |= tag[ei];
+                tag[ei] |= tag[eg];
+            }
+        }
+
+        // the periodic ghost copies of one level, axis after axis (a later axis
+        // reads the ghosts an earlier one wrote: the corners)
+        void periodic_copies(Ctx& c, const DeviceMesh& m, int l, double* u)
+        {
+            const Geom& g = c.g;
+            if (!g.periodic || l < 0 || l >= g.nlev)
+            {
+                return;
+            }
+            const long long per = periodic_side_items(g, l);
+            for (int d = 0; d < g.dim; ++d)
+            {
+                if ((g.periodic >> d) & 1)
+                {
+                    k_periodic_copy<<<static_cast<int>((2 * per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.d_geom, l, d, per, m.ref, u);
+                    ++c.n_launches;
+                }
+            }
+        }
+
+        void periodic_tags(Ctx& c, const DeviceMesh& m, int l)
+        {
+            const Geom& g = c.g;
+            if (!g.periodic || l < 0 || l >= g.nlev)
+            {
+                return;
+            }
+            const long long per = periodic_side_items(g, l);
+            for (int d = 0; d < g.dim; ++d)
+            {
+                if ((g.periodic >> d) & 1)
+                {
+                    for (int side = 0; side < 2; ++side)
+                    {
+                        k_periodic_tag<<<static_cast<int>((per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.d_geom, l, d, side, per, m.ref, c.tag);
+                        ++c.n_launches;
+                    }
+                }
+            }
         }
 
         struct GhostChainArgs
@@ -1393,6 +1518,28 @@ namespace sg
         int ghost_launches(Ctx& c, DeviceMesh& m, const A& u, bool has_bc, double bcv, int ft, bool split, After after)
         {
             const Geom& g   = c.g;
+            if (g.periodic)
+            {
+                // the periodic copies sit between the levels of both passes: no
+                // level is fused into a one-block chain
+                ft = -2 * MAXLEV;
+            }
+            // update_ghost_periodic after the boundary conditions of a level and
+            // after its prediction (update_ghost_mr.hpp:205-234).  The copy the
+            // reference also makes before the boundary conditions is overwritten
+            // by this one before anything reads it: the boundary conditions of a
+            // serial run read and write no ghost across a periodic axis.
+            auto periodic = [&](int lev)
+            {
+                if constexpr (std::is_same<A, ValAcc>::value)
+                {
+                    if (g.periodic)
+                    {
+                        periodic_copies(c, m, lev, u.u);
+                        after();
+                    }
+                }
+            };
             const int minl  = c.cfg.min_level;
             const int maxl  = c.cfg.max_level;
             const int lmin  = minl >= 2 ? minl - 2 : 0; // no reference cell below min_level-2
@@ -1448,6 +1595,7 @@ namespace sg
                     ++c.n_launches;
                     after();
                 }
+                periodic(l);
             }
             const int lp0 = lmin > 1 ? lmin : 1;
             int lp        = lp0;
@@ -1497,6 +1645,7 @@ namespace sg
                 }
                 ++c.n_launches;
                 after();
+                periodic(lp);
             }
             return check(c, "update_ghost_mr");
         }
@@ -1612,8 +1761,12 @@ namespace sg
                 // has a leaf child, so the operator has nothing to do there
                 const int lstop = std::max(1, c.cfg.min_level);
                 int l           = maxl;
-                for (; l >= lstop && l - 1 > c.fuse_top_max; --l)
+                // periodic axes: update_tag_periodic before each level's operator
+                // (mr/adapt.hpp:348-357), so no level is fused into a one-block chain
+                const int top   = g.periodic ? -2 * MAXLEV : c.fuse_top_max;
+                for (; l >= lstop && l - 1 > top; --l)
                 {
+                    periodic_tags(c, m, l);
                     if (g.dim == 2)
                     {
                         k_maximum<2><<<blocks_words(c, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
@@ -1635,6 +1788,11 @@ namespace sg
                         k_maximum_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     ++c.n_launches;
+                }
+                // the levels below hold no operator but still exchange their tags
+                for (int lt = lstop - 1; g.periodic && lt >= 1; --lt)
+                {
+                    periodic_tags(c, m, lt);
                 }
             }
             timer_stop(c, T_FINALIZE);

@@ -486,6 +486,19 @@ namespace sg
         {
             cudaMemcpyAsync(ref, cag, bytes, cudaMemcpyDeviceToDevice, c.stream);
             cudaMemsetAsync(proj, 0, bytes, c.stream);
+            if (g.periodic)
+            {
+                // the translated cells expanded by the stencil radius, within the
+                // expanded domain (mr/mesh.hpp:294-317)
+                st = launch_words(c, minl, maxl,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                  { ref[w] |= periodic_translates(g, cag, l, row, wi) & box_mask(g, l, row, wi, r, r); },
+                                  "ref_periodic");
+                if (st)
+                {
+                    return st;
+                }
+            }
             return scan_rank(c, m);
         }
 
@@ -545,6 +558,60 @@ namespace sg
         if (st)
         {
             return st;
+        }
+
+        if (g.periodic)
+        {
+            // periodic parts of the reference (mr/mesh.hpp:294-317, 356-368): the
+            // translates of cells_and_ghosts within the domain expanded by the
+            // stencil radius, and those of the two prediction-ghost sets (the
+            // dilations above, written in full into scratch bitmaps) within the
+            // domain.  translate commutes with on() and the dilations.
+            uint32_t* pa = c.t0;
+            uint32_t* pb = c.t1; // cells_and_ghosts.on(l) is no longer needed
+            if (g.dim == 2)
+            {
+                uint32_t* t2 = c.t2;
+                st           = launch_words(c, lmin, maxl,
+                                            [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                            {
+                                                pa[w] = (l >= t1lo && l <= t1hi) ? dilate_xy_word(g, t1, l, row, wi, p) : 0u;
+                                                t2[w] = dilate_xy_word(g, hc2, l, row, wi, p);
+                                            },
+                                            "ref_periodic_sources");
+                pb = t2;
+            }
+            else
+            {
+                uint32_t* t2 = c.t2;
+                uint32_t* t3 = c.t3;
+                st           = launch_words(c, lmin, maxl,
+                                            [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                            {
+                                                pa[w] = dilate_z_word(g, t2, l, row, wi, p);
+                                                pb[w] = dilate_z_word(g, t3, l, row, wi, p);
+                                            },
+                                            "ref_periodic_sources");
+            }
+            if (!st)
+            {
+                st = launch_words(c, lmin, maxl,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                  {
+                                      uint32_t v = ref[w];
+                                      if (l >= minl)
+                                      {
+                                          v |= periodic_translates(g, cag, l, row, wi) & box_mask(g, l, row, wi, r, r);
+                                      }
+                                      v |= (periodic_translates(g, pa, l, row, wi) | periodic_translates(g, pb, l, row, wi)) & box_mask(g, l, row, wi, 0, 0);
+                                      ref[w] = v;
+                                  },
+                                  "ref_periodic");
+            }
+            if (st)
+            {
+                return st;
+            }
         }
 
         // children of the projection cells, bottom-up:
@@ -776,6 +843,24 @@ namespace sg
         if (st)
         {
             return st;
+        }
+        if (g.periodic)
+        {
+            // with periodic axes the finer cells also act through their
+            // translates (graduation.hpp:309-318): ec1 gains its translates
+            // within the domain (translation commutes with the dilation and
+            // with on(), so the chain below carries them down); the coarsened
+            // cells in hcn are no longer needed and take the result
+            const uint32_t* src = ec1;
+            st                  = launch_words(c, elo, ehi,
+                                               [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                               { hcn[w] = src[w] | (periodic_translates(g, src, l, row, wi) & box_mask(g, l, row, wi, 0, 0)); },
+                                               "grad_periodic");
+            if (st)
+            {
+                return st;
+            }
+            ec1 = hcn;
         }
         // d[l] = (ec1[l+1] | d[l+1]).on(l), levels max-2 .. min_level; d and rr
         // are written on every word of those levels and read as 0 outside them
