@@ -427,24 +427,84 @@ namespace sg
         const int minl = c.cfg.min_level;
         const int lmin = minl >= 2 ? minl - 2 : 0; // lowest level of the reference
 
-        // cells with a leaf child (levels min-1 .. max-1) / grandchild (min-2 .. max-2)
-        st = launch_words(c, std::max(minl - 1, 0), maxl - 1,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { hc[w] = coarsen_word(g, cells, l, row, wi); },
-                          "hc");
+        // Passes that read the same inputs share a launch:
+        //  1. hc = cells[l+1].on(l) (levels min-1 .. max-1: cells with a leaf
+        //     child) and the expansion of the cells by the stencil radius
+        //     (cells_and_ghosts, levels min .. max; in 3D its xy part);
+        //  2. hc2 = hc.on(l) (cells with a leaf grandchild, min-2 .. max-2) with,
+        //     in 2D, cells_and_ghosts.on(l) (t1, min-1 .. max-1) and, in 3D, the
+        //     z part of cells_and_ghosts;
+        //  3. (3D) t1 = cells_and_ghosts.on(l).
+        const int hlo  = std::max(minl - 1, 0), hhi = maxl - 1;
+        const int h2lo = std::max(minl - 2, 0), h2hi = maxl - 2;
+        const int t1lo = std::max(minl - 1, 0), t1hi = maxl - 1; // t1 is read on these levels only
+        uint32_t* t0   = c.t0;
+        uint32_t* cxy  = (g.dim == 2) ? cag : t0;
+        st = launch_words(c, std::min(hlo, minl), maxl,
+                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                          {
+                              if (l >= hlo && l <= hhi)
+                              {
+                                  hc[w] = coarsen_word(g, cells, l, row, wi);
+                              }
+                              if (l >= minl)
+                              {
+                                  cxy[w] = dilate_xy_word(g, cells, l, row, wi, r);
+                              }
+                          },
+                          "hc_cag");
         if (st)
         {
             return st;
         }
-        st = launch_words(c, std::max(minl - 2, 0), maxl - 2,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { hc2[w] = coarsen_word(g, hc, l, row, wi); },
-                          "hc2");
+        if (g.dim == 2)
+        {
+            const bool with_t1 = multi;
+            const int lo2      = with_t1 ? std::min(h2lo, t1lo) : h2lo;
+            const int hi2      = with_t1 ? std::max(h2hi, t1hi) : h2hi;
+            st                 = launch_words(c, lo2, hi2,
+                                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                              {
+                                                  if (l >= h2lo && l <= h2hi)
+                                                  {
+                                                      hc2[w] = coarsen_word(g, hc, l, row, wi);
+                                                  }
+                                                  if (with_t1 && l >= t1lo && l <= t1hi)
+                                                  {
+                                                      t1[w] = coarsen_word(g, cag, l, row, wi);
+                                                  }
+                                              },
+                                              "hc2_cag_on");
+        }
+        else
+        {
+            st = launch_words(c, std::min(h2lo, minl), maxl,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                              {
+                                  if (l >= h2lo && l <= h2hi)
+                                  {
+                                      hc2[w] = coarsen_word(g, hc, l, row, wi);
+                                  }
+                                  if (l >= minl)
+                                  {
+                                      cag[w] = dilate_z_word(g, t0, l, row, wi, r);
+                                  }
+                              },
+                              "hc2_cag_z");
+            if (!st && multi)
+            {
+                st = launch_words(c, t1lo, t1hi,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { t1[w] = coarsen_word(g, cag, l, row, wi); },
+                                  "cag_on");
+            }
+        }
         if (st)
         {
             return st;
         }
 
-        // union cells, top-down: union[l] = (cells[l+1] | union[l+1]).on(l)
-        cudaMemsetAsync(uni, 0, bytes, c.stream);
+        // union cells, top-down: union[l] = (cells[l+1] | union[l+1]).on(l) on
+        // levels max-1 .. 0; union[max] is never written and stays zero
         if (maxl >= 1)
         {
             st = launch_chain(c, maxl - 1, 0,
@@ -455,31 +515,6 @@ namespace sg
             {
                 return st;
             }
-        }
-
-        // cells_and_ghosts: box expansion of the cells by max_stencil_radius
-        if (g.dim == 2)
-        {
-            st = launch_words(c, minl, maxl,
-                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = dilate_xy_word(g, cells, l, row, wi, r); },
-                              "cag");
-        }
-        else
-        {
-            uint32_t* t0 = c.t0;
-            st           = launch_words(c, minl, maxl,
-                                        [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { t0[w] = dilate_xy_word(g, cells, l, row, wi, r); },
-                                        "cag_xy");
-            if (!st)
-            {
-                st = launch_words(c, minl, maxl,
-                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { cag[w] = dilate_z_word(g, t0, l, row, wi, r); },
-                                  "cag_z");
-            }
-        }
-        if (st)
-        {
-            return st;
         }
 
         if (!multi)
@@ -502,18 +537,8 @@ namespace sg
             return scan_rank(c, m);
         }
 
-        // prediction ghosts: cag[l+1].on(l) expanded by p within the expanded
-        // domain, and cells[l+2].on(l) expanded by p
-        // t1 = cag[l+1].on(l) on levels min-1 .. max-1; the other levels of the
-        // scratch bitmap are not read below
-        const int t1lo = std::max(minl - 1, 0), t1hi = maxl - 1;
-        st = launch_words(c, t1lo, t1hi,
-                          [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { t1[w] = coarsen_word(g, cag, l, row, wi); },
-                          "cag_on");
-        if (st)
-        {
-            return st;
-        }
+        // prediction ghosts: cag[l+1].on(l) (= t1, above) expanded by p within the
+        // expanded domain, and cells[l+2].on(l) expanded by p
         // the reference starts at level min-2: cag (min .. max), t1 (min-1 ..
         // max-1) and hc2 (min-2 .. max-2)
         if (g.dim == 2)
@@ -645,6 +670,9 @@ namespace sg
                                   }
                                   const long long cw = C.woff + ((g.dim == 2) ? ry : static_cast<long long>(rz) * C.R + ry) * C.W + wc;
                                   const uint32_t pc  = ref[cw] & uni[cw];
+                                  // proj_cells of the coarse level, final once the chain has passed it;
+                                  // the fine words of one coarse word all write this same value
+                                  proj[cw]           = pc;
                                   const uint32_t add = spread16(((k + 1) & 1) ? (pc >> 16) : pc);
                                   if (add)
                                   {
@@ -657,10 +685,14 @@ namespace sg
                 return st;
             }
         }
-        st = launch_words(c, lmin, maxl, [=] __device__(const Geom&, int, long long w, long long, int) { proj[w] = ref[w] & uni[w]; }, "proj");
-        if (st)
+        if (maxl < ref_lo)
         {
-            return st;
+            // no chain ran: proj_cells = reference & union directly
+            st = launch_words(c, lmin, maxl, [=] __device__(const Geom&, int, long long w, long long, int) { proj[w] = ref[w] & uni[w]; }, "proj");
+            if (st)
+            {
+                return st;
+            }
         }
         return scan_rank(c, m);
     }

@@ -1,10 +1,12 @@
 // demos/FiniteVolume/advection_2d.cpp of samurai, written against the
 // GB300 drop-in header: the samurai calls are the demo's own (the output and
 // CLI parts are replaced by printing the final cells).  Usage:
-//   advection_2d <pred 0|1> <out.txt> [upwind|convection [<dir> <name>]]
+//   advection_2d <pred 0|1> <out.txt> [upwind|convection|periodic [<dir> <name>]]
 // With "convection" the step is the flux form of
 // demos/FiniteVolume/linear_convection.cpp: unp1 = u - dt * conv(u) with
-// conv = make_convection_upwind<decltype(u)>(a).  With <dir> <name> the final
+// conv = make_convection_upwind<decltype(u)>(a); "periodic" runs the upwind
+// operator on a mesh periodic along both axes (mesh_config::periodic(true)).
+// With <dir> <name> the final
 // state is also written as the demo's save() does (samurai::save(path,
 // filename, mesh, u), advection_2d.cpp:46-66) and as a restart file
 // (samurai::dump), then read back with samurai::load.
@@ -39,7 +41,7 @@ void init(Field& u)
 }
 
 template <int pred>
-int run(const char* out_path, bool flux_form, const char* save_dir, const char* save_name)
+int run(const char* out_path, bool flux_form, bool periodic, const char* save_dir, const char* save_name)
 {
     constexpr std::size_t dim = 2;
     std::array<double, dim> a{{1, 1}};
@@ -49,6 +51,10 @@ int run(const char* out_path, bool flux_form, const char* save_dir, const char* 
 
     const samurai::Box<double, dim> box({0., 0.}, {1., 1.});
     auto config = samurai::mesh_config<dim, pred>().min_level(4).max_level(10).max_stencil_size(2).disable_minimal_ghost_width();
+    if (periodic)
+    {
+        config.periodic(true);
+    }
     auto mesh   = samurai::mra::make_mesh(box, config);
     auto u      = samurai::make_scalar_field<double>("u", mesh);
     init(u);
@@ -128,15 +134,17 @@ int main(int argc, char** argv)
 {
     if (argc < 3)
     {
-        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt> [upwind|convection [<dir> <name>]]\n");
+        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt> [upwind|convection|periodic [<dir> <name>]]\n");
         return 2;
     }
     const bool flux_form = argc > 3 && std::string(argv[3]) == "convection";
+    const bool periodic  = argc > 3 && std::string(argv[3]) == "periodic";
     const char* save_dir  = argc > 5 ? argv[4] : nullptr;
     const char* save_name = argc > 5 ? argv[5] : nullptr;
     try
     {
-        return std::atoi(argv[1]) == 0 ? run<0>(argv[2], flux_form, save_dir, save_name) : run<1>(argv[2], flux_form, save_dir, save_name);
+        return std::atoi(argv[1]) == 0 ? run<0>(argv[2], flux_form, periodic, save_dir, save_name)
+                                       : run<1>(argv[2], flux_form, periodic, save_dir, save_name);
     }
     catch (const std::exception& e)
     {

@@ -132,3 +132,27 @@ def test_vector_demo_matches_oracle(tmp_path, relative):
     assert np.array_equal(rows[:, 1:3].astype(int), co)
     assert np.array_equal(rows[:, 3], o.cell_values())
     assert np.array_equal(rows[:, 4], o.cell_values_k(k1))
+
+
+@pytest.mark.gpu
+def test_demo_periodic_matches_oracle(tmp_path):
+    """The demo on a mesh periodic along both axes (config.periodic(true) in
+    the C++ header), against the oracle running the same loop."""
+    from advection_cases import demo_time_loop, disc
+    from oracle.pyoracle import OracleSim
+
+    exe = compile_demo(tmp_path)
+    out = os.path.join(str(tmp_path), "out.txt")
+    subprocess.check_call([exe, "1", out, "periodic"])
+    lines = open(out).read().split("\n")
+    rows = np.array([[float(v) for v in l.split()] for l in lines[1:] if l.strip()])
+    o = OracleSim(2, 4, 10, 1, 1, periodic=(True, True, False))
+    lv, co, _ = o.cells()
+    o.set_cell_values(disc(lv, co))
+    o.adapt(2e-4, 1.0)
+    nt = demo_time_loop(o, 0.5 / 1024, 0.01, 2e-4, 1.0, (1.0, 1.0))
+    assert int(lines[0]) == nt
+    lv, co, _ = o.cells()
+    assert np.array_equal(rows[:, 0].astype(int), lv)
+    assert np.array_equal(rows[:, 1:3].astype(int), co)
+    assert np.array_equal(rows[:, 3], o.cell_values())
