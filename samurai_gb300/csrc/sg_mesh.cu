@@ -551,7 +551,10 @@ namespace sg
                                   {
                                       v |= dilate_xy_word(g, t1, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
                                   }
-                                  v |= dilate_xy_word(g, hc2, l, row, wi, p);
+                                  if (l >= h2lo && l <= h2hi) // hc2 is empty elsewhere
+                                  {
+                                      v |= dilate_xy_word(g, hc2, l, row, wi, p);
+                                  }
                                   ref[w] = v;
                               },
                               "ref0");
@@ -564,7 +567,7 @@ namespace sg
                                         [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                                         {
                                             t2[w] = (l >= t1lo && l <= t1hi) ? dilate_xy_word(g, t1, l, row, wi, p) : 0u;
-                                            t3[w] = dilate_xy_word(g, hc2, l, row, wi, p);
+                                            t3[w] = (l >= h2lo && l <= h2hi) ? dilate_xy_word(g, hc2, l, row, wi, p) : 0u;
                                         },
                                         "ref0_xy");
             if (!st)
@@ -573,8 +576,15 @@ namespace sg
                                   [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                                   {
                                       uint32_t v = cag[w];
-                                      v |= dilate_z_word(g, t2, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
-                                      v |= dilate_z_word(g, t3, l, row, wi, p);
+                                      // t2 and t3 are empty outside the levels of t1 and hc2
+                                      if (l >= t1lo && l <= t1hi)
+                                      {
+                                          v |= dilate_z_word(g, t2, l, row, wi, p) & box_mask(g, l, row, wi, p, p);
+                                      }
+                                      if (l >= h2lo && l <= h2hi)
+                                      {
+                                          v |= dilate_z_word(g, t3, l, row, wi, p);
+                                      }
                                       ref[w] = v;
                                   },
                                   "ref0_z");
