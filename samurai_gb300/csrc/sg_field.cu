@@ -60,6 +60,117 @@ namespace sg
             }
         }
 
+        // Compacted traversal for the FP64-heavy kernels.  On the traversal
+        // above a warp works on one word and the lanes of its empty bits idle
+        // while the others issue FP64 instructions, which the narrow FP64 pipe
+        // executes for the whole warp (42 % of the lanes of the leaf-cell
+        // words of the 2D max_level-12 workload hold a cell).  Here a warp
+        // takes ch consecutive words of the list, ranks their set bits with a
+        // warp prefix sum and processes them 32 at a time, one per lane.
+        // item(valid, w, b) is called by every lane of the warp (so that it
+        // may shuffle); only lanes with valid set hold an item, bit b of word w.
+        constexpr unsigned FULL_MASK = 0xffffffffu;
+
+        // words per warp: the largest power of two (<= 32) that still leaves
+        // every warp of the launch a chunk; 1 on lists shorter than two words
+        // per warp, where the launch is latency-bound and the compaction does
+        // not pay
+        __device__ __forceinline__ int items_chunk(long long n, long long nwarps)
+        {
+            const long long per = n / (nwarps > 0 ? nwarps : 1);
+            int ch              = 1;
+            while (ch < 32 && 2 * ch <= per)
+            {
+                ch <<= 1;
+            }
+            return ch;
+        }
+
+        template <class WordF, class ItemF>
+        __device__ __forceinline__ void warp_items(const int* list, long long begin, long long end, long long warp0, long long nwarps, int ch,
+                                                   WordF word_of, ItemF item)
+        {
+            const int lane = threadIdx.x & 31;
+            for (long long c0 = begin + warp0 * ch; c0 < end; c0 += nwarps * ch)
+            {
+                long long w = 0;
+                uint32_t m  = 0u;
+                if (lane < ch && c0 + lane < end)
+                {
+                    w = __ldg(list + c0 + lane);
+                    m = word_of(w);
+                }
+                int incl = __popc(m); // inclusive prefix of the item counts over the lanes
+                for (int o = 1; o < 32; o <<= 1)
+                {
+                    const int t = __shfl_up_sync(FULL_MASK, incl, o);
+                    if (lane >= o)
+                    {
+                        incl += t;
+                    }
+                }
+                const int total = __shfl_sync(FULL_MASK, incl, 31);
+                for (int base = 0; base < total; base += 32)
+                {
+                    const int j = base + lane;
+                    // the word of item j: the first lane whose inclusive prefix exceeds j
+                    int lo_k = 0, hi_k = 31;
+                    for (int s = 0; s < 5; ++s)
+                    {
+                        const int mid = (lo_k + hi_k) >> 1;
+                        if (__shfl_sync(FULL_MASK, incl, mid) > j)
+                        {
+                            hi_k = mid;
+                        }
+                        else
+                        {
+                            lo_k = mid + 1;
+                        }
+                    }
+                    const long long wk = __shfl_sync(FULL_MASK, w, lo_k);
+                    const uint32_t mk  = __shfl_sync(FULL_MASK, m, lo_k);
+                    const int before   = __shfl_sync(FULL_MASK, incl, lo_k) - __popc(mk);
+                    const bool valid   = j < total;
+                    // position of set bit number r (from 0) of mk
+                    int r = valid ? j - before : 0, pos = 0;
+                    uint32_t x = mk;
+                    for (int sh = 16; sh > 0; sh >>= 1)
+                    {
+                        const int cnt = __popc(x & ((1u << sh) - 1u));
+                        if (r >= cnt)
+                        {
+                            r -= cnt;
+                            x >>= sh;
+                            pos += sh;
+                        }
+                    }
+                    item(valid, wk, pos);
+                }
+            }
+        }
+
+        // warp_list with the compacted traversal where the list is long enough:
+        // cell(w, b) for every set bit
+        template <class WordF, class CellF>
+        __device__ __forceinline__ void warp_list_compact(const int* list, long long begin, long long end, long long warp0, long long nwarps,
+                                                          WordF word_of, CellF cell)
+        {
+            const int ch = items_chunk(end - begin, nwarps);
+            if (ch == 1)
+            {
+                warp_list(list, begin, end, warp0, nwarps, word_of, cell);
+                return;
+            }
+            warp_items(list, begin, end, warp0, nwarps, ch, word_of,
+                       [&](bool valid, long long w, int b)
+                       {
+                           if (valid)
+                           {
+                               cell(w, b);
+                           }
+                       });
+        }
+
         __device__ __forceinline__ long long warp_id()
         {
             return (blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) >> 5;
@@ -499,7 +610,7 @@ namespace sg
         __device__ __forceinline__ void predict_level(const Geom& g, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
                                                       const uint32_t* proj, const uint32_t* ref, const A& u, long long warp0, long long nwarps)
         {
-            warp_list(wl_ref, lo[LO_REF + l], lo[LO_REF + l + 1], warp0, nwarps,
+            warp_list_compact(wl_ref, lo[LO_REF + l], lo[LO_REF + l + 1], warp0, nwarps,
                       [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, l, w);
@@ -759,7 +870,7 @@ namespace sg
             {
                 return;
             }
-            warp_list(wl, lo[LO_REF + l0], lo[LO_REF + le + 1], warp_id(), warp_count(), [&](long long w) { return ref[w] & (hc[w] | hc2[w]); },
+            warp_list_compact(wl, lo[LO_REF + l0], lo[LO_REF + le + 1], warp_id(), warp_count(), [&](long long w) { return ref[w] & (hc[w] | hc2[w]); },
                       [&](long long w, int b)
                       {
                           const int l    = level_of(g, w);
@@ -1091,75 +1202,82 @@ namespace sg
         __global__ void k_upwind(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* cells, const double* __restrict__ u,
                                  double* __restrict__ unp1, UpwindArgs p)
         {
-            const Geom& g       = *gp;
-            const int lane      = threadIdx.x & 31;
-            const long long n   = lo[LO_CELLS + g.nlev];
-            for (long long i = lo[LO_CELLS] + warp_id(); i < n; i += warp_count())
-            {
-                const long long w  = __ldg(wl + i);
-                const uint32_t v   = __ldg(cells + w);
-                const bool is_cell = (v >> lane) & 1u;
-                const int l        = level_of(g, w);
-                const LevelGeom& L = g.lv[l];
-                const long long e  = 32 * w + lane;
-                const long long sy = 32LL * L.W;
-                const long long sz = sy * L.R;
-                if (p.scheme == 1)
-                {
-                    if (is_cell)
-                    {
-                        const double uc = u[e];
-                        double s        = uc - u[e - 1];
-                        s               = s + uc;
-                        s               = s - u[e - sy];
-                        if (DIM == 3)
-                        {
-                            s = s + uc;
-                            s = s - u[e - sz];
-                        }
-                        unp1[e] = uc - (p.dt * pow2(l)) * s;
-                    }
-                    continue;
-                }
-                double uc = 0., rf = 0.;
-                if (is_cell)
-                {
-                    uc              = u[e];
-                    const double ur = u[e + 1];
-                    rf              = p.ha[0] * (uc + ur) + p.hb[0] * (uc - ur);
-                }
-                const double rf_left = __shfl_up_sync(0xffffffffu, rf, 1);
-                if (!is_cell)
-                {
-                    continue;
-                }
-                double lf;
-                if (lane > 0 && ((v >> (lane - 1)) & 1u))
-                {
-                    lf = rf_left;
-                }
-                else
-                {
-                    const double ul = u[e - 1];
-                    lf              = p.ha[0] * (ul + uc) + p.hb[0] * (ul - uc);
-                }
-                const double ud = u[e - sy], uu = u[e + sy];
-                const double df = p.ha[1] * (ud + uc) + p.hb[1] * (ud - uc);
-                const double uf = p.ha[1] * (uc + uu) + p.hb[1] * (uc - uu);
-                double s        = -lf + rf;
-                s               = s + -df;
-                s               = s + uf;
-                if (DIM == 3)
-                {
-                    const double uf2 = u[e - sz], ub2 = u[e + sz];
-                    const double ff  = p.ha[2] * (uf2 + uc) + p.hb[2] * (uf2 - uc);
-                    const double bf  = p.ha[2] * (uc + ub2) + p.hb[2] * (uc - ub2);
-                    s                = s + -ff;
-                    s                = s + bf;
-                }
-                const double up = scale2(s, l); // s / dx with dx = 2^-l
-                unp1[e]         = uc - p.dt * up;
-            }
+            const Geom& g  = *gp;
+            const int lane = threadIdx.x & 31;
+            // the leaf cells compacted over the lanes (warp_items); a cell's left
+            // flux is its left neighbour's right flux when that neighbour is the
+            // previous lane's cell (the same face, the same expression)
+            const long long nb = lo[LO_CELLS], ne = lo[LO_CELLS + g.nlev];
+            warp_items(wl, nb, ne, warp_id(), warp_count(), items_chunk(ne - nb, warp_count()), [&](long long w) { return __ldg(cells + w); },
+                           [&](bool valid, long long w, int b)
+                           {
+                               int l = 0;
+                               long long e = 0, sy = 0, sz = 0;
+                               double uc = 0., rf = 0.;
+                               if (valid)
+                               {
+                                   l                  = level_of(g, w);
+                                   const LevelGeom& L = g.lv[l];
+                                   e                  = 32 * w + b;
+                                   sy                 = 32LL * L.W;
+                                   sz                 = sy * L.R;
+                                   uc                 = u[e];
+                               }
+                               if (p.scheme == 1)
+                               {
+                                   if (valid)
+                                   {
+                                       double s = uc - u[e - 1];
+                                       s        = s + uc;
+                                       s        = s - u[e - sy];
+                                       if (DIM == 3)
+                                       {
+                                           s = s + uc;
+                                           s = s - u[e - sz];
+                                       }
+                                       unp1[e] = uc - (p.dt * pow2(l)) * s;
+                                   }
+                                   return;
+                               }
+                               if (valid)
+                               {
+                                   const double ur = u[e + 1];
+                                   rf              = p.ha[0] * (uc + ur) + p.hb[0] * (uc - ur);
+                               }
+                               const double rf_left = __shfl_up_sync(FULL_MASK, rf, 1);
+                               const long long wl_  = __shfl_up_sync(FULL_MASK, w, 1);
+                               const int bl         = __shfl_up_sync(FULL_MASK, valid ? b : -2, 1);
+                               if (!valid)
+                               {
+                                   return;
+                               }
+                               double lf;
+                               if (lane > 0 && wl_ == w && bl == b - 1)
+                               {
+                                   lf = rf_left;
+                               }
+                               else
+                               {
+                                   const double ul = u[e - 1];
+                                   lf              = p.ha[0] * (ul + uc) + p.hb[0] * (ul - uc);
+                               }
+                               const double ud = u[e - sy], uu = u[e + sy];
+                               const double df = p.ha[1] * (ud + uc) + p.hb[1] * (ud - uc);
+                               const double uf = p.ha[1] * (uc + uu) + p.hb[1] * (uc - uu);
+                               double s        = -lf + rf;
+                               s               = s + -df;
+                               s               = s + uf;
+                               if (DIM == 3)
+                               {
+                                   const double uf2 = u[e - sz], ub2 = u[e + sz];
+                                   const double ff  = p.ha[2] * (uf2 + uc) + p.hb[2] * (uf2 - uc);
+                                   const double bf  = p.ha[2] * (uc + ub2) + p.hb[2] * (uc - ub2);
+                                   s                = s + -ff;
+                                   s                = s + bf;
+                               }
+                               const double up = scale2(s, l); // s / dx with dx = 2^-l
+                               unp1[e]         = uc - p.dt * up;
+                           });
         }
 
 
