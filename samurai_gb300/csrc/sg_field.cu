@@ -591,7 +591,7 @@ namespace sg
                                                       const A& u, long long warp0, long long nwarps)
         {
             const int lc = l - 1;
-            warp_list(wl_ref, lo[LO_REF + lc], lo[LO_REF + lc + 1], warp0, nwarps,
+            warp_list_compact(wl_ref, lo[LO_REF + lc], lo[LO_REF + lc + 1], warp0, nwarps,
                       [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, lc, w);
@@ -1126,7 +1126,7 @@ namespace sg
                                         const uint32_t* ncells, const uint32_t* oref, const uint32_t* ocells, const uint32_t* ohc, A uo, A un)
         {
             const Geom& g = *gp;
-            warp_list(wl, lo[LO_REF], lo[LO_REF + g.nlev], warp_id(), warp_count(), [&](long long w) { return nref[w]; },
+            warp_list_compact(wl, lo[LO_REF], lo[LO_REF + g.nlev], warp_id(), warp_count(), [&](long long w) { return nref[w]; },
                       [&](long long w, int b)
                       {
                           const long long e = 32 * w + b;
@@ -1308,161 +1308,156 @@ namespace sg
                                      double* __restrict__ unp1, UpwindArgs p, const double* __restrict__ av)
         {
             const Geom& g     = *gp;
-            const int lane    = threadIdx.x & 31;
             const long long n = lo[LO_CELLS + g.nlev];
-            for (long long i = lo[LO_CELLS] + warp_id(); i < n; i += warp_count())
-            {
-                const long long w = __ldg(wl + i);
-                if (!((__ldg(cells + w) >> lane) & 1u))
-                {
-                    continue;
-                }
-                const int m        = level_of(g, w);
-                const Cell cc      = cell_of(g, m, w, lane);
-                const int c[3]     = {cc.x, cc.y, cc.z};
-                const long long eX = 32 * w + lane;
-                const double uX    = u[eX];
-                const int nm       = 1 << m;
-                auto leaf = [&](int l, const int* q) { return l >= 0 && l <= g.max_level && test(cells, g, l, q[0], q[1], DIM == 3 ? q[2] : 0); };
-                auto val  = [&](int l, const int* q) { return u[elem_at(g, l, q[0], q[1], DIM == 3 ? q[2] : 0)]; };
-                double acc = 0.;
-                for (int d = 0; d < DIM; ++d)
-                {
-                    const double a  = av[d];
-                    const double fl = a >= 0 ? a : 0.;
-                    const double fr = a >= 0 ? 0. : a;
-                    int xp[3] = {c[0], c[1], c[2]}, xm[3] = {c[0], c[1], c[2]};
-                    ++xp[d];
-                    --xm[d];
-                    const double s2   = pow2(m);
-                    const double lc0 = s2 * fl, lc1 = s2 * fr;
-                    const double rc0 = -lc0, rc1 = -lc1;
-                    const bool rs = leaf(m, xp), ls = leaf(m, xm);
-                    // same level
-                    if (d == 0)
-                    {
-                        if (rs) acc = acc + lc0 * uX;
-                        if (ls) acc = acc + rc0 * val(m, xm);
-                        if (rs) acc = acc + lc1 * val(m, xp);
-                        if (ls) acc = acc + rc1 * uX;
-                    }
-                    else
-                    {
-                        if (ls)
-                        {
-                            acc = acc + rc0 * val(m, xm);
-                            acc = acc + rc1 * uX;
-                        }
-                        if (rs)
-                        {
-                            acc = acc + lc0 * uX;
-                            acc = acc + lc1 * val(m, xp);
-                        }
-                    }
-                    const bool out_r = xp[d] >= nm, out_l = xm[d] < 0;
-                    // level jumps with X the fine cell
-                    int pp[3] = {xp[0] >> 1, xp[1] >> 1, xp[2] >> 1}, pm[3] = {xm[0] >> 1, xm[1] >> 1, xm[2] >> 1};
-                    const bool lcoarse = !ls && !out_l && m >= 1 && leaf(m - 1, pm);
-                    const bool rcoarse = !rs && !out_r && m >= 1 && leaf(m - 1, pp);
-                    if (lcoarse)
-                    {
-                        acc = acc + rc0 * val(m, xm);
-                        acc = acc + rc1 * uX;
-                    }
-                    if (rcoarse)
-                    {
-                        acc = acc + lc0 * uX;
-                        acc = acc + lc1 * val(m, xp);
-                    }
-                    // level jumps with X the coarse cell: its face children at m+1
-                    const double sf = pow2(m - DIM + 1);
-                    int ch[3]       = {2 * c[0], 2 * c[1], 2 * c[2]};
-                    ch[d]           = 2 * c[d] + 2;
-                    const bool rfine = !rs && !rcoarse && !out_r && leaf(m + 1, ch);
-                    ch[d]            = 2 * c[d] - 1;
-                    const bool lfine = !ls && !lcoarse && !out_l && leaf(m + 1, ch);
-                    // fine rows of the face in row order (z outer, y inner); a face
-                    // normal to y or z has the pair of fine cells within each row
-                    const int nrow = (d == 0) ? (DIM == 3 ? 4 : 2) : (DIM == 3 ? 2 : 1);
-                    if (rfine)
-                    {
-                        const double j0 = sf * fl, j1 = sf * fr;
-                        for (int r = 0; r < nrow; ++r)
-                        {
-                            int q[3] = {2 * c[0], 2 * c[1], 2 * c[2]};
-                            q[d]     = 2 * c[d] + 1;
-                            if (d == 0)
-                            {
-                                q[1] += r & 1;
-                                if (DIM == 3)
-                                {
-                                    q[2] += r >> 1;
-                                }
-                                int qe[3] = {q[0] + 1, q[1], q[2]};
-                                acc       = acc + j0 * val(m + 1, q);
-                                acc       = acc + j1 * val(m + 1, qe);
-                            }
-                            else
-                            {
-                                if (DIM == 3)
-                                {
-                                    q[d == 1 ? 2 : 1] += r;
-                                }
-                                int qb[3] = {q[0] + 1, q[1], q[2]};
-                                int qe[3] = {q[0], q[1], q[2]}, qbe[3] = {qb[0], qb[1], qb[2]};
-                                ++qe[d];
-                                ++qbe[d];
-                                acc = acc + (j0 * val(m + 1, q) + j0 * val(m + 1, qb));
-                                acc = acc + (j1 * val(m + 1, qe) + j1 * val(m + 1, qbe));
-                            }
-                        }
-                    }
-                    if (lfine)
-                    {
-                        const double j0 = -sf * fl, j1 = -sf * fr;
-                        for (int r = 0; r < nrow; ++r)
-                        {
-                            int q[3] = {2 * c[0], 2 * c[1], 2 * c[2]}; // Q, inside X on its left face
-                            if (d == 0)
-                            {
-                                q[1] += r & 1;
-                                if (DIM == 3)
-                                {
-                                    q[2] += r >> 1;
-                                }
-                                int qm[3] = {q[0] - 1, q[1], q[2]};
-                                acc       = acc + j0 * val(m + 1, qm);
-                                acc       = acc + j1 * val(m + 1, q);
-                            }
-                            else
-                            {
-                                if (DIM == 3)
-                                {
-                                    q[d == 1 ? 2 : 1] += r;
-                                }
-                                int qb[3] = {q[0] + 1, q[1], q[2]};
-                                int qm[3] = {q[0], q[1], q[2]}, qbm[3] = {qb[0], qb[1], qb[2]};
-                                --qm[d];
-                                --qbm[d];
-                                acc = acc + (j0 * val(m + 1, qm) + j0 * val(m + 1, qbm));
-                                acc = acc + (j1 * val(m + 1, q) + j1 * val(m + 1, qb));
-                            }
-                        }
-                    }
-                    // boundary interfaces
-                    if (out_r)
-                    {
-                        acc = acc + lc0 * uX;
-                        acc = acc + lc1 * val(m, xp);
-                    }
-                    if (out_l)
-                    {
-                        acc = acc + (-lc0) * val(m, xm);
-                        acc = acc + (-lc1) * uX;
-                    }
-                }
-                unp1[eX] = uX - p.dt * acc;
-            }
+            warp_list_compact(wl, lo[LO_CELLS], n, warp_id(), warp_count(), [&](long long w) { return __ldg(cells + w); },
+                              [&](long long w, int b)
+                              {
+                                  const int m        = level_of(g, w);
+                                  const Cell cc      = cell_of(g, m, w, b);
+                                  const int c[3]     = {cc.x, cc.y, cc.z};
+                                  const long long eX = 32 * w + b;
+                                  const double uX    = u[eX];
+                                  const int nm       = 1 << m;
+                                  auto leaf = [&](int l, const int* q) { return l >= 0 && l <= g.max_level && test(cells, g, l, q[0], q[1], DIM == 3 ? q[2] : 0); };
+                                  auto val  = [&](int l, const int* q) { return u[elem_at(g, l, q[0], q[1], DIM == 3 ? q[2] : 0)]; };
+                                  double acc = 0.;
+                                  for (int d = 0; d < DIM; ++d)
+                                  {
+                                      const double a  = av[d];
+                                      const double fl = a >= 0 ? a : 0.;
+                                      const double fr = a >= 0 ? 0. : a;
+                                      int xp[3] = {c[0], c[1], c[2]}, xm[3] = {c[0], c[1], c[2]};
+                                      ++xp[d];
+                                      --xm[d];
+                                      const double s2   = pow2(m);
+                                      const double lc0 = s2 * fl, lc1 = s2 * fr;
+                                      const double rc0 = -lc0, rc1 = -lc1;
+                                      const bool rs = leaf(m, xp), ls = leaf(m, xm);
+                                      // same level
+                                      if (d == 0)
+                                      {
+                                          if (rs) acc = acc + lc0 * uX;
+                                          if (ls) acc = acc + rc0 * val(m, xm);
+                                          if (rs) acc = acc + lc1 * val(m, xp);
+                                          if (ls) acc = acc + rc1 * uX;
+                                      }
+                                      else
+                                      {
+                                          if (ls)
+                                          {
+                                              acc = acc + rc0 * val(m, xm);
+                                              acc = acc + rc1 * uX;
+                                          }
+                                          if (rs)
+                                          {
+                                              acc = acc + lc0 * uX;
+                                              acc = acc + lc1 * val(m, xp);
+                                          }
+                                      }
+                                      const bool out_r = xp[d] >= nm, out_l = xm[d] < 0;
+                                      // level jumps with X the fine cell
+                                      int pp[3] = {xp[0] >> 1, xp[1] >> 1, xp[2] >> 1}, pm[3] = {xm[0] >> 1, xm[1] >> 1, xm[2] >> 1};
+                                      const bool lcoarse = !ls && !out_l && m >= 1 && leaf(m - 1, pm);
+                                      const bool rcoarse = !rs && !out_r && m >= 1 && leaf(m - 1, pp);
+                                      if (lcoarse)
+                                      {
+                                          acc = acc + rc0 * val(m, xm);
+                                          acc = acc + rc1 * uX;
+                                      }
+                                      if (rcoarse)
+                                      {
+                                          acc = acc + lc0 * uX;
+                                          acc = acc + lc1 * val(m, xp);
+                                      }
+                                      // level jumps with X the coarse cell: its face children at m+1
+                                      const double sf = pow2(m - DIM + 1);
+                                      int ch[3]       = {2 * c[0], 2 * c[1], 2 * c[2]};
+                                      ch[d]           = 2 * c[d] + 2;
+                                      const bool rfine = !rs && !rcoarse && !out_r && leaf(m + 1, ch);
+                                      ch[d]            = 2 * c[d] - 1;
+                                      const bool lfine = !ls && !lcoarse && !out_l && leaf(m + 1, ch);
+                                      // fine rows of the face in row order (z outer, y inner); a face
+                                      // normal to y or z has the pair of fine cells within each row
+                                      const int nrow = (d == 0) ? (DIM == 3 ? 4 : 2) : (DIM == 3 ? 2 : 1);
+                                      if (rfine)
+                                      {
+                                          const double j0 = sf * fl, j1 = sf * fr;
+                                          for (int r = 0; r < nrow; ++r)
+                                          {
+                                              int q[3] = {2 * c[0], 2 * c[1], 2 * c[2]};
+                                              q[d]     = 2 * c[d] + 1;
+                                              if (d == 0)
+                                              {
+                                                  q[1] += r & 1;
+                                                  if (DIM == 3)
+                                                  {
+                                                      q[2] += r >> 1;
+                                                  }
+                                                  int qe[3] = {q[0] + 1, q[1], q[2]};
+                                                  acc       = acc + j0 * val(m + 1, q);
+                                                  acc       = acc + j1 * val(m + 1, qe);
+                                              }
+                                              else
+                                              {
+                                                  if (DIM == 3)
+                                                  {
+                                                      q[d == 1 ? 2 : 1] += r;
+                                                  }
+                                                  int qb[3] = {q[0] + 1, q[1], q[2]};
+                                                  int qe[3] = {q[0], q[1], q[2]}, qbe[3] = {qb[0], qb[1], qb[2]};
+                                                  ++qe[d];
+                                                  ++qbe[d];
+                                                  acc = acc + (j0 * val(m + 1, q) + j0 * val(m + 1, qb));
+                                                  acc = acc + (j1 * val(m + 1, qe) + j1 * val(m + 1, qbe));
+                                              }
+                                          }
+                                      }
+                                      if (lfine)
+                                      {
+                                          const double j0 = -sf * fl, j1 = -sf * fr;
+                                          for (int r = 0; r < nrow; ++r)
+                                          {
+                                              int q[3] = {2 * c[0], 2 * c[1], 2 * c[2]}; // Q, inside X on its left face
+                                              if (d == 0)
+                                              {
+                                                  q[1] += r & 1;
+                                                  if (DIM == 3)
+                                                  {
+                                                      q[2] += r >> 1;
+                                                  }
+                                                  int qm[3] = {q[0] - 1, q[1], q[2]};
+                                                  acc       = acc + j0 * val(m + 1, qm);
+                                                  acc       = acc + j1 * val(m + 1, q);
+                                              }
+                                              else
+                                              {
+                                                  if (DIM == 3)
+                                                  {
+                                                      q[d == 1 ? 2 : 1] += r;
+                                                  }
+                                                  int qb[3] = {q[0] + 1, q[1], q[2]};
+                                                  int qm[3] = {q[0], q[1], q[2]}, qbm[3] = {qb[0], qb[1], qb[2]};
+                                                  --qm[d];
+                                                  --qbm[d];
+                                                  acc = acc + (j0 * val(m + 1, qm) + j0 * val(m + 1, qbm));
+                                                  acc = acc + (j1 * val(m + 1, q) + j1 * val(m + 1, qb));
+                                              }
+                                          }
+                                      }
+                                      // boundary interfaces
+                                      if (out_r)
+                                      {
+                                          acc = acc + lc0 * uX;
+                                          acc = acc + lc1 * val(m, xp);
+                                      }
+                                      if (out_l)
+                                      {
+                                          acc = acc + (-lc0) * val(m, xm);
+                                          acc = acc + (-lc1) * uX;
+                                      }
+                                  }
+                                  unp1[eX] = uX - p.dt * acc;
+            });
         }
 
         // --------------------------------------------------- layout moves
