@@ -38,7 +38,7 @@ CFG_3D = dict(dim=3, min_level=3, max_level=9, a=(1.0, 1.0, 1.0), eps=1e-3, regu
 METRIC = "active cell-updates/s"
 UNIT = "cell-updates/s"
 L2_BYTES = 129 * 1024 * 1024
-UPWIND_DRAM_BYTES_PER_CELL = 8346368.0 / 536428.0
+UPWIND_DRAM_BYTES_PER_CELL = 8572672.0 / 511813.0
 
 
 def workload_config(extra=None):
@@ -289,10 +289,10 @@ def run_gpu(args):
         fp64_peak = sg.device_fp64_rate()
     except Exception:
         fp64_peak = None
-    # DRAM bytes of one k_upwind launch, from the ncu capture summarised in
-    # profiles/k_upwind_2d_L12.md (8 346 368 B read + 0 B written for 536 428
-    # leaf cells), scaled to this launch's leaf cells: the traffic grows with
-    # the cells read and written
+    # DRAM bytes of one k_upwind launch of this workload, from an ncu capture
+    # (8 572 672 B read + 768 B written on a mesh of about 511 813 leaf cells:
+    # the sixth step of a run of this benchmark), scaled to this launch's leaf
+    # cells: the traffic grows with the cells read and written
     traffic = UPWIND_DRAM_BYTES_PER_CELL * nc
 
     # ---- samurai's named timers over a few extra steps (per-phase GPU time)
