@@ -104,7 +104,13 @@ namespace sg
             bool save(const std::string& filename, std::string& err)
             {
                 m_out.assign(96, 0);
+                m_too_many = false;
                 const uint64_t root = emit_group(m_root);
+                if (m_too_many)
+                {
+                    err = "a group has more than 256 members, more than one B-tree node holds";
+                    return false;
+                }
                 // superblock version 0
                 std::memcpy(m_out.data(), "\x89HDF\r\n\x1a\n", 8);
                 m_out[13] = 8;                   // size of offsets
@@ -340,8 +346,14 @@ namespace sg
                 {
                     std::memcpy(&m_out[segd + name_off[k]], members[k].first.c_str(), members[k].first.size());
                 }
-                // symbol table nodes, 8 entries each
+                // symbol table nodes, 8 entries each, under one B-tree node of at most
+                // 2 * 16 children
                 const size_t per = 8, nsnod = std::max<size_t>(1, (members.size() + per - 1) / per);
+                if (nsnod > 32)
+                {
+                    m_too_many = true;
+                    return 0;
+                }
                 std::vector<uint64_t> snods;
                 for (size_t s = 0; s < nsnod; ++s)
                 {
@@ -396,6 +408,7 @@ namespace sg
 
             Group m_root;
             std::vector<uint8_t> m_out;
+            bool m_too_many = false;
         };
 
         // --------------------------------------------------------------- reader

@@ -2,6 +2,7 @@
 //   h5_tool write <file.h5>            writes a fixed set of groups and datasets
 //   h5_tool read <file.h5> <path>      prints "class size signed shape..." then the values
 //   h5_tool exists <file.h5> <path>    prints 1 or 0
+//   h5_tool toomany <file.h5>          a group of 300 members: exits 3 (refused)
 #include <cinttypes>
 #include <cstdio>
 #include <cstring>
@@ -102,8 +103,30 @@ static int read_path(const char* name, const char* path)
     return 0;
 }
 
+// a group of 300 members: beyond one B-tree node, refused
+static int too_many(const char* name)
+{
+    h5::Writer w;
+    for (int k = 0; k < 300; ++k)
+    {
+        const double v = k;
+        w.add("/g/m" + std::to_string(k), h5::Kind::F64, {}, &v);
+    }
+    std::string err;
+    if (w.save(name, err))
+    {
+        return 0;
+    }
+    std::fprintf(stderr, "%s\n", err.c_str());
+    return 3;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc >= 3 && std::string(argv[1]) == "toomany")
+    {
+        return too_many(argv[2]);
+    }
     if (argc >= 3 && std::string(argv[1]) == "write")
     {
         return write_file(argv[2]);

@@ -58,6 +58,8 @@ def test_writer_reader_roundtrip(tool, tmp_path):
     assert subprocess.check_output([tool, "exists", f, "/many/m7"]).strip() == b"1"
     assert subprocess.check_output([tool, "exists", f, "/many/m77"]).strip() == b"0"
     assert subprocess.run([tool, "read", f, "/nothing"], capture_output=True).returncode == 1
+    r = subprocess.run([tool, "toomany", str(tmp_path / "big.h5")], capture_output=True)
+    assert r.returncode == 3 and b"256 members" in r.stderr
 
 
 def test_io_argument_checks():
