@@ -1,0 +1,109 @@
+"""The benchmark's workloads at their full sizes: 2D min_level 4 / max_level 12
+(16 squares + 16 Gaussians) and 3D min_level 3 / max_level 9 (ball + 8
+Gaussians).
+
+2D: the initial adaptation and one time step against the oracle, bit for
+bit (the oracle finishes them in seconds).  2D and 3D, size-independent
+properties of every adapted mesh: the leaves tile the unit box exactly once
+(painted on the finest grid), neighbouring leaves (faces and corners) differ
+by at most one level (2:1 graduation), the storage indices of the leaves are
+distinct and every value is finite."""
+import numpy as np
+import pytest
+
+from advection_cases import ball_3d, shapes_2d
+from oracle.pyoracle import OracleSim
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sg():
+    import samurai_gb300
+
+    samurai_gb300.lib()
+    return samurai_gb300
+
+
+def paint(level, coords, maxl):
+    """finest-grid map of the level of a leaf covering each cell (-1: none)"""
+    dim = coords.shape[1]
+    n = 1 << maxl
+    grid = np.full((n,) * dim, -1, np.int16)
+    for l in np.unique(level):
+        sel = level == l
+        s = 1 << (maxl - int(l))
+        base = coords[sel].astype(np.int64) * s
+        offs = np.stack(np.meshgrid(*([np.arange(s)] * dim), indexing="ij"), axis=-1).reshape(-1, dim)
+        step = max(1, (1 << 22) // (s ** dim))
+        for chunk in range(0, len(base), step):
+            pts = (base[chunk:chunk + step, None, :] + offs[None, :, :]).reshape(-1, dim)
+            grid[tuple(pts[:, d] for d in reversed(range(dim)))] = l  # grid[z][y][x]
+    return grid
+
+
+def check_mesh(level, coords, index, values, maxl):
+    dim = coords.shape[1]
+    # exact tiling: the leaves' volumes add up to the box and every finest
+    # cell is covered, so no cell is covered twice
+    assert int(np.sum(np.left_shift(np.int64(1), dim * (maxl - level.astype(np.int64))))) == 1 << (dim * maxl)
+    grid = paint(level, coords, maxl)
+    assert grid.min() >= 0, "a finest cell is covered by no leaf"
+    # 2:1 graduation across faces and corners
+    for axes in range(1, 1 << dim):
+        sl_a, sl_b = [], []
+        for d in reversed(range(dim)):  # grid axes are (z,) y, x
+            if (axes >> d) & 1:
+                sl_a.append(slice(1, None))
+                sl_b.append(slice(None, -1))
+            else:
+                sl_a.append(slice(None))
+                sl_b.append(slice(None))
+        assert np.abs(grid[tuple(sl_a)] - grid[tuple(sl_b)]).max() <= 1, "graduation"
+        if dim == 2:
+            # the other diagonal
+            if axes == 3:
+                assert np.abs(grid[1:, :-1] - grid[:-1, 1:]).max() <= 1, "graduation"
+    assert len(np.unique(index)) == len(index)
+    assert np.all(np.isfinite(values))
+
+
+def test_2d_full_size_against_oracle(sg):
+    minl, maxl = 4, 12
+    g = sg.AdvectionSim(2, minl, maxl, 1, 1)
+    o = OracleSim(2, minl, maxl, 1, 1)
+    lv, co, _ = o.cells()
+    vals = shapes_2d(2026)(lv, co)
+    g.set_cell_values(vals)
+    o.set_cell_values(vals)
+    assert g.adapt(1e-4, 2.0) == o.adapt(1e-4, 2.0)
+    a, dt = (1.0, 0.5), 0.5 / (1 << maxl)
+    for step in range(2):
+        lg, cg, ig = g.cells()
+        lo_, co_, io_ = o.cells()
+        assert np.array_equal(lg, lo_) and np.array_equal(cg, co_) and np.array_equal(ig, io_), "step %d: cells" % step
+        ug = g.cell_values()
+        assert np.array_equal(ug, o.cell_values()), "step %d: values" % step
+        check_mesh(lg, cg, ig, ug, maxl)
+        if step == 1:
+            break
+        g.update_ghost()
+        o.update_ghost()
+        g.upwind(a, dt)
+        o.upwind(a, dt)
+        assert g.adapt(1e-4, 2.0) == o.adapt(1e-4, 2.0)
+
+
+def test_3d_full_size_properties(sg):
+    minl, maxl = 3, 9
+    g = sg.AdvectionSim(3, minl, maxl, 1, 1)
+    lv, co, _ = g.cells()
+    g.set_cell_values(ball_3d(2026)(lv, co))
+    g.adapt(1e-3, 1.0)
+    a, dt = (1.0, 1.0, 1.0), 0.3 / (1 << maxl)
+    for step in range(3):
+        lg, cg, ig = g.cells()
+        check_mesh(lg, cg, ig, g.cell_values(), maxl)
+        g.update_ghost()
+        g.upwind(a, dt)
+        g.adapt(1e-3, 1.0)
