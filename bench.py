@@ -21,6 +21,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -85,6 +86,13 @@ def cpu_info():
     except OSError:
         pass
     return model or os.uname().machine
+
+
+def clock_dir():
+    """where the raw nvidia-smi samples go: $SG_CLOCK_LOG_DIR, else the temporary directory"""
+    d = os.environ.get("SG_CLOCK_LOG_DIR") or tempfile.gettempdir()
+    os.makedirs(d, exist_ok=True)
+    return d
 
 
 class ClockSampler:
@@ -199,7 +207,7 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     # ---- device-resident timed region
-    sampler = ClockSampler(local, os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % rank)) if rank == 0 else None
+    sampler = ClockSampler(local, os.path.join(clock_dir(), "clocks_rank%d.csv" % rank)) if rank == 0 else None
     barrier()
     total_ms = 0.0
     cell_updates = 0
@@ -507,7 +515,7 @@ def run_batch(args):
             updates += n
         return total, updates
 
-    sampler = ClockSampler(local, os.path.join(ROOT, "gpurun_out", "clocks_batch.csv")) if rank == 0 else None
+    sampler = ClockSampler(local, os.path.join(clock_dir(), "clocks_batch.csv")) if rank == 0 else None
     b_s, b_updates = timed(lambda: (batch.step(eps, reg, a, dt), batch.synchronize()), args.steps)
     clocks = sampler.stop() if sampler else None
     b_ms, b_updates = reduce_over_ranks(1e3 * b_s, b_updates, world, device="cuda")
@@ -673,7 +681,6 @@ def main():
     args = p.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
     if args.workload == "advection3d":
         CFG.clear()
         CFG.update(CFG_3D)
