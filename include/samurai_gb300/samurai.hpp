@@ -8,6 +8,8 @@
 //   auto mesh   = samurai::mra::make_mesh(box, config);                      // mr/mesh.hpp:511-518
 //   auto u      = samurai::make_scalar_field<double>("u", mesh);             // field/scalar_field.hpp:173-216
 //   samurai::for_each_cell(mesh, [&](auto& cell) { u[cell] = ...; });        // algorithm.hpp:301-363 (host mirror)
+//   samurai::for_each_interval(mesh, [&](auto level, auto& i, auto& index) {  // algorithm.hpp:75-123 (host mirror)
+//       for (int x = i.start; x < i.end; ++x) u(level, x, index[0]) = ...; });
 //   samurai::make_bc<samurai::Dirichlet<1>>(u, 0.);                          // bc/bc.hpp:786-800
 //   auto MRadaptation = samurai::make_MRAdapt(u);                            // mr/adapt.hpp:391-397
 //   MRadaptation(samurai::mra_config().epsilon(2e-4));                       // mr/adapt.hpp:147-195
@@ -24,6 +26,7 @@
 #include <array>
 #include <cstddef>
 #include <filesystem>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -213,10 +216,13 @@ namespace samurai
         }
     };
 
+    // Interval<int, long long> (interval.hpp:51-254): [start, end) with step 1;
+    // index + x is the storage index of cell x
     struct Interval
     {
         int start, end;
         long long index;
+        int step = 1;
 
         int size() const
         {
@@ -315,10 +321,79 @@ namespace samurai
             return out;
         }
 
+        // the intervals of a mesh id at a level, rows in for_each_interval order
+        // (z outer, y inner); yz[k] holds the dim-1 other coordinates of interval k
+        void intervals(int mesh_id, std::size_t level, std::vector<Interval>& iv, std::vector<std::array<int, dim - 1>>& yz) const
+        {
+            long long n = 0;
+            detail::check(sg_mesh_count_intervals(handle(), mesh_id, static_cast<int>(level), &n), "intervals");
+            std::vector<long long> rec(static_cast<std::size_t>(n) * (dim + 2));
+            if (n > 0)
+            {
+                detail::check(sg_mesh_get_intervals(handle(), mesh_id, static_cast<int>(level), rec.data(), n), "intervals");
+            }
+            iv.resize(static_cast<std::size_t>(n));
+            yz.resize(static_cast<std::size_t>(n));
+            for (long long k = 0; k < n; ++k)
+            {
+                const long long* r = rec.data() + k * (dim + 2);
+                iv[k]              = {static_cast<int>(r[0]), static_cast<int>(r[1]), r[dim + 1]};
+                for (std::size_t d = 0; d + 1 < dim; ++d)
+                {
+                    yz[k][d] = static_cast<int>(r[2 + d]);
+                }
+            }
+        }
+
+        // storage index of cell (x, yz) of the reference mesh at a level, -1 if absent
+        // (find / get_index, algorithm.hpp:391-467 and level_cell_array.hpp:669-743)
+        long long find(std::size_t level, int x, const std::array<int, dim - 1>& yz) const
+        {
+            const auto& lv = reference_rows(level);
+            auto it        = lv.find(yz);
+            if (it == lv.end())
+            {
+                return -1;
+            }
+            for (const Interval& i : it->second)
+            {
+                if (x >= i.start && x < i.end)
+                {
+                    return i.index + x;
+                }
+            }
+            return -1;
+        }
+
       private:
+
+        // reference-mesh rows of a level, cached for the current mesh version
+        const std::map<std::array<int, dim - 1>, std::vector<Interval>>& reference_rows(std::size_t level) const
+        {
+            unsigned long long version = 0;
+            detail::check(sg_mesh_version(handle(), &version), "find");
+            if (m_rows.size() <= level || m_rows_version != version)
+            {
+                m_rows.assign(m_max + 1, {});
+                for (int l = 0; l <= m_max; ++l)
+                {
+                    std::vector<Interval> iv;
+                    std::vector<std::array<int, dim - 1>> yz;
+                    intervals(SG_REFERENCE, static_cast<std::size_t>(l), iv, yz);
+                    for (std::size_t k = 0; k < iv.size(); ++k)
+                    {
+                        m_rows[static_cast<std::size_t>(l)][yz[k]].push_back(iv[k]);
+                    }
+                }
+                m_rows_version = version;
+            }
+            return m_rows[level];
+        }
 
         std::shared_ptr<sg_mesh_s> m_h;
         int m_min = 0, m_max = 0;
+        mutable std::vector<std::map<std::array<int, dim - 1>, std::vector<Interval>>> m_rows;
+        mutable unsigned long long m_rows_version = 0;
     };
 
     namespace mra
@@ -418,6 +493,28 @@ namespace samurai
         {
             const_cast<ScalarField*>(this)->pull();
             return m_host.values[static_cast<std::size_t>(cell.index)];
+        }
+
+        // u(level, i, j[, k]): the value of a reference cell (field_base.hpp, access through
+        // get_index, algorithm.hpp:391-467); std::out_of_range for a cell outside the reference mesh
+        template <class... T>
+        double& operator()(std::size_t level, int i, T... yz)
+        {
+            static_assert(sizeof...(T) == dim - 1, "u(level, i, j[, k])");
+            const long long e = m_mesh->find(level, i, {static_cast<int>(yz)...});
+            if (e < 0)
+            {
+                throw std::out_of_range("samurai_gb300: u(level, i, ...) outside the reference mesh");
+            }
+            pull();
+            m_host.dirty = true;
+            return m_host.values[static_cast<std::size_t>(e)];
+        }
+
+        template <class... T>
+        double operator()(std::size_t level, int i, T... yz) const
+        {
+            return (*const_cast<ScalarField*>(this))(level, i, yz...);
         }
 
         void resize()
@@ -585,6 +682,20 @@ namespace samurai
             return CellValues(m_host.values.data() + static_cast<std::size_t>(cell.index) * n_comp);
         }
 
+        template <class... T>
+        CellValues operator()(std::size_t level, int i, T... yz)
+        {
+            static_assert(sizeof...(T) == dim - 1, "v(level, i, j[, k])");
+            const long long e = m_mesh->find(level, i, {static_cast<int>(yz)...});
+            if (e < 0)
+            {
+                throw std::out_of_range("samurai_gb300: v(level, i, ...) outside the reference mesh");
+            }
+            pull();
+            m_host.dirty = true;
+            return CellValues(m_host.values.data() + static_cast<std::size_t>(e) * n_comp);
+        }
+
         std::array<double, n_comp> operator[](const Cell<dim>& cell) const
         {
             const_cast<VectorField*>(this)->pull();
@@ -728,6 +839,24 @@ namespace samurai
         for (auto& c : mesh.cells())
         {
             f(c);
+        }
+    }
+
+    // for_each_interval(mesh, f(level, i, index)) (algorithm.hpp:75-123) on the leaf cells: levels
+    // ascending, rows with z outer and y inner; index holds the dim-1 other coordinates and
+    // i.index + x is the storage index of cell x
+    template <class Mesh, class F>
+    void for_each_interval(const Mesh& mesh, F&& f)
+    {
+        std::vector<Interval> iv;
+        std::vector<std::array<int, Mesh::dim - 1>> yz;
+        for (std::size_t l = mesh.min_level(); l <= mesh.max_level(); ++l)
+        {
+            mesh.intervals(SG_CELLS, l, iv, yz);
+            for (std::size_t k = 0; k < iv.size(); ++k)
+            {
+                f(l, iv[k], yz[k]);
+            }
         }
     }
 

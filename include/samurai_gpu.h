@@ -88,6 +88,9 @@ int sg_mesh_stream(sg_mesh_t mesh, void** stream);
 int sg_mesh_synchronize(sg_mesh_t mesh);
 /* kernel launches issued on the mesh since the last reset (instrumentation) */
 int sg_mesh_launch_count(sg_mesh_t mesh, int reset, long long* count);
+/* a number that changes whenever the mesh's cells change (adaptation, sg_mesh_set_cells, sg_load): host caches of
+ * the mesh (intervals, cell lists) are current while it stays the same */
+int sg_mesh_version(sg_mesh_t mesh, unsigned long long* version);
 
 /* samurai's named timers (timers.hpp:111-1036, printed with --timers): CUDA-event timers per phase.
  * ids: 0 mesh adaptation, 1 ghost update, 2 detail computation, 3 tag cells, 4 tag finalization,

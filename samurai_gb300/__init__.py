@@ -63,6 +63,7 @@ def lib():
         "sg_mesh_stream": (i, [vp, ctypes.POINTER(vp)]),
         "sg_mesh_synchronize": (i, [vp]),
         "sg_mesh_launch_count": (i, [vp, i, pl]),
+        "sg_mesh_version": (i, [vp, ctypes.POINTER(ctypes.c_ulonglong)]),
         "sg_timers_enable": (i, [vp, i]),
         "sg_timers_get": (i, [vp, i, ctypes.POINTER(d), pl]),
         "sg_timers_reset": (i, [vp]),
@@ -317,6 +318,27 @@ class MRMesh:
         _check(lib().sg_mesh_get_intervals(self.h, mid, level, _ptr(out), n.value), "sg_mesh_get_intervals")
         return out if with_index else out[:, : self.dim + 1].astype(np.int32)
 
+    def version(self):
+        """changes whenever the cells change (adaptation, set_cells, load)"""
+        v = ctypes.c_ulonglong()
+        _check(lib().sg_mesh_version(self.h, ctypes.byref(v)), "sg_mesh_version")
+        return v.value
+
+    def find(self, level, i, *yz):
+        """storage index of cell (i, yz...) of the reference mesh at a level, -1 if absent
+        (get_index, algorithm.hpp:391-467)"""
+        v = self.version()
+        if getattr(self, "_rows_version", None) != v:
+            rows = {}
+            for l in range(self._max_level + 1):
+                for r in self.intervals("reference", l, with_index=True):
+                    rows.setdefault((l,) + tuple(int(t) for t in r[2:self.dim + 1]), []).append((int(r[0]), int(r[1]), int(r[self.dim + 1])))
+            self._rows, self._rows_version = rows, v
+        for s0, e0, idx in self._rows.get((int(level),) + tuple(int(t) for t in yz), ()):
+            if s0 <= i < e0:
+                return idx + int(i)
+        return -1
+
     def set_cells(self, level, coords):
         level = np.ascontiguousarray(level, np.int32)
         coords = np.ascontiguousarray(coords, np.int32)
@@ -383,6 +405,13 @@ class ScalarField:
     def components(self):
         return [self]
 
+    def __call__(self, level, i, *yz):
+        """u(level, i, j[, k]): the value of a reference cell (host copy)"""
+        e = self.mesh.find(level, i, *yz)
+        if e < 0:
+            raise IndexError("u(level, i, ...) outside the reference mesh")
+        return float(self.array()[e])
+
     def __del__(self):
         if getattr(self, "h", None) and getattr(self, "_owner", False):
             try:
@@ -446,6 +475,26 @@ def device_fp64_rate():
 
 def make_scalar_field(name, mesh):
     return ScalarField(name, mesh)
+
+
+class Interval:
+    """Interval<int, long long> (interval.hpp:51-254): [start, end), index + x = storage index"""
+
+    __slots__ = ("start", "end", "index", "step")
+
+    def __init__(self, start, end, index):
+        self.start, self.end, self.index, self.step = int(start), int(end), int(index), 1
+
+    def size(self):
+        return self.end - self.start
+
+
+def for_each_interval(mesh, f):
+    """for_each_interval(mesh, f(level, i, index)) (algorithm.hpp:75-123) on the leaf cells: levels
+    ascending, rows with z outer and y inner; index holds the dim-1 other coordinates"""
+    for l in range(mesh.min_level(), mesh.max_level() + 1):
+        for r in mesh.intervals("cells", l, with_index=True):
+            f(l, Interval(r[0], r[1], r[mesh.dim + 1]), tuple(int(t) for t in r[2:mesh.dim + 1]))
 
 
 class VectorField:

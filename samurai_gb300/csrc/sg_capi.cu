@@ -721,6 +721,16 @@ extern "C"
         return from_ctx(mesh->ctx, sg::device_error(mesh->ctx));
     }
 
+    int sg_mesh_version(sg_mesh_t mesh, unsigned long long* version)
+    {
+        if (!mesh || !version)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_version: null argument");
+        }
+        *version = mesh->ctx.mesh_version;
+        return SG_OK;
+    }
+
     int sg_mesh_launch_count(sg_mesh_t mesh, int reset, long long* count)
     {
         if (!mesh)

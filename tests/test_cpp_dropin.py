@@ -11,6 +11,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "advection_2d.cpp")
 VSRC = os.path.join(ROOT, "tests", "cpp", "vector_advection_2d.cpp")
+ISRC = os.path.join(ROOT, "tests", "cpp", "intervals_2d.cpp")
 GOLD = os.path.join(ROOT, "tests", "golden")
 
 
@@ -32,6 +33,11 @@ def test_demo_compiles(tmp_path):
 
 def test_vector_demo_compiles(tmp_path):
     exe = compile_demo(tmp_path, VSRC)
+    assert os.path.exists(exe)
+
+
+def test_interval_program_compiles(tmp_path):
+    exe = compile_demo(tmp_path, ISRC)
     assert os.path.exists(exe)
 
 
@@ -156,3 +162,30 @@ def test_demo_periodic_matches_oracle(tmp_path):
     assert np.array_equal(rows[:, 0].astype(int), lv)
     assert np.array_equal(rows[:, 1:3].astype(int), co)
     assert np.array_equal(rows[:, 3], o.cell_values())
+
+
+@pytest.mark.gpu
+def test_for_each_interval_through_the_header(tmp_path):
+    """for_each_interval and u(level, i, j) of the C++ header after an
+    adaptation: the oracle's leaf intervals and values."""
+    from advection_cases import centers
+    from oracle.pyoracle import OracleSim
+
+    exe = compile_demo(tmp_path, ISRC)
+    out = os.path.join(str(tmp_path), "out.txt")
+    subprocess.check_call([exe, out])
+    lines = [l.split() for l in open(out).read().split("\n") if l.strip()]
+    o = OracleSim(2, 3, 7, 1, 1)
+    lv, co, _ = o.cells()
+    c = centers(lv, co)
+    o.set_cell_values(np.where((c[:, 0] - 0.4) * (c[:, 0] - 0.4) + (c[:, 1] - 0.6) * (c[:, 1] - 0.6) < 0.04, 1.0, 0.0))
+    o.adapt(1e-3, 1.0)
+    ivs = [(int(l[1]), int(l[2]), int(l[3]), int(l[4])) for l in lines if l[0] == "I"]
+    want = []
+    for level in range(3, 8):
+        want.extend((level,) + tuple(int(v) for v in r) for r in o.intervals("cells", level))
+    assert ivs == want
+    cells = np.array([[float(v) for v in l[1:]] for l in lines if l[0] == "C"])
+    lv, co, _ = o.cells()
+    assert np.array_equal(cells[:, 0].astype(int), lv) and np.array_equal(cells[:, 1:3].astype(int), co)
+    assert np.array_equal(cells[:, 3], o.cell_values())

@@ -350,3 +350,37 @@ def test_vector_field(sg, dim, minl, maxl, rel):
     got = v.cell_values()
     for c, k in enumerate(ks):
         assert np.array_equal(got[:, c], o.cell_values_k(k)), "final component %d" % c
+
+
+@pytest.mark.parametrize("dim,minl,maxl", [(2, 3, 8), (3, 2, 5)])
+def test_for_each_interval_and_cell_access(sg, dim, minl, maxl):
+    """for_each_interval(mesh, f(level, i, index)) gives the leaf intervals of
+    the oracle in samurai's order with their storage offsets, and u(level, i,
+    j[, k]) reads the value of a reference cell (a ghost included)."""
+    g, o = pair(sg, dim, minl, maxl)
+    f = shapes_2d(4, 3, 3) if dim == 2 else ball_3d(4)
+    init_both(g, o, f)
+    g.adapt(1e-3, 1.0)
+    o.adapt(1e-3, 1.0)
+    got = []
+    sg.for_each_interval(g.mesh, lambda level, i, index: got.append((level, i.start, i.end) + index + (i.index,)))
+    ref = []
+    for l in range(minl, maxl + 1):
+        ref.extend((l,) + tuple(int(v) for v in r) for r in g.mesh.intervals("cells", l, with_index=True))
+    assert got == ref
+    want = []
+    for l in range(minl, maxl + 1):
+        want.extend((l,) + tuple(int(v) for v in r) for r in o.intervals("cells", l))
+    assert [t[:dim + 2] for t in got] == want
+    g.update_ghost()
+    field = g.field()
+    lv, co, ix = g.cells()
+    for k in range(0, len(lv), max(1, len(lv) // 200)):
+        assert g.u(int(lv[k]), *[int(c) for c in co[k]]) == field[ix[k]]
+    # a ghost: the left neighbour of the first leaf of the finest level
+    iv = g.mesh.intervals("reference", maxl, with_index=True)[0]
+    e = g.mesh.find(maxl, int(iv[0]), *[int(v) for v in iv[2:dim + 1]])
+    assert e == int(iv[dim + 1]) + int(iv[0])
+    assert g.u(maxl, int(iv[0]), *[int(v) for v in iv[2:dim + 1]]) == field[e]
+    with pytest.raises(IndexError):
+        g.u(maxl, -30, *([0] * (dim - 1)))
