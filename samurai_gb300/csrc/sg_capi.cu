@@ -43,21 +43,6 @@ namespace
         return (end && *end == '\0' && x >= 0) ? x : dflt;
     }
 
-    // The device address of page-locked host memory (cudaHostAlloc /
-    // cudaHostRegister, mapped under unified addressing), nullptr for other
-    // memory.  The gather and scatter kernels read and write such a buffer
-    // directly over the host link, without a staging copy.
-    const void* mapped_host(const void* p)
-    {
-        cudaPointerAttributes a{};
-        if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
-        {
-            cudaGetLastError();
-            return nullptr;
-        }
-        return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
-    }
-
     int from_ctx(sg::Ctx& c, int st)
     {
         if (st != sg::SG_OK)
@@ -944,18 +929,13 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_field_upload: size differs from the reference mesh");
         }
-        field->f.ghosts_valid = false;
-        const double* src     = static_cast<const double*>(mapped_host(values));
-        if (!src)
+        if (stage(h, n))
         {
-            if (stage(h, n))
-            {
-                return from_ctx(c, SG_ERR_CUDA);
-            }
-            cudaMemcpyAsync(h->staging, values, static_cast<size_t>(n) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
-            src = h->staging;
+            return from_ctx(c, SG_ERR_CUDA);
         }
-        int st = sg::scatter_compact(c, c.m(), src, field->f.data);
+        cudaMemcpyAsync(h->staging, values, static_cast<size_t>(n) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        field->f.ghosts_valid = false;
+        int st = sg::scatter_compact(c, c.m(), h->staging, field->f.data);
         if (!st && cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
             st = sg::check(c, "upload");
@@ -979,27 +959,16 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_field_download: size differs from the reference mesh");
         }
-        double* dst = static_cast<double*>(const_cast<void*>(mapped_host(values)));
-        if (dst)
+        if (stage(h, n))
         {
-            // the gather writes the page-locked host buffer directly
-            if (int st = sg::gather_compact(c, c.m(), field->f.data, dst))
-            {
-                return from_ctx(c, st);
-            }
+            return from_ctx(c, SG_ERR_CUDA);
         }
-        else
+        int st = sg::gather_compact(c, c.m(), field->f.data, h->staging);
+        if (st)
         {
-            if (stage(h, n))
-            {
-                return from_ctx(c, SG_ERR_CUDA);
-            }
-            if (int st = sg::gather_compact(c, c.m(), field->f.data, h->staging))
-            {
-                return from_ctx(c, st);
-            }
-            cudaMemcpyAsync(values, h->staging, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+            return from_ctx(c, st);
         }
+        cudaMemcpyAsync(values, h->staging, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
         if (cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
             return from_ctx(c, sg::check(c, "download"));

@@ -384,25 +384,3 @@ def test_for_each_interval_and_cell_access(sg, dim, minl, maxl):
     assert g.u(maxl, int(iv[0]), *[int(v) for v in iv[2:dim + 1]]) == field[e]
     with pytest.raises(IndexError):
         g.u(maxl, -30, *([0] * (dim - 1)))
-
-
-def test_page_locked_host_buffers(sg):
-    """u.array() to and from page-locked host memory (read and written by the
-    gather and scatter kernels directly) equals the staged copies of
-    ordinary host memory."""
-    import ctypes
-
-    torch = pytest.importorskip("torch")
-    g, o = pair(sg, 2, 3, 8)
-    init_both(g, o, shapes_2d(5, 3, 3))
-    g.adapt(1e-3, 1.0)
-    g.update_ghost()
-    n = g.nb_ref()
-    plain = g.field()
-    pinned = torch.empty(n + 64, dtype=torch.float64, pin_memory=True).numpy()
-    pinned[:] = np.nan
-    sg._check(sg.lib().sg_field_download(g.u.h, pinned.ctypes.data_as(ctypes.c_void_p), n), "download")
-    assert np.array_equal(pinned[:n], plain) and np.all(np.isnan(pinned[n:]))
-    pinned[:n] = plain * 2.0 - 1.0
-    sg._check(sg.lib().sg_field_upload(g.u.h, pinned.ctypes.data_as(ctypes.c_void_p), n), "upload")
-    assert np.array_equal(g.field(), plain * 2.0 - 1.0)
