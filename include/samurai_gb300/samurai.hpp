@@ -187,6 +187,16 @@ namespace samurai
         static constexpr int prediction_stencil_radius = 1;
     };
 
+    // coordinates of a point: c[d] and samurai's c(d) (coords_t, cell.hpp)
+    template <std::size_t dim>
+    struct Coords : std::array<double, dim>
+    {
+        double operator()(std::size_t d) const
+        {
+            return (*this)[d];
+        }
+    };
+
     template <std::size_t dim>
     struct Cell
     {
@@ -195,9 +205,9 @@ namespace samurai
         long long index;
         double length;
 
-        std::array<double, dim> center() const
+        Coords<dim> center() const
         {
-            std::array<double, dim> c;
+            Coords<dim> c;
             for (std::size_t d = 0; d < dim; ++d)
             {
                 c[d] = length * (indices[d] + 0.5); // cell.hpp:130-133 with a zero origin
@@ -299,6 +309,55 @@ namespace samurai
             long long nc = 0, nr = 0;
             detail::check(sg_mesh_counts(handle(), &nc, &nr), "nb_cells");
             return static_cast<std::size_t>(nc);
+        }
+
+        // MRMeshId (mr/mesh.hpp:25-33)
+        enum class mesh_id_t : int
+        {
+            cells            = SG_CELLS,
+            cells_and_ghosts = SG_CELLS_AND_GHOSTS,
+            proj_cells       = SG_PROJ_CELLS,
+            union_cells      = SG_UNION_CELLS,
+            all_cells        = SG_REFERENCE,
+            reference        = SG_REFERENCE
+        };
+
+        // mesh.nb_cells(mesh_id) (mesh.hpp:530-550)
+        std::size_t nb_cells(mesh_id_t id) const
+        {
+            if (id == mesh_id_t::cells)
+            {
+                return nb_leaf_cells();
+            }
+            if (id == mesh_id_t::reference)
+            {
+                return nb_cells();
+            }
+            std::size_t n = 0;
+            std::vector<Interval> iv;
+            std::vector<std::array<int, dim - 1>> yz;
+            for (int l = 0; l <= m_max; ++l)
+            {
+                intervals(static_cast<int>(id), static_cast<std::size_t>(l), iv, yz);
+                for (const auto& i : iv)
+                {
+                    n += static_cast<std::size_t>(i.size());
+                }
+            }
+            return n;
+        }
+
+        // mesh[mesh_id]: the cell set of one id, for for_each_interval / for_each_cell
+        struct IdView
+        {
+            static constexpr std::size_t dim = MRMesh::dim;
+            const MRMesh* mesh;
+            mesh_id_t id;
+        };
+
+        IdView operator[](mesh_id_t id) const
+        {
+            return {this, id};
         }
 
         std::vector<Cell<dim>> cells() const
@@ -481,6 +540,19 @@ namespace samurai
             return *m_mesh;
         }
 
+        const std::string& name() const
+        {
+            return m_name;
+        }
+
+        // u.fill(value) (field/access_base.hpp:63-66): every reference cell, on the device
+        void fill(double value)
+        {
+            m_host.dirty = false;
+            m_host.valid = false;
+            detail::check(sg_field_fill(handle(), value), "fill");
+        }
+
         // host mirror access (for_each_cell initialisation, inspection)
         double& operator[](const Cell<dim>& cell)
         {
@@ -598,6 +670,27 @@ namespace samurai
     {
         static_assert(std::is_same_v<value_t, double>, "samurai_gb300 fields are FP64");
         return ScalarField<Mesh>(name, mesh);
+    }
+
+    template <class Mesh, class F>
+    auto for_each_cell(const Mesh& mesh, F&& f) -> decltype(mesh.cells(), void());
+
+    // make_scalar_field<double>(name, mesh, init_value) and make_scalar_field<double>(name, mesh, f)
+    // with f(center) (field/scalar_field.hpp:178-216)
+    template <class value_t, class Mesh, class Init>
+    auto make_scalar_field(const std::string& name, Mesh& mesh, Init&& init)
+    {
+        auto u = make_scalar_field<value_t>(name, mesh);
+        if constexpr (std::is_invocable_v<Init, Coords<Mesh::dim>>)
+        {
+            u.fill(0.);
+            for_each_cell(mesh, [&](const auto& cell) { u[cell] = init(cell.center()); });
+        }
+        else
+        {
+            u.fill(static_cast<double>(init));
+        }
+        return u;
     }
 
     // VectorField<Mesh, double, n_comp> (field/vector_field.hpp:134-216): n_comp scalar
@@ -834,7 +927,7 @@ namespace samurai
     }
 
     template <class Mesh, class F>
-    void for_each_cell(const Mesh& mesh, F&& f)
+    auto for_each_cell(const Mesh& mesh, F&& f) -> decltype(mesh.cells(), void())
     {
         for (auto& c : mesh.cells())
         {
@@ -842,11 +935,49 @@ namespace samurai
         }
     }
 
+    // for_each_interval(mesh[mesh_id], f) and for_each_cell(mesh[mesh_id], f) on any cell set of the mesh
+    template <class View, class F>
+    auto for_each_interval(const View& v, F&& f) -> decltype(v.mesh, v.id, void())
+    {
+        std::vector<Interval> iv;
+        std::vector<std::array<int, View::dim - 1>> yz;
+        for (std::size_t l = 0; l <= v.mesh->max_level(); ++l)
+        {
+            v.mesh->intervals(static_cast<int>(v.id), l, iv, yz);
+            for (std::size_t k = 0; k < iv.size(); ++k)
+            {
+                f(l, iv[k], yz[k]);
+            }
+        }
+    }
+
+    template <class View, class F>
+    auto for_each_cell(const View& v, F&& f) -> decltype(v.mesh, v.id, void())
+    {
+        for_each_interval(v,
+                          [&](std::size_t level, const Interval& i, const std::array<int, View::dim - 1>& yz)
+                          {
+                              for (int x = i.start; x < i.end; ++x)
+                              {
+                                  Cell<View::dim> c;
+                                  c.level      = level;
+                                  c.indices[0] = x;
+                                  for (std::size_t d = 1; d < View::dim; ++d)
+                                  {
+                                      c.indices[d] = yz[d - 1];
+                                  }
+                                  c.index  = i.index + x;
+                                  c.length = v.mesh->cell_length(level);
+                                  f(c);
+                              }
+                          });
+    }
+
     // for_each_interval(mesh, f(level, i, index)) (algorithm.hpp:75-123) on the leaf cells: levels
     // ascending, rows with z outer and y inner; index holds the dim-1 other coordinates and
     // i.index + x is the storage index of cell x
     template <class Mesh, class F>
-    void for_each_interval(const Mesh& mesh, F&& f)
+    auto for_each_interval(const Mesh& mesh, F&& f) -> decltype(mesh.min_level(), void())
     {
         std::vector<Interval> iv;
         std::vector<std::array<int, Mesh::dim - 1>> yz;

@@ -117,6 +117,8 @@ int sg_field_download_device(sg_field_t field, double* dvalues, long long n);
 /* u[cell] for the leaf cells in for_each_cell order (n = nb_cells); other entries become 0 on upload */
 int sg_field_set_cells(sg_field_t field, const double* values, long long n);
 int sg_field_get_cells(sg_field_t field, double* values, long long n);
+/* u.fill(value) (field/field_base.hpp): every reference cell, ghosts included */
+int sg_field_fill(sg_field_t field, double value);
 /* std::swap(u.array(), unp1.array()) (demos/FiniteVolume/advection_2d.cpp:146) */
 int sg_field_swap(sg_field_t a, sg_field_t b);
 

@@ -79,6 +79,7 @@ def lib():
         "sg_field_set_cells": (i, [vp, vp, ll]),
         "sg_field_get_cells": (i, [vp, vp, ll]),
         "sg_field_swap": (i, [vp, vp]),
+        "sg_field_fill": (i, [vp, d]),
         "sg_adapt": (i, [vp, d, d, pi]),
         "sg_harten": (i, [vp, i, d, d, pi]),
         "sg_adapt_ex": (i, [vp, d, d, i, pi]),
@@ -405,6 +406,10 @@ class ScalarField:
     def components(self):
         return [self]
 
+    def fill(self, value):
+        """u.fill(value) (field/access_base.hpp:63-66): every reference cell"""
+        _check(lib().sg_field_fill(self.h, float(value)), "sg_field_fill")
+
     def __call__(self, level, i, *yz):
         """u(level, i, j[, k]): the value of a reference cell (host copy)"""
         e = self.mesh.find(level, i, *yz)
@@ -473,8 +478,20 @@ def device_fp64_rate():
     return v.value
 
 
-def make_scalar_field(name, mesh):
-    return ScalarField(name, mesh)
+def make_scalar_field(name, mesh, init=None):
+    """make_scalar_field<double>(name, mesh[, init_value | f]) (field/scalar_field.hpp:173-216): init a
+    value for every cell, or a function of the cell centre (an array of shape (n, dim)) for the leaves"""
+    u = ScalarField(name, mesh)
+    if init is None:
+        return u
+    if callable(init):
+        u.fill(0.0)
+        lv, co, _ = mesh.cells()
+        length = 1.0 / np.left_shift(1, lv.astype(np.int64)).astype(np.float64)
+        u.set_cells(np.asarray(init(length[:, None] * (co.astype(np.float64) + 0.5)), np.float64))
+    else:
+        u.fill(float(init))
+    return u
 
 
 class Interval:

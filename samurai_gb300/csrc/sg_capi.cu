@@ -1036,6 +1036,21 @@ extern "C"
         return SG_OK;
     }
 
+    int sg_field_fill(sg_field_t field, double value)
+    {
+        if (!field)
+        {
+            return fail(SG_ERR_ARG, "sg_field_fill: null field");
+        }
+        sg::Ctx& c = field->mesh->ctx;
+        if (int st = sg::host_counts(c, c.m()))
+        {
+            return from_ctx(c, st);
+        }
+        field->f.ghosts_valid = false;
+        return from_ctx(c, sg::fill_ref(c, c.m(), field->f.data, value));
+    }
+
     int sg_field_swap(sg_field_t a, sg_field_t b)
     {
         if (!a || !b || a->mesh != b->mesh)

@@ -12,6 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "advection_2d.cpp")
 VSRC = os.path.join(ROOT, "tests", "cpp", "vector_advection_2d.cpp")
 ISRC = os.path.join(ROOT, "tests", "cpp", "intervals_2d.cpp")
+FSRC = os.path.join(ROOT, "tests", "cpp", "fields_api_2d.cpp")
 GOLD = os.path.join(ROOT, "tests", "golden")
 
 
@@ -38,6 +39,11 @@ def test_vector_demo_compiles(tmp_path):
 
 def test_interval_program_compiles(tmp_path):
     exe = compile_demo(tmp_path, ISRC)
+    assert os.path.exists(exe)
+
+
+def test_fields_api_program_compiles(tmp_path):
+    exe = compile_demo(tmp_path, FSRC)
     assert os.path.exists(exe)
 
 
@@ -189,3 +195,38 @@ def test_for_each_interval_through_the_header(tmp_path):
     lv, co, _ = o.cells()
     assert np.array_equal(cells[:, 0].astype(int), lv) and np.array_equal(cells[:, 1:3].astype(int), co)
     assert np.array_equal(cells[:, 3], o.cell_values())
+
+
+@pytest.mark.gpu
+def test_fields_and_mesh_ids_through_the_header(tmp_path):
+    """make_scalar_field with a value and with a function, u.fill,
+    mesh.nb_cells(mesh_id) and for_each_cell / for_each_interval over
+    mesh[mesh_id]: the oracle's counts and values."""
+    from advection_cases import centers
+    from oracle.pyoracle import OracleSim
+
+    exe = compile_demo(tmp_path, FSRC)
+    out = os.path.join(str(tmp_path), "out.txt")
+    subprocess.check_call([exe, out])
+    got = {l.split()[0]: float(l.split()[1]) for l in open(out).read().split("\n") if l.strip()}
+    o = OracleSim(2, 2, 6, 1, 1)
+    lv, co, _ = o.cells()
+    c = centers(lv, co)
+    x, y = c[:, 0], c[:, 1]
+    o.set_cell_values(np.where((x >= 0.3) & (x <= 0.6) & (y >= 0.4) & (y <= 0.7), 1.0, 0.0))
+    o.adapt(1e-3, 1.0)
+    n_cells, n_ref = o.nb_cells(), o.nb_ref()
+
+    def count(mid):
+        return sum(int(r[1] - r[0]) for l in range(7) for r in o.intervals(mid, l))
+
+    assert got["cells"] == n_cells and got["reference"] == n_ref
+    for mid in ("cells_and_ghosts", "proj_cells", "union_cells"):
+        assert got[mid] == count(mid), mid
+    su = 0.0
+    for v in o.cell_values():
+        su += v
+    assert got["sum_u"] == su
+    assert got["sum_v"] == 2.5 * n_cells
+    assert got["nref_walk"] == n_ref and got["nproj_walk"] == count("proj_cells")
+    assert got["sum_fill"] == -n_cells

@@ -384,3 +384,16 @@ def test_for_each_interval_and_cell_access(sg, dim, minl, maxl):
     assert g.u(maxl, int(iv[0]), *[int(v) for v in iv[2:dim + 1]]) == field[e]
     with pytest.raises(IndexError):
         g.u(maxl, -30, *([0] * (dim - 1)))
+
+
+def test_field_fill_and_factories(sg):
+    """u.fill and make_scalar_field with a value or a function of the centre"""
+    mesh = sg.MRMesh(2, 2, 6, 1, 1)
+    u = sg.make_scalar_field("u", mesh, 1.25)
+    assert np.all(u.array() == 1.25)
+    v = sg.make_scalar_field("v", mesh, lambda c: c[:, 0] + 2.0 * c[:, 1])
+    lv, co, _ = mesh.cells()
+    c = centers(lv, co)
+    assert np.array_equal(v.cell_values(), c[:, 0] + 2.0 * c[:, 1])
+    v.fill(-3.0)
+    assert np.all(v.array() == -3.0)
