@@ -419,7 +419,8 @@ namespace sg
             size_t size  = 0;    // element size in bytes
             std::vector<uint64_t> shape;
             std::vector<uint8_t> bytes;
-            std::map<std::string, size_t> members; // compound member name -> byte offset
+            std::map<std::string, size_t> members;     // compound member name -> byte offset
+            std::map<std::string, size_t> member_size; // compound member name -> byte size
 
             uint64_t count() const
             {
@@ -429,6 +430,14 @@ namespace sg
                     n *= s;
                 }
                 return n;
+            }
+
+            // a compound member of `n` bytes lying inside the record
+            bool member(const std::string& name, size_t n) const
+            {
+                auto o = members.find(name);
+                auto z = member_size.find(name);
+                return o != members.end() && z != member_size.end() && z->second == n && o->second <= size && n <= size - o->second;
             }
         };
 
@@ -483,7 +492,8 @@ namespace sg
                     {
                         return UNDEF;
                     }
-                    obj = lookup(btree, heap, name, err);
+                    int budget = 1 << 16;
+                    obj        = lookup(btree, heap, name, err, 0, budget);
                     if (obj == UNDEF)
                     {
                         return UNDEF;
@@ -519,11 +529,17 @@ namespace sg
                 uint64_t addr = UNDEF, len = 0;
                 for (auto& m : msgs)
                 {
+                    // every field read below lies inside the message's own m.size bytes
                     if (m.type == 0x0001)
                     {
                         // version 1: dims after 8 bytes; version 2: after 4 (a scalar has no dims)
-                        const int ver = m_b[m.at], nd = m_b[m.at + 1];
+                        const int ver = m.size >= 2 ? m_b[m.at] : 0, nd = m.size >= 2 ? m_b[m.at + 1] : 0;
                         const uint64_t p = m.at + (ver == 1 ? 8 : 4);
+                        if ((ver != 1 && ver != 2) || nd > 32 || p + 8 * static_cast<uint64_t>(nd) > m.at + m.size)
+                        {
+                            err = m_name + ": " + path + ": malformed dataspace";
+                            return false;
+                        }
                         out.shape.clear();
                         for (int k = 0; k < nd; ++k)
                         {
@@ -533,7 +549,7 @@ namespace sg
                     }
                     else if (m.type == 0x0003)
                     {
-                        if (!datatype(m.at, out, err))
+                        if (!datatype(m.at, m.at + m.size, out, err))
                         {
                             return false;
                         }
@@ -546,14 +562,14 @@ namespace sg
                     }
                     else if (m.type == 0x0008)
                     {
-                        const int ver = m_b[m.at];
+                        const int ver = m.size >= 4 ? m_b[m.at] : 0;
                         if (ver != 3)
                         {
                             err = m_name + ": " + path + ": layout message version " + std::to_string(ver) + " is not read";
                             return false;
                         }
                         const int cls = m_b[m.at + 1];
-                        if (cls == 1)
+                        if (cls == 1 && m.size >= 18)
                         {
                             addr = u64(m.at + 2);
                             len  = u64(m.at + 10);
@@ -562,6 +578,16 @@ namespace sg
                         {
                             len  = static_cast<uint64_t>(m_b[m.at + 2]) | (static_cast<uint64_t>(m_b[m.at + 3]) << 8);
                             addr = m.at + 4;
+                            if (len > m.size - 4u)
+                            {
+                                err = m_name + ": " + path + ": malformed compact layout";
+                                return false;
+                            }
+                        }
+                        else if (cls == 1)
+                        {
+                            err = m_name + ": " + path + ": malformed contiguous layout";
+                            return false;
                         }
                         else
                         {
@@ -576,7 +602,22 @@ namespace sg
                     err = m_name + ": " + path + " is not a dataset";
                     return false;
                 }
-                const uint64_t nbytes = out.count() * out.size;
+                // the element count and byte size, refused where they would overflow
+                uint64_t nbytes = out.size;
+                for (auto d : out.shape)
+                {
+                    if (d != 0 && nbytes > m_b.size() / d)
+                    {
+                        nbytes = UNDEF;
+                        break;
+                    }
+                    nbytes *= d;
+                }
+                if (out.size == 0 && out.count() != 0)
+                {
+                    err = m_name + ": " + path + ": zero-sized elements";
+                    return false;
+                }
                 if (nbytes == 0)
                 {
                     out.bytes.clear();
@@ -654,6 +695,11 @@ namespace sg
                         }
                         if (m.type == 0x0010)
                         {
+                            if (m.size < 16 || blocks.size() > 4096)
+                            {
+                                err = m_name + ": malformed object header continuation";
+                                return false;
+                            }
                             blocks.push_back({u64(m.at), u64(m.at + 8)});
                         }
                         out.push_back(m);
@@ -672,7 +718,7 @@ namespace sg
                 }
                 for (auto& m : msgs)
                 {
-                    if (m.type == 0x0011)
+                    if (m.type == 0x0011 && m.size >= 16)
                     {
                         btree = u64(m.at);
                         heap  = u64(m.at + 8);
@@ -699,9 +745,10 @@ namespace sg
                 return std::string(s, strnlen(s, static_cast<size_t>(size - off)));
             }
 
-            uint64_t lookup(uint64_t node, uint64_t heap, const std::string& name, std::string& err, int depth = 0) const
+            // `budget` bounds the nodes visited, so that a B-tree whose children repeat ends quickly
+            uint64_t lookup(uint64_t node, uint64_t heap, const std::string& name, std::string& err, int depth, int& budget) const
             {
-                if (depth > 64 || !in_file(node, 24) || std::memcmp(&m_b[node], "TREE", 4) != 0 || m_b[node + 4] != 0)
+                if (depth > 64 || --budget < 0 || !in_file(node, 24) || std::memcmp(&m_b[node], "TREE", 4) != 0 || m_b[node + 4] != 0)
                 {
                     err = m_name + ": malformed group B-tree";
                     return UNDEF;
@@ -719,7 +766,7 @@ namespace sg
                     const uint64_t child = u64(p);
                     if (level > 0)
                     {
-                        const uint64_t r = lookup(child, heap, name, err, depth + 1);
+                        const uint64_t r = lookup(child, heap, name, err, depth + 1, budget);
                         if (r != UNDEF || !err.empty())
                         {
                             return r;
@@ -749,8 +796,14 @@ namespace sg
                 return UNDEF;
             }
 
-            bool datatype(uint64_t at, Array& out, std::string& err) const
+            // a datatype message at [at, lim)
+            bool datatype(uint64_t at, uint64_t lim, Array& out, std::string& err) const
             {
+                if (at + 8 > lim)
+                {
+                    err = m_name + ": malformed datatype";
+                    return false;
+                }
                 const int cls = m_b[at] & 0x0F, ver = m_b[at] >> 4;
                 out.cls       = cls;
                 out.size      = u32(at + 4);
@@ -779,14 +832,24 @@ namespace sg
                     uint64_t p   = at + 8;
                     for (int m = 0; m < nm; ++m)
                     {
+                        if (p >= lim)
+                        {
+                            err = m_name + ": malformed compound datatype";
+                            return false;
+                        }
                         const char* s   = reinterpret_cast<const char*>(&m_b[p]);
-                        const size_t ln = strnlen(s, 256);
+                        const size_t ln = strnlen(s, static_cast<size_t>(std::min<uint64_t>(lim - p, 256)));
                         std::string mname(s, ln);
                         size_t off = 0;
                         if (ver == 3)
                         {
                             p += ln + 1;
                             const int nb = out.size < 256 ? 1 : out.size < 65536 ? 2 : out.size < (1u << 24) ? 3 : 4;
+                            if (p + nb > lim)
+                            {
+                                err = m_name + ": malformed compound datatype";
+                                return false;
+                            }
                             for (int k = 0; k < nb; ++k)
                             {
                                 off |= static_cast<size_t>(m_b[p + k]) << (8 * k);
@@ -796,25 +859,35 @@ namespace sg
                         else
                         {
                             p += (ln + 1 + 7) & ~size_t(7);
+                            if (p + 4 > lim)
+                            {
+                                err = m_name + ": malformed compound datatype";
+                                return false;
+                            }
                             off = u32(p);
                             p += ver == 1 ? 4 + 1 + 3 + 4 + 4 + 16 : 4;
                         }
-                        out.members[mname] = off;
-                        // skip the member's datatype message (fixed-point and floating-point members only)
-                        const int mcls = m_b[p] & 0x0F;
-                        if (mcls == 0)
+                        // the member's own datatype message (fixed-point and floating-point members only)
+                        if (p + 8 > lim)
                         {
-                            p += 8 + 4;
+                            err = m_name + ": malformed compound datatype";
+                            return false;
                         }
-                        else if (mcls == 1)
-                        {
-                            p += 8 + 12;
-                        }
-                        else
+                        const int mcls     = m_b[p] & 0x0F;
+                        const size_t msize = u32(p + 4);
+                        if (mcls != 0 && mcls != 1)
                         {
                             err = m_name + ": nested compound members are not read";
                             return false;
                         }
+                        p += mcls == 0 ? 8 + 4 : 8 + 12;
+                        if (p > lim || off > out.size || msize > out.size - off)
+                        {
+                            err = m_name + ": malformed compound datatype";
+                            return false;
+                        }
+                        out.members[mname]     = off;
+                        out.member_size[mname] = msize;
                     }
                     return true;
                 }

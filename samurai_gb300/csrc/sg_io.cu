@@ -12,6 +12,8 @@
 #include <cinttypes>
 #include <cstdio>
 #include <cstring>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -131,6 +133,24 @@ namespace
         }
         return SG_OK;
     }
+
+    // host allocations sized from the mesh or from a file's contents can throw; no exception leaves the C ABI
+    template <class F>
+    int guarded(const char* what, F&& body)
+    {
+        try
+        {
+            return body();
+        }
+        catch (const std::bad_alloc&)
+        {
+            return iofail(SG_ERR_CAPACITY, std::string(what) + ": out of host memory");
+        }
+        catch (const std::exception& e)
+        {
+            return iofail(SG_ERR_ARG, std::string(what) + ": " + e.what());
+        }
+    }
 } // namespace
 
 extern "C"
@@ -171,7 +191,7 @@ extern "C"
         return SG_OK;
     }
 
-    int sg_save(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    static int save_body(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
     {
         if (!filename || !*filename || !mesh)
         {
@@ -300,7 +320,7 @@ extern "C"
         return SG_OK;
     }
 
-    int sg_dump(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    static int dump_body(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
     {
         if (!filename || !*filename || !mesh)
         {
@@ -388,7 +408,7 @@ extern "C"
         return SG_OK;
     }
 
-    int sg_restart_levels(const char* path, const char* filename, int* dim, int* min_level, int* max_level)
+    static int restart_levels_body(const char* path, const char* filename, int* dim, int* min_level, int* max_level)
     {
         if (!filename || !dim || !min_level || !max_level)
         {
@@ -416,7 +436,7 @@ extern "C"
         return SG_OK;
     }
 
-    int sg_load(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    static int load_body(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
     {
         if (!filename || !mesh)
         {
@@ -481,8 +501,8 @@ extern "C"
             {
                 sg::h5::Array a, part;
                 const std::string p = base + std::to_string(d) + "/intervals";
-                if (!r.read(p + "/data", a, err) || a.cls != 6 || a.size != 24 || !a.members.count("start") || !a.members.count("end")
-                    || !a.members.count("index"))
+                if (!r.read(p + "/data", a, err) || a.cls != 6 || a.size != 24 || !a.member("start", 4) || !a.member("end", 4)
+                    || !a.member("index", 8))
                 {
                     return iofail(SG_ERR_ARG, "sg_load: " + (err.empty() ? p + " is not an Interval array" : err));
                 }
@@ -490,9 +510,16 @@ extern "C"
                 for (size_t k = 0; k < iv[d].size(); ++k)
                 {
                     const uint8_t* q = a.bytes.data() + 24 * k;
-                    std::memcpy(&iv[d][k].start, q + a.members["start"], 4);
-                    std::memcpy(&iv[d][k].end, q + a.members["end"], 4);
-                    std::memcpy(&iv[d][k].index, q + a.members["index"], 8);
+                    std::memcpy(&iv[d][k].start, q + a.members.at("start"), 4);
+                    std::memcpy(&iv[d][k].end, q + a.members.at("end"), 4);
+                    std::memcpy(&iv[d][k].index, q + a.members.at("index"), 8);
+                    // inside the level's box, so that the walk below stays bounded and index + coordinate cannot overflow
+                    const auto& rec = iv[d][k];
+                    if (rec.start < 0 || rec.start > rec.end || static_cast<int64_t>(rec.end) > (int64_t(1) << l) || rec.index < -(int64_t(1) << 62)
+                        || rec.index > (int64_t(1) << 62))
+                    {
+                        return iofail(SG_ERR_ARG, "sg_load: " + fname + ": interval outside the level-" + std::to_string(l) + " box in " + p);
+                    }
                 }
             }
             for (int d = 1; d < D; ++d)
@@ -625,5 +652,25 @@ extern "C"
             }
         }
         return SG_OK;
+    }
+
+    int sg_save(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    {
+        return guarded("sg_save", [&] { return save_body(path, filename, mesh, fields); });
+    }
+
+    int sg_dump(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    {
+        return guarded("sg_dump", [&] { return dump_body(path, filename, mesh, fields); });
+    }
+
+    int sg_restart_levels(const char* path, const char* filename, int* dim, int* min_level, int* max_level)
+    {
+        return guarded("sg_restart_levels", [&] { return restart_levels_body(path, filename, dim, min_level, max_level); });
+    }
+
+    int sg_load(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    {
+        return guarded("sg_load", [&] { return load_body(path, filename, mesh, fields); });
     }
 }

@@ -3,8 +3,11 @@
 //   h5_tool read <file.h5> <path>      prints "class size signed shape..." then the values
 //   h5_tool exists <file.h5> <path>    prints 1 or 0
 //   h5_tool toomany <file.h5>          a group of 300 members: exits 3 (refused)
+//   h5_tool fuzz <file.h5> <seed> <n>  n corrupted copies of <file.h5>, each opened and read along
+//                                      every path of the write mode; prints "opened read_ok read_err"
 #include <cinttypes>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -121,8 +124,128 @@ static int too_many(const char* name)
     return 3;
 }
 
+// Corrupted copies: truncations, flipped bits, overwritten 16-bit and 64-bit fields (offsets, sizes,
+// counts).  The reader must return on each, true or false, and what it returns as read must be
+// consistent; the test builds this tool with the address and undefined-behaviour sanitizers, which
+// turn any read outside the buffer into a failure.
+static int fuzz(const char* name, uint64_t seed, int n)
+{
+    std::vector<uint8_t> orig;
+    {
+        FILE* f = std::fopen(name, "rb");
+        if (!f)
+        {
+            return 1;
+        }
+        uint8_t buf[4096];
+        size_t got;
+        while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0)
+        {
+            orig.insert(orig.end(), buf, buf + got);
+        }
+        std::fclose(f);
+    }
+    if (orig.size() < 64)
+    {
+        return 1;
+    }
+    const char* paths[] = {"/n_process",    "/mesh/points", "/mesh/connectivity", "/mesh/fields/signed", "/mesh/fields/small",
+                           "/mesh/level/4/dim/0/intervals/data", "/many/m0", "/many/m20", "/empty", "/nothing", "/mesh/nothing/x"};
+    uint64_t x = seed * 0x9E3779B97F4A7C15ull + 1;
+    auto rnd   = [&]
+    {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        return x;
+    };
+    const std::string tmp = std::string(name) + ".fuzz";
+    int opened = 0, read_ok = 0, read_err = 0;
+    for (int it = 0; it < n; ++it)
+    {
+        std::vector<uint8_t> b = orig;
+        const uint64_t kind    = rnd() % 4;
+        if (kind == 0)
+        {
+            b.resize(rnd() % b.size());
+        }
+        else if (kind == 1)
+        {
+            for (uint64_t k = 0, nk = 1 + rnd() % 8; k < nk; ++k)
+            {
+                b[rnd() % b.size()] ^= static_cast<uint8_t>(1u << (rnd() % 8));
+            }
+        }
+        else if (kind == 2)
+        {
+            const size_t at      = (rnd() & 1) ? (rnd() % (b.size() / 8)) * 8 : rnd() % (b.size() - 8);
+            const uint64_t cands[] = {0, ~uint64_t(0), rnd(), b.size(), b.size() - 1, uint64_t(1) << 40, rnd() % b.size()};
+            const uint64_t v     = cands[rnd() % 7];
+            std::memcpy(&b[at], &v, 8);
+        }
+        else
+        {
+            const size_t at = rnd() % (b.size() - 2);
+            const uint16_t v = static_cast<uint16_t>(rnd());
+            std::memcpy(&b[at], &v, 2);
+        }
+        FILE* f = std::fopen(tmp.c_str(), "wb");
+        if (!f || std::fwrite(b.data(), 1, b.size(), f) != b.size())
+        {
+            return 1;
+        }
+        std::fclose(f);
+        h5::Reader r;
+        std::string err;
+        if (!r.open(tmp, err))
+        {
+            continue;
+        }
+        ++opened;
+        for (const char* p : paths)
+        {
+            h5::Array a;
+            std::string e;
+            if (r.read(p, a, e))
+            {
+                ++read_ok;
+                if (a.bytes.size() != a.count() * a.size)
+                {
+                    std::fprintf(stderr, "iteration %d: %s: %zu bytes for %" PRIu64 " elements of %zu\n", it, p, a.bytes.size(), a.count(), a.size);
+                    return 4;
+                }
+                for (auto& m : a.members)
+                {
+                    if (m.second + a.member_size.at(m.first) > a.size)
+                    {
+                        std::fprintf(stderr, "iteration %d: %s: member %s outside the record\n", it, p, m.first.c_str());
+                        return 4;
+                    }
+                }
+            }
+            else
+            {
+                ++read_err;
+                if (e.empty())
+                {
+                    std::fprintf(stderr, "iteration %d: %s: refused without a message\n", it, p);
+                    return 4;
+                }
+            }
+            r.exists(p);
+        }
+    }
+    std::remove(tmp.c_str());
+    std::printf("%d %d %d\n", opened, read_ok, read_err);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc >= 5 && std::string(argv[1]) == "fuzz")
+    {
+        return fuzz(argv[2], std::strtoull(argv[3], nullptr, 10), std::atoi(argv[4]));
+    }
     if (argc >= 3 && std::string(argv[1]) == "toomany")
     {
         return too_many(argv[2]);

@@ -2,7 +2,8 @@
 by the writer is decoded identically by the library's reader and by the
 independent pure-Python reader of tests/h5lite.py (scalars, 2-D arrays,
 signed and unsigned integers, binary64, samurai's Interval compound, a group
-spread over several symbol-table nodes, an empty dataset)."""
+spread over several symbol-table nodes, an empty dataset), and corrupted
+files are refused without reads outside the buffer."""
 import os
 import subprocess
 
@@ -60,6 +61,31 @@ def test_writer_reader_roundtrip(tool, tmp_path):
     assert subprocess.run([tool, "read", f, "/nothing"], capture_output=True).returncode == 1
     r = subprocess.run([tool, "toomany", str(tmp_path / "big.h5")], capture_output=True)
     assert r.returncode == 3 and b"256 members" in r.stderr
+
+
+@pytest.fixture(scope="module")
+def fuzz_tool(tmp_path_factory):
+    """the same tool under the address and undefined-behaviour sanitizers
+    (a plain build where the compiler has no sanitizer runtime)"""
+    exe = str(tmp_path_factory.mktemp("h5fuzz") / "h5_tool")
+    src = os.path.join(ROOT, "tests", "cpp", "h5_tool.cpp")
+    san = ["-fsanitize=address,undefined", "-fno-sanitize-recover=all", "-g"]
+    if subprocess.run(["g++", "-std=c++17", "-O1"] + san + [src, "-o", exe], capture_output=True).returncode != 0:
+        subprocess.check_call(["g++", "-std=c++17", "-O1", src, "-o", exe])
+    return exe
+
+
+@pytest.mark.parametrize("seed", range(1, 9))
+def test_reader_refuses_corrupted_files(fuzz_tool, tmp_path, seed):
+    """restart files come from users: truncated files, flipped bits and
+    overwritten offsets, sizes and counts make the reader return an error
+    (or a consistent array), never read outside the file"""
+    f = str(tmp_path / "t.h5")
+    subprocess.check_call([fuzz_tool, "write", f])
+    r = subprocess.run([fuzz_tool, "fuzz", f, str(seed), "4000"], capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()[-2000:]
+    opened, ok, refused = (int(v) for v in r.stdout.split())
+    assert opened > 3000 and ok > 0 and refused > 0
 
 
 def test_io_argument_checks():
