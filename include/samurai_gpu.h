@@ -5,7 +5,7 @@
  * FFI of its own; its "interface" for this path is the set of C++ calls a
  * user program makes.  Each entry point below replaces one of them, cited
  * next to it (paths relative to the samurai source tree).  The C++ drop-in
- * headers under include/samurai/ and the Python package samurai_gb300 are
+ * header include/samurai_gb300/samurai.hpp and the Python package samurai_gb300 are
  * thin layers over these functions.
  *
  * Conventions
@@ -16,6 +16,10 @@
  *    (interval.index + x, level_cell_array.hpp:727-743).
  *  - one mesh owns one CUDA stream; calls on a mesh are issued in order on
  *    that stream by one host thread.
+ *  - a mesh may be destroyed before or after its fields: its memory goes
+ *    with the last of them.  An IO list (sg_io_t) and a batch borrow the
+ *    fields given to them, which must outlive them; an adjoint copies what
+ *    it needs at creation.
  *  - there is no CPU fallback: without a usable sm_103a device every call
  *    that computes returns SG_ERR_CUDA.
  */

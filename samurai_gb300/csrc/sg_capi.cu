@@ -472,9 +472,13 @@ extern "C"
 
     int sg_mesh_destroy(sg_mesh_t mesh)
     {
-        if (mesh)
+        if (mesh && !mesh->destroyed)
         {
-            destroy_ctx(mesh);
+            mesh->destroyed = true;
+            if (mesh->attached == 0)
+            {
+                destroy_ctx(mesh);
+            }
         }
         return SG_OK;
     }
@@ -849,6 +853,7 @@ extern "C"
             return fail(SG_ERR_CUDA, "sg_field_create: ", mesh->ctx.err.c_str());
         }
         cudaMemsetAsync(f->f.data, 0, static_cast<size_t>(mesh->ctx.capacity) * sizeof(double), mesh->ctx.stream);
+        ++mesh->attached;
         *out = f;
         return SG_OK;
     }
@@ -857,10 +862,15 @@ extern "C"
     {
         if (field)
         {
-            cudaStreamSynchronize(field->mesh->ctx.stream);
+            sg_mesh_s* mesh = field->mesh;
+            cudaStreamSynchronize(mesh->ctx.stream);
             dfree(field->f.data);
             dfree(field->f.spare);
             delete field;
+            if (--mesh->attached == 0 && mesh->destroyed)
+            {
+                destroy_ctx(mesh);
+            }
         }
         return SG_OK;
     }

@@ -9,6 +9,10 @@ struct sg_mesh_s
     sg::Ctx ctx;
     double* staging     = nullptr; // compact host<->device staging (nb_ref doubles)
     long long staging_n = 0;
+    // fields created on the mesh and not yet destroyed: sg_mesh_destroy of a mesh that still has fields
+    // only marks it, and the last sg_field_destroy frees it, so that no destruction order touches freed memory
+    long long attached = 0;
+    bool destroyed     = false;
 };
 
 struct sg_field_s

@@ -397,3 +397,25 @@ def test_field_fill_and_factories(sg):
     assert np.array_equal(v.cell_values(), c[:, 0] + 2.0 * c[:, 1])
     v.fill(-3.0)
     assert np.all(v.array() == -3.0)
+
+
+def test_mesh_destroyed_before_its_fields(sg):
+    """sg_mesh_destroy of a mesh that still has fields (a reference cycle
+    collected in any order, a C caller) releases it with the last field"""
+    import ctypes
+
+    L = sg.lib()
+    m, f, v = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    assert L.sg_mesh_create(2, 2, 6, 1, 1, 1, ctypes.byref(m)) == 0
+    assert L.sg_field_create(m, b"u", ctypes.byref(f)) == 0
+    assert L.sg_vector_field_create(m, b"v", 2, ctypes.byref(v)) == 0
+    assert L.sg_field_fill(f, 2.0) == 0
+    assert L.sg_mesh_destroy(m) == 0
+    assert L.sg_vector_field_destroy(v) == 0
+    assert L.sg_field_destroy(f) == 0
+    # the library and the device stay usable
+    g = sg.AdvectionSim(2, 2, 6, 1, 1)
+    o = OracleSim(2, 2, 6, 1, 1)
+    init_both(g, o, disc)
+    assert g.adapt(1e-3, 1.0) == o.adapt(1e-3, 1.0)
+    compare_cells(g, o, "after the out-of-order destruction")
