@@ -1,5 +1,6 @@
 // C ABI of libsamurai_gpu.so (declared in include/samurai_gpu.h).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -362,6 +363,20 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_mesh_create: only max_stencil_radius 1 is implemented");
         }
+        {
+            // the dense slabs of all levels (the bitmap words of sg::make_geom, 32 cells each), counted in
+            // floating point so that levels whose sizes overflow 64-bit integers (3D beyond about 20) are refused
+            double words = 0.0;
+            for (int l = 0; l <= max_level; ++l)
+            {
+                const double n = std::ldexp(1.0, l), W = std::ceil(n / 32.0) + 2.0, R = n + 2.0 * sg::PY;
+                words += (dim == 2 ? R : R * R) * W;
+            }
+            if (words * 32.0 * sizeof(double) > std::ldexp(1.0, 47))
+            {
+                return fail(SG_ERR_CAPACITY, "sg_mesh_create: max_level too fine: one field's dense slabs would exceed 128 TiB");
+            }
+        }
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         {
@@ -668,9 +683,9 @@ extern "C"
 
     int sg_mesh_set_cells(sg_mesh_t mesh, long long n, const int* level, const int* coords)
     {
-        if (!mesh || (n > 0 && (!level || !coords)))
+        if (!mesh || n < 0 || (n > 0 && (!level || !coords)))
         {
-            return fail(SG_ERR_ARG, "sg_mesh_set_cells: null argument");
+            return fail(SG_ERR_ARG, "sg_mesh_set_cells: null argument or negative count");
         }
         sg::Ctx& c = mesh->ctx;
         const int D = c.g.dim;

@@ -96,6 +96,10 @@ def test_mesh_create_rejects_unsupported_configurations():
         assert L.sg_mesh_create(*args, ctypes.byref(h)) == 1, args
         assert L.sg_last_error()
     assert L.sg_mesh_create(2, 2, 5, 1, 1, 1, None) == 1
+    # 3D levels whose bitmap sizes overflow 64-bit integers are refused before any device call
+    for maxl in (16, 20, 23):
+        assert L.sg_mesh_create(3, 2, maxl, 1, 1, 1, ctypes.byref(h)) == 3, maxl
+        assert b"too fine" in L.sg_last_error()
 
 
 def test_adjoint_argument_checks():

@@ -410,6 +410,7 @@ def test_mesh_destroyed_before_its_fields(sg):
     assert L.sg_field_create(m, b"u", ctypes.byref(f)) == 0
     assert L.sg_vector_field_create(m, b"v", 2, ctypes.byref(v)) == 0
     assert L.sg_field_fill(f, 2.0) == 0
+    assert L.sg_mesh_set_cells(m, -1, None, None) == 1
     assert L.sg_mesh_destroy(m) == 0
     assert L.sg_vector_field_destroy(v) == 0
     assert L.sg_field_destroy(f) == 0
