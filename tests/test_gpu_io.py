@@ -177,3 +177,42 @@ def test_load_rejects_other_levels_and_missing_fields(sg, tmp_path):
         sg.load(str(tmp_path), "r", same.mesh, v)
     with pytest.raises(sg.SamuraiGpuError):
         sg.load(str(tmp_path), "missing", same.mesh, same.u)
+
+
+def test_load_refuses_corrupted_restart_files(sg, tmp_path):
+    """an interval outside the level's box, an offsets entry past the
+    interval array and a truncated file are refused with an error; a valid
+    file still loads afterwards"""
+    g = sg.AdvectionSim(2, 2, 6, 1, 1)
+    lv, co, _ = g.cells()
+    g.set_cell_values(shapes_2d(9, 2, 2)(lv, co))
+    g.adapt(1e-3, 1.0)
+    sg.dump(str(tmp_path), "good", g.mesh, g.u)
+    good = os.path.join(str(tmp_path), "good.h5")
+    raw = open(good, "rb").read()
+    h = H5(good)
+    lev = max(l for l in range(7) if h.exists("/mesh/level/%d" % l))
+    ivx = h.read("/mesh/level/%d/dim/0/intervals/data" % lev)
+    offs = h.read("/mesh/level/%d/dim/1/offsets/data" % lev)
+    at_iv = raw.find(ivx.tobytes())
+    at_off = raw.find(offs.tobytes())
+    assert at_iv > 0 and at_off > 0
+
+    def corrupted(name, data):
+        with open(os.path.join(str(tmp_path), name + ".h5"), "wb") as f:
+            f.write(data)
+
+    b = bytearray(raw)
+    b[at_iv + 4:at_iv + 8] = np.int32(1 << 30).tobytes()  # end of the first x-interval
+    corrupted("far", bytes(b))
+    b = bytearray(raw)
+    b[at_off + 8:at_off + 16] = np.uint64(1 << 40).tobytes()  # second offsets entry
+    corrupted("offsets", bytes(b))
+    corrupted("short", raw[: len(raw) // 2])
+    for name, what in (("far", "outside"), ("offsets", "inconsistent"), ("short", "")):
+        r = sg.AdvectionSim(2, 2, 6, 1, 1)
+        with pytest.raises(sg.SamuraiGpuError, match=what):
+            sg.load(str(tmp_path), name, r.mesh, r.u)
+    r = sg.AdvectionSim(2, 2, 6, 1, 1)
+    sg.load(str(tmp_path), "good", r.mesh, r.u)
+    assert np.array_equal(r.cell_values(), g.cell_values())
