@@ -209,7 +209,7 @@ def test_load_refuses_corrupted_restart_files(sg, tmp_path):
     b[at_off + 8:at_off + 16] = np.uint64(1 << 40).tobytes()  # second offsets entry
     corrupted("offsets", bytes(b))
     corrupted("short", raw[: len(raw) // 2])
-    for name, what in (("far", "outside"), ("offsets", "inconsistent"), ("short", "")):
+    for name, what in (("far", "outside"), ("offsets", "inconsistent"), ("short", None)):
         r = sg.AdvectionSim(2, 2, 6, 1, 1)
         with pytest.raises(sg.SamuraiGpuError, match=what):
             sg.load(str(tmp_path), name, r.mesh, r.u)
