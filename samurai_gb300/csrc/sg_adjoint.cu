@@ -35,7 +35,6 @@
 
 namespace sg
 {
-    void set_last_error(const char* msg, const char* detail);
     int ensure_spare(Ctx& c, DeviceField& f);
 
     namespace
@@ -726,6 +725,7 @@ namespace
 extern "C"
 {
     int sg_adjoint_create(sg_field_t u, int checkpoint_every, sg_adjoint_t* out)
+    try
     {
         if (!u || !out || checkpoint_every < 1)
         {
@@ -795,8 +795,10 @@ extern "C"
         *out = adj;
         return SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_create)
 
     int sg_adjoint_destroy(sg_adjoint_t adj)
+    try
     {
         if (!adj)
         {
@@ -851,8 +853,10 @@ extern "C"
         delete adj;
         return SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_destroy)
 
     int sg_adjoint_counts(sg_adjoint_t adj, long long* n0, long long* nT, int* n_steps)
+    try
     {
         if (!adj)
         {
@@ -872,8 +876,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_counts)
 
     int sg_adjoint_cells(sg_adjoint_t adj, int which, int* level, int* coords, long long n)
+    try
     {
         if (!adj || (which != 0 && which != 1))
         {
@@ -899,9 +905,11 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_cells)
 
     int sg_adjoint_record(sg_adjoint_t adj, const double* u0, int n_steps, double eps, double regularity, const double* a, double dt, int scheme,
                           long long* nT)
+    try
     {
         if (!adj || !u0 || !a || n_steps < 0 || (scheme != SG_UPWIND_OP && scheme != SG_README))
         {
@@ -977,8 +985,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_record)
 
     int sg_adjoint_final(sg_adjoint_t adj, double* uT, long long n)
+    try
     {
         if (!adj || !uT)
         {
@@ -996,8 +1006,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_final)
 
     int sg_adjoint_replay(sg_adjoint_t adj, const double* u0, const double* a, double* uT)
+    try
     {
         if (!adj || !u0 || !a)
         {
@@ -1026,8 +1038,10 @@ extern "C"
         sg::k_leaf_gather<<<sg::grid_of(adj->nT), sg::ABLOCK, 0, c.stream>>>(adj->d_elT, adj->u->f.data, adj->nT, adj->d_uT);
         return uT ? sg_adjoint_final(adj, uT, adj->nT) : SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_replay)
 
     int sg_adjoint_backward(sg_adjoint_t adj, const double* gT, double* g0, double* ga)
+    try
     {
         if (!adj || !gT || !g0)
         {
@@ -1129,4 +1143,5 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_adjoint_backward)
 }

@@ -25,7 +25,6 @@
 
 namespace sg
 {
-    void set_last_error(const char* msg, const char* detail);
     int ensure_spare(Ctx& c, DeviceField& f);
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words);
     void set_fusion_tops(Ctx& c, int mesh_top, int field_top, int max_top);
@@ -288,6 +287,7 @@ namespace
 extern "C"
 {
     int sg_batch_create(int n, const sg_field_t* u, const sg_field_t* unp1, int n_threads, sg_batch_t* out)
+    try
     {
         if (!out || n <= 0 || !u || !unp1 || n_threads <= 0)
         {
@@ -355,8 +355,10 @@ extern "C"
         *out = b;
         return SG_OK;
     }
+    SG_API_CATCH(sg_batch_create)
 
     int sg_batch_destroy(sg_batch_t b)
+    try
     {
         if (b)
         {
@@ -368,8 +370,10 @@ extern "C"
         delete b;
         return SG_OK;
     }
+    SG_API_CATCH(sg_batch_destroy)
 
     int sg_batch_size(sg_batch_t b, int* n)
+    try
     {
         if (!b || !n)
         {
@@ -378,8 +382,10 @@ extern "C"
         *n = static_cast<int>(b->u.size());
         return SG_OK;
     }
+    SG_API_CATCH(sg_batch_size)
 
     int sg_batch_adapt(sg_batch_t b, const double* eps, const double* regularity, int* n_harten)
+    try
     {
         if (!b || !eps || !regularity)
         {
@@ -387,8 +393,10 @@ extern "C"
         }
         return b->run([&](int t) { adapt_share(*b, t, eps, regularity, n_harten); });
     }
+    SG_API_CATCH(sg_batch_adapt)
 
     int sg_batch_update_ghost_mr(sg_batch_t b)
+    try
     {
         if (!b)
         {
@@ -396,8 +404,10 @@ extern "C"
         }
         return b->run([&](int t) { ghost_share(*b, t); });
     }
+    SG_API_CATCH(sg_batch_update_ghost_mr)
 
     int sg_batch_upwind(sg_batch_t b, const double* a, const double* dt, int scheme)
+    try
     {
         if (!b)
         {
@@ -409,8 +419,10 @@ extern "C"
         }
         return b->run([&](int t) { upwind_share(*b, t, a, dt, scheme, false); });
     }
+    SG_API_CATCH(sg_batch_upwind)
 
     int sg_batch_swap(sg_batch_t b)
+    try
     {
         if (!b)
         {
@@ -424,9 +436,11 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_batch_swap)
 
     int sg_batch_step(sg_batch_t b, const double* eps, const double* regularity, const double* a, const double* dt, int scheme,
                       int* n_harten)
+    try
     {
         if (!b || !eps || !regularity)
         {
@@ -448,8 +462,10 @@ extern "C"
                 upwind_share(*b, t, a, dt, scheme, true);
             });
     }
+    SG_API_CATCH(sg_batch_step)
 
     int sg_batch_synchronize(sg_batch_t b)
+    try
     {
         if (!b)
         {
@@ -465,4 +481,5 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_batch_synchronize)
 }

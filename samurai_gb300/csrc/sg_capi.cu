@@ -322,6 +322,7 @@ extern "C"
     }
 
     int sg_version(int* major, int* minor)
+    try
     {
         if (major)
         {
@@ -333,14 +334,18 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_version)
 
     int sg_mesh_create(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width, sg_mesh_t* out)
+    try
     {
         return sg_mesh_create_periodic(dim, min_level, max_level, max_stencil_radius, prediction_radius, graduation_width, nullptr, out);
     }
+    SG_API_CATCH(sg_mesh_create)
 
     int sg_mesh_create_periodic(int dim, int min_level, int max_level, int max_stencil_radius, int prediction_radius, int graduation_width,
                                 const int* periodic, sg_mesh_t* out)
+    try
     {
         if (!out)
         {
@@ -484,8 +489,10 @@ extern "C"
         *out = h;
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_create_periodic)
 
     int sg_mesh_destroy(sg_mesh_t mesh)
+    try
     {
         if (mesh && !mesh->destroyed)
         {
@@ -497,8 +504,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_destroy)
 
     int sg_mesh_counts(sg_mesh_t mesh, long long* nb_cells, long long* nb_reference)
+    try
     {
         if (!mesh)
         {
@@ -518,8 +527,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_counts)
 
     int sg_mesh_get_cells(sg_mesh_t mesh, int* level, int* coords, long long* index, long long capacity)
+    try
     {
         if (!mesh)
         {
@@ -576,8 +587,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_get_cells)
 
     int sg_mesh_count_intervals(sg_mesh_t mesh, int mesh_id, int level, long long* n)
+    try
     {
         if (!mesh || !n)
         {
@@ -613,8 +626,10 @@ extern "C"
         *n = cnt;
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_count_intervals)
 
     int sg_mesh_get_intervals(sg_mesh_t mesh, int mesh_id, int level, long long* out, long long capacity)
+    try
     {
         if (!mesh || !out)
         {
@@ -680,8 +695,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_get_intervals)
 
     int sg_mesh_set_cells(sg_mesh_t mesh, long long n, const int* level, const int* coords)
+    try
     {
         if (!mesh || n < 0 || (n > 0 && (!level || !coords)))
         {
@@ -715,8 +732,10 @@ extern "C"
         }
         return from_ctx(c, st);
     }
+    SG_API_CATCH(sg_mesh_set_cells)
 
     int sg_mesh_stream(sg_mesh_t mesh, void** stream)
+    try
     {
         if (!mesh || !stream)
         {
@@ -725,8 +744,10 @@ extern "C"
         *stream = mesh->ctx.stream;
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_stream)
 
     int sg_mesh_synchronize(sg_mesh_t mesh)
+    try
     {
         if (!mesh)
         {
@@ -739,8 +760,10 @@ extern "C"
         }
         return from_ctx(mesh->ctx, sg::device_error(mesh->ctx));
     }
+    SG_API_CATCH(sg_mesh_synchronize)
 
     int sg_mesh_version(sg_mesh_t mesh, unsigned long long* version)
+    try
     {
         if (!mesh || !version)
         {
@@ -749,8 +772,10 @@ extern "C"
         *version = mesh->ctx.mesh_version;
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_version)
 
     int sg_mesh_launch_count(sg_mesh_t mesh, int reset, long long* count)
+    try
     {
         if (!mesh)
         {
@@ -766,8 +791,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_mesh_launch_count)
 
     int sg_device_fp64_rate(double* gflops)
+    try
     {
         if (!gflops)
         {
@@ -804,8 +831,10 @@ extern "C"
         *gflops          = ops / (ms * 1e-3) / 1e9;
         return SG_OK;
     }
+    SG_API_CATCH(sg_device_fp64_rate)
 
     int sg_timers_enable(sg_mesh_t mesh, int enable)
+    try
     {
         if (!mesh)
         {
@@ -814,8 +843,10 @@ extern "C"
         mesh->ctx.timers.enabled = enable != 0;
         return SG_OK;
     }
+    SG_API_CATCH(sg_timers_enable)
 
     int sg_timers_get(sg_mesh_t mesh, int timer_id, double* total_ms, long long* calls)
+    try
     {
         if (!mesh || timer_id < 0 || timer_id >= sg::T_COUNT)
         {
@@ -832,8 +863,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_timers_get)
 
     int sg_timers_reset(sg_mesh_t mesh)
+    try
     {
         if (!mesh)
         {
@@ -847,8 +880,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_timers_reset)
 
     int sg_field_create(sg_mesh_t mesh, const char* name, sg_field_t* out)
+    try
     {
         if (!mesh || !out)
         {
@@ -872,8 +907,10 @@ extern "C"
         *out = f;
         return SG_OK;
     }
+    SG_API_CATCH(sg_field_create)
 
     int sg_field_destroy(sg_field_t field)
+    try
     {
         if (field)
         {
@@ -889,8 +926,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_field_destroy)
 
     int sg_field_set_dirichlet(sg_field_t field, double value)
+    try
     {
         if (!field)
         {
@@ -900,8 +939,10 @@ extern "C"
         field->f.bc_value = value;
         return SG_OK;
     }
+    SG_API_CATCH(sg_field_set_dirichlet)
 
     int sg_field_upload_device(sg_field_t field, const double* dvalues, long long n)
+    try
     {
         if (!field || !dvalues)
         {
@@ -919,8 +960,10 @@ extern "C"
         field->f.ghosts_valid = false;
         return from_ctx(c, sg::scatter_compact(c, c.m(), dvalues, field->f.data));
     }
+    SG_API_CATCH(sg_field_upload_device)
 
     int sg_field_download_device(sg_field_t field, double* dvalues, long long n)
+    try
     {
         if (!field || !dvalues)
         {
@@ -937,8 +980,10 @@ extern "C"
         }
         return from_ctx(c, sg::gather_compact(c, c.m(), field->f.data, dvalues));
     }
+    SG_API_CATCH(sg_field_download_device)
 
     int sg_field_upload(sg_field_t field, const double* values, long long n)
+    try
     {
         if (!field || !values)
         {
@@ -967,8 +1012,10 @@ extern "C"
         }
         return from_ctx(c, st);
     }
+    SG_API_CATCH(sg_field_upload)
 
     int sg_field_download(sg_field_t field, double* values, long long n)
+    try
     {
         if (!field || !values)
         {
@@ -1000,8 +1047,10 @@ extern "C"
         }
         return from_ctx(c, sg::device_error(c));
     }
+    SG_API_CATCH(sg_field_download)
 
     int sg_field_set_cells(sg_field_t field, const double* values, long long n)
+    try
     {
         if (!field || !values)
         {
@@ -1028,8 +1077,10 @@ extern "C"
         }
         return sg_field_upload(field, full.data(), c.m().nb_ref);
     }
+    SG_API_CATCH(sg_field_set_cells)
 
     int sg_field_get_cells(sg_field_t field, double* values, long long n)
+    try
     {
         if (!field || !values)
         {
@@ -1060,8 +1111,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_field_get_cells)
 
     int sg_field_fill(sg_field_t field, double value)
+    try
     {
         if (!field)
         {
@@ -1075,8 +1128,10 @@ extern "C"
         field->f.ghosts_valid = false;
         return from_ctx(c, sg::fill_ref(c, c.m(), field->f.data, value));
     }
+    SG_API_CATCH(sg_field_fill)
 
     int sg_field_swap(sg_field_t a, sg_field_t b)
+    try
     {
         if (!a || !b || a->mesh != b->mesh)
         {
@@ -1087,13 +1142,17 @@ extern "C"
         b->f.ghosts_valid = false;
         return SG_OK;
     }
+    SG_API_CATCH(sg_field_swap)
 
     int sg_adapt(sg_field_t u, double eps, double regularity, int* n_harten)
+    try
     {
         return sg_adapt_ex(u, eps, regularity, 0, n_harten);
     }
+    SG_API_CATCH(sg_adapt)
 
     int sg_adapt_ex(sg_field_t u, double eps, double regularity, int relative_detail, int* n_harten)
+    try
     {
         if (!u)
         {
@@ -1106,14 +1165,18 @@ extern "C"
         }
         return from_ctx(c, sg::adapt(c, u->f, eps, regularity, n_harten, relative_detail != 0));
     }
+    SG_API_CATCH(sg_adapt_ex)
 
     int sg_harten(sg_field_t u, int ite, double eps, double regularity, int* converged)
+    try
     {
         return sg_harten_ex(u, ite, eps, regularity, 0, converged);
     }
+    SG_API_CATCH(sg_harten)
 
     int sg_adapt_fields(int n, const sg_field_t* fields, int n_other, const sg_field_t* others, double eps, double regularity,
                         int relative_detail, int* n_harten)
+    try
     {
         if (n < 1 || !fields || n_other < 0 || (n_other > 0 && !others) || !fields[0])
         {
@@ -1169,8 +1232,10 @@ extern "C"
         }
         return from_ctx(c, sg::adapt_fields(c, fs, os, eps, regularity, relative_detail != 0, n_harten));
     }
+    SG_API_CATCH(sg_adapt_fields)
 
     int sg_update_ghost_mr_fields(int n, const sg_field_t* fields)
+    try
     {
         if (n < 0 || (n > 0 && !fields))
         {
@@ -1185,8 +1250,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_update_ghost_mr_fields)
 
     int sg_harten_ex(sg_field_t u, int ite, double eps, double regularity, int relative_detail, int* converged)
+    try
     {
         if (!u)
         {
@@ -1205,8 +1272,10 @@ extern "C"
         }
         return from_ctx(c, st);
     }
+    SG_API_CATCH(sg_harten_ex)
 
     int sg_update_ghost_mr(sg_field_t u)
+    try
     {
         if (!u)
         {
@@ -1214,8 +1283,10 @@ extern "C"
         }
         return from_ctx(u->mesh->ctx, sg::update_ghost_mr(u->mesh->ctx, u->f));
     }
+    SG_API_CATCH(sg_update_ghost_mr)
 
     int sg_upwind(sg_field_t u, sg_field_t unp1, const double* a, double dt, int scheme)
+    try
     {
         if (!u || !unp1 || !a || u->mesh != unp1->mesh || u == unp1)
         {
@@ -1237,8 +1308,10 @@ extern "C"
         unp1->f.ghosts_valid = false;
         return from_ctx(c, sg::upwind(c, u->f, unp1->f, a, dt, scheme));
     }
+    SG_API_CATCH(sg_upwind)
 
     int sg_detail_download(sg_field_t u, double* values, long long n)
+    try
     {
         if (!u || !values)
         {
@@ -1270,8 +1343,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_detail_download)
 
     int sg_tag_download(sg_field_t u, unsigned char* values, long long n)
+    try
     {
         if (!u || !values)
         {
@@ -1309,4 +1384,5 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_tag_download)
 }

@@ -1,8 +1,35 @@
 // Opaque handle types of the C ABI (include/samurai_gpu.h).
 #pragma once
 
+#include <exception>
+#include <new>
+
 #include "../../include/samurai_gpu.h"
 #include "sg_ctx.cuh"
+
+namespace sg
+{
+    void set_last_error(const char* msg, const char* detail);
+}
+
+// The handler of every C entry point's function-try-block: no C++ exception (a host allocation that fails,
+// a library throw) leaves the C ABI; it becomes a status code and sg_last_error().
+#define SG_API_CATCH(fn)                                                                                                   \
+    catch (const std::bad_alloc&)                                                                                          \
+    {                                                                                                                      \
+        sg::set_last_error(#fn ": out of host memory", nullptr);                                                          \
+        return SG_ERR_CAPACITY;                                                                                            \
+    }                                                                                                                      \
+    catch (const std::exception& e)                                                                                        \
+    {                                                                                                                      \
+        sg::set_last_error(#fn ": ", e.what());                                                                            \
+        return SG_ERR_ARG;                                                                                                 \
+    }                                                                                                                      \
+    catch (...)                                                                                                            \
+    {                                                                                                                      \
+        sg::set_last_error(#fn ": unexpected exception", nullptr);                                                        \
+        return SG_ERR_ARG;                                                                                                 \
+    }
 
 struct sg_mesh_s
 {

@@ -25,10 +25,6 @@
 
 #include "sg_handles.cuh"
 
-namespace sg
-{
-    void set_last_error(const char* msg, const char* detail);
-}
 
 // an ordered list of scalar and vector fields for save / dump / load
 struct sg_io_s
@@ -133,29 +129,12 @@ namespace
         }
         return SG_OK;
     }
-
-    // host allocations sized from the mesh or from a file's contents can throw; no exception leaves the C ABI
-    template <class F>
-    int guarded(const char* what, F&& body)
-    {
-        try
-        {
-            return body();
-        }
-        catch (const std::bad_alloc&)
-        {
-            return iofail(SG_ERR_CAPACITY, std::string(what) + ": out of host memory");
-        }
-        catch (const std::exception& e)
-        {
-            return iofail(SG_ERR_ARG, std::string(what) + ": " + e.what());
-        }
-    }
 } // namespace
 
 extern "C"
 {
     int sg_io_create(sg_io_t* out)
+    try
     {
         if (!out)
         {
@@ -164,14 +143,18 @@ extern "C"
         *out = new (std::nothrow) sg_io_s();
         return *out ? SG_OK : iofail(SG_ERR_CAPACITY, "sg_io_create: out of host memory");
     }
+    SG_API_CATCH(sg_io_create)
 
     int sg_io_destroy(sg_io_t io)
+    try
     {
         delete io;
         return SG_OK;
     }
+    SG_API_CATCH(sg_io_destroy)
 
     int sg_io_add_field(sg_io_t io, sg_field_t f)
+    try
     {
         if (!io || !f)
         {
@@ -180,8 +163,10 @@ extern "C"
         io->items.push_back({f, nullptr});
         return SG_OK;
     }
+    SG_API_CATCH(sg_io_add_field)
 
     int sg_io_add_vector_field(sg_io_t io, sg_vfield_t v)
+    try
     {
         if (!io || !v)
         {
@@ -190,6 +175,7 @@ extern "C"
         io->items.push_back({nullptr, v});
         return SG_OK;
     }
+    SG_API_CATCH(sg_io_add_vector_field)
 
     static int save_body(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
     {
@@ -655,22 +641,30 @@ extern "C"
     }
 
     int sg_save(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    try
     {
-        return guarded("sg_save", [&] { return save_body(path, filename, mesh, fields); });
+        return save_body(path, filename, mesh, fields);
     }
+    SG_API_CATCH(sg_save)
 
     int sg_dump(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    try
     {
-        return guarded("sg_dump", [&] { return dump_body(path, filename, mesh, fields); });
+        return dump_body(path, filename, mesh, fields);
     }
+    SG_API_CATCH(sg_dump)
 
     int sg_restart_levels(const char* path, const char* filename, int* dim, int* min_level, int* max_level)
+    try
     {
-        return guarded("sg_restart_levels", [&] { return restart_levels_body(path, filename, dim, min_level, max_level); });
+        return restart_levels_body(path, filename, dim, min_level, max_level);
     }
+    SG_API_CATCH(sg_restart_levels)
 
     int sg_load(const char* path, const char* filename, sg_mesh_t mesh, sg_io_t fields)
+    try
     {
-        return guarded("sg_load", [&] { return load_body(path, filename, mesh, fields); });
+        return load_body(path, filename, mesh, fields);
     }
+    SG_API_CATCH(sg_load)
 }

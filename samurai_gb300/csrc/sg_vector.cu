@@ -26,10 +26,6 @@
 
 #include "sg_handles.cuh"
 
-namespace sg
-{
-    void set_last_error(const char* msg, const char* detail);
-}
 
 namespace
 {
@@ -108,6 +104,7 @@ namespace
 extern "C"
 {
     int sg_vector_field_create(sg_mesh_t mesh, const char* name, int n_comp, sg_vfield_t* out)
+    try
     {
         if (!mesh || !out || n_comp < 1 || n_comp > SG_MAX_COMPONENTS)
         {
@@ -136,8 +133,10 @@ extern "C"
         *out = v;
         return SG_OK;
     }
+    SG_API_CATCH(sg_vector_field_create)
 
     int sg_vector_field_destroy(sg_vfield_t v)
+    try
     {
         if (v)
         {
@@ -149,8 +148,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_vector_field_destroy)
 
     int sg_vector_field_n_comp(sg_vfield_t v, int* n_comp)
+    try
     {
         if (!v || !n_comp)
         {
@@ -159,8 +160,10 @@ extern "C"
         *n_comp = static_cast<int>(v->comp.size());
         return SG_OK;
     }
+    SG_API_CATCH(sg_vector_field_n_comp)
 
     int sg_vector_field_component(sg_vfield_t v, int c, sg_field_t* out)
+    try
     {
         if (!v || !out || c < 0 || c >= static_cast<int>(v->comp.size()))
         {
@@ -169,8 +172,10 @@ extern "C"
         *out = v->comp[static_cast<size_t>(c)];
         return SG_OK;
     }
+    SG_API_CATCH(sg_vector_field_component)
 
     int sg_vector_field_set_dirichlet(sg_vfield_t v, const double* values)
+    try
     {
         if (!v || !values)
         {
@@ -185,28 +190,38 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_vector_field_set_dirichlet)
 
     int sg_vector_field_upload(sg_vfield_t v, const double* values, long long n)
+    try
     {
         return move_host(v, const_cast<double*>(values), n, false, true, sg_field_upload, "sg_vector_field_upload: null argument");
     }
+    SG_API_CATCH(sg_vector_field_upload)
 
     int sg_vector_field_download(sg_vfield_t v, double* values, long long n)
+    try
     {
         return move_host(v, values, n, false, false, sg_field_download, "sg_vector_field_download: null argument");
     }
+    SG_API_CATCH(sg_vector_field_download)
 
     int sg_vector_field_set_cells(sg_vfield_t v, const double* values, long long n)
+    try
     {
         return move_host(v, const_cast<double*>(values), n, true, true, sg_field_set_cells, "sg_vector_field_set_cells: null argument");
     }
+    SG_API_CATCH(sg_vector_field_set_cells)
 
     int sg_vector_field_get_cells(sg_vfield_t v, double* values, long long n)
+    try
     {
         return move_host(v, values, n, true, false, sg_field_get_cells, "sg_vector_field_get_cells: null argument");
     }
+    SG_API_CATCH(sg_vector_field_get_cells)
 
     int sg_vector_field_swap(sg_vfield_t a, sg_vfield_t b)
+    try
     {
         if (!same_shape(a, b) || a == b)
         {
@@ -221,8 +236,10 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_vector_field_swap)
 
     int sg_vector_adapt(sg_vfield_t v, double eps, double regularity, int relative_detail, int* n_harten)
+    try
     {
         if (!v)
         {
@@ -230,8 +247,10 @@ extern "C"
         }
         return sg_adapt_fields(static_cast<int>(v->comp.size()), v->comp.data(), 0, nullptr, eps, regularity, relative_detail, n_harten);
     }
+    SG_API_CATCH(sg_vector_adapt)
 
     int sg_vector_update_ghost_mr(sg_vfield_t v)
+    try
     {
         if (!v)
         {
@@ -239,8 +258,10 @@ extern "C"
         }
         return sg_update_ghost_mr_fields(static_cast<int>(v->comp.size()), v->comp.data());
     }
+    SG_API_CATCH(sg_vector_update_ghost_mr)
 
     int sg_vector_upwind(sg_vfield_t u, sg_vfield_t unp1, const double* a, double dt, int scheme)
+    try
     {
         if (!same_shape(u, unp1) || u == unp1 || !a)
         {
@@ -255,4 +276,5 @@ extern "C"
         }
         return SG_OK;
     }
+    SG_API_CATCH(sg_vector_upwind)
 }
