@@ -21,7 +21,7 @@ def compile_demo(tmp_path, src=SRC):
 
     lib = build.build()
     exe = os.path.join(str(tmp_path), os.path.splitext(os.path.basename(src))[0])
-    cmd = ["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), src, "-L" + os.path.dirname(lib), "-lsamurai_gpu",
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"), src, "-L" + os.path.dirname(lib), "-lsamurai_gpu",
            "-Wl,-rpath," + os.path.dirname(lib), "-o", exe]
     subprocess.check_call(cmd)
     return exe

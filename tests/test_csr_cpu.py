@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 @pytest.fixture(scope="module")
 def tool(tmp_path_factory):
     exe = str(tmp_path_factory.mktemp("csr") / "csr_tool")
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", os.path.join(ROOT, "tests", "cpp", "csr_tool.cpp"), "-o", exe])
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", os.path.join(ROOT, "tests", "cpp", "csr_tool.cpp"), "-o", exe])
     return exe
 
 
