@@ -109,5 +109,89 @@ namespace sg
                 }
             }
         }
+
+        enum class Decode
+        {
+            ok,
+            outside,     // an interval leaves the level's box [0, 2^level)
+            inconsistent // an offsets slot or range that the arrays do not hold
+        };
+
+        // The inverse of build_csr for a restart file's level: the cells of the layout in for_each_cell order
+        // (z outer, y, x inner), appended to `coords` as x, y[, z].  The layout comes from a file, so every
+        // interval is checked against the box (which also bounds the walk and keeps index + coordinate from
+        // overflowing) and every offsets slot and range against the arrays, before it is used.
+        inline Decode decode_csr(int dim, int level, const LevelCSR& c, std::vector<int>& coords)
+        {
+            const int64_t n = int64_t(1) << level;
+            for (int d = 0; d < dim; ++d)
+            {
+                for (const auto& r : c.iv[d])
+                {
+                    if (r.start < 0 || r.start > r.end || r.end > n || r.index < -(int64_t(1) << 62) || r.index > (int64_t(1) << 62))
+                    {
+                        return Decode::outside;
+                    }
+                }
+            }
+            auto range = [&](int d, int64_t slot, uint64_t& b, uint64_t& e) -> bool
+            {
+                const auto& o = c.off[d - 1];
+                if (slot < 0 || static_cast<uint64_t>(slot) + 1 >= o.size())
+                {
+                    return false;
+                }
+                b = o[static_cast<size_t>(slot)];
+                e = o[static_cast<size_t>(slot) + 1];
+                return b <= e && e <= c.iv[d - 1].size();
+            };
+            auto row = [&](uint64_t b, uint64_t e, int y, int z)
+            {
+                for (uint64_t k = b; k < e; ++k)
+                {
+                    for (int x = c.iv[0][k].start; x < c.iv[0][k].end; ++x)
+                    {
+                        coords.push_back(x);
+                        coords.push_back(y);
+                        if (dim == 3)
+                        {
+                            coords.push_back(z);
+                        }
+                    }
+                }
+            };
+            auto plane = [&](uint64_t yb, uint64_t ye, int z) -> bool
+            {
+                for (uint64_t k = yb; k < ye; ++k)
+                {
+                    for (int y = c.iv[1][k].start; y < c.iv[1][k].end; ++y)
+                    {
+                        uint64_t b = 0, e = 0;
+                        if (!range(1, c.iv[1][k].index + y, b, e))
+                        {
+                            return false;
+                        }
+                        row(b, e, y, z);
+                    }
+                }
+                return true;
+            };
+            if (dim == 2)
+            {
+                return plane(0, c.iv[1].size(), 0) ? Decode::ok : Decode::inconsistent;
+            }
+            for (const auto& rz : c.iv[2])
+            {
+                for (int z = rz.start; z < rz.end; ++z)
+                {
+                    uint64_t b = 0, e = 0;
+                    if (!range(2, rz.index + z, b, e) || !plane(b, e, z))
+                    {
+                        return Decode::inconsistent;
+                    }
+                }
+            }
+            return Decode::ok;
+        }
     } // namespace csr
 } // namespace sg

@@ -481,107 +481,44 @@ extern "C"
             {
                 continue;
             }
-            std::vector<sg::csr::IntervalRec> iv[3];
-            std::vector<uint64_t> off[2];
+            sg::csr::LevelCSR csr;
             for (int d = 0; d < D; ++d)
             {
-                sg::h5::Array a, part;
+                sg::h5::Array a;
                 const std::string p = base + std::to_string(d) + "/intervals";
                 if (!r.read(p + "/data", a, err) || a.cls != 6 || a.size != 24 || !a.member("start", 4) || !a.member("end", 4)
                     || !a.member("index", 8))
                 {
                     return iofail(SG_ERR_ARG, "sg_load: " + (err.empty() ? p + " is not an Interval array" : err));
                 }
-                iv[d].resize(static_cast<size_t>(a.count()));
-                for (size_t k = 0; k < iv[d].size(); ++k)
+                auto& iv = csr.iv[d];
+                iv.resize(static_cast<size_t>(a.count()));
+                for (size_t k = 0; k < iv.size(); ++k)
                 {
                     const uint8_t* q = a.bytes.data() + 24 * k;
-                    std::memcpy(&iv[d][k].start, q + a.members.at("start"), 4);
-                    std::memcpy(&iv[d][k].end, q + a.members.at("end"), 4);
-                    std::memcpy(&iv[d][k].index, q + a.members.at("index"), 8);
-                    // inside the level's box, so that the walk below stays bounded and index + coordinate cannot overflow
-                    const auto& rec = iv[d][k];
-                    if (rec.start < 0 || rec.start > rec.end || static_cast<int64_t>(rec.end) > (int64_t(1) << l) || rec.index < -(int64_t(1) << 62)
-                        || rec.index > (int64_t(1) << 62))
-                    {
-                        return iofail(SG_ERR_ARG, "sg_load: " + fname + ": interval outside the level-" + std::to_string(l) + " box in " + p);
-                    }
+                    std::memcpy(&iv[k].start, q + a.members.at("start"), 4);
+                    std::memcpy(&iv[k].end, q + a.members.at("end"), 4);
+                    std::memcpy(&iv[k].index, q + a.members.at("index"), 8);
                 }
             }
             for (int d = 1; d < D; ++d)
             {
-                if (!read_u64(base + std::to_string(d) + "/offsets/data", off[d - 1]))
+                if (!read_u64(base + std::to_string(d) + "/offsets/data", csr.off[d - 1]))
                 {
                     return iofail(SG_ERR_ARG, "sg_load: " + err);
                 }
             }
-            // walk the CSR: rows in for_each_interval order, bounds checked against the arrays
-            auto row_range = [&](int d, long long slot, uint64_t& b, uint64_t& e) -> bool
+            const size_t before = co.size();
+            const sg::csr::Decode dec = sg::csr::decode_csr(D, l, csr, co);
+            if (dec == sg::csr::Decode::outside)
             {
-                const auto& o = off[d - 1];
-                if (slot < 0 || static_cast<uint64_t>(slot) + 1 >= o.size())
-                {
-                    return false;
-                }
-                b = o[static_cast<size_t>(slot)];
-                e = o[static_cast<size_t>(slot) + 1];
-                return b <= e && e <= iv[d - 1].size();
-            };
-            bool ok = true;
-            auto emit_row = [&](uint64_t b, uint64_t e, int y, int z)
-            {
-                for (uint64_t k = b; k < e; ++k)
-                {
-                    for (int x = iv[0][k].start; x < iv[0][k].end; ++x)
-                    {
-                        lv.push_back(l);
-                        co.push_back(x);
-                        co.push_back(y);
-                        if (D == 3)
-                        {
-                            co.push_back(z);
-                        }
-                    }
-                }
-            };
-            auto walk_y = [&](uint64_t yb, uint64_t ye, int z)
-            {
-                for (uint64_t k = yb; k < ye && ok; ++k)
-                {
-                    for (int y = iv[1][k].start; y < iv[1][k].end && ok; ++y)
-                    {
-                        uint64_t b = 0, e = 0;
-                        ok = row_range(1, iv[1][k].index + y, b, e);
-                        if (ok)
-                        {
-                            emit_row(b, e, y, z);
-                        }
-                    }
-                }
-            };
-            if (D == 2)
-            {
-                walk_y(0, iv[1].size(), 0);
+                return iofail(SG_ERR_ARG, "sg_load: " + fname + ": interval outside the level-" + std::to_string(l) + " box");
             }
-            else
-            {
-                for (size_t k = 0; k < iv[2].size() && ok; ++k)
-                {
-                    for (int z = iv[2][k].start; z < iv[2][k].end && ok; ++z)
-                    {
-                        uint64_t b = 0, e = 0;
-                        ok = row_range(2, iv[2][k].index + z, b, e);
-                        if (ok)
-                        {
-                            walk_y(b, e, z);
-                        }
-                    }
-                }
-            }
-            if (!ok)
+            if (dec != sg::csr::Decode::ok)
             {
                 return iofail(SG_ERR_ARG, "sg_load: " + fname + ": inconsistent intervals and offsets at level " + std::to_string(l));
             }
+            lv.insert(lv.end(), (co.size() - before) / static_cast<size_t>(D), l);
         }
         if (int st = sg_mesh_set_cells(mesh, static_cast<long long>(lv.size()), lv.data(), co.data()))
         {

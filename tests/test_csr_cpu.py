@@ -51,3 +51,57 @@ def test_streaming_builder_matches_the_restatement(tool, dim):
         want = ["iv%d" % d + "".join(" %d,%d,%d" % t for t in ivs[d]) for d in range(dim)]
         want += ["off%d" % d + "".join(" %d" % v for v in offs[d]) for d in range(dim - 1)]
         assert out[:len(want)] == want
+
+
+def rows_in_box(rng, dim, n=12):
+    """random_rows shifted into the level-4 box [0, 16)"""
+    rows = random_rows(rng, dim, n)
+    out = []
+    for r in rows:
+        s, e, y = r[0] + 3, r[1] + 3, r[2] + 5
+        key = [y] + ([r[3] + 2] if dim == 3 else [])
+        out.append([s, e] + key + [r[-1] - 3])
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_decode_inverts_the_builder(tool, dim):
+    """decode_csr (what sg_load walks) gives back the cells of the rows the
+    layout was built from, in for_each_cell order"""
+    rng = np.random.default_rng(11 + dim)
+    for _ in range(40):
+        rows = rows_in_box(rng, dim)
+        text = "%d %d\n" % (dim, len(rows)) + "\n".join(" ".join(map(str, r)) for r in rows)
+        out = subprocess.run([tool, "decode", "4"], input=text.encode(), capture_output=True, check=True).stdout.decode().split("\n")
+        want = []
+        for r in rows:
+            for x in range(r[0], r[1]):
+                want.append(",".join(map(str, [x] + r[2:2 + dim - 1])))
+        assert out[dim + dim - 1] == "dec 0"
+        assert out[dim + dim].split()[1:] == want
+
+
+@pytest.fixture(scope="module")
+def fuzz_tool(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("csrfuzz") / "csr_tool")
+    src = os.path.join(ROOT, "tests", "cpp", "csr_tool.cpp")
+    san = ["-fsanitize=address,undefined", "-fno-sanitize-recover=all", "-g"]
+    if subprocess.run(["g++", "-std=c++17", "-O1"] + san + [src, "-o", exe], capture_output=True).returncode != 0:
+        subprocess.check_call(["g++", "-std=c++17", "-O1", src, "-o", exe])
+    return exe
+
+
+@pytest.mark.parametrize("dim,seed", [(2, 1), (2, 2), (3, 3), (3, 4)])
+def test_decode_refuses_corrupted_layouts(fuzz_tool, dim, seed):
+    """restart layouts come from files: overwritten interval bounds and
+    indices and offsets entries are refused (outside the box or
+    inconsistent), never read outside the arrays"""
+    rng = np.random.default_rng(100 + seed)
+    rows = rows_in_box(rng, dim)
+    while len(rows) < 4:
+        rows = rows_in_box(rng, dim)
+    text = "%d %d\n" % (dim, len(rows)) + "\n".join(" ".join(map(str, r)) for r in rows)
+    r = subprocess.run([fuzz_tool, "fuzz", "4", str(seed), "3000"], input=text.encode(), capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()[-2000:]
+    ok, outside, inconsistent = (int(v) for v in r.stdout.split())
+    assert ok + outside + inconsistent == 3000 and outside > 0 and inconsistent > 0
