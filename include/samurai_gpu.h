@@ -242,7 +242,9 @@ int sg_batch_synchronize(sg_batch_t batch);
  * decisions are piecewise constant).  Fields are leaf values in for_each_cell order (algorithm.hpp:301-363):
  * u0 on the initial mesh (the leaf cells of u when the adjoint is created), uT on the final mesh.  The dense
  * field is checkpointed every checkpoint_every steps; the backward pass recomputes each segment from its
- * checkpoint.  a has dim entries; ga receives dim entries. */
+ * checkpoint.  a has dim entries; ga receives dim entries.  The leaf-value arrays u0, uT, gT and g0 may be host
+ * memory or device memory of the mesh's GPU (told apart by unified addressing); device inputs must be complete
+ * before the call, and every call returns with its outputs written. */
 typedef struct sg_adjoint_s* sg_adjoint_t;
 int sg_adjoint_create(sg_field_t u, int checkpoint_every, sg_adjoint_t* out);
 int sg_adjoint_destroy(sg_adjoint_t adj);

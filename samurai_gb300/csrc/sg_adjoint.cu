@@ -442,7 +442,8 @@ namespace
             return st;
         }
         cudaMemsetAsync(dense, 0, dense_bytes(c), c.stream);
-        cudaMemcpyAsync(adj->d_vals, u0, static_cast<size_t>(adj->n0) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        // u0: host memory or device memory of the mesh's GPU (unified addressing tells them apart)
+        cudaMemcpyAsync(adj->d_vals, u0, static_cast<size_t>(adj->n0) * sizeof(double), cudaMemcpyDefault, c.stream);
         sg::k_leaf_scatter<<<sg::grid_of(adj->n0), sg::ABLOCK, 0, c.stream>>>(adj->d_el0, adj->d_vals, adj->n0, dense);
         return cuda_ok(c, "adjoint initial field");
     }
@@ -999,7 +1000,7 @@ extern "C"
             return afail(SG_ERR_STATE, "sg_adjoint_final: no forward run, or n differs from the final number of cells");
         }
         Ctx& c = ctx_of(adj);
-        cudaMemcpyAsync(uT, adj->d_uT, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        cudaMemcpyAsync(uT, adj->d_uT, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDefault, c.stream); // host or device
         if (cudaStreamSynchronize(c.stream) != cudaSuccess)
         {
             return afail(SG_ERR_CUDA, "sg_adjoint_final: CUDA error");
@@ -1061,7 +1062,7 @@ extern "C"
             return afail(st, c.err.c_str());
         }
         cudaMemsetAsync(adj->lam[0], 0, dense_bytes(c), c.stream);
-        cudaMemcpyAsync(adj->d_vals, gT, static_cast<size_t>(adj->nT) * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+        cudaMemcpyAsync(adj->d_vals, gT, static_cast<size_t>(adj->nT) * sizeof(double), cudaMemcpyDefault, c.stream); // host or device
         sg::k_leaf_scatter<<<sg::grid_of(adj->nT), sg::ABLOCK, 0, c.stream>>>(adj->d_elT, adj->d_vals, adj->nT, adj->lam[0]);
         cudaMemsetAsync(adj->d_ga, 0, 3 * sizeof(double), c.stream);
         while (static_cast<int>(adj->ug.size()) < std::min(K, std::max(T, 1)))
@@ -1127,7 +1128,7 @@ extern "C"
             return afail(st, c.err.c_str());
         }
         sg::k_leaf_gather<<<sg::grid_of(adj->n0), sg::ABLOCK, 0, c.stream>>>(adj->d_el0, adj->lam[0], adj->n0, adj->d_vals);
-        cudaMemcpyAsync(g0, adj->d_vals, static_cast<size_t>(adj->n0) * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        cudaMemcpyAsync(g0, adj->d_vals, static_cast<size_t>(adj->n0) * sizeof(double), cudaMemcpyDefault, c.stream); // host or device
         double h_ga[3] = {0., 0., 0.};
         cudaMemcpyAsync(h_ga, adj->d_ga, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
         if (cudaStreamSynchronize(c.stream) != cudaSuccess)

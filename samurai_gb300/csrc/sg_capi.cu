@@ -413,7 +413,7 @@ extern "C"
         c.fuse_top_field           = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS_FIELD", sg::FUSE_WORDS_FIELD));
         c.fuse_top_max             = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS_MAX", sg::FUSE_WORDS_MAX));
         c.max_blocks               = std::max(1LL, tuned("SG_MAX_BLOCKS", c.max_blocks));
-        if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
+        if (cudaGetDevice(&c.device) != cudaSuccess || cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
         {
             cudaGetLastError();
             delete h;

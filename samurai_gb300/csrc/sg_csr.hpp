@@ -120,10 +120,22 @@ namespace sg
         // The inverse of build_csr for a restart file's level: the cells of the layout in for_each_cell order
         // (z outer, y, x inner), appended to `coords` as x, y[, z].  The layout comes from a file, so every
         // interval is checked against the box (which also bounds the walk and keeps index + coordinate from
-        // overflowing) and every offsets slot and range against the arrays, before it is used.
-        inline Decode decode_csr(int dim, int level, const LevelCSR& c, std::vector<int>& coords)
+        // overflowing) and every offsets slot and range against the arrays, before it is used.  Offsets that
+        // point many rows at the same intervals would make the walk emit the same cells again and again: a
+        // layout that yields more than max_cells cells (at most the box's 2^(dim level) cells, fewer when the
+        // caller knows a tighter bound) is inconsistent, and is refused before its cells are appended.
+        inline Decode decode_csr(int dim, int level, const LevelCSR& c, std::vector<int>& coords, uint64_t max_cells = ~uint64_t(0))
         {
             const int64_t n = int64_t(1) << level;
+            const uint64_t box = (dim * level >= 64) ? ~uint64_t(0) : uint64_t(1) << (dim * level);
+            if (max_cells > box)
+            {
+                max_cells = box;
+            }
+            uint64_t emitted = 0;
+            // in a layout built by build_csr every x-interval belongs to one row and every y-interval to one
+            // plane, so the walk uses each once; a layout that sends two rows to the same intervals is refused
+            std::vector<uint8_t> used_x(c.iv[0].size(), 0), used_y(c.iv[1].size(), 0);
             for (int d = 0; d < dim; ++d)
             {
                 for (const auto& r : c.iv[d])
@@ -145,8 +157,23 @@ namespace sg
                 e = o[static_cast<size_t>(slot) + 1];
                 return b <= e && e <= c.iv[d - 1].size();
             };
-            auto row = [&](uint64_t b, uint64_t e, int y, int z)
+            auto row = [&](uint64_t b, uint64_t e, int y, int z) -> bool
             {
+                uint64_t cells = 0;
+                for (uint64_t k = b; k < e; ++k)
+                {
+                    if (used_x[k])
+                    {
+                        return false;
+                    }
+                    used_x[k] = 1;
+                    cells += static_cast<uint64_t>(c.iv[0][k].end - c.iv[0][k].start); // end >= start: checked above
+                    if (cells > max_cells - emitted)
+                    {
+                        return false;
+                    }
+                }
+                emitted += cells;
                 for (uint64_t k = b; k < e; ++k)
                 {
                     for (int x = c.iv[0][k].start; x < c.iv[0][k].end; ++x)
@@ -159,19 +186,24 @@ namespace sg
                         }
                     }
                 }
+                return true;
             };
             auto plane = [&](uint64_t yb, uint64_t ye, int z) -> bool
             {
                 for (uint64_t k = yb; k < ye; ++k)
                 {
+                    if (used_y[k])
+                    {
+                        return false;
+                    }
+                    used_y[k] = 1;
                     for (int y = c.iv[1][k].start; y < c.iv[1][k].end; ++y)
                     {
                         uint64_t b = 0, e = 0;
-                        if (!range(1, c.iv[1][k].index + y, b, e))
+                        if (!range(1, c.iv[1][k].index + y, b, e) || !row(b, e, y, z))
                         {
                             return false;
                         }
-                        row(b, e, y, z);
                     }
                 }
                 return true;

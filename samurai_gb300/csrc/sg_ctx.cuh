@@ -103,6 +103,7 @@ namespace sg
         bool rel_detail = false;                // the Harten pass in flight divides the details by max |u|
         double* h_eps = nullptr; // pinned staging of d_eps
         cudaStream_t stream = nullptr;
+        int device          = -1; // the device current at creation: every buffer of the mesh lives there
         DeviceMesh mesh[2];
         int cur = 0;
         // scratch bitmaps

@@ -9,6 +9,7 @@
 //    values in for_each_cell order.
 // Host code: the mesh and the fields are read or written through the C ABI
 // of the library (leaf cells, interval lists, field downloads and uploads).
+#include <algorithm>
 #include <cinttypes>
 #include <cstdio>
 #include <cstring>
@@ -472,8 +473,13 @@ extern "C"
             return iofail(SG_ERR_ARG, "sg_load: the file's dimension and levels (" + std::to_string(fd) + ", " + std::to_string(fmin) + ", "
                                           + std::to_string(fmax) + ") differ from the mesh's; create the mesh with sg_restart_levels");
         }
-        // leaf cells, for_each_cell order (io/restart.hpp:288-321, level_cell_array.hpp:1005-1077)
+        // leaf cells, for_each_cell order (io/restart.hpp:288-321, level_cell_array.hpp:1005-1077).  The leaves
+        // of a mesh tile the box, so their volume, counted in cells of the finest level, is at most the box's:
+        // each level may decode at most the cells that the volume left over by the coarser levels still holds
+        // (and the library holds fewer than 2^31 cells)
         std::vector<int> lv, co;
+        const int vbits     = D * fmax; // at most 3 * 21 bits (sg_mesh_create's level limits)
+        uint64_t vol_left   = (vbits >= 64) ? ~uint64_t(0) : (uint64_t(1) << vbits);
         for (int l = fmin; l <= fmax; ++l)
         {
             const std::string base = "/mesh/level/" + std::to_string(l) + "/dim/";
@@ -508,8 +514,12 @@ extern "C"
                     return iofail(SG_ERR_ARG, "sg_load: " + err);
                 }
             }
-            const size_t before = co.size();
-            const sg::csr::Decode dec = sg::csr::decode_csr(D, l, csr, co);
+            const size_t before    = co.size();
+            const int shift        = D * (fmax - l); // finest cells per cell of level l: 2^shift
+            uint64_t budget        = vol_left >> shift;
+            const uint64_t cap     = (uint64_t(1) << 31) - 1 - lv.size();
+            budget                 = budget < cap ? budget : cap;
+            const sg::csr::Decode dec = sg::csr::decode_csr(D, l, csr, co, budget);
             if (dec == sg::csr::Decode::outside)
             {
                 return iofail(SG_ERR_ARG, "sg_load: " + fname + ": interval outside the level-" + std::to_string(l) + " box");
@@ -518,11 +528,57 @@ extern "C"
             {
                 return iofail(SG_ERR_ARG, "sg_load: " + fname + ": inconsistent intervals and offsets at level " + std::to_string(l));
             }
-            lv.insert(lv.end(), (co.size() - before) / static_cast<size_t>(D), l);
+            const size_t got = (co.size() - before) / static_cast<size_t>(D);
+            vol_left -= static_cast<uint64_t>(got) << shift; // got <= budget <= vol_left >> shift
+            lv.insert(lv.end(), got, l);
+        }
+        {
+            // the leaves tile the box: their volume is the box's, and no leaf lies inside a coarser one
+            if (vol_left != 0)
+            {
+                return iofail(SG_ERR_ARG, "sg_load: " + fname + ": the file's leaf cells do not cover the box");
+            }
+            std::vector<std::vector<uint64_t>> keys(static_cast<size_t>(fmax + 1));
+            auto key = [&](int x, int y, int z) { return (uint64_t(uint32_t(z)) << 42) | (uint64_t(uint32_t(y)) << 21) | uint64_t(uint32_t(x)); };
+            for (size_t i = 0; i < lv.size(); ++i)
+            {
+                keys[static_cast<size_t>(lv[i])].push_back(key(co[D * i], co[D * i + 1], D == 3 ? co[D * i + 2] : 0));
+            }
+            for (auto& k : keys)
+            {
+                std::sort(k.begin(), k.end());
+            }
+            for (size_t i = 0; i < lv.size(); ++i)
+            {
+                for (int l = fmin; l < lv[i]; ++l)
+                {
+                    const int s = lv[i] - l;
+                    const uint64_t a = key(co[D * i] >> s, co[D * i + 1] >> s, D == 3 ? co[D * i + 2] >> s : 0);
+                    if (std::binary_search(keys[static_cast<size_t>(l)].begin(), keys[static_cast<size_t>(l)].end(), a))
+                    {
+                        return iofail(SG_ERR_ARG, "sg_load: " + fname + ": a leaf cell of level " + std::to_string(lv[i])
+                                                      + " lies inside a leaf of level " + std::to_string(l));
+                    }
+                }
+            }
         }
         if (int st = sg_mesh_set_cells(mesh, static_cast<long long>(lv.size()), lv.data(), co.data()))
         {
             return st;
+        }
+        {
+            // samurai's restart holds exactly the file's leaves: cells repeated in the file, or overlapping
+            // across levels, would merge into fewer cells, and the file's values would then belong to other cells
+            long long nc = 0, nr = 0;
+            if (int st = sg_mesh_counts(mesh, &nc, &nr))
+            {
+                return st;
+            }
+            if (nc != static_cast<long long>(lv.size()))
+            {
+                return iofail(SG_ERR_ARG, "sg_load: " + fname + ": the file's leaf cells repeat or overlap (" + std::to_string(lv.size())
+                                              + " cells read, " + std::to_string(nc) + " distinct leaves)");
+            }
         }
         // fields (io/restart.hpp:323-372): leaf values in for_each_cell order of the cells read
         if (fields)

@@ -16,6 +16,9 @@
 //  - the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current, once per device; make
 //    that first call before any stream capture;
+//  - the device current at the call must be the one the mesh was created on
+//    (SG_ERR_ARG otherwise), since the address looked up is that of the
+//    current device's copy of the array;
 //  - every call shares the one array and leaves its contents behind; each
 //    call overwrites the n entries it returns, so nothing needs clearing, but
 //    calls that overlap on the GPU (several host threads or meshes at once)
@@ -47,14 +50,19 @@ namespace
         return code;
     }
 
-    // device address of the array for the current device, looked up once
-    int scratch_for_current_device(double** out)
+    // device address of the array on the mesh's device, looked up once per device; that device must be the
+    // current one, since the address belongs to the current device's copy of the array
+    int scratch_for_device(int mesh_device, double** out)
     {
         int dev       = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess)
         {
             return noalloc_fail(SG_ERR_CUDA, "sg_field_download_noalloc: cudaGetDevice: ", cudaGetErrorString(e));
+        }
+        if (dev != mesh_device)
+        {
+            return noalloc_fail(SG_ERR_ARG, "sg_field_download_noalloc: the current device is not the one the mesh was created on");
         }
         if (dev < 0 || dev >= MAX_DEVICES)
         {
@@ -77,6 +85,7 @@ namespace
 }
 
 extern "C" int sg_field_download_noalloc(sg_field_t field, double* values, long long n)
+try
 {
     if (!field || !values)
     {
@@ -105,7 +114,7 @@ extern "C" int sg_field_download_noalloc(sg_field_t field, double* values, long 
                                              "use sg_field_download");
     }
     double* scratch = nullptr;
-    if (int st = scratch_for_current_device(&scratch))
+    if (int st = scratch_for_device(c.device, &scratch))
     {
         return st;
     }
@@ -129,3 +138,4 @@ extern "C" int sg_field_download_noalloc(sg_field_t field, double* values, long 
     }
     return SG_OK;
 }
+SG_API_CATCH(sg_field_download_noalloc)

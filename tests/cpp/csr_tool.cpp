@@ -7,6 +7,9 @@
 //                                     "dec <code>" and "cells x,y[,z] ..."
 //   csr_tool fuzz <level> <seed> <n>  n corrupted copies of the layout (intervals and offsets
 //                                     overwritten), each decoded; prints "ok outside inconsistent"
+//   csr_tool raw <level>              reads a layout as written in a file instead: "dim", then per
+//                                     dimension d a count and "start end index" records, then per
+//                                     offsets array a count and its entries; prints "dec <code> <cells>"
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -80,9 +83,67 @@ static int fuzz(int dim, int level, const sg::csr::LevelCSR& good, unsigned long
     return 0;
 }
 
+// a layout given array by array, as a restart file holds it
+static int raw(int level)
+{
+    int dim = 0;
+    if (std::scanf("%d", &dim) != 1 || (dim != 2 && dim != 3))
+    {
+        return 2;
+    }
+    sg::csr::LevelCSR c;
+    for (int d = 0; d < dim; ++d)
+    {
+        long long n = 0;
+        if (std::scanf("%lld", &n) != 1 || n < 0)
+        {
+            return 2;
+        }
+        for (long long k = 0; k < n; ++k)
+        {
+            long long s = 0, e = 0, i = 0;
+            if (std::scanf("%lld %lld %lld", &s, &e, &i) != 3)
+            {
+                return 2;
+            }
+            sg::csr::IntervalRec r{};
+            r.start = static_cast<int32_t>(s);
+            r.end   = static_cast<int32_t>(e);
+            r.step  = 1;
+            r.index = i;
+            c.iv[d].push_back(r);
+        }
+    }
+    for (int d = 0; d + 1 < dim; ++d)
+    {
+        long long n = 0;
+        if (std::scanf("%lld", &n) != 1 || n < 0)
+        {
+            return 2;
+        }
+        for (long long k = 0; k < n; ++k)
+        {
+            unsigned long long v = 0;
+            if (std::scanf("%llu", &v) != 1)
+            {
+                return 2;
+            }
+            c.off[d].push_back(v);
+        }
+    }
+    std::vector<int> co;
+    const auto d = sg::csr::decode_csr(dim, level, c, co);
+    std::printf("dec %d %zu\n", static_cast<int>(d), co.size() / static_cast<size_t>(dim));
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     const std::string mode = argc >= 2 ? argv[1] : "";
+    if (mode == "raw" && argc >= 3)
+    {
+        return raw(std::atoi(argv[2]));
+    }
     int dim       = 0;
     long long n   = 0;
     if (std::scanf("%d %lld", &dim, &n) != 2 || (dim != 2 && dim != 3) || n < 0)

@@ -105,3 +105,31 @@ def test_decode_refuses_corrupted_layouts(fuzz_tool, dim, seed):
     assert r.returncode == 0, r.stderr.decode()[-2000:]
     ok, outside, inconsistent = (int(v) for v in r.stdout.split())
     assert ok + outside + inconsistent == 3000 and outside > 0 and inconsistent > 0
+
+
+def decode_raw(tool, level, dim, ivs, offs):
+    text = "%d\n" % dim
+    for d in range(dim):
+        text += "%d\n" % len(ivs[d]) + "".join("%d %d %d\n" % t for t in ivs[d])
+    for d in range(dim - 1):
+        text += "%d\n" % len(offs[d]) + "".join("%d\n" % v for v in offs[d])
+    out = subprocess.run([tool, "raw", str(level)], input=text.encode(), capture_output=True, check=True, timeout=60).stdout.split()
+    return int(out[1]), int(out[2])
+
+
+def test_decode_refuses_rows_sent_to_the_same_intervals(tool):
+    """offsets that point many rows at one x-interval would make the walk repeat
+    its cells without bound (a level-20 row repeated 1000 times is 2^30 cells);
+    the layout is refused when an interval is reached a second time, so at most
+    the cells of its first visit were appended"""
+    level = 20
+    full = [(0, 1 << level, 0)]
+    # 1000 one-row y-intervals, each sent to offsets slot 0 (index = -y): the same full x-row every time
+    ys = [(y, y + 1, -y) for y in range(1000)]
+    assert decode_raw(tool, level, 2, [full, ys], [[0, 1]]) == (2, 1 << level)
+    # 3D: many z-planes sent to the same y-interval
+    zs = [(z, z + 1, -z) for z in range(60)]
+    assert decode_raw(tool, 6, 3, [[(0, 64, 0)], [(0, 1, 0)], zs], [[0, 1], [0, 1]]) == (2, 64)
+    # the one-row layouts themselves are accepted
+    assert decode_raw(tool, level, 2, [full, [(5, 6, -5)]], [[0, 1]]) == (0, 1 << level)
+    assert decode_raw(tool, 6, 3, [[(0, 64, 0)], [(0, 1, 0)], [(3, 4, -3)]], [[0, 1], [0, 1]]) == (0, 64)

@@ -59,7 +59,9 @@ def test_noalloc_download_matches_download_on_consecutive_calls():
             assert status == 0, lib.sg_last_error().decode()
             assert np.array_equal(got, expected)  # bit-identical, as every parity test here
         outputs.append(got)
-    assert not np.array_equal(outputs[0][: min(map(len, outputs))], outputs[1][: min(map(len, outputs))])
+    # the second step's state differs from the first one's (its mesh or its values), so the shared array held
+    # other contents when the second step's calls rewrote it
+    assert outputs[0].shape != outputs[1].shape or not np.array_equal(outputs[0], outputs[1])
 
 
 def test_noalloc_download_rejects_meshes_beyond_its_array():
