@@ -909,11 +909,29 @@ class Adjoint:
 
     def record(self, u0, n_steps, eps, regularity, a, dt, scheme=UPWIND_OP):
         u0 = np.ascontiguousarray(u0, np.float64)
+        self.record_ptr(_ptr(u0), n_steps, eps, regularity, a, dt, scheme)
+        return self.final()
+
+    def record_ptr(self, u0_ptr, n_steps, eps, regularity, a, dt, scheme=UPWIND_OP):
+        """record() from a pointer to the n0 initial leaf values: host memory or
+        device memory of the mesh's GPU; returns the final leaf count"""
         nT = ctypes.c_longlong()
         av = self._vel(a)
-        _check(lib().sg_adjoint_record(self._h, _ptr(u0), int(n_steps), float(eps), float(regularity), _ptr(av), float(dt), int(scheme),
+        src = ctypes.c_void_p(u0_ptr) if isinstance(u0_ptr, int) else u0_ptr
+        _check(lib().sg_adjoint_record(self._h, src, int(n_steps), float(eps), float(regularity), _ptr(av), float(dt), int(scheme),
                                        ctypes.byref(nT)), "sg_adjoint_record")
-        return self.final()
+        return nT.value
+
+    def final_ptr(self, uT_ptr, nT):
+        """the final leaf values into host or device memory at uT_ptr"""
+        _check(lib().sg_adjoint_final(self._h, ctypes.c_void_p(uT_ptr), int(nT)), "sg_adjoint_final")
+
+    def backward_ptr(self, gT_ptr, g0_ptr):
+        """backward() between host or device buffers: gT_ptr holds nT values,
+        g0_ptr receives n0; returns dJ/da"""
+        ga = np.zeros(3, np.float64)
+        _check(lib().sg_adjoint_backward(self._h, ctypes.c_void_p(gT_ptr), ctypes.c_void_p(g0_ptr), _ptr(ga)), "sg_adjoint_backward")
+        return ga[: self.dim].copy()
 
     def final(self):
         _, nT, _ = self.counts()

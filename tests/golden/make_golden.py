@@ -11,8 +11,8 @@ demos/FiniteVolume/advection_2d.cpp run with --Tf 0.01
 few HDF5 structures those files use (superblock v0, v1 object headers, v1
 B-tree group nodes, local heaps, contiguous layout) are decoded by hand.
 
-Run once in a container where the reference tree is mounted:
-    python tests/golden/make_golden.py /root/reference
+Run once where a checkout of the reference tree is available, giving its root:
+    python tests/golden/make_golden.py <path to the samurai checkout>
 """
 import hashlib
 import os
@@ -58,7 +58,9 @@ def convert(src_dir, name, out_dir):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <root of the samurai checkout>")
+    ref = sys.argv[1]
     src = os.path.join(ref, "tests", "reference", "finite_volume")
     out = os.path.dirname(os.path.abspath(__file__))
     for name in NAMES:
