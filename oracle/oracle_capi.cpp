@@ -11,7 +11,8 @@ namespace
     struct Base
     {
         virtual ~Base() = default;
-        int dim         = 2;
+        int dim              = 2;
+        bool refine_boundary = false; // --refine-boundary for this problem's adaptations
     };
 
     template <std::size_t D>
@@ -258,7 +259,7 @@ extern "C"
                              os.push_back(&field_k(s, k));
                              obs.push_back(&bc_k(s, k));
                          }
-                         oracle::MRConfig mr{eps, regularity, relative_detail != 0};
+                         oracle::MRConfig mr{eps, regularity, relative_detail != 0, s->refine_boundary};
                          const int minl = s->mesh.cfg.min_level, maxl = s->mesh.cfg.max_level;
                          for (int i = 0; minl != maxl && i < maxl - minl; ++i)
                          {
@@ -303,7 +304,7 @@ extern "C"
             int it = 0;
             DISPATCH(h,
                      {
-                         oracle::MRConfig mr{eps, regularity, relative_detail != 0};
+                         oracle::MRConfig mr{eps, regularity, relative_detail != 0, s->refine_boundary};
                          const int minl = s->mesh.cfg.min_level, maxl = s->mesh.cfg.max_level;
                          if (minl != maxl)
                          {
@@ -334,7 +335,7 @@ extern "C"
             int r = 0;
             DISPATCH(h,
                      {
-                         oracle::MRConfig mr{eps, regularity};
+                         oracle::MRConfig mr{eps, regularity, false, s->refine_boundary};
                          r = oracle::harten(s->mesh, s->u, ite, mr, s->bc, &s->last_detail, &s->last_tag) ? 1 : 0;
                      });
             return r;
@@ -433,6 +434,57 @@ extern "C"
                 }
             }
         }
+    }
+
+    // One recorded mesh transition of a frozen-mesh replay: the mesh becomes
+    // the one of the given leaf cells and field 0 follows it through
+    // update_fields (algorithm/update_fields.hpp:27-127), as the end of a
+    // Harten pass that changed the mesh does (mr/adapt.hpp:380-386).  The
+    // caller updates the ghosts before, as that pass did.
+    int oracle_transfer_cells(void* h, long long n, const int* level, const int* coords)
+    {
+        try
+        {
+            if (dim_of(h) == 2)
+            {
+                auto* s = as<2>(h);
+                std::vector<oracle::LSet<2>> cells;
+                oracle::init_levels(cells);
+                for (long long i = 0; i < n; ++i)
+                {
+                    cells[level[i]].add({coords[2 * i + 1]}, {coords[2 * i], coords[2 * i] + 1});
+                }
+                oracle::Mesh<2> nm = oracle::make_mesh_from_cells<2>(s->mesh.cfg, cells);
+                oracle::Field nu   = oracle::update_fields<2>(s->mesh, nm, s->u);
+                s->mesh            = std::move(nm);
+                s->u               = std::move(nu);
+            }
+            else
+            {
+                auto* s = as<3>(h);
+                std::vector<oracle::LSet<3>> cells;
+                oracle::init_levels(cells);
+                for (long long i = 0; i < n; ++i)
+                {
+                    cells[level[i]].add({coords[3 * i + 1], coords[3 * i + 2]}, {coords[3 * i], coords[3 * i] + 1});
+                }
+                oracle::Mesh<3> nm = oracle::make_mesh_from_cells<3>(s->mesh.cfg, cells);
+                oracle::Field nu   = oracle::update_fields<3>(s->mesh, nm, s->u);
+                s->mesh            = std::move(nm);
+                s->u               = std::move(nu);
+            }
+            return 0;
+        }
+        catch (...)
+        {
+            return -1;
+        }
+    }
+
+    // args::refine_boundary (--refine-boundary) for this problem's adaptations
+    void oracle_set_refine_boundary(void* h, int enable)
+    {
+        static_cast<Base*>(h)->refine_boundary = enable != 0;
     }
 
     // rebuild the mesh from leaf cells given as (level, coords) lists; used by

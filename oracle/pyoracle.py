@@ -58,6 +58,9 @@ def lib():
         L.oracle_get_intervals.argtypes = [vp, i, i, vp]
         L.oracle_set_cells.restype = i
         L.oracle_set_cells.argtypes = [vp, ll, vp, vp]
+        L.oracle_set_refine_boundary.argtypes = [vp, i]
+        L.oracle_transfer_cells.restype = i
+        L.oracle_transfer_cells.argtypes = [vp, ll, vp, vp]
         _lib = L
     return _lib
 
@@ -167,6 +170,18 @@ class OracleSim:
         coords = np.ascontiguousarray(coords, np.int32)
         if lib().oracle_set_cells(self.h, len(level), _ptr(level), _ptr(coords)) != 0:
             raise RuntimeError("oracle set_cells failed")
+
+    def set_refine_boundary(self, enable):
+        """--refine-boundary (args::refine_boundary) for the adaptations of this problem"""
+        lib().oracle_set_refine_boundary(self.h, 1 if enable else 0)
+
+    def transfer_cells(self, level, coords):
+        """the mesh becomes that of the given leaf cells; the field follows it
+        through update_fields (one recorded transition of a frozen-mesh replay)"""
+        level = np.ascontiguousarray(level, np.int32)
+        coords = np.ascontiguousarray(coords, np.int32)
+        if lib().oracle_transfer_cells(self.h, len(level), _ptr(level), _ptr(coords)) != 0:
+            raise RuntimeError("oracle transfer_cells failed")
 
     # ---- more fields on the same mesh (field 0 is the one above)
     def add_field(self, dirichlet=0.0):

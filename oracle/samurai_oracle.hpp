@@ -1757,6 +1757,7 @@ namespace oracle
         double epsilon       = 1e-4; // mr/config.hpp:63-65
         double regularity    = 1.;
         bool relative_detail = false; // mr/config.hpp, mr/rel_detail.hpp
+        bool refine_boundary = false; // args::refine_boundary (--refine-boundary, arguments.hpp:26, 67)
     };
 
     // compute_relative_detail (mr/rel_detail.hpp:75-111) for one scalar field:
@@ -1925,6 +1926,27 @@ namespace oracle
                         {
                             tag[o] |= static_cast<std::uint8_t>(above(o, fine_eps) * FLAG_REFINE);
                         }
+                    }
+                });
+        }
+
+        // keep_boundary_refined (mr/adapt.hpp:245-274, called at :342-345 when --refine-boundary is given): in
+        // each Cartesian direction, the cells of max_level outside the domain translated by -max_stencil_radius
+        // times the direction (domain_boundary_layer, boundary.hpp:6-21) are tagged keep, overwriting their tag
+        if (mr.refine_boundary)
+        {
+            const int n = 1 << maxl, w = m.cfg.max_stencil_radius;
+            m.cells[maxl].for_each_cell(
+                [&](const Coord<D>& c)
+                {
+                    bool near = false;
+                    for (int d = 0; d < static_cast<int>(D); ++d)
+                    {
+                        near = near || c[d] < w || c[d] >= n - w;
+                    }
+                    if (near)
+                    {
+                        tag[static_cast<std::size_t>(m.idx(maxl, c))] = FLAG_KEEP;
                     }
                 });
         }

@@ -132,3 +132,29 @@ def test_torch_autograd(sg):
     # the transposed launches accumulate with atomics: equal up to rounding order
     np.testing.assert_allclose(u0.grad.numpy(), g0, rtol=1e-12, atol=1e-18)
     np.testing.assert_allclose(a.grad.numpy(), ga, rtol=1e-12)
+
+
+def test_torch_autograd_cuda_tensors(sg):
+    """FP64 CUDA tensors cross the C ABI as device pointers: the same
+    gradients as through host arrays, returned on the tensors' device"""
+    torch = pytest.importorskip("torch")
+    from samurai_gb300.autograd import advection_loop
+
+    s = initial_sim(sg)
+    adj = sg.Adjoint(s.u, checkpoint_every=8)
+    u0h = s.cell_values()
+    u0 = torch.tensor(u0h, dtype=torch.float64, device="cuda", requires_grad=True)
+    a = torch.tensor(A, dtype=torch.float64, requires_grad=True)
+    uT = advection_loop(u0, a, adj, STEPS, EPS, REG, DT)
+    assert uT.is_cuda
+    lv, co = adj.cells("final")
+    tgt = torch.from_numpy(gaussian_target(5)(lv, co)).cuda()
+    vol = torch.from_numpy(cell_volumes(lv)).cuda()
+    J = (vol * (uT - tgt) ** 2).sum()
+    J.backward()
+    assert u0.grad.is_cuda
+    uT_host = adj.record(u0h, STEPS, EPS, REG, A, DT)
+    assert np.array_equal(uT.detach().cpu().numpy(), uT_host)
+    g0, ga = adj.backward((2 * vol * (uT - tgt)).detach().cpu().numpy())
+    np.testing.assert_allclose(u0.grad.cpu().numpy(), g0, rtol=1e-12, atol=1e-18)
+    np.testing.assert_allclose(a.grad.numpy(), ga, rtol=1e-12)

@@ -1,6 +1,9 @@
 """Batched mode (sg_batch_*): independent problems advanced together must give,
 instance by instance, exactly what the serial calls give (meshes identical,
 FP64 fields bit-identical), and the serial calls match the oracle."""
+import multiprocessing as mp
+import os
+
 import numpy as np
 import pytest
 
@@ -103,3 +106,48 @@ def test_batch_rejects_shared_mesh(sg):
     s = sg.AdvectionSim(2, 2, 5)
     with pytest.raises(sg.SamuraiGpuError, match="share a mesh"):
         sg.Batch([s, s])
+
+
+def test_batch_benchmark_instances_against_oracle(sg):
+    """18 instances of the benchmark's batched workload (seed 2027: max_level 7
+    to 11, both thresholds, max_level 11 with each), through the batched
+    calls for the initial adaptation and 3 steps, against the oracle stepping
+    each instance alone: every mesh id, the leaf cells and their values, bit
+    for bit, and the Harten pass counts."""
+    seed, n, steps = 2027, 256, 3
+    idx = list(range(16)) + [20, 23]
+    probs = batch_instances(seed, n)
+    assert {probs[k]["max_level"] for k in idx} == {7, 8, 9, 10, 11}
+    assert {probs[k]["eps"] for k in idx if probs[k]["max_level"] == 11} == {1e-3, 1e-4}
+    # the oracle runs while the GPU works: spawned workers (no fork after CUDA initialisation)
+    pool = mp.get_context("spawn").Pool(min(len(idx), os.cpu_count() or 1))
+    from oracle_batch import run_instance
+
+    pending = pool.map_async(run_instance, [(seed, n, k, steps) for k in idx])
+    sims = []
+    for k in idx:
+        p = probs[k]
+        s = sg.AdvectionSim(2, p["min_level"], p["max_level"])
+        lv, co, _ = s.cells()
+        s.set_cell_values(p["u0"](lv, co))
+        sims.append(s)
+    batch = sg.Batch(sims, n_threads=4)
+    eps = [probs[k]["eps"] for k in idx]
+    reg = [probs[k]["regularity"] for k in idx]
+    passes = [list(batch.adapt(eps, reg))]
+    for _ in range(steps):
+        passes.append(list(batch.step(eps, reg, [probs[k]["a"] for k in idx], [probs[k]["dt"] for k in idx])))
+    batch.synchronize()
+    results = pending.get(timeout=1800)
+    pool.close()
+    pool.join()
+    for j, (k, g) in enumerate(zip(idx, sims)):
+        (lo, coo, io), vo, ivs, po = results[j]
+        where = "instance %d (max_level %d)" % (k, probs[k]["max_level"])
+        assert [p[j] for p in passes] == po, where + ": Harten passes"
+        lg, cg, ig = g.cells()
+        assert np.array_equal(lg, lo) and np.array_equal(cg, coo) and np.array_equal(ig, io), where + ": leaf cells"
+        assert np.array_equal(g.cell_values(), vo), where + ": leaf values"
+        for (mid, lev), iv in ivs.items():
+            assert np.array_equal(g.intervals(mid, lev), iv), "%s: %s level %d" % (where, mid, lev)
+    batch.close()

@@ -2,17 +2,32 @@
 (16 squares + 16 Gaussians) and 3D min_level 3 / max_level 9 (ball + 8
 Gaussians).
 
-2D: the initial adaptation and one time step against the oracle, bit for
-bit (the oracle finishes them in seconds).  2D and 3D, size-independent
+2D: the initial adaptation and one time step against the oracle run live, bit
+for bit (the oracle finishes them in seconds), and the initial adaptation plus
+the 25 steps the benchmark times against digests of the oracle's states.  3D:
+the initial adaptation from the uniform level-9 mesh (134 M cells) and three
+steps against digests of the oracle's states: the oracle needs minutes and
+GBs for that run, so tests/golden/make_state_digests.py ran it once and
+stored a SHA-256 digest of the leaf cells and values after each stage
+(equal digests: bit-identical meshes and values), on the aarch64 GPU hosts
+(numpy's exp, which evaluates the initial Gaussians, differs in the last bit
+between architectures, so the digests hold for the architecture that made them).  2D and 3D, size-independent
 properties of every adapted mesh: the leaves tile the unit box exactly once
 (painted on the finest grid), neighbouring leaves (faces and corners) differ
 by at most one level (2:1 graduation), the storage indices of the leaves are
 distinct and every value is finite."""
+import json
+import os
+import platform
+
 import numpy as np
 import pytest
 
 from advection_cases import ball_3d, shapes_2d
+from golden.make_state_digests import RUNS, state_digest
 from oracle.pyoracle import OracleSim
+
+DIGESTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "state_digests.json")
 
 pytestmark = pytest.mark.gpu
 
@@ -107,3 +122,33 @@ def test_3d_full_size_properties(sg):
         g.update_ghost()
         g.upwind(a, dt)
         g.adapt(1e-3, 1.0)
+
+
+@pytest.mark.parametrize("name", ["2d", "3d"])
+def test_full_size_runs_against_oracle_digests(sg, name):
+    """every stage of the run bit for bit against the oracle's digests"""
+    ref = json.load(open(DIGESTS))[name]
+    if ref.get("machine") != platform.machine():
+        pytest.skip("the digests were generated on %s (numpy's exp differs in the last bit between architectures)" % ref.get("machine"))
+    r = RUNS[name]
+    assert ref["run"] == r
+    g = sg.AdvectionSim(r["dim"], r["min_level"], r["max_level"], 1, 1)
+    lv, co, _ = g.cells()
+    u0 = shapes_2d(2026) if r["u0"] == "shapes_2d(2026)" else ball_3d(2026)
+    g.set_cell_values(u0(lv, co))
+    del lv, co
+    passes = [g.adapt(r["eps"], r["regularity"])]
+
+    def check(stage):
+        lv, co, _ = g.cells()
+        assert len(lv) == ref["cells"][stage], "%s stage %d: %d leaf cells, the oracle %d" % (name, stage, len(lv), ref["cells"][stage])
+        assert state_digest(lv, co, g.cell_values()) == ref["digests"][stage], "%s stage %d: cells or values differ" % (name, stage)
+
+    check(0)
+    dt = r["cfl"] / (1 << r["max_level"])
+    for k in range(r["steps"]):
+        passes.append(g.adapt(r["eps"], r["regularity"]))
+        g.update_ghost()
+        g.upwind(r["a"], dt)
+        check(k + 1)
+    assert passes == ref["passes"]
