@@ -139,6 +139,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+UPWIND_ISSUED = {2: 10 * 2 + 3 + 2, 3: 10 * 3 + 5 + 2}
+# DRAM bytes per launch of the kernels named dominant, from ncu captures (profiles/)
+DOMINANT_TRAFFIC = {}
+
+
+def left_shared(level, coords):
+    """leaves whose left x-neighbour is a leaf of the same level"""
+    key_bits = 21
+    dim = coords.shape[1]
+    total = 0
+    for l in np.unique(level):
+        c = coords[level == l].astype(np.int64) + 64
+        k = c[:, 0] | (c[:, 1] << key_bits)
+        if dim == 3:
+            k = k | (c[:, 2] << (2 * key_bits))
+        total += int(np.isin(k - 1, k).sum())
+    return total
+
+
 def halo_count(level, coords):
     """Distinct same-level non-leaf neighbours (+-1 along each axis) of the
     leaf cells: the ghost values the upwind stencil reads."""
@@ -164,6 +183,114 @@ def halo_count(level, coords):
         nb = np.unique(np.concatenate(nb))
         total += int(np.setdiff1d(nb, np.unique(keys), assume_unique=True).size)
     return total
+
+
+# ------------------------------------------------- per-kernel step table
+PX, PY = 32, 8  # padding of the level boxes (samurai_gb300/csrc/sg_core.cuh)
+
+
+def level_words(dim, maxl):
+    """32-bit words per level of the dense bitmaps (sg::make_geom)"""
+    out = []
+    for l in range(maxl + 1):
+        n = 1 << l
+        W = (n + 31) // 32 + 2
+        R = n + 2 * PY
+        out.append(W * (R if dim == 2 else R * R))
+    return out
+
+
+def mesh_id_counts(sim, maxl):
+    """cells of each MRMesh id over all levels, from the exported intervals"""
+    out = {}
+    for mid in ("cells", "proj_cells", "union_cells", "reference"):
+        tot = 0
+        for lev in range(maxl + 1):
+            iv = sim.mesh.intervals(mid, lev)
+            tot += int(np.sum(iv[:, 1].astype(np.int64) - iv[:, 0]))
+        out[mid] = tot
+    return out
+
+
+# bitmaps a word kernel reads or writes, per word of the levels it covers
+# (4 bytes each): the algorithmic traffic of the integer mesh kernels
+WORD_KERNEL_BITMAPS = {
+    "hc_cag": 3, "hc2_cag_on": 4, "hc2_cag_z": 4, "cag_on": 2, "union": 3, "ref0": 4, "ref0_xy": 4, "ref0_z": 4, "ref_children": 4,
+    "proj": 3, "scan_sums": 2, "scan_write": 5, "tag_flags": 3, "new_cells": 4, "grad_coarsen": 2, "grad_expand": 2, "grad_expand_xy": 2,
+    "grad_expand_z": 2, "grad_down": 5, "grad_apply": 3, "compare": 2,
+}
+
+
+def kernel_bytes(name, dim, counts, halo, words_all, words_ref, passes):
+    """Algorithmic bytes of one step's launches of kernel `name` (each array
+    element counted once per kernel): passes = (fronts, backs) of the step's
+    Harten passes.  FP64 kernels from the mesh-id counts, word kernels from the
+    words of the levels they cover."""
+    nc, nr, npj = counts["cells"], counts["reference"], counts["proj_cells"]
+    ch = 1 << dim
+    fronts, backs = passes
+    ghosts = max(nr - nc - npj, 0)
+    per_front = {
+        "tag_init": 9 * nr,
+        "ghost_level": 8 * (ch + 1) * npj,           # projection: 2^d children read, 1 written
+        "ghost_levels_small": 0,
+        "ghost_corner_projection": 0,
+        "predict": 8 * ghosts + 8 * ghosts // ch,    # ghost written + its coarse parent read
+        "predict_small": 0,
+        "detail": 8 * (1 + 2 * ch) * npj,            # parent + children read, children's details written
+        "criteria": (8 * (ch + 1) + ch) * npj,       # details read, tags written
+        "maximum": 2 * (ch + 1) * npj,               # tags read and written
+        "maximum_small": 0,
+        "keep_boundary": 0,
+    }
+    if name == "upwind" or name == "convection":
+        return 16 * nc + 8 * halo
+    if name in per_front:
+        return per_front[name] * fronts
+    if name == "update_fields":
+        return 16 * nr * backs
+    if name in WORD_KERNEL_BITMAPS:
+        words = words_all if name in ("tag_flags", "new_cells", "compare", "scan_sums", "scan_write") else words_ref
+        # the scan and mesh construction run once per back half, the others once per front half
+        n = backs if name in ("hc_cag", "hc2_cag_on", "hc2_cag_z", "cag_on", "union", "ref0", "ref0_xy", "ref0_z", "ref_children", "proj",
+                              "scan_sums", "scan_write") else fronts
+        return 4 * WORD_KERNEL_BITMAPS[name] * words * n
+    return 0
+
+
+def step_kernel_table(sim, step, dim, maxl, minl, halo, peak):
+    """One traced step: per kernel its launches, device time (from the
+    per-launch trace events, inside the captured graphs), algorithmic bytes and
+    achieved GB/s against the measured HBM peak."""
+    sim.mesh.kernel_trace(True)  # capture the traced launch sequences once
+    step()
+    sim.mesh.kernel_trace(False)
+    counts = mesh_id_counts(sim, maxl)
+    sim.mesh.synchronize()
+    sim.mesh.kernel_trace(True)
+    passes = step()
+    rows, valid = sim.mesh.kernel_trace(False)
+    words = level_words(dim, maxl)
+    lmin = max(minl - 2, 0)
+    words_ref, words_all = sum(words[lmin:]), sum(words)
+    fronts = passes
+    backs = passes - 1 if passes < maxl - minl else passes
+    table = []
+    total_b = 0
+    total_ms = 0.0
+    for name, n, ms in sorted(rows, key=lambda r: -r[2]):
+        b = kernel_bytes(name, dim, counts, halo, words_all, words_ref, (fronts, backs))
+        total_b += b
+        total_ms += ms
+        gbs = b / (ms * 1e-3) / 1e9 if ms > 0 else None
+        table.append({"kernel": name, "launches": n, "us": round(1e3 * ms, 2), "algorithmic_bytes": int(b),
+                      "GB_s": round(gbs, 2) if gbs is not None else None, "frac_of_hbm": round(gbs / peak, 5) if gbs is not None else None})
+    return {"valid": valid, "harten_passes": passes, "launches": sum(r[1] for r in rows), "traced_ms": total_ms,
+            "algorithmic_bytes": int(total_b), "kernels": table,
+            "mesh_counts": counts,
+            "note": "one step traced inside its captured graphs: each launch's time runs from the previous launch's end event to its own "
+                    "(kernel time plus the gap before it); bytes: each array element once per kernel (FP64 kernels from the mesh-id "
+                    "counts, word kernels 4 B per bitmap word of the levels they cover)"}
 
 
 # --------------------------------------------------------------- GPU arm
@@ -193,9 +320,10 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
 
     def step():
-        sim.adapt(CFG["eps"], CFG["regularity"])
+        passes = sim.adapt(CFG["eps"], CFG["regularity"])
         sim.update_ghost()
         sim.upwind(a, dt)
+        return passes
 
     for _ in range(args.warmup):
         step()
@@ -265,6 +393,7 @@ def run_gpu(args):
     # ---- roofline of the upwind kernel, timed alone on its launch stream
     nc, _ = sim.mesh.counts()
     lv, co, _ = sim.cells()
+    lv_all, co_all = lv, co
     halo = halo_count(lv, co)
     alg_bytes = 16 * nc + 8 * halo
     reps = 20
@@ -292,7 +421,12 @@ def run_gpu(args):
     # per face flux plus 5 (2D) to assemble the update: 26 per cell in 2D
     # the reference's formula: 5 FP64 operations per face flux (2 dim fluxes),
     # 2 dim - 1 to combine them, 3 to scale and update: 26 in 2D, 38 in 3D
-    fp64_ops = (10 * dim + 2 * dim - 1 + 3) * nc
+    fp64_ref_ops = (10 * dim + 2 * dim - 1 + 3) * nc
+    # FP64 instructions issued by k_upwind: 5 per face flux (2 dim faces), 2 dim - 1
+    # additions to combine them and 2 for u - dt * s (the 2^l scaling moves the
+    # exponent); the left x-flux is taken from the previous lane when that lane
+    # holds the left neighbour (5 fewer)
+    fp64_ops = UPWIND_ISSUED[dim] * nc - 5 * left_shared(lv_all, co_all)
     try:
         fp64_peak = sg.device_fp64_rate()
     except Exception:
@@ -309,6 +443,30 @@ def run_gpu(args):
     for _ in range(phase_steps):
         step()
     phases = {k: round(v[0] / phase_steps, 4) for k, v in sim.mesh.timers(enable=False).items()}
+
+    # ---- one step traced launch by launch: per-kernel time, bytes, GB/s; the
+    # step's algorithmic bytes over the device-timed step
+    lv, co, _ = sim.cells()
+    ktab = step_kernel_table(sim, step, dim, maxl, minl, halo_count(lv, co), peak)
+    step_ms = total_ms_max / args.steps
+    # the dominant kernel: the largest share of the traced step
+    dom = ktab["kernels"][0]
+    dom_launch_ms = dom["us"] / 1e3 / max(dom["launches"], 1)
+    dom_bytes = dom["algorithmic_bytes"] / max(dom["launches"], 1)
+    roofline = {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom_bytes / (dom_launch_ms * 1e-3) / 1e9 if dom_launch_ms > 0 else None,
+                "peak": peak, "peak_source": peak_src, "unit": "GB/s", "traffic": DOMINANT_TRAFFIC.get(dom["kernel"]),
+                "algorithmic_bytes_per_launch": int(dom_bytes), "launch_ms": dom_launch_ms, "launches_per_step": dom["launches"],
+                "share_of_step": dom["us"] / 1e3 / ktab["traced_ms"] if ktab["traced_ms"] > 0 else None,
+                "timing": "per-launch trace events inside the captured graphs, one step"}
+    roofline["frac"] = roofline["achieved"] / peak if roofline["achieved"] else None
+    roofline_step = {"algorithmic_bytes": ktab["algorithmic_bytes"], "ms_per_step": step_ms,
+                     "achieved": ktab["algorithmic_bytes"] / (step_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s"}
+    roofline_step["frac"] = roofline_step["achieved"] / peak
+
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras["adjoint"] = adjoint_record(args, fd_directions=8, steps=256)
+        extras["batch"] = batch_record(args, steps=10, warmup=3, serial_steps=3)
 
     cpu = cpu_baseline(sim, a, dt) if (rank == 0 and not args.no_cpu_baseline) else None
 
@@ -330,19 +488,29 @@ def run_gpu(args):
                                        "cells_final": int(nc), "reference_cells_final": int(sim.nb_ref())}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps),
                     "steps": e2e_steps, "api": "sg_field_upload + sg_adapt + sg_update_ghost_mr + sg_upwind + sg_field_swap + sg_field_download"},
-            "roofline": {"bound": "hbm", "kernel": "k_upwind", "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "traffic_source": "ncu dram__bytes of a 536 428-cell launch, scaled by leaf cells",
-                         "algorithmic_bytes": int(alg_bytes), "launch_ms": upw_ms,
-                         "cells": int(nc), "halo": int(halo),
-                         "fp64": {"achieved_gflops": fp64_ops / (upw_ms / 1e3) / 1e9, "peak_gflops": fp64_peak,
-                                  "peak_source": "measured in this run (sg_device_fp64_rate probe)",
-                                  "frac": (fp64_ops / (upw_ms / 1e3) / 1e9 / fp64_peak) if fp64_peak else None,
-                                  "ops_per_launch": int(fp64_ops), "note": "FP64 operations per leaf cell in the reference's formula: 26 (2D), 38 (3D)"}},
+            "roofline": roofline,
+            "roofline_step": roofline_step,
+            "kernels_step": ktab,
+            "upwind_roofline": {"bound": "hbm", "kernel": "k_upwind", "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+                                "frac": achieved / peak, "traffic": traffic,
+                                "traffic_source": "ncu dram__bytes of a 536 428-cell launch, scaled by leaf cells",
+                                "algorithmic_bytes": int(alg_bytes), "launch_ms": upw_ms, "timing": "k_upwind alone, L2 flushed, 20 launches",
+                                "cells": int(nc), "halo": int(halo),
+                                "fp64": {"achieved_gflops": fp64_ops / (upw_ms / 1e3) / 1e9, "peak_gflops": fp64_peak,
+                                         "peak_source": "measured in this run (sg_device_fp64_rate probe)",
+                                         "frac": (fp64_ops / (upw_ms / 1e3) / 1e9 / fp64_peak) if fp64_peak else None,
+                                         "ops_per_launch": int(fp64_ops), "reference_formula_ops": int(fp64_ref_ops),
+                                         "note": "FP64 instructions the kernel issues: %d per leaf cell, %d fewer when the left x-face flux "
+                                                 "comes from the previous lane (counted for every leaf whose left neighbour is a leaf of the same "
+                                                 "level: an upper bound on the sharing); the reference's formula counts %d"
+                                                 % (UPWIND_ISSUED[dim], 5, 10 * dim + 2 * dim - 1 + 3)}},
             "gpu_launches": int(launches),
             "launches_per_step": launches / args.steps,
             "phases_ms_per_step": phases,
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "adjoint": extras.get("adjoint"),
+            "batch": extras.get("batch"),
         }
         print(json.dumps(line))
     if world > 1:
@@ -416,7 +584,7 @@ def run_reference(args):
     lv, co, _ = o.cells()
     o.set_cell_values(initial_values(lv, co))
     o.adapt(CFG["eps"], CFG["regularity"])
-    for _ in range(min(args.warmup, 1)):
+    for _ in range(args.warmup):
         o.adapt(CFG["eps"], CFG["regularity"])
         o.update_ghost()
         o.upwind(list(CFG["a"]), dt, 0)
@@ -443,7 +611,7 @@ def run_reference(args):
         "unit": UNIT,
         "n_gpus": world,
         "steps": n,
-        "warmup": min(args.warmup, 1),
+        "warmup": args.warmup,
         "ms_per_step": 1e3 * el / n,
         "higher_is_better": True,
         "scaling": "weak",
@@ -458,10 +626,18 @@ def run_reference(args):
 
 
 def run_batch(args):
+    """The batched workload as its own benchmark line (--workload batch)."""
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")  # one hardware queue per busy stream
+    line = batch_record(args, args.steps, args.warmup, max(1, min(args.steps, 10)), full=True)
+    if line is not None:
+        print(json.dumps(line))
+
+
+def batch_record(args, steps, warmup, serial_steps, full=False):
     """256 independent 2D problems (max_level U{7..11}, min_level 2, a U[-1,1]^2,
     1-8 shapes, eps 1e-3 or 1e-4) stepped together through sg_batch_step, and
-    the same problems stepped one after the other through the serial calls."""
-    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")  # one hardware queue per busy stream
+    the same problems stepped one after the other through the serial calls.
+    Returns the record (rank 0) or None."""
     import torch
 
     from samurai_gb300 import build as gpu_build
@@ -492,7 +668,7 @@ def run_batch(args):
     a = [p["a"] for p in probs]
     dt = [p["dt"] for p in probs]
     batch.adapt(eps, reg)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.step(eps, reg, a, dt)
     batch.synchronize()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
@@ -515,8 +691,8 @@ def run_batch(args):
             updates += n
         return total, updates
 
-    sampler = ClockSampler(local, os.path.join(clock_dir(), "clocks_batch.csv")) if rank == 0 else None
-    b_s, b_updates = timed(lambda: (batch.step(eps, reg, a, dt), batch.synchronize()), args.steps)
+    sampler = ClockSampler(local, os.path.join(clock_dir(), "clocks_batch.csv")) if (rank == 0 and full) else None
+    b_s, b_updates = timed(lambda: (batch.step(eps, reg, a, dt), batch.synchronize()), steps)
     clocks = sampler.stop() if sampler else None
     b_ms, b_updates = reduce_over_ranks(1e3 * b_s, b_updates, world, device="cuda")
     b_s = b_ms / 1e3
@@ -529,22 +705,21 @@ def run_batch(args):
 
     # the serial calls with the instances' own launch shapes (the batch sets its own)
     batch.close()
-    serial_steps = max(1, min(args.steps, 10))
     s_s, s_updates = timed(serial_step, serial_steps)
     s_ms, s_updates = reduce_over_ranks(1e3 * s_s, s_updates, world, device="cuda")
     s_s = s_ms / 1e3
     cells = [s.nb_cells() for s in sims]
     if rank != 0:
-        return
-    cpu = None if args.no_cpu_baseline else batch_cpu_baseline(probs, sims)
+        return None
+    cpu = None if (args.no_cpu_baseline or not full) else batch_cpu_baseline(probs, sims)
     line = {
         "metric": METRIC,
         "value": b_updates / b_s,
         "unit": UNIT,
         "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": 1e3 * b_s / args.steps,
+        "steps": steps,
+        "warmup": warmup,
+        "ms_per_step": 1e3 * b_s / steps,
         "higher_is_better": True,
         "scaling": "strong",  # a fixed set of instances shared by the ranks
         "vs_baseline": None,
@@ -562,17 +737,23 @@ def run_batch(args):
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
-    print(json.dumps(line))
     batch.close()
+    del sims
+    return line
 
 
 def run_adjoint(args):
+    """The adjoint workload as its own benchmark line (--workload adjoint)."""
+    print(json.dumps(adjoint_record(args, args.fd_directions, args.adjoint_steps)))
+
+
+def adjoint_record(args, fd_directions, steps):
     """The adjoint workload: 2D, min_level 3, max_level 10, a = (1, 0.7), 256
     steps, J = sum vol (u_T - u_tgt)^2 with a seeded Gaussian target,
-    checkpoints every 16 steps.  Times the recorded forward and the backward
-    pass, and checks the gradient: dot-product test and central finite
-    differences on the recorded meshes along 64 seeded directions in u0 and
-    along each velocity component."""
+    checkpoints every 16 steps.  Times a plain forward (the loop through the
+    serial calls), the recorded forward and the backward pass, and checks the
+    gradient: dot-product test and central finite differences on the recorded
+    meshes along seeded directions in u0 and along each velocity component."""
     import torch
 
     from samurai_gb300 import build as gpu_build
@@ -582,7 +763,7 @@ def run_adjoint(args):
     from advection_cases import cell_volumes, gaussian_target
 
     torch.cuda.set_device(0)
-    minl, maxl, steps, eps, reg, K = 3, 10, args.adjoint_steps, 1e-4, 2.0, 16
+    minl, maxl, eps, reg, K = 3, 10, 1e-4, 2.0, 16
     a = (1.0, 0.7)
     dt = 0.5 / (1 << maxl)
     s = sg.AdvectionSim(2, minl, maxl)
@@ -602,10 +783,31 @@ def run_adjoint(args):
     adj.record(u0, steps, eps, reg, a, dt)  # warm-up (graphs, allocations)
     _, gT = objective(adj.final())
     adj.backward(gT)
+    # the plain forward: the same loop from the same state through the serial
+    # calls, no recording (warmed up, then reset to the initial mesh and u0)
+    plain = sg.AdvectionSim(2, minl, maxl)
+    lv0, co0 = adj.cells("initial")
+
+    def plain_loop(n):
+        plain.mesh.set_cells(lv0, co0)
+        plain.set_cell_values(u0)
+        plain.mesh.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(n):
+            plain.adapt(eps, reg)
+            plain.update_ghost()
+            plain.upwind(a, dt)
+        plain.mesh.synchronize()
+        return time.perf_counter() - t0
+
+    plain_loop(16)  # warm-up (graph captures)
+    t_plain = plain_loop(steps)
+    plain_uT = plain.cell_values()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     uT = adj.record(u0, steps, eps, reg, a, dt)
     t_fwd = time.perf_counter() - t0
+    assert np.array_equal(plain_uT, uT), "the recorded forward differs from the plain loop"
     J, gT = objective(uT)
     t0 = time.perf_counter()
     g0, ga = adj.backward(gT)
@@ -621,7 +823,7 @@ def run_adjoint(args):
     LTw, _ = adj.backward(w)
     dot_err = abs(float(Lv @ w) - float(v @ LTw)) / max(abs(float(Lv @ w)), 1e-300)
     fd_u = []
-    for _ in range(args.fd_directions):
+    for _ in range(fd_directions):
         d = rng.standard_normal(n0)
         h = 1e-3
         jp, _ = objective(adj.replay(u0 + h * d, a))
@@ -650,17 +852,19 @@ def run_adjoint(args):
         "config": {"workload": "adjoint of the 2D MR advection loop: min_level 3, max_level 10, a=(1,0.7), eps 1e-4, regularity 2, "
                                "%d steps, checkpoints every %d steps, J = sum vol (u_T - u_tgt)^2" % (steps, K),
                    "cells_initial": int(n0), "cells_final": int(nT), "timing": "wall clock between device synchronisations"},
+        "plain_forward_ms_per_step": 1e3 * t_plain / steps,
         "forward_record_ms_per_step": 1e3 * t_fwd / steps,
         "replay_ms_per_step": 1e3 * t_rep / steps,
         "backward_ms_per_step": 1e3 * t_bwd / steps,
         "backward_over_forward": t_bwd / t_fwd,
+        "gradient_over_plain_forward": (t_fwd + t_bwd) / t_plain,
         "J": J,
         "dJ_da": [float(x) for x in ga],
         "checks": {"dot_product_rel_err": dot_err, "fd_u0_directions": len(fd_u), "fd_u0_max_rel_err": max(fd_u) if fd_u else None,
                    "fd_a_rel_err": fd_a, "fd_note": "central differences on the recorded meshes, h = 1e-3 (u0, exact for quadratic J), 1e-6 (a)"},
     }
-    print(json.dumps(line))
     adj.close()
+    return line
 
 
 def main():
@@ -670,6 +874,7 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch sub-records of the default run")
     p.add_argument("--workload", default="advection2d", choices=["advection2d", "advection3d", "batch", "adjoint"],
                    help="advection2d: the max_level-12 2D problem (default); batch: independent problems through sg_batch_step; "
                         "adjoint: the discrete adjoint of a max_level-10 loop")
@@ -679,7 +884,9 @@ def main():
     p.add_argument("--instances", type=int, default=256)
     p.add_argument("--batch-threads", type=int, default=8)
     args = p.parse_args()
-    if args.warmup < 3 and args.impl != "reference":
+    # one hardware queue per busy stream for the batched instances (set before CUDA starts)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    if args.warmup < 3:
         args.warmup = 3
     if args.workload == "advection3d":
         CFG.clear()

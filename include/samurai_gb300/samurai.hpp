@@ -74,6 +74,13 @@ namespace samurai
         static constexpr int prediction_stencil_radius = 1;
     }
 
+    // samurai's command-line switches that act on this path (arguments.hpp:26, 67): refine_boundary
+    // (--refine-boundary) keeps the boundary cells of max_level refined in every adaptation
+    namespace args
+    {
+        inline bool refine_boundary = false;
+    }
+
     template <std::size_t dim_, int prediction_stencil_radius_ = default_config::prediction_stencil_radius>
     class mesh_config
     {
@@ -1059,6 +1066,7 @@ namespace samurai
                 },
                 m_fields);
             ((others.sync_to_device(), others.append_handles(os)), ...);
+            detail::check(sg_mesh_set_refine_boundary(std::get<0>(m_fields)->mesh().handle(), args::refine_boundary ? 1 : 0), "MRadaptation");
             const int rel = cfg.relative_detail() ? 1 : 0;
             if (fs.size() == 1 && os.empty())
             {

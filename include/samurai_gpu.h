@@ -96,12 +96,34 @@ int sg_mesh_launch_count(sg_mesh_t mesh, int reset, long long* count);
  * the mesh (intervals, cell lists) are current while it stays the same */
 int sg_mesh_version(sg_mesh_t mesh, unsigned long long* version);
 
+/* args::refine_boundary, samurai's --refine-boundary flag (arguments.hpp:26, 67; mr/adapt.hpp:341-346): when set,
+ * every Harten pass of this mesh tags keep the leaves of max_level within max_stencil_radius cells of the domain
+ * boundary (keep_boundary_refined, mr/adapt.hpp:245-274), so the boundary stays refined at max_level.  Off by default,
+ * as in samurai; it applies to the adaptations of this mesh (a process-wide flag in samurai). */
+int sg_mesh_set_refine_boundary(sg_mesh_t mesh, int enable);
+
+/* Without a samurai counterpart: how an adaptation runs.  enable = 1 (the default): the whole of sg_adapt /
+ * sg_adapt_fields is one captured graph in which each Harten pass, the second half of a pass (new mesh,
+ * update_fields) and the graduation iterations run under device-side conditions, with one host synchronisation at
+ * the end; enable = 0: pass by pass, the host reading the fixed-point test after each pass.  Both give the same
+ * results; the named timers and the kernel trace use the pass-by-pass path while they are on. */
+int sg_mesh_set_adapt_graph(sg_mesh_t mesh, int enable);
+
 /* samurai's named timers (timers.hpp:111-1036, printed with --timers): CUDA-event timers per phase.
  * ids: 0 mesh adaptation, 1 ghost update, 2 detail computation, 3 tag cells, 4 tag finalization,
  * 5 mesh update, 6 make_graduation, 7 mesh construction, 8 fields update, 9 field expressions (upwind). */
 int sg_timers_enable(sg_mesh_t mesh, int enable);
 int sg_timers_get(sg_mesh_t mesh, int timer_id, double* total_ms, long long* calls);
 int sg_timers_reset(sg_mesh_t mesh);
+
+/* Instrumentation without a samurai counterpart: a per-launch trace of the mesh's kernels.  While on
+ * (sg_kernel_trace(mesh, 1)), every kernel launch on the mesh's stream is followed by an event (inside
+ * captured launch sequences too), and the time from the previous event to it is that launch's share of
+ * the timeline.  sg_kernel_trace(mesh, 0) stops; sg_kernel_trace_read then returns, for entry i (0, 1, ...;
+ * SG_ERR_NOTFOUND past the last), a kernel name, its launches and their summed time in ms, in order of first
+ * launch.  *valid is 0 when one captured sequence ran twice in the window (trace one step at a time). */
+int sg_kernel_trace(sg_mesh_t mesh, int enable);
+int sg_kernel_trace_read(sg_mesh_t mesh, int i, const char** name, long long* launches, double* ms, int* valid);
 
 /* Instrumentation without a samurai counterpart: the device's FP64 rate (non-fused adds and multiplies
  * per second, in GFLOP/s), measured by a throughput probe kernel.  The FP64 pipe bounds this path on GB300. */

@@ -67,6 +67,10 @@ def lib():
         "sg_timers_enable": (i, [vp, i]),
         "sg_timers_get": (i, [vp, i, ctypes.POINTER(d), pl]),
         "sg_timers_reset": (i, [vp]),
+        "sg_kernel_trace": (i, [vp, i]),
+        "sg_mesh_set_refine_boundary": (i, [vp, i]),
+        "sg_mesh_set_adapt_graph": (i, [vp, i]),
+        "sg_kernel_trace_read": (i, [vp, i, ctypes.POINTER(ctypes.c_char_p), pl, ctypes.POINTER(d), pi]),
         "sg_device_fp64_rate": (i, [ctypes.POINTER(d)]),
         "sg_field_create": (i, [vp, ctypes.c_char_p, ctypes.POINTER(vp)]),
         "sg_field_destroy": (i, [vp]),
@@ -368,6 +372,34 @@ class MRMesh:
             _check(lib().sg_timers_get(self.h, k, ctypes.byref(ms), ctypes.byref(n)), "sg_timers_get")
             out[name] = (ms.value, n.value)
         return out
+
+    def set_adapt_graph(self, enable):
+        """each adaptation as one captured graph (True, the default) or pass by pass (False)"""
+        _check(lib().sg_mesh_set_adapt_graph(self.h, 1 if enable else 0), "sg_mesh_set_adapt_graph")
+
+    def set_refine_boundary(self, enable):
+        """samurai's --refine-boundary (args::refine_boundary) for this mesh's adaptations"""
+        _check(lib().sg_mesh_set_refine_boundary(self.h, 1 if enable else 0), "sg_mesh_set_refine_boundary")
+
+    def kernel_trace(self, enable):
+        """start (True) or stop (False) the per-launch kernel trace; stopping
+        returns (rows, valid), rows = [(kernel, launches, ms)] in order of first
+        launch; valid is False when a captured sequence ran twice in the window"""
+        _check(lib().sg_kernel_trace(self.h, 1 if enable else 0), "sg_kernel_trace")
+        if enable:
+            return None
+        rows, valid = [], True
+        k = 0
+        while True:
+            name, n, ms, ok = ctypes.c_char_p(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_int()
+            st = lib().sg_kernel_trace_read(self.h, k, ctypes.byref(name), ctypes.byref(n), ctypes.byref(ms), ctypes.byref(ok))
+            if st == 5:  # SG_ERR_NOTFOUND: past the last entry
+                break
+            _check(st, "sg_kernel_trace_read")
+            rows.append((name.value.decode(), n.value, ms.value))
+            valid = valid and bool(ok.value)
+            k += 1
+        return rows, valid
 
     def launch_count(self, reset=False):
         n = ctypes.c_longlong()

@@ -127,15 +127,20 @@ namespace
             cudaStreamSynchronize(c.stream);
         }
         sg::timers_flush(c);
+        sg::clear_graphs(c);
+        for (const auto& mk : c.trace.marks)
+        {
+            sg::give_event(c, mk.second);
+        }
+        c.trace.marks.clear();
+        sg::give_event(c, c.trace.start);
+        c.trace.start = nullptr;
+        std::sort(c.timers.pool.begin(), c.timers.pool.end());
+        c.timers.pool.erase(std::unique(c.timers.pool.begin(), c.timers.pool.end()), c.timers.pool.end());
         for (cudaEvent_t e : c.timers.pool)
         {
             cudaEventDestroy(e);
         }
-        for (auto& ge : c.graphs)
-        {
-            cudaGraphExecDestroy(ge.exec);
-        }
-        c.graphs.clear();
         dfree(c.d_ite);
         if (c.h_ite)
         {
@@ -170,6 +175,18 @@ namespace
         if (c.h_flags)
         {
             cudaFreeHost(c.h_flags);
+        }
+        dfree(c.d_adapt);
+        if (c.h_adapt)
+        {
+            cudaFreeHost(c.h_adapt);
+        }
+        for (cudaStream_t cs : c.cap_streams)
+        {
+            if (cs)
+            {
+                cudaStreamDestroy(cs);
+            }
         }
         if (c.stream)
         {
@@ -291,11 +308,7 @@ namespace sg
         c.fuse_top       = mesh_top;
         c.fuse_top_field = field_top;
         c.fuse_top_max   = max_top;
-        for (auto& ge : c.graphs)
-        {
-            cudaGraphExecDestroy(ge.exec);
-        }
-        c.graphs.clear();
+        sg::clear_graphs(c);
     }
 
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words)
@@ -388,6 +401,31 @@ extern "C"
             cudaGetLastError();
             return fail(SG_ERR_CUDA, "sg_mesh_create: no CUDA device");
         }
+        {
+            // device memory of the mesh (two meshes of 10 word arrays, 6 scratch bitmaps, the dense detail and tag
+            // slabs) and of one field with its update_fields buffer, against the free memory of the device: a
+            // configuration that cannot fit is refused here rather than by a failing allocation midway
+            const sg::Geom gg    = sg::make_geom(dim, min_level, max_level);
+            const double words   = static_cast<double>(gg.total_words);
+            const double cap     = 32.0 * words;
+            const double mesh_b  = (2.0 * 10.0 + 6.0) * 4.0 * words + 9.0 * cap;
+            const double field_b = 16.0 * cap;
+            size_t free_b = 0, total_b = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess)
+            {
+                cudaGetLastError();
+                return fail(SG_ERR_CUDA, "sg_mesh_create: cudaMemGetInfo failed");
+            }
+            if (mesh_b + field_b > static_cast<double>(free_b))
+            {
+                char msg[256];
+                std::snprintf(msg, sizeof msg,
+                              "sg_mesh_create: the mesh needs %.1f GB of device memory and each field %.1f GB (dense level slabs), "
+                              "%.1f GB are free",
+                              mesh_b / 1e9, field_b / 1e9, static_cast<double>(free_b) / 1e9);
+                return fail(SG_ERR_CAPACITY, msg);
+            }
+        }
         sg_mesh_s* h = new (std::nothrow) sg_mesh_s();
         if (!h)
         {
@@ -419,6 +457,15 @@ extern "C"
             delete h;
             return fail(SG_ERR_CUDA, "sg_mesh_create: cudaStreamCreate failed");
         }
+        for (auto& cs : c.cap_streams)
+        {
+            if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+            {
+                cudaGetLastError();
+                cs = nullptr;
+            }
+        }
+        c.graphed_adapt = tuned("SG_GRAPHED_ADAPT", 1) != 0;
         const size_t nw = static_cast<size_t>(c.g.total_words);
         int st          = alloc_mesh(c, c.mesh[0]);
         st |= alloc_mesh(c, c.mesh[1]);
@@ -434,6 +481,7 @@ extern "C"
         st |= dalloc(c, &c.block_sums, 4 * static_cast<size_t>(c.n_scan_blocks) + 4);
         st |= dalloc(c, &c.d_counts, static_cast<size_t>(sg::COUNTS));
         st |= dalloc(c, &c.d_flags, 8);
+        st |= dalloc(c, &c.d_adapt, static_cast<size_t>(sg::A_COUNT));
         st |= dalloc(c, &c.d_geom, 1);
         st |= dalloc(c, &c.d_ite, 1);
         st |= dalloc(c, &c.d_eps, sg::EPS_VELOCITY + 3);
@@ -444,7 +492,8 @@ extern "C"
             if (cudaMallocHost(reinterpret_cast<void**>(&c.h_ite), sizeof(int)) != cudaSuccess
                 || cudaMallocHost(reinterpret_cast<void**>(&c.h_eps), 3 * sg::MAXLEV * sizeof(double)) != cudaSuccess
                 || cudaMallocHost(reinterpret_cast<void**>(&c.h_counts), sg::COUNTS * sizeof(long long)) != cudaSuccess
-                || cudaMallocHost(reinterpret_cast<void**>(&c.h_flags), 8 * sizeof(int)) != cudaSuccess)
+                || cudaMallocHost(reinterpret_cast<void**>(&c.h_flags), 8 * sizeof(int)) != cudaSuccess
+                || cudaMallocHost(reinterpret_cast<void**>(&c.h_adapt), sg::A_COUNT * sizeof(int)) != cudaSuccess)
             {
                 st = SG_ERR_CUDA;
                 c.err = "cudaMallocHost failed";
@@ -833,6 +882,143 @@ extern "C"
     }
     SG_API_CATCH(sg_device_fp64_rate)
 
+    int sg_mesh_set_adapt_graph(sg_mesh_t mesh, int enable)
+    try
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_set_adapt_graph: null mesh");
+        }
+        mesh->ctx.graphed_adapt = enable != 0;
+        return SG_OK;
+    }
+    SG_API_CATCH(sg_mesh_set_adapt_graph)
+
+    int sg_mesh_set_refine_boundary(sg_mesh_t mesh, int enable)
+    try
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_mesh_set_refine_boundary: null mesh");
+        }
+        mesh->ctx.refine_boundary = enable != 0;
+        return SG_OK;
+    }
+    SG_API_CATCH(sg_mesh_set_refine_boundary)
+
+    int sg_kernel_trace(sg_mesh_t mesh, int enable)
+    try
+    {
+        if (!mesh)
+        {
+            return fail(SG_ERR_ARG, "sg_kernel_trace: null mesh");
+        }
+        sg::Ctx& c = mesh->ctx;
+        if (enable)
+        {
+            if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+            {
+                return fail(SG_ERR_CUDA, "sg_kernel_trace: CUDA error");
+            }
+            // the events of the previous window that no captured sequence holds go back to the pool
+            for (const auto& mk : c.trace.marks)
+            {
+                bool held = false;
+                for (const auto& ge : c.graphs)
+                {
+                    for (const auto& gm : ge.marks)
+                    {
+                        held = held || gm.second == mk.second;
+                    }
+                }
+                if (!held)
+                {
+                    sg::give_event(c, mk.second);
+                }
+            }
+            c.trace.marks.clear();
+            c.trace.reused = false;
+            c.trace.results.clear();
+            if (!c.trace.start)
+            {
+                c.trace.start = sg::take_event(c);
+            }
+            cudaEventRecord(c.trace.start, c.stream);
+            c.trace.enabled = true;
+            return SG_OK;
+        }
+        if (!c.trace.enabled)
+        {
+            return SG_OK;
+        }
+        c.trace.enabled = false;
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return fail(SG_ERR_CUDA, "sg_kernel_trace: CUDA error");
+        }
+        cudaEvent_t prev = c.trace.start;
+        for (const auto& mk : c.trace.marks)
+        {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, prev, mk.second) != cudaSuccess)
+            {
+                cudaGetLastError();
+                c.trace.reused = true;
+                ms             = 0.f;
+            }
+            prev   = mk.second;
+            bool found = false;
+            for (auto& r : c.trace.results)
+            {
+                if (r.name == mk.first)
+                {
+                    r.launches += 1;
+                    r.ms += ms;
+                    found = true;
+                    break;
+                }
+            }
+            if (!found)
+            {
+                c.trace.results.push_back({mk.first, 1, static_cast<double>(ms)});
+            }
+        }
+        return SG_OK;
+    }
+    SG_API_CATCH(sg_kernel_trace)
+
+    int sg_kernel_trace_read(sg_mesh_t mesh, int i, const char** name, long long* launches, double* ms, int* valid)
+    try
+    {
+        if (!mesh || i < 0)
+        {
+            return fail(SG_ERR_ARG, "sg_kernel_trace_read: null mesh or negative index");
+        }
+        const auto& res = mesh->ctx.trace.results;
+        if (static_cast<size_t>(i) >= res.size())
+        {
+            return SG_ERR_NOTFOUND;
+        }
+        if (name)
+        {
+            *name = res[static_cast<size_t>(i)].name;
+        }
+        if (launches)
+        {
+            *launches = res[static_cast<size_t>(i)].launches;
+        }
+        if (ms)
+        {
+            *ms = res[static_cast<size_t>(i)].ms;
+        }
+        if (valid)
+        {
+            *valid = mesh->ctx.trace.reused ? 0 : 1;
+        }
+        return SG_OK;
+    }
+    SG_API_CATCH(sg_kernel_trace_read)
+
     int sg_timers_enable(sg_mesh_t mesh, int enable)
     try
     {
@@ -897,6 +1083,20 @@ extern "C"
         f->mesh  = mesh;
         f->f.ctx = &mesh->ctx;
         f->f.name = name ? name : "";
+        {
+            // the field's slab and the buffer update_fields gives it on the first adaptation
+            size_t free_b = 0, total_b = 0;
+            const double need = 16.0 * static_cast<double>(mesh->ctx.capacity);
+            if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && need > static_cast<double>(free_b))
+            {
+                delete f;
+                char msg[200];
+                std::snprintf(msg, sizeof msg, "sg_field_create: the field needs %.1f GB of device memory, %.1f GB are free", need / 1e9,
+                              static_cast<double>(free_b) / 1e9);
+                return fail(SG_ERR_CAPACITY, msg);
+            }
+            cudaGetLastError();
+        }
         if (dalloc(mesh->ctx, &f->f.data, static_cast<size_t>(mesh->ctx.capacity)))
         {
             delete f;
@@ -1224,11 +1424,7 @@ extern "C"
             }
             cudaMemsetAsync(c.detail, 0, static_cast<size_t>(c.capacity) * n * sizeof(double), c.stream);
             c.detail_comps = n;
-            for (auto& ge : c.graphs)
-            {
-                cudaGraphExecDestroy(ge.exec); // they hold the old detail buffer
-            }
-            c.graphs.clear();
+            sg::clear_graphs(c); // they hold the old detail buffer
         }
         return from_ctx(c, sg::adapt_fields(c, fs, os, eps, regularity, relative_detail != 0, n_harten));
     }

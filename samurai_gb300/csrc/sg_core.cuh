@@ -310,6 +310,121 @@ namespace sg
         return spread16(((k + 1) & 1) ? (cw >> 16) : cw);
     }
 
+    // The word one level coarser that holds the parents of the cells of word
+    // (row, wi) at level l: bit 0 of the word is x = 32 wi - PX, whose parent
+    // x = 16 wi - PX/2 sits at position 16 wi + 16 of the coarse row, so the 16
+    // parents of the word's 32 cells occupy bits [shift, shift + 16) of one
+    // coarse word.  ok is false when the parents' row leaves the coarse box.
+    struct ParentWord
+    {
+        long long row;
+        int wi;
+        int shift;
+        bool ok;
+    };
+
+    __host__ __device__ __forceinline__ ParentWord parent_word(const Geom& g, int l, long long row, int wi)
+    {
+        const LevelGeom& F = g.lv[l];
+        const LevelGeom& C = g.lv[l - 1];
+        int y, z;
+        if (g.dim == 2)
+        {
+            y = static_cast<int>(row) - PY;
+            z = 0;
+        }
+        else
+        {
+            split_row(F, row, &y, &z);
+            y -= PY;
+            z -= PY;
+        }
+        const int ry = (y >> 1) + PY, rz = (z >> 1) + PY; // floor halves
+        const int base = 16 * wi + 16;
+        ParentWord p;
+        p.wi    = base >> 5;
+        p.shift = base & 31;
+        p.ok    = ry >= 0 && ry < C.R && (g.dim == 2 || (rz >= 0 && rz < C.R)) && p.wi < C.W;
+        p.row   = (g.dim == 2) ? ry : static_cast<long long>(rz) * C.R + ry;
+        return p;
+    }
+
+    // Marks in bm the ancestors, at levels l-1 down to lstop, of the cells h
+    // of word (row, wi) at level l (bm's coarser levels accumulate by atomic
+    // OR).  A walk stops at the first level where its bits were already set:
+    // the walk that set them marks everything above.
+    __device__ __forceinline__ void mark_ancestors(const Geom& g, uint32_t* bm, int l, long long row, int wi, uint32_t h, int lstop)
+    {
+        for (int lc = l - 1; lc >= lstop && h; --lc)
+        {
+            const ParentWord p = parent_word(g, lc + 1, row, wi);
+            if (!p.ok)
+            {
+                return;
+            }
+            const uint32_t bits = (compress_pairs(h, 0u) & 0xFFFFu) << p.shift;
+            const LevelGeom& C  = g.lv[lc];
+            const uint32_t old  = atomicOr(bm + C.woff + p.row * C.W + p.wi, bits);
+            if ((old & bits) == bits)
+            {
+                return;
+            }
+            h   = bits;
+            row = p.row;
+            wi  = p.wi;
+        }
+    }
+
+    // Cells of word (row, wi) at level l that lie in bm at level l or whose
+    // ancestor (levels l-1 .. lstop) lies in bm: the ancestors of the 32
+    // cells at level l - k are 32 >> k cells of one word (one cell from
+    // k = 5 on), read independently for every k and spread back.
+    __device__ __forceinline__ uint32_t self_or_ancestor(const Geom& g, const uint32_t* bm, int l, long long row, int wi, int lstop)
+    {
+        const LevelGeom& L = g.lv[l];
+        uint32_t acc       = __ldg(bm + L.woff + row * L.W + wi);
+        int y, z;
+        if (g.dim == 2)
+        {
+            y = static_cast<int>(row) - PY;
+            z = 0;
+        }
+        else
+        {
+            split_row(L, row, &y, &z);
+            y -= PY;
+            z -= PY;
+        }
+        const int x0 = 32 * wi - PX;
+        for (int k = 1; l - k >= lstop; ++k)
+        {
+            const LevelGeom& A = g.lv[l - k];
+            const int ry = (y >> k) + PY, rz = (z >> k) + PY;
+            if (ry < 0 || ry >= A.R || (g.dim == 3 && (rz < 0 || rz >= A.R)))
+            {
+                continue;
+            }
+            const int pos        = (x0 >> (k < 31 ? k : 31)) + PX;
+            const long long arow = (g.dim == 2) ? ry : static_cast<long long>(rz) * A.R + ry;
+            const int width      = k >= 5 ? 1 : (32 >> k);
+            const uint32_t word  = __ldg(bm + A.woff + arow * A.W + (pos >> 5));
+            uint32_t bits        = (word >> (pos & 31)) & (width == 32 ? 0xFFFFFFFFu : ((1u << width) - 1u));
+            if (k >= 5)
+            {
+                acc |= bits ? 0xFFFFFFFFu : 0u;
+            }
+            else
+            {
+                for (int s = 0; s < k; ++s)
+                {
+                    bits = spread16(bits);
+                }
+                acc |= bits;
+            }
+        }
+        return acc;
+    }
+
     // x-dilation of one word by r (< 32) using its neighbours in the row
     __device__ __forceinline__ uint32_t dilate_x(uint32_t left, uint32_t mid, uint32_t right, int r)
     {

@@ -52,6 +52,17 @@ namespace sg
     constexpr int LO_CELLS = LO_REF + MAXLEV + 1;
     constexpr int COUNTS   = LO_CELLS + MAXLEV + 1;
 
+    // state of an adaptation run as one graph (device words, mirrored to pinned host at its end)
+    enum AdaptSlot : int
+    {
+        A_GO     = 0,  // the next Harten pass runs (the previous one changed the mesh)
+        A_PASSES = 1,  // Harten passes run
+        A_TRANS  = 2,  // passes that changed the mesh
+        A_LOOP   = 3,  // condition of the graduation loop
+        A_ITER   = 4,  // iterations of the graduation loop
+        A_COUNT  = 8
+    };
+
     // flags written by the adaptation kernels (device, mirrored to pinned host)
     enum FlagSlot : int
     {
@@ -81,6 +92,26 @@ namespace sg
         T_COUNT
     };
 
+    // Kernel trace: while enabled, every launch records an event on the mesh
+    // stream right after the kernel (inside captured graphs the events become
+    // event-record nodes, replayed with the graph), so that the time between
+    // consecutive events is one launch's share of the timeline: its run time
+    // plus the gap before it.  Times are read once the stream is idle.
+    struct KernelTrace
+    {
+        bool enabled = false;
+        cudaEvent_t start = nullptr;
+        std::vector<std::pair<const char*, cudaEvent_t>> marks; // launch order
+        bool reused = false; // an event was recorded twice in the window (a graph replayed twice)
+        struct Result
+        {
+            const char* name;
+            long long launches;
+            double ms;
+        };
+        std::vector<Result> results; // per kernel name, filled when the trace stops
+    };
+
     struct Timers
     {
         bool enabled = false;
@@ -94,6 +125,7 @@ namespace sg
     struct Ctx
     {
         Timers timers;
+        KernelTrace trace;
         MeshCfg cfg;
         Geom g{};                // host copy
         Geom* d_geom = nullptr;  // device copy: kernels read the geometry through this pointer
@@ -101,9 +133,17 @@ namespace sg
         unsigned long long* d_absmax = nullptr; // bits of max |u| over the leaf cells (relative details)
         int detail_comps             = 1;       // dense detail slabs allocated (one per adapted field)
         bool rel_detail = false;                // the Harten pass in flight divides the details by max |u|
+        bool refine_boundary = false;           // args::refine_boundary: keep the boundary cells of max_level
         double* h_eps = nullptr; // pinned staging of d_eps
         cudaStream_t stream = nullptr;
         int device          = -1; // the device current at creation: every buffer of the mesh lives there
+        // streams that capture the bodies of conditional graph nodes (one per nesting depth)
+        static constexpr int CAPTURE_DEPTH = 4;
+        cudaStream_t cap_streams[CAPTURE_DEPTH] = {};
+        int cap_depth = 0;
+        int* d_adapt  = nullptr; // device state of a graphed adaptation (AdaptSlot)
+        int* h_adapt  = nullptr; // pinned mirror of d_adapt
+        bool graphed_adapt = true; // the whole adaptation as one graph with conditional nodes
         DeviceMesh mesh[2];
         int cur = 0;
         // scratch bitmaps
@@ -139,6 +179,7 @@ namespace sg
             unsigned long long key[4];
             cudaGraphExec_t exec;
             int kernels;
+            std::vector<std::pair<const char*, cudaEvent_t>> marks; // trace events captured into the graph
         };
         std::vector<GraphEntry> graphs;
         int n_launches      = 0;       // kernel launches since the last reset (instrumentation)
@@ -201,6 +242,13 @@ namespace sg
     void timer_start(Ctx& c, int id);
     void timer_stop(Ctx& c, int id);
     void timers_flush(Ctx& c); // synchronises and accumulates
+
+    // bookkeeping after every kernel launch: the launch counter and, while the
+    // kernel trace is on, the trace event of the launch
+    void launched(Ctx& c, const char* name, int count = 1);
+    void clear_graphs(Ctx& c); // drops the captured launch sequences (their trace events go back to the pool)
+    cudaEvent_t take_event(Ctx& c);
+    void give_event(Ctx& c, cudaEvent_t e);
 
     struct ScopedTimer
     {

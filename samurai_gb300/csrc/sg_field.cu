@@ -756,7 +756,7 @@ namespace sg
                 if ((g.periodic >> d) & 1)
                 {
                     k_periodic_copy<<<static_cast<int>((2 * per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.d_geom, l, d, per, m.ref, u);
-                    ++c.n_launches;
+                    launched(c, "periodic_copy");
                 }
             }
         }
@@ -776,7 +776,7 @@ namespace sg
                     for (int side = 0; side < 2; ++side)
                     {
                         k_periodic_tag<<<static_cast<int>((per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.d_geom, l, d, side, per, m.ref, c.tag);
-                        ++c.n_launches;
+                        launched(c, "periodic_tag");
                     }
                 }
             }
@@ -1051,6 +1051,24 @@ namespace sg
             const double inv = 1. / mx;
             warp_list(wl, lo[LO_REF], lo[LO_REF + nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; },
                       [&](long long w, int b) { det[32 * w + b] *= inv; });
+        }
+
+        // keep_boundary_refined (mr/adapt.hpp:245-274): in each Cartesian
+        // direction, the cells of max_level outside the domain translated by
+        // -max_stencil_radius times the direction (domain_boundary_layer,
+        // boundary.hpp:6-21), i.e. the leaves of max_level within r cells of
+        // the boundary, are tagged keep (the tag is overwritten)
+        __global__ void k_keep_boundary(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* cells, int r, uint8_t* tag)
+        {
+            const Geom& g = *gp;
+            const int l   = g.max_level;
+            warp_list(wl, lo[LO_CELLS + l], lo[LO_CELLS + l + 1], warp_id(), warp_count(),
+                      [&](long long w)
+                      {
+                          const WordLoc loc = word_loc(g, l, w);
+                          return cells[w] & ~box_mask(g, l, loc.row, loc.wi, -r, -r);
+                      },
+                      [&](long long w, int b) { tag[32 * w + b] = 1; });
         }
 
         // maximum_op (mr/operators.hpp:22-96), children at level l
@@ -1497,7 +1515,7 @@ namespace sg
     cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
     {
         k_gather<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
-        ++c.n_launches;
+        launched(c, "gather");
         return cudaGetLastError();
     }
 
@@ -1529,14 +1547,14 @@ namespace sg
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense)
     {
         k_scatter<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, compact, dense);
-        ++c.n_launches;
+        launched(c, "scatter");
         return check(c, "scatter");
     }
 
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value)
     {
         k_fill<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, dense, value);
-        ++c.n_launches;
+        launched(c, "fill");
         return check(c, "fill");
     }
 
@@ -1552,6 +1570,11 @@ namespace sg
         {
             return seq();
         }
+        // a traced sequence carries its trace events as graph nodes: a graph of its own
+        if (c.trace.enabled)
+        {
+            k0 |= 1ull << 63;
+        }
         for (auto& e : c.graphs)
         {
             if (e.key[0] == k0 && e.key[1] == k1 && e.key[2] == k2 && e.key[3] == k3)
@@ -1561,6 +1584,17 @@ namespace sg
                     return check(c, "cudaGraphLaunch");
                 }
                 c.n_launches += e.kernels;
+                if (c.trace.enabled)
+                {
+                    for (const auto& mk : e.marks)
+                    {
+                        for (const auto& seen : c.trace.marks)
+                        {
+                            c.trace.reused = c.trace.reused || seen.second == mk.second;
+                        }
+                        c.trace.marks.push_back(mk);
+                    }
+                }
                 return SG_OK;
             }
         }
@@ -1568,15 +1602,24 @@ namespace sg
         {
             return check(c, "cudaStreamBeginCapture");
         }
-        const int before = c.n_launches;
-        int st           = seq();
-        cudaGraph_t graph = nullptr;
-        cudaError_t e     = cudaStreamEndCapture(c.stream, &graph);
+        const int before      = c.n_launches;
+        const size_t marks0   = c.trace.marks.size();
+        int st                = seq();
+        cudaGraph_t graph     = nullptr;
+        cudaError_t e         = cudaStreamEndCapture(c.stream, &graph);
+        // the trace events recorded during the capture belong to the graph
+        std::vector<std::pair<const char*, cudaEvent_t>> marks(c.trace.marks.begin() + static_cast<long>(std::min(marks0, c.trace.marks.size())),
+                                                               c.trace.marks.end());
+        c.trace.marks.resize(std::min(marks0, c.trace.marks.size()));
         if (st || e != cudaSuccess)
         {
             if (graph)
             {
                 cudaGraphDestroy(graph);
+            }
+            for (const auto& mk : marks)
+            {
+                give_event(c, mk.second);
             }
             if (!st)
             {
@@ -1591,15 +1634,24 @@ namespace sg
         cudaGraphDestroy(graph);
         if (e != cudaSuccess)
         {
+            for (const auto& mk : marks)
+            {
+                give_event(c, mk.second);
+            }
             return check(c, "cudaGraphInstantiate");
         }
         if (c.graphs.size() >= 64)
         {
             cudaGraphExecDestroy(c.graphs.front().exec);
+            for (const auto& mk : c.graphs.front().marks)
+            {
+                give_event(c, mk.second);
+            }
             c.graphs.erase(c.graphs.begin());
         }
         const int kernels = c.n_launches - before;
-        c.graphs.push_back({{k0, k1, k2, k3}, exec, kernels});
+        c.graphs.push_back({{k0, k1, k2, k3}, exec, kernels, marks});
+        c.trace.marks.insert(c.trace.marks.end(), marks.begin(), marks.end());
         if (cudaGraphLaunch(exec, c.stream) != cudaSuccess)
         {
             return check(c, "cudaGraphLaunch");
@@ -1609,6 +1661,135 @@ namespace sg
 
     namespace
     {
+        // the Harten pass index and the criteria thresholds of one pass, baked
+        // into a captured graph (the host computes them exactly as for the
+        // staged copies of the per-pass path)
+        struct PassSetup
+        {
+            double eps[3 * MAXLEV];
+            int ite;
+        };
+
+        __global__ void k_pass_setup(PassSetup p, double* d_eps, int* d_ite)
+        {
+            for (int i = threadIdx.x; i < 3 * MAXLEV; i += blockDim.x)
+            {
+                d_eps[i] = p.eps[i];
+            }
+            if (threadIdx.x == 0)
+            {
+                *d_ite = p.ite;
+            }
+        }
+
+        // the condition of a conditional graph node from a device word
+        __global__ void k_cond_set(cudaGraphConditionalHandle h, const int* flag, int invert)
+        {
+            cudaGraphSetConditional(h, ((*flag != 0) ? 1u : 0u) ^ static_cast<unsigned>(invert));
+        }
+
+        // end of a loop body: repeat while *flag is set, at most limit times
+        // (the count at *iter, reset before the loop); past the limit the
+        // mesh's error word records it and the loop stops
+        __global__ void k_loop_next(cudaGraphConditionalHandle h, const int* flag, int* iter, int limit, int* err)
+        {
+            const int n = ++*iter;
+            bool go     = *flag != 0;
+            if (go && n >= limit)
+            {
+                atomicOr(err, 4);
+                go = false;
+            }
+            cudaGraphSetConditional(h, go ? 1u : 0u);
+        }
+
+        __global__ void k_adapt_words(int* a, int slot, const int* src, int value, int add)
+        {
+            // a[slot] = src ? *src : value, or += when add
+            const int v = src ? *src : value;
+            a[slot]     = add ? a[slot] + v : v;
+        }
+
+        // Appends to the graph captured on c.stream a conditional node (IF:
+        // its body runs once when the condition holds; WHILE: while it holds)
+        // whose condition is set by set_cond(handle) just before the node and
+        // whose body is captured from body(handle) on a capture stream of its
+        // own.  Conditional bodies hold kernels, memsets and copies only.
+        template <class SetCond, class Body>
+        int capture_conditional(Ctx& c, cudaGraphConditionalNodeType type, SetCond set_cond, Body body)
+        {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            cudaGraph_t graph          = nullptr;
+            if (cudaStreamGetCaptureInfo(c.stream, &cs, nullptr, &graph) != cudaSuccess || cs != cudaStreamCaptureStatusActive)
+            {
+                c.err = "conditional node outside a capture";
+                return SG_ERR_STATE;
+            }
+            if (c.cap_depth >= Ctx::CAPTURE_DEPTH || !c.cap_streams[c.cap_depth])
+            {
+                c.err = "conditional nodes nested too deep";
+                return SG_ERR_STATE;
+            }
+            cudaGraphConditionalHandle h{};
+            if (cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault) != cudaSuccess)
+            {
+                return check(c, "cudaGraphConditionalHandleCreate");
+            }
+            set_cond(h);
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd                   = 0;
+            if (cudaStreamGetCaptureInfo(c.stream, &cs, nullptr, &graph, &deps, nullptr, &nd) != cudaSuccess)
+            {
+                return check(c, "cudaStreamGetCaptureInfo");
+            }
+            cudaGraphNodeParams np{};
+            np.type                 = cudaGraphNodeTypeConditional;
+            np.conditional.handle   = h;
+            np.conditional.type     = type;
+            np.conditional.size     = 1;
+            cudaGraphNode_t node    = nullptr;
+            if (cudaGraphAddNode(&node, graph, deps, nullptr, nd, &np) != cudaSuccess)
+            {
+                return check(c, "cudaGraphAddNode (conditional)");
+            }
+            cudaGraph_t bodyg = np.conditional.phGraph_out[0];
+            if (cudaStreamUpdateCaptureDependencies(c.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+            {
+                return check(c, "cudaStreamUpdateCaptureDependencies");
+            }
+            cudaStream_t s2 = c.cap_streams[c.cap_depth];
+            if (cudaStreamBeginCaptureToGraph(s2, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            {
+                return check(c, "cudaStreamBeginCaptureToGraph");
+            }
+            ++c.cap_depth;
+            std::swap(c.stream, s2);
+            int st = body(h);
+            std::swap(c.stream, s2);
+            --c.cap_depth;
+            cudaGraph_t out = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(s2, &out);
+            if (!st && e != cudaSuccess)
+            {
+                c.err = std::string("conditional body capture: ") + cudaGetErrorString(e);
+                st    = SG_ERR_CUDA;
+            }
+            return st;
+        }
+
+        template <class Body>
+        int capture_if(Ctx& c, const int* flag, Body body)
+        {
+            return capture_conditional(
+                c, cudaGraphCondTypeIf,
+                [&](cudaGraphConditionalHandle h)
+                {
+                    k_cond_set<<<1, 1, 0, c.stream>>>(h, flag, 0);
+                    launched(c, "cond_set");
+                },
+                [&](cudaGraphConditionalHandle) { return body(); });
+        }
+
         unsigned long long bits_of(double v)
         {
             unsigned long long b;
@@ -1687,7 +1868,7 @@ namespace sg
                     {
                         k_ghost_level<3><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
-                    ++c.n_launches;
+                    launched(c, "ghost_level");
                     after();
                 }
                 if (split && a.nb_corner > 0)
@@ -1705,7 +1886,7 @@ namespace sg
                     {
                         k_ghost_level<3><<<b.nb_corner, BLOCK, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
-                    ++c.n_launches;
+                    launched(c, "ghost_corner_projection");
                     after();
                 }
                 periodic(l);
@@ -1725,7 +1906,7 @@ namespace sg
                     {
                         k_ghost_levels_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
-                    ++c.n_launches;
+                    launched(c, "ghost_levels_small");
                     after();
                 }
                 if (lp <= maxl && lp <= ft)
@@ -1739,7 +1920,7 @@ namespace sg
                     {
                         k_predict_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
                     }
-                    ++c.n_launches;
+                    launched(c, "predict_small");
                     after();
                     lp = e + 1;
                 }
@@ -1756,7 +1937,7 @@ namespace sg
                     k_predict<3><<<blocks_words(c, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
                                                                                    m.ref, u);
                 }
-                ++c.n_launches;
+                launched(c, "predict");
                 after();
                 periodic(lp);
             }
@@ -1784,7 +1965,7 @@ namespace sg
                 k_update_fields<3><<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
                                                                                             nm.cells, m.ref, m.cells, m.hc, uo, un);
             }
-            ++c.n_launches;
+            launched(c, "update_fields");
         }
 
         // Adapt::harten up to the fixed-point test (mr/adapt.hpp:276-375):
@@ -1794,22 +1975,30 @@ namespace sg
         // the flags in pinned memory.  No host synchronisation.
         // The fields fs drive the criteria, one detail component each, the
         // components stored one dense slab after the other.
-        int seq_front(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const std::vector<DeviceField*>& fs)
+        int seq_front(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const std::vector<DeviceField*>& fs, const PassSetup* graphed = nullptr)
         {
             const Geom& g  = c.g;
             const int minl = c.cfg.min_level;
             const int maxl = c.cfg.max_level;
             const int nf   = static_cast<int>(fs.size());
             int st;
-            cudaMemcpyAsync(c.d_ite, c.h_ite, sizeof(int), cudaMemcpyHostToDevice, c.stream);
-            cudaMemcpyAsync(c.d_eps, c.h_eps, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+            if (graphed)
+            {
+                k_pass_setup<<<1, 128, 0, c.stream>>>(*graphed, c.d_eps, c.d_ite);
+                launched(c, "pass_setup");
+            }
+            else
+            {
+                cudaMemcpyAsync(c.d_ite, c.h_ite, sizeof(int), cudaMemcpyHostToDevice, c.stream);
+                cudaMemcpyAsync(c.d_eps, c.h_eps, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+            }
             cudaMemsetAsync(c.d_flags, 0, F_COUNT * sizeof(int), c.stream);
             k_tag_init<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
-            ++c.n_launches;
+            launched(c, "tag_init");
             for (int k = 1; k < nf; ++k)
             {
                 k_fill<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.detail + k * c.capacity, 0.);
-                ++c.n_launches;
+                launched(c, "fill");
             }
             if ((st = check(c, "tag_init")))
             {
@@ -1840,14 +2029,14 @@ namespace sg
                     k_detail<3><<<blocks_words(c, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
                                                                                     m.ref, m.hc, m.hc2, u, det);
                 }
-                ++c.n_launches;
+                launched(c, "detail");
             }
             for (int k = 0; k < nf && c.rel_detail; ++k)
             {
                 k_absmax_init<<<1, 1, 0, c.stream>>>(c.d_absmax);
                 k_absmax<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_cells, m.d_lo, g.nlev, m.cells, fs[k]->data, c.d_absmax);
                 k_rel_scale<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.d_absmax, c.detail + k * c.capacity);
-                c.n_launches += 3;
+                launched(c, "absmax", 3);
             }
             timer_stop(c, T_DETAIL);
 
@@ -1864,7 +2053,14 @@ namespace sg
                     k_criteria<3><<<blocks_words(c, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
                                                                                                 m.ref, m.hc, c.detail, c.tag, nf, c.capacity);
                 }
-                ++c.n_launches;
+                launched(c, "criteria");
+            }
+            if (c.refine_boundary)
+            {
+                // "refine boundary" (mr/adapt.hpp:341-346), between tag cells and tag finalization
+                k_keep_boundary<<<blocks_words(c, maxl, maxl), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, c.cfg.max_stencil_radius,
+                                                                                   c.tag);
+                launched(c, "keep_boundary");
             }
             timer_stop(c, T_TAG);
 
@@ -1888,7 +2084,7 @@ namespace sg
                     {
                         k_maximum<3><<<blocks_words(c, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
-                    ++c.n_launches;
+                    launched(c, "maximum");
                 }
                 if (l >= lstop)
                 {
@@ -1900,7 +2096,7 @@ namespace sg
                     {
                         k_maximum_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
-                    ++c.n_launches;
+                    launched(c, "maximum_small");
                 }
                 // the levels below hold no operator but still exchange their tags
                 for (int lt = lstop - 1; g.periodic && lt >= 1; --lt)
@@ -1917,13 +2113,50 @@ namespace sg
             timer_start(c, T_MESH_UPDATE);
             // the second pass runs on the device only if the first one refined
             if ((st = new_cells_from_tags(c, m, nm.cells)) || (st = grad_pass(c, nm.cells, F_GRAD0, nullptr))
-                || (st = grad_pass(c, nm.cells, F_GRAD1, c.d_flags + F_GRAD0))
-                || (st = bitmaps_differ(c, nm.cells, m.cells, F_DIFFER)))
+                || (!graphed && (st = grad_pass(c, nm.cells, F_GRAD1, c.d_flags + F_GRAD0))))
+            {
+                return st;
+            }
+            if (graphed)
+            {
+                // make_graduation to its fixed point on the device: further passes while the last one refined
+                // (at most 64, as on the host path)
+                k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_LOOP, c.d_flags + F_GRAD0, 0, 0);
+                k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_ITER, nullptr, 0, 0);
+                launched(c, "adapt_words", 2);
+                st = capture_conditional(
+                    c, cudaGraphCondTypeWhile,
+                    [&](cudaGraphConditionalHandle h)
+                    {
+                        k_cond_set<<<1, 1, 0, c.stream>>>(h, c.d_adapt + A_LOOP, 0);
+                        launched(c, "cond_set");
+                    },
+                    [&](cudaGraphConditionalHandle h)
+                    {
+                        cudaMemsetAsync(c.d_flags + F_GRADX, 0, sizeof(int), c.stream);
+                        int s2 = grad_pass(c, nm.cells, F_GRADX, nullptr);
+                        if (!s2)
+                        {
+                            k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_LOOP, c.d_flags + F_GRADX, 0, 0);
+                            k_loop_next<<<1, 1, 0, c.stream>>>(h, c.d_adapt + A_LOOP, c.d_adapt + A_ITER, 64, c.g.err);
+                            launched(c, "loop_next", 2);
+                        }
+                        return s2;
+                    });
+                if (st)
+                {
+                    return st;
+                }
+            }
+            if ((st = bitmaps_differ(c, nm.cells, m.cells, F_DIFFER)))
             {
                 return st;
             }
             timer_stop(c, T_MESH_UPDATE);
-            cudaMemcpyAsync(c.h_flags, c.d_flags, F_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+            if (!graphed)
+            {
+                cudaMemcpyAsync(c.h_flags, c.d_flags, F_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+            }
             return check(c, "harten front");
         }
 
@@ -2006,6 +2239,28 @@ namespace sg
         return harten_begin_fields(c, {&f}, ite, eps, regularity, relative_detail);
     }
 
+    namespace
+    {
+        // the criteria thresholds of Harten pass ite (mr/adapt.hpp:325-339,
+        // mr/criteria.hpp:20-113): per level eps_l, 2^(reg+dim) eps_l and that
+        // over 2^dim, zero on the levels the pass does not examine
+        void pass_thresholds(const Ctx& c, int ite, double eps, double regularity, double* out)
+        {
+            const int minl = c.cfg.min_level, maxl = c.cfg.max_level, dim = c.g.dim;
+            for (int l = 0; l < 3 * MAXLEV; ++l)
+            {
+                out[l] = 0.;
+            }
+            for (int l = minl; l <= maxl - ite; ++l)
+            {
+                const int exponent     = dim * (maxl - l);
+                out[l]                 = eps / (1 << exponent);
+                out[MAXLEV + l]        = std::pow(2.0, regularity + dim) * out[l];
+                out[2 * MAXLEV + l]    = out[MAXLEV + l] / (1 << dim);
+            }
+        }
+    } // namespace
+
     int harten_begin_fields(Ctx& c, const std::vector<DeviceField*>& fs, int ite, double eps, double regularity, bool relative_detail)
     {
         if (c.cfg.ghost_width != 1)
@@ -2021,27 +2276,19 @@ namespace sg
         // the pinned inputs staged here were consumed by the previous pass,
         // which ended with harten_end's synchronisation
         *c.h_ite = ite;
-        for (int l = 0; l < MAXLEV; ++l)
-        {
-            c.h_eps[l] = c.h_eps[MAXLEV + l] = c.h_eps[2 * MAXLEV + l] = 0.;
-        }
-        for (int l = minl; l <= maxl - ite; ++l)
-        {
-            const int exponent      = dim * (maxl - l);
-            c.h_eps[l]              = eps / (1 << exponent);
-            c.h_eps[MAXLEV + l]     = std::pow(2.0, regularity + dim) * c.h_eps[l];
-            c.h_eps[2 * MAXLEV + l] = c.h_eps[MAXLEV + l] / (1 << dim);
-        }
+        pass_thresholds(c, ite, eps, regularity, c.h_eps);
         // the captured front differs with relative details and with the
         // number of fields: keys of their own
         c.rel_detail = relative_detail;
+        // the keep_boundary launch is part of the captured front only with --refine-boundary
+        const unsigned long long rb = c.refine_boundary ? 256ull : 0ull;
         if (fs.size() == 1)
         {
             DeviceField& f = *fs[0];
-            return run_cached(c, relative_detail ? 4 : 2, static_cast<unsigned long long>(c.cur), ptr_key(f.data), f.has_bc ? bits_of(f.bc_value) : 1ull,
-                              [&]() { return seq_front(c, m, nm, fs); });
+            return run_cached(c, (relative_detail ? 4 : 2) | rb, static_cast<unsigned long long>(c.cur), ptr_key(f.data),
+                              f.has_bc ? bits_of(f.bc_value) : 1ull, [&]() { return seq_front(c, m, nm, fs); });
         }
-        return run_cached(c, relative_detail ? 6 : 5, static_cast<unsigned long long>(c.cur), fields_key(fs, false), fs.size(),
+        return run_cached(c, (relative_detail ? 6 : 5) | rb, static_cast<unsigned long long>(c.cur), fields_key(fs, false), fs.size(),
                           [&]() { return seq_front(c, m, nm, fs); });
     }
 
@@ -2170,11 +2417,161 @@ namespace sg
         return check(c, "update_fields (tape)");
     }
 
+    namespace
+    {
+        // The whole adaptation (Adapt::operator(), mr/adapt.hpp:147-195) as one
+        // captured graph: Harten pass i (at most max_level - min_level of them)
+        // runs under a conditional node that holds while the previous pass
+        // changed the mesh, and its second half (new mesh, update_fields) under
+        // one that holds when this pass changed it; graduation iterates in a
+        // conditional loop.  Pass i works on mesh buffer (cur + i) mod 2 and on
+        // the field buffers that many swaps away, all known when capturing.
+        int seq_adapt(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity)
+        {
+            const int passes = c.cfg.max_level - c.cfg.min_level;
+            std::vector<DeviceField> fa, oa; // the fields as they stand at each pass (buffers swapped per transition)
+            for (DeviceField* f : fs)
+            {
+                fa.push_back(*f);
+            }
+            for (DeviceField* f : os)
+            {
+                oa.push_back(*f);
+            }
+            cudaMemsetAsync(c.d_adapt, 0, A_COUNT * sizeof(int), c.stream);
+            k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_GO, nullptr, 1, 0);
+            launched(c, "adapt_words");
+            int st = SG_OK;
+            for (int i = 0; i < passes && !st; ++i)
+            {
+                const int cur = (c.cur + i) & 1;
+                DeviceMesh& m  = c.mesh[cur];
+                DeviceMesh& nm = c.mesh[1 - cur];
+                std::vector<DeviceField*> fp, op;
+                for (auto& f : fa)
+                {
+                    fp.push_back(&f);
+                }
+                for (auto& f : oa)
+                {
+                    op.push_back(&f);
+                }
+                PassSetup ps{};
+                pass_thresholds(c, i, eps, regularity, ps.eps);
+                ps.ite    = i;
+                auto pass = [&]()
+                {
+                    int s1 = seq_front(c, m, nm, fp, &ps);
+                    if (s1)
+                    {
+                        return s1;
+                    }
+                    k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_PASSES, nullptr, i + 1, 0);
+                    k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_GO, c.d_flags + F_DIFFER, 0, 0);
+                    launched(c, "adapt_words", 2);
+                    return capture_if(c, c.d_flags + F_DIFFER,
+                                      [&]()
+                                      {
+                                          int s2 = seq_back(c, m, nm, fp, op);
+                                          k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_TRANS, nullptr, 1, 1);
+                                          launched(c, "adapt_words");
+                                          return s2;
+                                      });
+                };
+                st = i == 0 ? pass() : capture_if(c, c.d_adapt + A_GO, pass);
+                for (auto* list : {&fa, &oa})
+                {
+                    for (auto& f : *list)
+                    {
+                        std::swap(f.data, f.spare);
+                    }
+                }
+            }
+            if (!st)
+            {
+                cudaMemcpyAsync(c.h_adapt, c.d_adapt, A_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+            }
+            return st ? st : check(c, "adaptation graph");
+        }
+
+        // the adaptation through seq_adapt's graph; false when that path does
+        // not apply (graphs off, timers or the kernel trace on)
+        bool adapt_graphed(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
+                           bool relative_detail, int* n_harten, int* status)
+        {
+            if (!c.graphed_adapt || !c.use_graphs || c.timers.enabled || c.trace.enabled || c.cfg.max_level == c.cfg.min_level)
+            {
+                return false;
+            }
+            if (c.cfg.ghost_width != 1)
+            {
+                c.err   = "harten: only a ghost width of 1 is implemented";
+                *status = SG_ERR_ARG;
+                return true;
+            }
+            c.rel_detail = relative_detail;
+            std::vector<DeviceField*> all(fs);
+            all.insert(all.end(), os.begin(), os.end());
+            const unsigned long long kind = 9ull | (relative_detail ? 16ull : 0ull) | (c.refine_boundary ? 256ull : 0ull)
+                                            | (static_cast<unsigned long long>(fs.size()) << 20);
+            const unsigned long long thr = bits_of(eps) * 0x9E3779B97F4A7C15ull ^ bits_of(regularity);
+            int st = run_cached(c, kind, static_cast<unsigned long long>(c.cur), fields_key(all, false) ^ (fields_key(all, true) << 1), thr,
+                                [&]() { return seq_adapt(c, fs, os, eps, regularity); });
+            if (!st && cudaStreamSynchronize(c.stream) != cudaSuccess)
+            {
+                st = check(c, "adaptation sync");
+            }
+            if (st)
+            {
+                *status = st;
+                return true;
+            }
+            const int passes = c.h_adapt[A_PASSES], trans = c.h_adapt[A_TRANS];
+            for (int t = 0; t < trans; ++t)
+            {
+                for (DeviceField* f : all)
+                {
+                    std::swap(f->data, f->spare);
+                }
+                c.cur = 1 - c.cur;
+                ++c.mesh_version;
+            }
+            if (trans > 0)
+            {
+                c.mesh[0].host_valid = c.mesh[1].host_valid = false;
+            }
+            // the last pass's ghost update ran on the final mesh when that pass kept it
+            for (DeviceField* f : all)
+            {
+                f->ghosts_valid = false;
+            }
+            if (passes > trans)
+            {
+                for (DeviceField* f : fs)
+                {
+                    f->ghosts_valid  = true;
+                    f->ghost_version = c.mesh_version;
+                }
+            }
+            if (n_harten)
+            {
+                *n_harten = passes;
+            }
+            *status = device_error(c);
+            return true;
+        }
+    } // namespace
+
     // Adapt<Fields...>::operator()(mra_config, other_fields...) (mr/adapt.hpp:147-195)
     int adapt_fields(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
                      bool relative_detail, int* n_harten)
     {
         ScopedTimer timer(c, T_ADAPT);
+        int gst = SG_OK;
+        if (adapt_graphed(c, fs, os, eps, regularity, relative_detail, n_harten, &gst))
+        {
+            return gst;
+        }
         const int minl = c.cfg.min_level, maxl = c.cfg.max_level;
         int it         = 0;
         for (int i = 0; minl != maxl && i < maxl - minl; ++i)
@@ -2206,6 +2603,11 @@ namespace sg
     int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten, bool relative_detail)
     {
         ScopedTimer timer(c, T_ADAPT);
+        int gst = SG_OK;
+        if (adapt_graphed(c, {&f}, {}, eps, regularity, relative_detail, n_harten, &gst))
+        {
+            return gst;
+        }
         const int minl = c.cfg.min_level, maxl = c.cfg.max_level;
         int it         = 0;
         if (minl != maxl)
@@ -2267,7 +2669,7 @@ namespace sg
         {
             k_upwind<3><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p);
         }
-        ++c.n_launches;
+        launched(c, scheme == 2 ? "convection" : "upwind");
         return check(c, "upwind");
     }
 } // namespace sg

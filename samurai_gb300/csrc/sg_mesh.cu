@@ -6,28 +6,78 @@
 // one level, coarser operands are refined, .on(l) coarsens to the parent of
 // any member (subset/projection.hpp:68-177).  On bitmaps these are word-wise
 // AND/OR/ANDNOT, bit-pair compression (coarsen) and bit spreading (refine).
+#include <nvtx3/nvToolsExt.h>
+
 #include "sg_ctx.cuh"
 
 namespace sg
 {
-    namespace
+    cudaEvent_t take_event(Ctx& c)
     {
-        cudaEvent_t take_event(Ctx& c)
+        if (!c.timers.pool.empty())
         {
-            if (!c.timers.pool.empty())
-            {
-                cudaEvent_t e = c.timers.pool.back();
-                c.timers.pool.pop_back();
-                return e;
-            }
-            cudaEvent_t e = nullptr;
-            cudaEventCreate(&e);
+            cudaEvent_t e = c.timers.pool.back();
+            c.timers.pool.pop_back();
             return e;
         }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+
+    void give_event(Ctx& c, cudaEvent_t e)
+    {
+        if (e)
+        {
+            c.timers.pool.push_back(e);
+        }
+    }
+
+    void clear_graphs(Ctx& c)
+    {
+        for (auto& ge : c.graphs)
+        {
+            cudaGraphExecDestroy(ge.exec);
+            for (const auto& mk : ge.marks)
+            {
+                bool in_window = false;
+                for (const auto& tm : c.trace.marks)
+                {
+                    in_window = in_window || tm.second == mk.second;
+                }
+                if (!in_window)
+                {
+                    give_event(c, mk.second);
+                }
+            }
+        }
+        c.graphs.clear();
+    }
+
+    void launched(Ctx& c, const char* name, int count)
+    {
+        c.n_launches += count;
+        if (c.trace.enabled)
+        {
+            // external: inside a stream capture the record becomes an event-record node of the graph (a plain
+            // record would only order the capture)
+            cudaEvent_t e = take_event(c);
+            cudaEventRecordWithFlags(e, c.stream, cudaEventRecordExternal);
+            c.trace.marks.push_back({name, e});
+        }
+    }
+
+    namespace
+    {
+        // samurai's timer names (timers.hpp:111-1036) as NVTX ranges, so that a
+        // profiler's timeline shows the phases under the reference's names
+        const char* const TIMER_NAMES[T_COUNT] = {"mesh adaptation",  "ghost update",    "detail computation", "tag cells",     "tag finalization",
+                                                  "mesh update",      "make_graduation", "mesh construction",  "fields update", "field expressions"};
     } // namespace
 
     void timer_start(Ctx& c, int id)
     {
+        nvtxRangePushA(TIMER_NAMES[id]);
         if (!c.timers.enabled)
         {
             return;
@@ -39,6 +89,7 @@ namespace sg
 
     void timer_stop(Ctx& c, int id)
     {
+        nvtxRangePop();
         if (!c.timers.enabled || !c.timers.pending[id])
         {
             return;
@@ -147,7 +198,7 @@ namespace sg
                 if (l >= l_last)
                 {
                     k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, l_last, f, c.guard);
-                    ++c.n_launches;
+                    launched(c, what);
                     st = check(c, what);
                 }
             }
@@ -158,7 +209,7 @@ namespace sg
                 {
                     const int e = l_last < ft ? l_last : ft;
                     k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, e, f, c.guard);
-                    ++c.n_launches;
+                    launched(c, what);
                     if ((st = check(c, what)))
                     {
                         return st;
@@ -185,7 +236,7 @@ namespace sg
             }
             const long long n = c.g.lv[l1].woff + c.g.lv[l1].nwords - c.g.lv[l0].woff;
             k_words<<<grid_for(n, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.d_geom, l0, l1, f, c.guard);
-            ++c.n_launches;
+            launched(c, what);
             return check(c, what);
         }
 
@@ -368,10 +419,12 @@ namespace sg
         const long long n  = c.g.total_words;
         const long long nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
         k_scan_sums<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(m.ref, m.cells, n, nb, c.block_sums);
+        launched(c, "scan_sums");
         k_scan_top<<<1, 1024, 0, c.stream>>>(c.block_sums, nb, m.d_lo, c.g.nlev);
+        launched(c, "scan_top");
         k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(c.d_geom, m.ref, m.cells, n, nb, c.block_sums, m.rank, m.wl_ref, m.wl_cells,
                                                                           m.d_lo);
-        c.n_launches += 3;
+        launched(c, "scan_write");
         cudaMemcpyAsync(m.h_lo, m.d_lo, COUNTS * sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
         m.host_valid = false;
         return check(c, "scan_rank");
@@ -440,12 +493,23 @@ namespace sg
         const int t1lo = std::max(minl - 1, 0), t1hi = maxl - 1; // t1 is read on these levels only
         uint32_t* t0   = c.t0;
         uint32_t* cxy  = (g.dim == 2) ? cag : t0;
+        // union cells (construct_union, mesh.hpp:1231-1262): union[l] =
+        // (cells[l+1] | union[l+1]).on(l) for levels max-1 .. 0, i.e. every
+        // cell with a leaf among its descendants: the same launch marks the
+        // ancestors of each word of hc = cells[l+1].on(l) into the zeroed union
+        // bitmap (union[max] stays zero)
+        cudaMemsetAsync(uni, 0, bytes, c.stream);
         st = launch_words(c, std::min(hlo, minl), maxl,
                           [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                           {
                               if (l >= hlo && l <= hhi)
                               {
-                                  hc[w] = coarsen_word(g, cells, l, row, wi);
+                                  const uint32_t h = coarsen_word(g, cells, l, row, wi);
+                                  hc[w]            = h;
+                                  if (h && (atomicOr(uni + w, h) & h) != h)
+                                  {
+                                      mark_ancestors(g, uni, l, row, wi, h, 0);
+                                  }
                               }
                               if (l >= minl)
                               {
@@ -503,19 +567,6 @@ namespace sg
             return st;
         }
 
-        // union cells, top-down: union[l] = (cells[l+1] | union[l+1]).on(l) on
-        // levels max-1 .. 0; union[max] is never written and stays zero
-        if (maxl >= 1)
-        {
-            st = launch_chain(c, maxl - 1, 0,
-                              [=] __device__(const Geom& g, int ll, long long w, long long row, int wi)
-                              { uni[w] = hc[w] | coarsen_word(g, uni, ll, row, wi); },
-                              "union");
-            if (st)
-            {
-                return st;
-            }
-        }
 
         if (!multi)
         {
@@ -541,6 +592,10 @@ namespace sg
         // expanded domain, and cells[l+2].on(l) expanded by p
         // the reference starts at level min-2: cag (min .. max), t1 (min-1 ..
         // max-1) and hc2 (min-2 .. max-2)
+        // the reference before the children of the projection cells (ref0) goes
+        // to a scratch bitmap (the refine flags of the adaptation, free here)
+        // in the non-periodic case: the pass below reads it while it writes ref
+        uint32_t* ref0 = g.periodic ? ref : c.rf;
         if (g.dim == 2)
         {
             st = launch_words(c, lmin, maxl,
@@ -555,7 +610,7 @@ namespace sg
                                   {
                                       v |= dilate_xy_word(g, hc2, l, row, wi, p);
                                   }
-                                  ref[w] = v;
+                                  ref0[w] = v;
                               },
                               "ref0");
         }
@@ -585,7 +640,7 @@ namespace sg
                                       {
                                           v |= dilate_z_word(g, t3, l, row, wi, p);
                                       }
-                                      ref[w] = v;
+                                      ref0[w] = v;
                                   },
                                   "ref0_z");
             }
@@ -653,6 +708,43 @@ namespace sg
         // reference[l+1] |= (reference[l] & union[l]) refined; the reference
         // starts at min_level - 2, so the first level with a source is above it
         const int ref_lo = std::max(1, std::max(c.cfg.min_level - 2, 0) + 1);
+        if (!g.periodic && maxl >= ref_lo)
+        {
+            // In one pass instead of level by level: the parent of a union cell
+            // is a union cell, so a cell whose parent p is in the union joins the
+            // reference exactly when p or one of p's ancestors (down to the
+            // reference's first level) is in ref0; and proj = reference & union.
+            // Each word reads its parent word's ancestors in ref0 directly.
+            const uint32_t* r0 = ref0;
+            const int rlo      = ref_lo;
+            st                 = launch_words(c, ref_lo - 1, maxl,
+                                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                              {
+                                                  uint32_t v = r0[w];
+                                                  if (l >= rlo)
+                                                  {
+                                                      const ParentWord pw = parent_word(g, l, row, wi);
+                                                      if (pw.ok)
+                                                      {
+                                                          const LevelGeom& C = g.lv[l - 1];
+                                                          const uint32_t pc  = self_or_ancestor(g, r0, l - 1, pw.row, pw.wi, rlo - 1)
+                                                                              & uni[C.woff + pw.row * C.W + pw.wi];
+                                                          v |= spread16(pc >> pw.shift);
+                                                      }
+                                                  }
+                                                  ref[w] = v;
+                                                  if (l < g.max_level)
+                                                  {
+                                                      proj[w] = v & uni[w];
+                                                  }
+                                              },
+                                              "ref_children");
+            if (st)
+            {
+                return st;
+            }
+            return scan_rank(c, m);
+        }
         if (maxl >= ref_lo)
         {
             st = launch_chain(c, ref_lo, maxl,
@@ -754,7 +846,7 @@ namespace sg
     {
         const Geom g = c.g;
         k_tag_flags<<<grid_for(g.total_words, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.d_geom, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
-        ++c.n_launches;
+        launched(c, "tag_flags");
         int st = check(c, "tag_flags");
         if (st)
         {
@@ -815,6 +907,29 @@ namespace sg
     // that finds nothing leaves the cells unchanged, so extra passes after the
     // fixed point are no-ops.  The contiguous-boundary pass
     // (graduation.hpp:121-249) is a no-op for a max_stencil_radius of 1.
+    namespace
+    {
+        // refine the cells flagged in rr (levels dlo .. dtop): levels dlo .. dtop + 1 change
+        int grad_apply(Ctx& c, uint32_t* nc, const uint32_t* rr, int dlo, int dtop)
+        {
+            return launch_words(c, dlo, dtop + 1,
+                                [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                {
+                                    const uint32_t r = l <= dtop ? rr[w] : 0u;
+                                    uint32_t v       = nc[w] & ~r;
+                                    if (l - 1 >= dlo)
+                                    {
+                                        v |= refine_word(g, rr, l, row, wi);
+                                    }
+                                    if (v != nc[w])
+                                    {
+                                        nc[w] = v;
+                                    }
+                                },
+                                "grad_apply");
+        }
+    } // namespace
+
     int grad_pass(Ctx& c, uint32_t* nc, int slot, const int* guard)
     {
         // every launch of the pass is skipped on the device when *guard == 0
@@ -862,6 +977,73 @@ namespace sg
         if (st)
         {
             return st;
+        }
+        if (!g.periodic)
+        {
+            // d[l] = (ec1[l+1] | d[l+1]).on(l) on levels max-2 .. min_level is
+            // the set of the cells with a cell of ec1 among their descendants:
+            // the expansion marks the ancestors of each ec1 word into the zeroed
+            // d (levels min_level .. max-2), and rr = nc & d follows in one pass
+            const size_t off   = static_cast<size_t>(g.lv[dlo].woff);
+            const size_t words = static_cast<size_t>(g.lv[dtop].woff + g.lv[dtop].nwords) - off;
+            cudaMemsetAsync(d + off, 0, words * 4, c.stream);
+            auto mark = [=] __device__(const Geom& g, int l, long long w, long long row, int wi, uint32_t e)
+            {
+                ec1[w] = e;
+                if (e)
+                {
+                    const ParentWord pw = parent_word(g, l, row, wi);
+                    if (pw.ok)
+                    {
+                        const LevelGeom& C  = g.lv[l - 1];
+                        const uint32_t bits = (compress_pairs(e, 0u) & 0xFFFFu) << pw.shift;
+                        if (bits && (atomicOr(d + C.woff + pw.row * C.W + pw.wi, bits) & bits) != bits)
+                        {
+                            mark_ancestors(g, d, l - 1, pw.row, pw.wi, bits, dlo);
+                        }
+                    }
+                }
+            };
+            if (g.dim == 2)
+            {
+                st = launch_words(c, elo, ehi,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                  { mark(g, l, w, row, wi, dilate_xy_word(g, hcn, l, row, wi, gw)); },
+                                  "grad_expand");
+            }
+            else
+            {
+                // xy part into rr (written again below), then z with the marking
+                st = launch_words(c, elo, ehi,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi) { rr[w] = dilate_xy_word(g, hcn, l, row, wi, gw); },
+                                  "grad_expand_xy");
+                if (!st)
+                {
+                    st = launch_words(c, elo, ehi,
+                                      [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                      { mark(g, l, w, row, wi, dilate_z_word(g, rr, l, row, wi, gw)); },
+                                      "grad_expand_z");
+                }
+            }
+            if (!st)
+            {
+                st = launch_words(c, dlo, dtop,
+                                  [=] __device__(const Geom&, int, long long w, long long, int)
+                                  {
+                                      const uint32_t rv = nc[w] & d[w];
+                                      rr[w]             = rv;
+                                      if (rv)
+                                      {
+                                          atomicOr(flag, 1);
+                                      }
+                                  },
+                                  "grad_refine");
+            }
+            if (st)
+            {
+                return st;
+            }
+            return grad_apply(c, nc, rr, dlo, dtop);
         }
         if (g.dim == 2)
         {
@@ -923,22 +1105,7 @@ namespace sg
         {
             return st;
         }
-        // refine the flagged cells: levels min_level .. max_level-1 change
-        return launch_words(c, dlo, dtop + 1,
-                            [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
-                            {
-                                const uint32_t r = l <= dtop ? rr[w] : 0u;
-                                uint32_t v       = nc[w] & ~r;
-                                if (l - 1 >= dlo)
-                                {
-                                    v |= refine_word(g, rr, l, row, wi);
-                                }
-                                if (v != nc[w])
-                                {
-                                    nc[w] = v;
-                                }
-                            },
-                            "grad_apply");
+        return grad_apply(c, nc, rr, dlo, dtop);
     }
 
     // make_graduation to the fixed point, with a host test after each pass

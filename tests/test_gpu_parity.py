@@ -97,12 +97,13 @@ def test_golden_replay(sg, pred):
 
 @pytest.mark.parametrize("scheme", [0, 1])
 def test_readme_demo(sg, scheme):
-    """README demo: min 2, max 8, square of side 0.2, eps 1e-4, regularity 2,
-    dt = 0.5 dx; 12 of its 50 iterations, both upwind forms."""
+    """README demo (README.md:88-155): min 2, max 8, square of side 0.2, eps
+    1e-4, regularity 2, dt = 0.5 dx; all 50 iterations, both upwind forms
+    (the upwind operator and the README's lambda)."""
     g, o = pair(sg, 2, 2, 8)
     init_both(g, o, readme_square)
     dt = 0.5 / (1 << 8)
-    for it in range(12):
+    for it in range(50):
         o.adapt(1e-4, 2.0)
         g.adapt(1e-4, 2.0)
         compare_cells(g, o, "it %d adapt" % it)
@@ -420,3 +421,71 @@ def test_mesh_destroyed_before_its_fields(sg):
     init_both(g, o, disc)
     assert g.adapt(1e-3, 1.0) == o.adapt(1e-3, 1.0)
     compare_cells(g, o, "after the out-of-order destruction")
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_refine_boundary(sg, dim):
+    """--refine-boundary (keep_boundary_refined, mr/adapt.hpp:245-274): the
+    boundary leaves of max_level are tagged keep in every pass; meshes, tags
+    and values bit-identical to the oracle through the adaptation and steps"""
+    minl, maxl = (3, 8) if dim == 2 else (2, 5)
+    g, o = pair(sg, dim, minl, maxl)
+    g.mesh.set_refine_boundary(True)
+    o.set_refine_boundary(True)
+    init_both(g, o, shapes_2d(17, 6, 6) if dim == 2 else ball_3d(9))
+    a = [1.0, -0.5] if dim == 2 else [1.0, -0.5, 0.25]
+    dt = 0.25 / (1 << maxl)
+    assert g.adapt(1e-3, 1.0) == o.adapt(1e-3, 1.0)
+    for it in range(4):
+        compare_cells(g, o, "it %d" % it)
+        compare_fields(g, o, "it %d" % it, cells_only=True)
+        g.update_ghost()
+        o.update_ghost()
+        g.upwind(a, dt)
+        o.upwind(a, dt)
+        assert g.adapt(1e-3, 1.0) == o.adapt(1e-3, 1.0)
+    compare_meshes(g, o, maxl, "refine boundary")
+    compare_cells(g, o, "final")
+    compare_fields(g, o, "final", cells_only=True)
+    for ite in range(maxl - minl):
+        ro, rg = o.harten(ite, 1e-3, 1.0), g.harten(ite, 1e-3, 1.0)
+        assert ro == rg
+        if ro:
+            assert np.array_equal(o.tag(), g.tag()), "tags of the converged pass"
+            break
+
+
+def test_mesh_beyond_device_memory_is_refused(sg):
+    """3D max_level 12: the dense level slabs of the mesh and of one field need
+    about 0.9 TB, more than the device holds: SG_ERR_CAPACITY (status 3) with
+    the sizes, before any allocation"""
+    with pytest.raises(sg.SamuraiGpuError, match=r"status 3\).*GB of device memory"):
+        sg.MRMesh(3, 3, 12)
+    # the device is still usable
+    m = sg.MRMesh(2, 2, 5)
+    assert m.nb_cells("cells") == 32 * 32
+
+
+@pytest.mark.parametrize("dim,minl,maxl", [(2, 2, 9), (3, 2, 6)])
+def test_adaptation_graph_matches_pass_by_pass(sg, dim, minl, maxl):
+    """the adaptation as one graph with device-side conditions (the default)
+    and pass by pass with host tests give identical meshes, values and pass
+    counts, from a uniform start (many passes, graduation loops) and along steps"""
+    a_graph = sg.AdvectionSim(dim, minl, maxl)
+    a_pass = sg.AdvectionSim(dim, minl, maxl)
+    a_pass.mesh.set_adapt_graph(False)
+    lv, co, _ = a_graph.cells()
+    f = shapes_2d(23, 8, 8) if dim == 2 else ball_3d(11)
+    for s in (a_graph, a_pass):
+        s.set_cell_values(f(lv, co))
+    vel = [1.0, -0.75] if dim == 2 else [1.0, -0.75, 0.5]
+    dt = 0.3 / (1 << maxl)
+    for it in range(6):
+        assert a_graph.adapt(1e-4, 2.0) == a_pass.adapt(1e-4, 2.0), "it %d: Harten passes" % it
+        lg, cg, ig = a_graph.cells()
+        lp, cp, ip = a_pass.cells()
+        assert np.array_equal(lg, lp) and np.array_equal(cg, cp) and np.array_equal(ig, ip), "it %d: cells" % it
+        assert np.array_equal(a_graph.field(), a_pass.field()), "it %d: field with ghosts" % it
+        for s in (a_graph, a_pass):
+            s.update_ghost()
+            s.upwind(vel, dt)
