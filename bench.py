@@ -320,11 +320,16 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
 
     def step():
-        passes = sim.adapt(CFG["eps"], CFG["regularity"])
-        sim.update_ghost()
-        sim.upwind(a, dt)
-        return passes
+        # MRadaptation, update_ghost_mr, upwind, swap: sg_step, one captured graph per step
+        return sim.step(CFG["eps"], CFG["regularity"], a, dt)
 
+    # the launch-shape autotuner on this problem (the timed steps below use its choice)
+    tune = None
+    if not args.no_tune:
+        d_ms, t_ms, shape = sim.autotune(CFG["eps"], CFG["regularity"], a, dt, steps=10)
+        tune = {"default_ms_per_step": d_ms, "tuned_ms_per_step": t_ms, "shape": shape,
+                "how": "sg_autotune: coordinate descent over threads per block, grid limit and one-block chain limits, "
+                       "10 steps from the same state per candidate, best of two"}
     for _ in range(args.warmup):
         step()
     sim.mesh.synchronize()
@@ -360,6 +365,11 @@ def run_gpu(args):
     ms = total_ms / args.steps
     total_ms_max, cell_updates_all = reduce_over_ranks(total_ms, cell_updates, world, device="cuda")
     value = cell_updates_all / (total_ms_max / 1e3)
+    if args.quick:
+        # profiling runs: the timed steps only
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": total_ms_max / args.steps, "quick": True}))
+        return
 
     # ---- end-to-end through the C ABI with host buffers
     cap = sim.mesh.nb_cells("reference") * 4 + 1024
@@ -487,7 +497,7 @@ def run_gpu(args):
             "config": workload_config({"parallelism": "replicas" if world > 1 else "single GPU",
                                        "cells_final": int(nc), "reference_cells_final": int(sim.nb_ref())}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d / e2e_steps), "d2h_bytes_per_step": int(d2h / e2e_steps),
-                    "steps": e2e_steps, "api": "sg_field_upload + sg_adapt + sg_update_ghost_mr + sg_upwind + sg_field_swap + sg_field_download"},
+                    "steps": e2e_steps, "api": "sg_field_upload + sg_step (MRadaptation, update_ghost_mr, upwind, swap) + sg_field_download"},
             "roofline": roofline,
             "roofline_step": roofline_step,
             "kernels_step": ktab,
@@ -509,6 +519,7 @@ def run_gpu(args):
             "phases_ms_per_step": phases,
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "autotune": tune,
             "adjoint": extras.get("adjoint"),
             "batch": extras.get("batch"),
         }
@@ -875,6 +886,8 @@ def main():
     p.add_argument("--impl", default="gb300")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch sub-records of the default run")
+    p.add_argument("--no-tune", action="store_true", help="time the default launch shape (no sg_autotune)")
+    p.add_argument("--quick", action="store_true", help="profiling runs: warm-up and timed steps only, a short line")
     p.add_argument("--workload", default="advection2d", choices=["advection2d", "advection3d", "batch", "adjoint"],
                    help="advection2d: the max_level-12 2D problem (default); batch: independent problems through sg_batch_step; "
                         "adjoint: the discrete adjoint of a max_level-10 loop")

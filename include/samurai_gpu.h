@@ -109,6 +109,20 @@ int sg_mesh_set_refine_boundary(sg_mesh_t mesh, int enable);
  * results; the named timers and the kernel trace use the pass-by-pass path while they are on. */
 int sg_mesh_set_adapt_graph(sg_mesh_t mesh, int enable);
 
+/* Without a samurai counterpart: the launch-shape autotuner.  Times sg_step(u, unp1, eps, regularity, a, dt, scheme)
+ * over `steps` steps from the problem's current state under candidate launch shapes (threads per block of the FP64
+ * list kernels, grid limit of the word launches, level sizes up to which the ghost-update and tag-finalisation
+ * chains run in one block), keeps the fastest on the mesh and caches it for this device and level range (later
+ * meshes start from it; SG_TUNE_FILE names a file that keeps the cache across processes; the SG_BLOCK,
+ * SG_MAX_BLOCKS, SG_FUSE_WORDS* environment variables override it).  The problem is left in the state it had.
+ * default_ms / tuned_ms receive the step time under the starting and the chosen shape. */
+int sg_autotune(sg_field_t u, sg_field_t unp1, double eps, double regularity, const double* a, double dt, int scheme, int steps,
+                double* default_ms, double* tuned_ms);
+/* the mesh's launch shape: threads per block, grid limit (blocks of 8 warps), one-block chain limits in words per
+ * level of the mesh, field and tag-finalisation chains */
+int sg_launch_shape(sg_mesh_t mesh, int* block, long long* max_blocks, long long* fuse_mesh_words, long long* fuse_field_words,
+                    long long* fuse_max_words);
+
 /* samurai's named timers (timers.hpp:111-1036, printed with --timers): CUDA-event timers per phase.
  * ids: 0 mesh adaptation, 1 ghost update, 2 detail computation, 3 tag cells, 4 tag finalization,
  * 5 mesh update, 6 make_graduation, 7 mesh construction, 8 fields update, 9 field expressions (upwind). */
@@ -170,6 +184,11 @@ int sg_update_ghost_mr_fields(int n, const sg_field_t* fields);
 int sg_update_ghost_mr(sg_field_t u);
 /* unp1 = u - dt * samurai::upwind(a, u) on mesh[cells] (a has dim entries), or one of the other schemes above */
 int sg_upwind(sg_field_t u, sg_field_t unp1, const double* a, double dt, int scheme);
+/* One iteration of the demo's time loop (demos/FiniteVolume/advection_2d.cpp:140-147): MRadaptation(eps, regularity),
+   samurai::update_ghost_mr(u), unp1 = u - dt * scheme(a, u), std::swap(u.array(), unp1.array()).  The same results as
+   the four calls; the whole step is one captured CUDA graph (passes and buffers decided on the device) with one host
+   synchronisation.  n_harten receives the adaptation's Harten passes. */
+int sg_step(sg_field_t u, sg_field_t unp1, double eps, double regularity, const double* a, double dt, int scheme, int* n_harten);
 /* detail and tag fields of the last Harten pass, reference numbering (n = nb_reference) */
 int sg_detail_download(sg_field_t u, double* values, long long n);
 int sg_tag_download(sg_field_t u, unsigned char* values, long long n);

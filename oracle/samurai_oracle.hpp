@@ -1664,9 +1664,9 @@ namespace oracle
     template <std::size_t D>
     int make_graduation(std::vector<LSet<D>>& ca, int grad_width, int max_stencil_radius, const MeshConfig* periodic_cfg = nullptr)
     {
-        if (max_stencil_radius != 1)
+        if (max_stencil_radius != 1 && max_stencil_radius != 2)
         {
-            throw std::runtime_error("oracle: graduation implemented for max_stencil_radius == 1");
+            throw std::runtime_error("oracle: graduation implemented for max_stencil_radius 1 and 2");
         }
         int nit = 0;
         bool changed = true;
@@ -1714,6 +1714,38 @@ namespace oracle
                             break;
                         }
                         proj = on(proj, cl - 1);
+                    }
+                }
+            }
+            // list_interval_to_refine_for_contiguous_boundary_cells (graduation.hpp:370-497), radius 2: with
+            // n = max(r, 2 (r - 2)) = 2 contiguous boundary cells, in each non-periodic Cartesian direction t, the
+            // cells of level L - 1 that hold a boundary cell of level L (a cell outside the domain translated by -t)
+            // translated by -2 t are refined, for L from the finest non-empty level down to the coarsest plus one;
+            // the jump to L + 1 (radius > 2) does not apply
+            if (max_stencil_radius == 2 && maxl >= 0)
+            {
+                for (int d = 0; d < static_cast<int>(D); ++d)
+                {
+                    if (periodic_cfg && periodic_cfg->periodic[d])
+                    {
+                        continue;
+                    }
+                    for (int sgn = 1; sgn >= -1; sgn -= 2)
+                    {
+                        Coord<D> t{};
+                        t[d] = sgn;
+                        for (int level = maxl; level != minl; --level)
+                        {
+                            LSet<D> dom(level);
+                            dom = box_set<D>(level, 0, 1 << level);
+                            auto bcells = on(diff(ca[level], translate(dom, scale<D>(t, -1))), level);
+                            auto tb     = translate(bcells, scale<D>(t, -2));
+                            auto sub    = on(inter(tb, ca[level - 1]), level - 1);
+                            if (!sub.empty())
+                            {
+                                R[level - 1] = uni(R[level - 1], sub);
+                            }
+                        }
                     }
                 }
             }

@@ -92,6 +92,9 @@ def lib():
         "sg_update_ghost_mr_fields": (i, [i, vp]),
         "sg_update_ghost_mr": (i, [vp]),
         "sg_upwind": (i, [vp, vp, vp, d, i]),
+        "sg_step": (i, [vp, vp, d, d, vp, d, i, pi]),
+        "sg_autotune": (i, [vp, vp, d, d, vp, d, i, i, ctypes.POINTER(d), ctypes.POINTER(d)]),
+        "sg_launch_shape": (i, [vp, pi, pl, pl, pl, pl]),
         "sg_detail_download": (i, [vp, vp, ll]),
         "sg_tag_download": (i, [vp, vp, ll]),
         "sg_batch_create": (i, [i, vp, vp, i, ctypes.POINTER(vp)]),
@@ -372,6 +375,13 @@ class MRMesh:
             _check(lib().sg_timers_get(self.h, k, ctypes.byref(ms), ctypes.byref(n)), "sg_timers_get")
             out[name] = (ms.value, n.value)
         return out
+
+    def launch_shape(self):
+        """{block, max_blocks, fuse_mesh_words, fuse_field_words, fuse_max_words} of this mesh's launches"""
+        b, mb, fm, ff, fx = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        _check(lib().sg_launch_shape(self.h, ctypes.byref(b), ctypes.byref(mb), ctypes.byref(fm), ctypes.byref(ff), ctypes.byref(fx)),
+               "sg_launch_shape")
+        return {"block": b.value, "max_blocks": mb.value, "fuse_mesh_words": fm.value, "fuse_field_words": ff.value, "fuse_max_words": fx.value}
 
     def set_adapt_graph(self, enable):
         """each adaptation as one captured graph (True, the default) or pass by pass (False)"""
@@ -819,6 +829,23 @@ class AdvectionSim:
     def upwind(self, a, dt, scheme=UPWIND_OP):
         self.unp1.assign_upwind(self.u, a, dt, scheme)
         swap(self.u, self.unp1)
+
+    def step(self, eps, regularity, a, dt, scheme=UPWIND_OP):
+        """adapt, update_ghost, upwind and swap as one call (sg_step); returns the Harten passes"""
+        av = np.zeros(3, np.float64)
+        av[: self.dim] = np.asarray(a, np.float64)[: self.dim]
+        n = ctypes.c_int()
+        _check(lib().sg_step(self.u.h, self.unp1.h, float(eps), float(regularity), _ptr(av), float(dt), int(scheme), ctypes.byref(n)), "sg_step")
+        return n.value
+
+    def autotune(self, eps, regularity, a, dt, steps=10, scheme=UPWIND_OP):
+        """sg_autotune: (step ms with the starting launch shape, with the chosen one, the chosen shape)"""
+        av = np.zeros(3, np.float64)
+        av[: self.dim] = np.asarray(a, np.float64)[: self.dim]
+        d0, d1 = ctypes.c_double(), ctypes.c_double()
+        _check(lib().sg_autotune(self.u.h, self.unp1.h, float(eps), float(regularity), _ptr(av), float(dt), int(scheme), int(steps),
+                                 ctypes.byref(d0), ctypes.byref(d1)), "sg_autotune")
+        return d0.value, d1.value, self.mesh.launch_shape()
 
     def intervals(self, mesh_id, level):
         return self.mesh.intervals(mesh_id, level)

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsamurai_gpu.so")
-SOURCES = ["sg_mesh.cu", "sg_field.cu", "sg_capi.cu", "sg_noalloc.cu", "sg_batch.cu", "sg_adjoint.cu", "sg_vector.cu", "sg_io.cu"]
+SOURCES = ["sg_mesh.cu", "sg_field.cu", "sg_capi.cu", "sg_noalloc.cu", "sg_batch.cu", "sg_adjoint.cu", "sg_vector.cu", "sg_io.cu", "sg_tune.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC,-O2", "-Xptxas", "-O3"]

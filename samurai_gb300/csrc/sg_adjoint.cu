@@ -36,6 +36,7 @@
 namespace sg
 {
     int ensure_spare(Ctx& c, DeviceField& f);
+    bool step_graph_applies(const Ctx& c);
 
     namespace
     {
@@ -261,7 +262,9 @@ struct sg_adjoint_s
         int mesh0;   // index in bits of the mesh at the start of the step
         int n_trans; // meshes bits[mesh0+1 .. mesh0+n_trans] visited by the adaptation
     };
-    std::vector<uint32_t*> bits; // leaf bitmaps, device
+    std::vector<uint32_t*> bits;       // leaf bitmaps, device
+    std::vector<uint32_t*> spare_bits; // bitmaps of earlier recordings, reused before allocating
+    uint32_t* rec_slots = nullptr;     // where the step graph leaves the meshes of a step's transitions
     std::vector<Step> steps;
     double a[3] = {0., 0., 0.};
     double dt = 0., eps = 0., reg = 0.;
@@ -362,18 +365,40 @@ namespace
         return st;
     }
 
-    int push_current_bits(sg_adjoint_t adj)
+    // a bitmap for the mesh sequence: one of an earlier recording's, or a new allocation
+    int take_bits(sg_adjoint_t adj, uint32_t** out)
     {
-        Ctx& c      = ctx_of(adj);
-        uint32_t* b = nullptr;
-        if (dmalloc(&b, static_cast<size_t>(c.g.total_words)))
+        Ctx& c = ctx_of(adj);
+        if (!adj->spare_bits.empty())
+        {
+            *out = adj->spare_bits.back();
+            adj->spare_bits.pop_back();
+            return SG_OK;
+        }
+        if (dmalloc(out, static_cast<size_t>(c.g.total_words)))
         {
             c.err = "adjoint: out of device memory for the mesh sequence";
             return SG_ERR_CUDA;
         }
-        cudaMemcpyAsync(b, c.m().cells, bitmap_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+        return SG_OK;
+    }
+
+    int push_bits_from(sg_adjoint_t adj, const uint32_t* src)
+    {
+        Ctx& c      = ctx_of(adj);
+        uint32_t* b = nullptr;
+        if (int st = take_bits(adj, &b))
+        {
+            return st;
+        }
+        cudaMemcpyAsync(b, src, bitmap_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
         adj->bits.push_back(b);
         return SG_OK;
+    }
+
+    int push_current_bits(sg_adjoint_t adj)
+    {
+        return push_bits_from(adj, ctx_of(adj).m().cells);
     }
 
     // leaf cells of the current mesh: levels, coordinates and dense elements
@@ -466,9 +491,10 @@ namespace
 
     void free_recording(sg_adjoint_t adj)
     {
+        // the bitmaps go back to the pool of the next recording (no allocation or free per transition)
         for (size_t k = 1; k < adj->bits.size(); ++k)
         {
-            dfree(adj->bits[k]);
+            adj->spare_bits.push_back(adj->bits[k]);
         }
         if (!adj->bits.empty())
         {
@@ -739,6 +765,10 @@ extern "C"
         {
             return afail(SG_ERR_ARG, "sg_adjoint_create: the adjoint is not available on a mesh with a periodic axis");
         }
+        if (cfg.ghost_width != 1)
+        {
+            return afail(SG_ERR_ARG, "sg_adjoint_create: the adjoint covers a ghost width of 1 (max_stencil_radius 1)");
+        }
         auto* adj    = new (std::nothrow) sg_adjoint_s();
         if (!adj)
         {
@@ -813,6 +843,11 @@ extern "C"
         {
             dfree(b);
         }
+        for (auto*& b : adj->spare_bits)
+        {
+            dfree(b);
+        }
+        dfree(adj->rec_slots);
         for (auto*& p : adj->ckpt)
         {
             dfree(p);
@@ -938,6 +973,11 @@ extern "C"
             return afail(st, c.err.c_str());
         }
         const int passes = c.cfg.max_level - c.cfg.min_level;
+        if (!adj->rec_slots && passes > 0 && dmalloc(&adj->rec_slots, static_cast<size_t>(passes) * static_cast<size_t>(c.g.total_words)))
+        {
+            adj->rec_slots = nullptr; // the pass-by-pass recording below needs no slots
+            cudaGetLastError();
+        }
         for (int n = 0; n < n_steps; ++n)
         {
             if (n % adj->K == 0)
@@ -949,6 +989,29 @@ extern "C"
                 cudaMemcpyAsync(adj->ckpt[static_cast<size_t>(n / adj->K)], u.data, dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
             }
             sg_adjoint_s::Step S{static_cast<int>(adj->bits.size()) - 1, 0};
+            if (sg::step_graph_applies(c) && adj->rec_slots)
+            {
+                // the whole step as one graph (sg_step) that leaves the mesh of each transition in a slot
+                int np       = 0;
+                c.rec_slots  = adj->rec_slots;
+                st           = sg::step(c, u, up1, eps, regularity, adj->a, dt, scheme, &np);
+                c.rec_slots  = nullptr;
+                if (st)
+                {
+                    return afail(st, c.err.c_str());
+                }
+                const int trans = c.h_adapt[sg::A_TRANS];
+                for (int t = 0; t < trans; ++t)
+                {
+                    if ((st = push_bits_from(adj, adj->rec_slots + static_cast<size_t>(t) * static_cast<size_t>(c.g.total_words))))
+                    {
+                        return afail(st, c.err.c_str());
+                    }
+                }
+                S.n_trans = trans;
+                adj->steps.push_back(S);
+                continue;
+            }
             for (int i = 0; i < passes; ++i)
             {
                 bool conv = false;

@@ -25,6 +25,9 @@
 
 namespace sg
 {
+    bool step_graph_applies(const Ctx& c);
+    int step_launch(Ctx& c, DeviceField& u, DeviceField& unp1, double eps, double regularity, const double* a, double dt, int scheme);
+    int step_finish(Ctx& c, DeviceField& u, DeviceField& unp1, int* n_harten);
     int ensure_spare(Ctx& c, DeviceField& f);
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words);
     void set_fusion_tops(Ctx& c, int mesh_top, int field_top, int max_top);
@@ -222,6 +225,45 @@ namespace
                            }
                        }
                    });
+    }
+
+    // the whole time step of the instances of thread t as their step graphs (sg_step): every instance's graph
+    // is launched on its stream before any is waited for, one wait per instance
+    void step_share(sg_batch_s& b, int t, const double* eps, const double* regularity, const double* a, const double* dt, int scheme,
+                    int* n_harten)
+    {
+        std::vector<size_t> started;
+        b.for_mine(t,
+                   [&](size_t k)
+                   {
+                       if (b.status != SG_OK)
+                       {
+                           return;
+                       }
+                       sg::Ctx& c                = b.u[k]->mesh->ctx;
+                       b.unp1[k]->f.ghosts_valid = false;
+                       const int st = sg::step_launch(c, b.u[k]->f, b.unp1[k]->f, eps[k], regularity[k], a + 3 * k, dt[k], scheme);
+                       if (st)
+                       {
+                           b.record(st, c.err.c_str());
+                           return;
+                       }
+                       started.push_back(k);
+                   });
+        for (size_t k : started)
+        {
+            sg::Ctx& c   = b.u[k]->mesh->ctx;
+            int passes   = 0;
+            const int st = sg::step_finish(c, b.u[k]->f, b.unp1[k]->f, &passes);
+            if (st)
+            {
+                b.record(st, c.err.c_str());
+            }
+            if (n_harten)
+            {
+                n_harten[k] = passes;
+            }
+        }
     }
 
     void ghost_share(sg_batch_s& b, int t)
@@ -449,6 +491,16 @@ extern "C"
         if (int st = check_upwind_args(b, a, dt, scheme))
         {
             return st;
+        }
+        // every instance through its step graph when that path applies to all of them, else pass by pass in lockstep
+        bool graphs = true;
+        for (auto* f : b->u)
+        {
+            graphs = graphs && sg::step_graph_applies(f->mesh->ctx) && f->f.spare;
+        }
+        if (graphs)
+        {
+            return b->run([&](int t) { step_share(*b, t, eps, regularity, a, dt, scheme, n_harten); });
         }
         return b->run(
             [&](int t)

@@ -313,6 +313,9 @@ namespace sg
 
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words)
     {
+        c.fuse_words_mesh  = mesh_words;
+        c.fuse_words_field = field_words;
+        c.fuse_words_max   = max_words;
         set_fusion_tops(c, fuse_top_of(c.g, mesh_words), fuse_top_of(c.g, field_words), fuse_top_of(c.g, max_words));
     }
 
@@ -377,9 +380,9 @@ extern "C"
         {
             return fail(SG_ERR_ARG, "sg_mesh_create: unsupported stencil radius / prediction radius / graduation width");
         }
-        if (max_stencil_radius != 1)
+        if (max_stencil_radius > 2)
         {
-            return fail(SG_ERR_ARG, "sg_mesh_create: only max_stencil_radius 1 is implemented");
+            return fail(SG_ERR_ARG, "sg_mesh_create: max_stencil_radius 1 and 2 are implemented (samurai's demos and its default)");
         }
         {
             // the dense slabs of all levels (the bitmap words of sg::make_geom, 32 cells each), counted in
@@ -447,10 +450,15 @@ extern "C"
             c.g.periodic |= periodic[d] ? (1 << d) : 0;
         }
         c.capacity                 = 32 * c.g.total_words;
-        c.fuse_top                 = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS", sg::FUSE_WORDS));
-        c.fuse_top_field           = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS_FIELD", sg::FUSE_WORDS_FIELD));
-        c.fuse_top_max             = sg::fuse_top_of(c.g, tuned("SG_FUSE_WORDS_MAX", sg::FUSE_WORDS_MAX));
+        c.fuse_words_mesh          = tuned("SG_FUSE_WORDS", sg::FUSE_WORDS);
+        c.fuse_words_field         = tuned("SG_FUSE_WORDS_FIELD", sg::FUSE_WORDS_FIELD);
+        c.fuse_words_max           = tuned("SG_FUSE_WORDS_MAX", sg::FUSE_WORDS_MAX);
         c.max_blocks               = std::max(1LL, tuned("SG_MAX_BLOCKS", c.max_blocks));
+        c.block                    = static_cast<int>(std::min(1024LL, std::max(32LL, tuned("SG_BLOCK", c.block))) / 32 * 32);
+        sg::apply_tuned_launch(c); // the autotuner's choice for this device and level range, unless overridden above
+        c.fuse_top                 = sg::fuse_top_of(c.g, c.fuse_words_mesh);
+        c.fuse_top_field           = sg::fuse_top_of(c.g, c.fuse_words_field);
+        c.fuse_top_max             = sg::fuse_top_of(c.g, c.fuse_words_max);
         if (cudaGetDevice(&c.device) != cudaSuccess || cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
         {
             cudaGetLastError();
@@ -1505,6 +1513,35 @@ extern "C"
         return from_ctx(c, sg::upwind(c, u->f, unp1->f, a, dt, scheme));
     }
     SG_API_CATCH(sg_upwind)
+
+    int sg_step(sg_field_t u, sg_field_t unp1, double eps, double regularity, const double* a, double dt, int scheme, int* n_harten)
+    try
+    {
+        if (!u || !unp1 || !a || u->mesh != unp1->mesh || u == unp1)
+        {
+            return fail(SG_ERR_ARG, "sg_step: need two distinct fields on the same mesh");
+        }
+        if (scheme != SG_UPWIND_OP && scheme != SG_README && scheme != SG_CONVECTION)
+        {
+            return fail(SG_ERR_ARG, "sg_step: unknown scheme");
+        }
+        sg::Ctx& c = u->mesh->ctx;
+        if (scheme == SG_README && c.g.dim != 2)
+        {
+            return fail(SG_ERR_ARG, "sg_step: the README scheme is two-dimensional");
+        }
+        if (scheme == SG_CONVECTION && c.g.periodic)
+        {
+            return fail(SG_ERR_ARG, "sg_step: the flux form is not available on a mesh with a periodic axis");
+        }
+        if (!u->f.spare && dalloc(c, &u->f.spare, static_cast<size_t>(c.capacity)))
+        {
+            return from_ctx(c, SG_ERR_CUDA);
+        }
+        unp1->f.ghosts_valid = false;
+        return from_ctx(c, sg::step(c, u->f, unp1->f, eps, regularity, a, dt, scheme, n_harten));
+    }
+    SG_API_CATCH(sg_step)
 
     int sg_detail_download(sg_field_t u, double* values, long long n)
     try

@@ -60,6 +60,9 @@ namespace sg
         A_TRANS  = 2,  // passes that changed the mesh
         A_LOOP   = 3,  // condition of the graduation loop
         A_ITER   = 4,  // iterations of the graduation loop
+        A_PAR0   = 5,  // a time step's tail: an even number of transitions (the starting buffers are final)
+        A_PAR1   = 6,  //   an odd number
+        A_NEEDG  = 7,  //   the last pass changed the mesh: the ghosts need an update
         A_COUNT  = 8
     };
 
@@ -144,6 +147,7 @@ namespace sg
         int* d_adapt  = nullptr; // device state of a graphed adaptation (AdaptSlot)
         int* h_adapt  = nullptr; // pinned mirror of d_adapt
         bool graphed_adapt = true; // the whole adaptation as one graph with conditional nodes
+        uint32_t* rec_slots = nullptr; // when set, the adaptation graph copies the leaf bitmap of transition t into slot t (adjoint recording)
         DeviceMesh mesh[2];
         int cur = 0;
         // scratch bitmaps
@@ -173,7 +177,11 @@ namespace sg
         int fuse_top_field  = -1;      // the same for the FP64 field chains
         int fuse_top_max    = -1;      // the same for the tag-finalisation chain
         const int* guard    = nullptr; // device flag: word launches do nothing while it is 0
-        long long max_blocks = 152LL * 8; // grid limit of the one-warp-per-word launches (x4 for one thread per word)
+        long long max_blocks = 152LL * 8; // grid limit of the one-warp-per-word launches, in blocks of 8 warps (x4 for one thread per word)
+        int block            = 256;       // threads per block of the FP64 list kernels
+        long long fuse_words_mesh  = 0; // one-block chain limits (words per level) behind fuse_top, fuse_top_field, fuse_top_max
+        long long fuse_words_field = 0;
+        long long fuse_words_max   = 0;
         struct GraphEntry
         {
             unsigned long long key[4];
@@ -218,6 +226,8 @@ namespace sg
     int update_ghost_mr(Ctx& c, DeviceField& f);     // update_ghost_mr(u)
     int adapt(Ctx& c, DeviceField& f, double eps, double regularity, int* n_harten, bool relative_detail = false);
     int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme);
+    int upwind_on(Ctx& c, const DeviceMesh& m, const double* ud, double* unp1d, const double* a, double dt, int scheme, bool baked);
+    int step(Ctx& c, DeviceField& u, DeviceField& unp1, double eps, double regularity, const double* a, double dt, int scheme, int* n_harten);
     int gather_compact(Ctx& c, const DeviceMesh& m, const double* dense, double* compact);
     cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact); // no error text
     cudaError_t read_device_error(Ctx& c, int* v);                                                  // reads and clears
@@ -247,6 +257,7 @@ namespace sg
     // kernel trace is on, the trace event of the launch
     void launched(Ctx& c, const char* name, int count = 1);
     void clear_graphs(Ctx& c); // drops the captured launch sequences (their trace events go back to the pool)
+    void apply_tuned_launch(Ctx& c); // the autotuner's cached launch shape for the mesh's device and levels (sg_tune.cu)
     cudaEvent_t take_event(Ctx& c);
     void give_event(Ctx& c, cudaEvent_t e);
 

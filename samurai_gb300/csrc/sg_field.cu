@@ -370,11 +370,24 @@ namespace sg
             d[0] = d[1] = d[2] = 0;
         }
 
-        // update_outer_corners_by_polynomial_extrapolation for a ghost width
-        // of 1 (bc/apply_field_bc.hpp:371-505) followed by project_corner_below
-        // (algorithm/update_outer_ghost.hpp:268-337), one block per diagonal
-        // direction.  parts: 1 the corners, 2 their projection below, 3 both
-        // (the projection reads the corners, after a block barrier).
+        // PolynomialExtrapolation of the second ghost layer (bc/polynomial_extrapolation.hpp:22-92, stencil of 4
+        // cells along d from c - d): u(c + 2d) = u(c - d) - 3 u(c) + 3 u(c + d), in the reference's operation order
+        template <class A>
+        __device__ __forceinline__ void extrapolate_layer2(const Geom& g, int l, const int* c, const int* d, const A& u)
+        {
+            const int z = g.dim == 3;
+            const long long em = elem_at(g, l, c[0] - d[0], c[1] - d[1], z ? c[2] - d[2] : 0);
+            const long long e0 = elem_at(g, l, c[0], c[1], z ? c[2] : 0);
+            const long long e1 = elem_at(g, l, c[0] + d[0], c[1] + d[1], z ? c[2] + d[2] : 0);
+            const long long e2 = elem_at(g, l, c[0] + 2 * d[0], c[1] + 2 * d[1], z ? c[2] + 2 * d[2] : 0);
+            u.put(e2, (u.get(em) - u.get(e0) * 3.0) + u.get(e1) * 3.0);
+        }
+
+        // update_outer_corners_by_polynomial_extrapolation (bc/apply_field_bc.hpp:371-505) followed by
+        // project_corner_below (algorithm/update_outer_ghost.hpp:268-337), one block per diagonal direction d:
+        // layer 1 copies the corner leaf, layer 2 (ghost width 2) extrapolates along d, then the other ghosts
+        // of the corner block copy the diagonal ones (the off-diagonal copies).  parts: 1 the corners, 2 their
+        // projection below, 3 both (the projection reads the corners, after a block barrier).
         template <class A>
         __device__ void corner_role(const Geom& g, const int* d, int l, const uint32_t* cells, const uint32_t* ref, const A& u, int parts = 3)
         {
@@ -401,6 +414,46 @@ namespace sg
                 {
                     const long long eg = elem_at(g, l, c[0] + d[0], c[1] + d[1], g.dim == 3 ? c[2] + d[2] : 0);
                     u.put(eg, u.get(elem(pc)));
+                    if (g.ghost_width >= 2)
+                    {
+                        if (test(ref, g, l, c[0] + 2 * d[0], c[1] + 2 * d[1], g.dim == 3 ? c[2] + 2 * d[2] : 0))
+                        {
+                            extrapolate_layer2(g, l, c, d, u);
+                        }
+                        // off-diagonal copies: from c + k d (k = 1, 2) to c + k d + delta, delta moving the
+                        // non-zero components after the first by g - (k - 1), g in [0, 2), not all zero
+                        int nz[3], nnz = 0;
+                        for (int k = 0; k < g.dim; ++k)
+                        {
+                            if (d[k] != 0)
+                            {
+                                nz[nnz++] = k;
+                            }
+                        }
+                        const int combos = nnz == 3 ? 4 : 2;
+                        for (int k = 1; k <= 2; ++k)
+                        {
+                            const int sx = c[0] + k * d[0], sy = c[1] + k * d[1], sz = g.dim == 3 ? c[2] + k * d[2] : 0;
+                            const long long es = elem_at(g, l, sx, sy, sz);
+                            for (int combo = 0; combo < combos; ++combo)
+                            {
+                                int delta[3] = {0, 0, 0};
+                                bool source  = true;
+                                int tmp      = combo;
+                                for (int p = 1; p < nnz; ++p)
+                                {
+                                    const int dp = (tmp % 2) - (k - 1);
+                                    tmp /= 2;
+                                    delta[nz[p]] += dp * d[nz[p]];
+                                    source = source && dp == 0;
+                                }
+                                if (!source)
+                                {
+                                    u.put(elem_at(g, l, sx + delta[0], sy + delta[1], sz + delta[2]), u.get(es));
+                                }
+                            }
+                        }
+                    }
                 }
             }
             if (parts != 3)
@@ -491,6 +544,7 @@ namespace sg
             long long nfaces; // face positions (2*dim directions)
             int do_proj;      // project the reference of level l onto proj_cells[l-1]
             int corner_parts; // corner_role parts run by the corner blocks
+            int do_dirichlet_layer2; // the second ghost layer next to non-leaf boundary cells (level >= min_level, a BC)
         };
 
         // One launch per level of the top-down pass of update_ghost_mr
@@ -528,6 +582,12 @@ namespace sg
                 {
                     v = A::konst(2 * a.value) - u.get(elem(pi));
                     u.put(eg, v);
+                    // update_further_ghosts_by_polynomial_extrapolation (bc/apply_field_bc.hpp:531-593), ghost
+                    // width 2: the second layer beyond a boundary leaf, where it is a reference cell
+                    if (g.ghost_width >= 2 && test(ref, g, l, gx + dir[0], gy + dir[1], gz + dir[2]))
+                    {
+                        extrapolate_layer2(g, l, in, dir, u);
+                    }
                 }
                 else
                 {
@@ -581,6 +641,12 @@ namespace sg
                     }
                 }
                 u.put(elem(pg), nch > 0 ? sum / static_cast<double>(nch) : A::konst(0.));
+                // the second ghost layer beyond a boundary cell that is not a leaf but has finer leaves
+                // (apply_extrapolation_bc_ghosts, bc/apply_field_bc.hpp:196-214), ghost width 2
+                if (g.ghost_width >= 2 && a.do_dirichlet_layer2 && test(ref, g, l, gx + dir[0], gy + dir[1], gz + dir[2]))
+                {
+                    extrapolate_layer2(g, l, in, dir, u);
+                }
             }
         }
 
@@ -807,6 +873,7 @@ namespace sg
                 a.l            = l;
                 a.do_project   = l < maxl;
                 a.do_dirichlet = (l >= minl) && ca.has_bc;
+                a.do_dirichlet_layer2 = a.do_dirichlet;
                 a.do_predict   = (l >= minl && l < maxl);
                 a.value        = ca.value;
                 if (l >= minl && l <= maxl)
@@ -1500,21 +1567,25 @@ namespace sg
     namespace
     {
         // one warp per word of levels l0..l1, at most the mesh's block limit
+        // blocks of c.block threads: one warp per word of levels l0..l1, at most
+        // max_blocks blocks of 8 warps' worth of warps
         int blocks_words(const Ctx& c, int l0, int l1)
         {
             if (l1 < l0)
             {
                 return 1;
             }
-            const Geom& g      = c.g;
-            const long long nb = (g.lv[l1].woff + g.lv[l1].nwords - g.lv[l0].woff + 7) / 8;
-            return static_cast<int>(nb < 1 ? 1 : (nb > c.max_blocks ? c.max_blocks : nb));
+            const Geom& g          = c.g;
+            const long long wpb    = c.block / 32;
+            const long long nb     = (g.lv[l1].woff + g.lv[l1].nwords - g.lv[l0].woff + wpb - 1) / wpb;
+            const long long cap    = std::max(1LL, c.max_blocks * 8 / wpb);
+            return static_cast<int>(nb < 1 ? 1 : (nb > cap ? cap : nb));
         }
     } // namespace
 
     cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
     {
-        k_gather<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
+        k_gather<<<blocks_words(c, 0, c.g.nlev - 1), c.block, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
         launched(c, "gather");
         return cudaGetLastError();
     }
@@ -1546,14 +1617,14 @@ namespace sg
 
     int scatter_compact(Ctx& c, const DeviceMesh& m, const double* compact, double* dense)
     {
-        k_scatter<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, compact, dense);
+        k_scatter<<<blocks_words(c, 0, c.g.nlev - 1), c.block, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, compact, dense);
         launched(c, "scatter");
         return check(c, "scatter");
     }
 
     int fill_ref(Ctx& c, const DeviceMesh& m, double* dense, double value)
     {
-        k_fill<<<blocks_words(c, 0, c.g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, dense, value);
+        k_fill<<<blocks_words(c, 0, c.g.nlev - 1), c.block, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, dense, value);
         launched(c, "fill");
         return check(c, "fill");
     }
@@ -1703,6 +1774,25 @@ namespace sg
             cudaGraphSetConditional(h, go ? 1u : 0u);
         }
 
+        // after the passes: which final buffers (parity of the transitions) and whether the ghosts need updating
+        __global__ void k_step_flags(int* a)
+        {
+            const int trans = a[A_TRANS];
+            a[A_PAR0]       = (trans & 1) == 0;
+            a[A_PAR1]       = (trans & 1) == 1;
+            a[A_NEEDG]      = a[A_PASSES] == trans;
+        }
+
+        // the leaf bitmap of a transition into recording slot a[A_TRANS] (before the count moves on)
+        __global__ void k_record_bits(const uint32_t* cells, uint32_t* slots, const int* a, long long words)
+        {
+            uint32_t* dst = slots + static_cast<long long>(a[A_TRANS]) * words;
+            for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < words; w += static_cast<long long>(gridDim.x) * blockDim.x)
+            {
+                dst[w] = cells[w];
+            }
+        }
+
         __global__ void k_adapt_words(int* a, int slot, const int* src, int value, int add)
         {
             // a[slot] = src ? *src : value, or += when add
@@ -1846,6 +1936,7 @@ namespace sg
                 a.do_corners   = (l >= minl && l <= maxl) ? 1 : 0;
                 a.do_project   = l < maxl;
                 a.do_dirichlet = (l >= minl) && has_bc;
+                a.do_dirichlet_layer2 = a.do_dirichlet;
                 a.do_predict   = (l >= minl && l < maxl);
                 a.value        = bcv;
                 a.nb_corner    = a.do_corners ? ndiag : 0;
@@ -1854,7 +1945,7 @@ namespace sg
                 a.nfaces       = (a.do_project || a.do_dirichlet || a.do_predict)
                                      ? static_cast<long long>(2 * g.dim) * ((g.dim == 2) ? n : static_cast<long long>(n) * n)
                                      : 0;
-                a.nb_face         = static_cast<int>((a.nfaces + BLOCK - 1) / BLOCK);
+                a.nb_face         = static_cast<int>((a.nfaces + c.block - 1) / c.block);
                 a.do_proj         = l > lmin;
                 const int nb_proj = a.do_proj ? blocks_words(c, l - 1, l - 1) : 0;
                 const int grid    = a.nb_corner + a.nb_face + nb_proj;
@@ -1862,11 +1953,11 @@ namespace sg
                 {
                     if (g.dim == 2)
                     {
-                        k_ghost_level<2><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<2><<<grid, c.block, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     else
                     {
-                        k_ghost_level<3><<<grid, BLOCK, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<3><<<grid, c.block, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     launched(c, "ghost_level");
                     after();
@@ -1880,11 +1971,11 @@ namespace sg
                     b.do_proj        = 0;
                     if (g.dim == 2)
                     {
-                        k_ghost_level<2><<<b.nb_corner, BLOCK, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<2><<<b.nb_corner, c.block, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     else
                     {
-                        k_ghost_level<3><<<b.nb_corner, BLOCK, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<3><<<b.nb_corner, c.block, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     launched(c, "ghost_corner_projection");
                     after();
@@ -1929,12 +2020,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_predict<2><<<blocks_words(c, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<2><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 else
                 {
-                    k_predict<3><<<blocks_words(c, lp, lp), BLOCK, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<3><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 launched(c, "predict");
@@ -1957,12 +2048,12 @@ namespace sg
             const Geom& g = c.g;
             if (g.dim == 2)
             {
-                k_update_fields<2><<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                k_update_fields<2><<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
                                                                                             nm.cells, m.ref, m.cells, m.hc, uo, un);
             }
             else
             {
-                k_update_fields<3><<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                k_update_fields<3><<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
                                                                                             nm.cells, m.ref, m.cells, m.hc, uo, un);
             }
             launched(c, "update_fields");
@@ -1993,11 +2084,11 @@ namespace sg
                 cudaMemcpyAsync(c.d_eps, c.h_eps, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
             }
             cudaMemsetAsync(c.d_flags, 0, F_COUNT * sizeof(int), c.stream);
-            k_tag_init<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
+            k_tag_init<<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
             launched(c, "tag_init");
             for (int k = 1; k < nf; ++k)
             {
-                k_fill<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.detail + k * c.capacity, 0.);
+                k_fill<<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.detail + k * c.capacity, 0.);
                 launched(c, "fill");
             }
             if ((st = check(c, "tag_init")))
@@ -2021,12 +2112,12 @@ namespace sg
                 double* det     = c.detail + k * c.capacity;
                 if (g.dim == 2)
                 {
-                    k_detail<2><<<blocks_words(c, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                    k_detail<2><<<blocks_words(c, dl0, dl1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
                                                                                     m.ref, m.hc, m.hc2, u, det);
                 }
                 else
                 {
-                    k_detail<3><<<blocks_words(c, dl0, dl1), BLOCK, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                    k_detail<3><<<blocks_words(c, dl0, dl1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
                                                                                     m.ref, m.hc, m.hc2, u, det);
                 }
                 launched(c, "detail");
@@ -2034,8 +2125,8 @@ namespace sg
             for (int k = 0; k < nf && c.rel_detail; ++k)
             {
                 k_absmax_init<<<1, 1, 0, c.stream>>>(c.d_absmax);
-                k_absmax<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_cells, m.d_lo, g.nlev, m.cells, fs[k]->data, c.d_absmax);
-                k_rel_scale<<<blocks_words(c, 0, g.nlev - 1), BLOCK, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.d_absmax, c.detail + k * c.capacity);
+                k_absmax<<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(m.wl_cells, m.d_lo, g.nlev, m.cells, fs[k]->data, c.d_absmax);
+                k_rel_scale<<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(m.wl_ref, m.d_lo, g.nlev, m.ref, c.d_absmax, c.detail + k * c.capacity);
                 launched(c, "absmax", 3);
             }
             timer_stop(c, T_DETAIL);
@@ -2045,12 +2136,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_criteria<2><<<blocks_words(c, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                    k_criteria<2><<<blocks_words(c, minl - 1, maxl - 1), c.block, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
                                                                                                 m.ref, m.hc, c.detail, c.tag, nf, c.capacity);
                 }
                 else
                 {
-                    k_criteria<3><<<blocks_words(c, minl - 1, maxl - 1), BLOCK, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                    k_criteria<3><<<blocks_words(c, minl - 1, maxl - 1), c.block, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
                                                                                                 m.ref, m.hc, c.detail, c.tag, nf, c.capacity);
                 }
                 launched(c, "criteria");
@@ -2058,7 +2149,7 @@ namespace sg
             if (c.refine_boundary)
             {
                 // "refine boundary" (mr/adapt.hpp:341-346), between tag cells and tag finalization
-                k_keep_boundary<<<blocks_words(c, maxl, maxl), BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, c.cfg.max_stencil_radius,
+                k_keep_boundary<<<blocks_words(c, maxl, maxl), c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, c.cfg.max_stencil_radius,
                                                                                    c.tag);
                 launched(c, "keep_boundary");
             }
@@ -2078,11 +2169,11 @@ namespace sg
                     periodic_tags(c, m, l);
                     if (g.dim == 2)
                     {
-                        k_maximum<2><<<blocks_words(c, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<2><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     else
                     {
-                        k_maximum<3><<<blocks_words(c, l - 1, l - 1), BLOCK, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<3><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     launched(c, "maximum");
                 }
@@ -2208,9 +2299,9 @@ namespace sg
 
     int update_ghost_mr(Ctx& c, DeviceField& f)
     {
-        if (c.cfg.ghost_width != 1)
+        if (c.cfg.ghost_width > 2)
         {
-            c.err = "update_ghost_mr: only a ghost width of 1 is implemented";
+            c.err = "update_ghost_mr: ghost widths 1 and 2 are implemented";
             return SG_ERR_ARG;
         }
         if (f.ghosts_valid && f.ghost_version == c.mesh_version)
@@ -2263,9 +2354,9 @@ namespace sg
 
     int harten_begin_fields(Ctx& c, const std::vector<DeviceField*>& fs, int ite, double eps, double regularity, bool relative_detail)
     {
-        if (c.cfg.ghost_width != 1)
+        if (c.cfg.ghost_width > 2)
         {
-            c.err = "harten: only a ghost width of 1 is implemented";
+            c.err = "harten: ghost widths 1 and 2 are implemented";
             return SG_ERR_ARG;
         }
         const int minl = c.cfg.min_level;
@@ -2426,7 +2517,17 @@ namespace sg
         // one that holds when this pass changed it; graduation iterates in a
         // conditional loop.  Pass i works on mesh buffer (cur + i) mod 2 and on
         // the field buffers that many swaps away, all known when capturing.
-        int seq_adapt(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity)
+        struct StepTail
+        {
+            DeviceField* u;    // the adapted field (fs[0])
+            DeviceField* unp1; // the upwind's output
+            double a[3];
+            double dt;
+            int scheme;
+        };
+
+        int seq_adapt(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
+                      const StepTail* tail = nullptr)
         {
             const int passes = c.cfg.max_level - c.cfg.min_level;
             std::vector<DeviceField> fa, oa; // the fields as they stand at each pass (buffers swapped per transition)
@@ -2473,6 +2574,12 @@ namespace sg
                                       [&]()
                                       {
                                           int s2 = seq_back(c, m, nm, fp, op);
+                                          if (c.rec_slots)
+                                          {
+                                              k_record_bits<<<grid_for(c.g.total_words), 256, 0, c.stream>>>(nm.cells, c.rec_slots, c.d_adapt,
+                                                                                                              c.g.total_words);
+                                              launched(c, "record_bits");
+                                          }
                                           k_adapt_words<<<1, 1, 0, c.stream>>>(c.d_adapt, A_TRANS, nullptr, 1, 1);
                                           launched(c, "adapt_words");
                                           return s2;
@@ -2487,6 +2594,29 @@ namespace sg
                     }
                 }
             }
+            if (!st && tail)
+            {
+                // the rest of the time step on the final mesh: the mesh buffer and the field's buffer depend on the
+                // parity of the number of transitions, the ghost update on whether the last pass changed the mesh
+                // (when it kept it, its own ghost update left the ghosts valid)
+                k_step_flags<<<1, 1, 0, c.stream>>>(c.d_adapt);
+                launched(c, "adapt_words");
+                for (int par = 0; par < 2 && !st; ++par)
+                {
+                    const int cur    = (c.cur + par) & 1;
+                    DeviceMesh& mf   = c.mesh[cur];
+                    double* ud       = par ? tail->u->spare : tail->u->data;
+                    const bool bc    = tail->u->has_bc;
+                    const double bcv = tail->u->bc_value;
+                    st               = capture_if(c, c.d_adapt + (par ? A_PAR1 : A_PAR0),
+                                                  [&]()
+                                                  {
+                                                      int s1 = capture_if(c, c.d_adapt + A_NEEDG,
+                                                                          [&]() { return ghost_launches(c, mf, ValAcc{ud}, bc, bcv, c.fuse_top_field, false, [] {}); });
+                                                      return s1 ? s1 : upwind_on(c, mf, ud, tail->unp1->data, tail->a, tail->dt, tail->scheme, true);
+                                                  });
+                }
+            }
             if (!st)
             {
                 cudaMemcpyAsync(c.h_adapt, c.d_adapt, A_COUNT * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
@@ -2494,38 +2624,50 @@ namespace sg
             return st ? st : check(c, "adaptation graph");
         }
 
-        // the adaptation through seq_adapt's graph; false when that path does
-        // not apply (graphs off, timers or the kernel trace on)
-        bool adapt_graphed(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
-                           bool relative_detail, int* n_harten, int* status)
+        bool graph_applies(const Ctx& c)
         {
-            if (!c.graphed_adapt || !c.use_graphs || c.timers.enabled || c.trace.enabled || c.cfg.max_level == c.cfg.min_level)
+            return c.graphed_adapt && c.use_graphs && !c.timers.enabled && !c.trace.enabled && c.cfg.max_level != c.cfg.min_level;
+        }
+
+        // launches seq_adapt's graph (captured on first use) without waiting
+        int adapt_graph_launch(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
+                               bool relative_detail, const StepTail* tail)
+        {
+            if (c.cfg.ghost_width > 2)
             {
-                return false;
-            }
-            if (c.cfg.ghost_width != 1)
-            {
-                c.err   = "harten: only a ghost width of 1 is implemented";
-                *status = SG_ERR_ARG;
-                return true;
+                c.err = "harten: ghost widths 1 and 2 are implemented";
+                return SG_ERR_ARG;
             }
             c.rel_detail = relative_detail;
             std::vector<DeviceField*> all(fs);
             all.insert(all.end(), os.begin(), os.end());
-            const unsigned long long kind = 9ull | (relative_detail ? 16ull : 0ull) | (c.refine_boundary ? 256ull : 0ull)
-                                            | (static_cast<unsigned long long>(fs.size()) << 20);
-            const unsigned long long thr = bits_of(eps) * 0x9E3779B97F4A7C15ull ^ bits_of(regularity);
-            int st = run_cached(c, kind, static_cast<unsigned long long>(c.cur), fields_key(all, false) ^ (fields_key(all, true) << 1), thr,
-                                [&]() { return seq_adapt(c, fs, os, eps, regularity); });
-            if (!st && cudaStreamSynchronize(c.stream) != cudaSuccess)
+            unsigned long long kind = 9ull | (relative_detail ? 16ull : 0ull) | (c.refine_boundary ? 256ull : 0ull)
+                                      | (static_cast<unsigned long long>(fs.size()) << 20);
+            unsigned long long thr  = bits_of(eps) * 0x9E3779B97F4A7C15ull ^ bits_of(regularity);
+            unsigned long long bufs = fields_key(all, false) ^ (fields_key(all, true) << 1) ^ (ptr_key(c.rec_slots) * 0x9E3779B97F4A7C15ull);
+            if (tail)
             {
-                st = check(c, "adaptation sync");
+                kind |= (static_cast<unsigned long long>(tail->scheme) + 1) << 10;
+                bufs ^= ptr_key(tail->unp1->data) * 0xC2B2AE3D27D4EB4Full;
+                for (double v : {tail->a[0], tail->a[1], tail->a[2], tail->dt})
+                {
+                    thr = (thr ^ bits_of(v)) * 0x100000001B3ull;
+                }
             }
-            if (st)
+            return run_cached(c, kind, static_cast<unsigned long long>(c.cur), bufs, thr, [&]() { return seq_adapt(c, fs, os, eps, regularity, tail); });
+        }
+
+        // waits for a launched adaptation graph and applies its outcome on the host: the buffer swaps of the
+        // transitions, the current mesh, ghost validity and the step's own swap
+        int adapt_graph_finish(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, const StepTail* tail,
+                               int* n_harten)
+        {
+            if (cudaStreamSynchronize(c.stream) != cudaSuccess)
             {
-                *status = st;
-                return true;
+                return check(c, "adaptation sync");
             }
+            std::vector<DeviceField*> all(fs);
+            all.insert(all.end(), os.begin(), os.end());
             const int passes = c.h_adapt[A_PASSES], trans = c.h_adapt[A_TRANS];
             for (int t = 0; t < trans; ++t)
             {
@@ -2545,22 +2687,110 @@ namespace sg
             {
                 f->ghosts_valid = false;
             }
-            if (passes > trans)
+            if (passes > trans || tail)
             {
+                // the last pass kept the mesh, or the step's tail updated the ghosts
                 for (DeviceField* f : fs)
                 {
                     f->ghosts_valid  = true;
                     f->ghost_version = c.mesh_version;
                 }
             }
+            if (tail)
+            {
+                // unp1 = u - dt * upwind(a, u) then std::swap(u.array(), unp1.array())
+                std::swap(tail->u->data, tail->unp1->data);
+                tail->u->ghosts_valid    = false;
+                tail->unp1->ghosts_valid = false;
+            }
             if (n_harten)
             {
                 *n_harten = passes;
             }
-            *status = device_error(c);
+            return device_error(c);
+        }
+
+        // the adaptation (and the rest of the step when tail is given) through
+        // the graph; false when that path does not apply (graphs off, timers or
+        // the kernel trace on)
+        bool adapt_graphed(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
+                           bool relative_detail, int* n_harten, int* status, const StepTail* tail = nullptr)
+        {
+            if (!graph_applies(c))
+            {
+                return false;
+            }
+            *status = adapt_graph_launch(c, fs, os, eps, regularity, relative_detail, tail);
+            if (!*status)
+            {
+                *status = adapt_graph_finish(c, fs, os, tail, n_harten);
+            }
             return true;
         }
+
+        StepTail make_tail(const Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme)
+        {
+            StepTail t{};
+            t.u    = &u;
+            t.unp1 = &unp1;
+            for (int d = 0; d < c.g.dim; ++d)
+            {
+                t.a[d] = a[d];
+            }
+            t.dt     = dt;
+            t.scheme = scheme;
+            return t;
+        }
     } // namespace
+
+    bool step_graph_applies(const Ctx& c)
+    {
+        return graph_applies(c);
+    }
+
+    // the time step's graph in two halves (batched mode: launch every instance's, then wait for each);
+    // step_launch returns SG_ERR_NOTFOUND when the graph path does not apply to this mesh
+    int step_launch(Ctx& c, DeviceField& u, DeviceField& unp1, double eps, double regularity, const double* a, double dt, int scheme)
+    {
+        if (!graph_applies(c))
+        {
+            return SG_ERR_NOTFOUND;
+        }
+        const StepTail t = make_tail(c, u, unp1, a, dt, scheme);
+        return adapt_graph_launch(c, {&u}, {}, eps, regularity, false, &t);
+    }
+
+    int step_finish(Ctx& c, DeviceField& u, DeviceField& unp1, int* n_harten)
+    {
+        const double zero[3] = {0., 0., 0.};
+        const StepTail t     = make_tail(c, u, unp1, zero, 0., 0);
+        return adapt_graph_finish(c, {&u}, {}, &t, n_harten);
+    }
+
+    // One iteration of the demo's time loop (demos/FiniteVolume/advection_2d.cpp:140-147): MRadaptation(eps,
+    // regularity), update_ghost_mr(u), unp1 = u - dt * upwind(a, u) (or the flux form / README scheme),
+    // std::swap(u.array(), unp1.array()) — one captured graph and one synchronisation when graphs apply,
+    // otherwise the separate calls.
+    int step(Ctx& c, DeviceField& u, DeviceField& unp1, double eps, double regularity, const double* a, double dt, int scheme, int* n_harten)
+    {
+        const StepTail t = make_tail(c, u, unp1, a, dt, scheme);
+        int st           = SG_OK;
+        {
+            ScopedTimer timer(c, T_ADAPT);
+            if (adapt_graphed(c, {&u}, {}, eps, regularity, false, n_harten, &st, &t))
+            {
+                return st;
+            }
+        }
+        if ((st = adapt(c, u, eps, regularity, n_harten, false)) || (st = update_ghost_mr(c, u)) || (st = upwind(c, u, unp1, a, dt, scheme)))
+        {
+            return st;
+        }
+        std::swap(u.data, unp1.data);
+        u.ghosts_valid    = false;
+        unp1.ghosts_valid = false;
+        return SG_OK;
+    }
 
     // Adapt<Fields...>::operator()(mra_config, other_fields...) (mr/adapt.hpp:147-195)
     int adapt_fields(Ctx& c, const std::vector<DeviceField*>& fs, const std::vector<DeviceField*>& os, double eps, double regularity,
@@ -2634,11 +2864,22 @@ namespace sg
         return device_error(c);
     }
 
-    int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme)
+    namespace
     {
-        ScopedTimer timer(c, T_UPWIND);
-        const Geom& g       = c.g;
-        const DeviceMesh& m = c.m();
+        __global__ void k_set_velocity(double* av, double a0, double a1, double a2)
+        {
+            av[0] = a0;
+            av[1] = a1;
+            av[2] = a2;
+        }
+    } // namespace
+
+    // the upwind step on mesh m from the values at ud into unp1d; baked: the
+    // velocity of the flux form is written by a kernel (inside a captured
+    // graph) instead of copied from the host array
+    int upwind_on(Ctx& c, const DeviceMesh& m, const double* ud, double* unp1d, const double* a, double dt, int scheme, bool baked)
+    {
+        const Geom& g = c.g;
         UpwindArgs p{};
         for (int d = 0; d < g.dim; ++d)
         {
@@ -2651,25 +2892,39 @@ namespace sg
         if (scheme == 2)
         {
             double* av = c.d_eps + EPS_VELOCITY;
-            cudaMemcpyAsync(av, a, g.dim * sizeof(double), cudaMemcpyHostToDevice, c.stream);
-            if (g.dim == 2)
+            if (baked)
             {
-                k_convection<2><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p, av);
+                k_set_velocity<<<1, 1, 0, c.stream>>>(av, a[0], a[1], g.dim == 3 ? a[2] : 0.);
+                launched(c, "set_velocity");
             }
             else
             {
-                k_convection<3><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p, av);
+                cudaMemcpyAsync(av, a, g.dim * sizeof(double), cudaMemcpyHostToDevice, c.stream);
+            }
+            if (g.dim == 2)
+            {
+                k_convection<2><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p, av);
+            }
+            else
+            {
+                k_convection<3><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p, av);
             }
         }
         else if (g.dim == 2)
         {
-            k_upwind<2><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p);
+            k_upwind<2><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p);
         }
         else
         {
-            k_upwind<3><<<nb, BLOCK, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, u.data, unp1.data, p);
+            k_upwind<3><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p);
         }
         launched(c, scheme == 2 ? "convection" : "upwind");
         return check(c, "upwind");
+    }
+
+    int upwind(Ctx& c, DeviceField& u, DeviceField& unp1, const double* a, double dt, int scheme)
+    {
+        ScopedTimer timer(c, T_UPWIND);
+        return upwind_on(c, c.m(), u.data, unp1.data, a, dt, scheme, false);
     }
 } // namespace sg

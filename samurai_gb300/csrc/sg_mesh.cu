@@ -59,10 +59,19 @@ namespace sg
         c.n_launches += count;
         if (c.trace.enabled)
         {
-            // external: inside a stream capture the record becomes an event-record node of the graph (a plain
-            // record would only order the capture)
+            // inside a stream capture an external record becomes an event-record node of the graph (a plain
+            // record would only order the capture); outside a capture it is a plain record
             cudaEvent_t e = take_event(c);
-            cudaEventRecordWithFlags(e, c.stream, cudaEventRecordExternal);
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            cudaStreamIsCapturing(c.stream, &cs);
+            if (cs == cudaStreamCaptureStatusActive)
+            {
+                cudaEventRecordWithFlags(e, c.stream, cudaEventRecordExternal);
+            }
+            else
+            {
+                cudaEventRecord(e, c.stream);
+            }
             c.trace.marks.push_back({name, e});
         }
     }
@@ -909,6 +918,96 @@ namespace sg
     // (graduation.hpp:121-249) is a no-op for a max_stencil_radius of 1.
     namespace
     {
+        // list_interval_to_refine_for_contiguous_boundary_cells for a max_stencil_radius of 2
+        // (algorithm/graduation.hpp:370-497): in each non-periodic Cartesian direction t, a leaf P of level lc is
+        // refined when a leaf b of level lc + 1 on the boundary the direction points to has b - 2 t among P's
+        // children, i.e. P sits at coordinate n - 2 (t = +e) or 1 (t = -e) along the axis and one of its children's
+        // neighbours across the boundary layer is a leaf.  The bits of word (row, wi) of level lc to refine.
+        __device__ __forceinline__ uint32_t contiguous_boundary_word(const Geom& g, const uint32_t* nc, int lc, long long w, long long row, int wi)
+        {
+            const uint32_t v = nc[w];
+            if (!v)
+            {
+                return 0u;
+            }
+            const LevelGeom& C = g.lv[lc];
+            const LevelGeom& F = g.lv[lc + 1];
+            int y, z;
+            if (g.dim == 2)
+            {
+                y = static_cast<int>(row) - PY;
+                z = 0;
+            }
+            else
+            {
+                split_row(C, row, &y, &z);
+                y -= PY;
+                z -= PY;
+            }
+            const int x0   = 32 * wi - PX;
+            const int nz   = g.dim == 3 ? 2 : 1;
+            uint32_t out   = 0u;
+            auto fine_word = [&](int fy, int fz, int k) -> uint32_t
+            {
+                const int ry = fy + PY, rz = fz + PY;
+                if (ry < 0 || ry >= F.R || (g.dim == 3 && (rz < 0 || rz >= F.R)) || k < 0 || k >= F.W)
+                {
+                    return 0u;
+                }
+                const long long frow = (g.dim == 2) ? ry : static_cast<long long>(rz) * F.R + ry;
+                return nc[F.woff + frow * F.W + k];
+            };
+            for (int d = 0; d < g.dim; ++d)
+            {
+                if ((g.periodic >> d) & 1)
+                {
+                    continue;
+                }
+                for (int sgn = 1; sgn >= -1; sgn -= 2)
+                {
+                    const int p  = sgn > 0 ? C.n - 2 : 1;  // coordinate of P along d
+                    const int bf = sgn > 0 ? F.n - 1 : 0;  // coordinate of b along d
+                    if (d == 0)
+                    {
+                        const int bit = p - x0;
+                        if (bit < 0 || bit >= 32 || !((v >> bit) & 1u))
+                        {
+                            continue;
+                        }
+                        const int xb = bf + PX;
+                        bool hit     = false;
+                        for (int sz = 0; sz < nz && !hit; ++sz)
+                        {
+                            for (int sy = 0; sy < 2 && !hit; ++sy)
+                            {
+                                hit = (fine_word(2 * y + sy, 2 * z + sz, xb >> 5) >> (xb & 31)) & 1u;
+                            }
+                        }
+                        out |= hit ? (1u << bit) : 0u;
+                    }
+                    else
+                    {
+                        if ((d == 1 ? y : z) != p)
+                        {
+                            continue;
+                        }
+                        // the fine boundary row (or plane) under the word's cells: any of a cell's two x children
+                        for (int s2 = 0; s2 < 2 && (d == 1 ? s2 < nz : true); ++s2)
+                        {
+                            const int fy = d == 1 ? bf : 2 * y + s2;
+                            const int fz = d == 1 ? 2 * z + s2 : bf;
+                            if (g.dim == 2 && s2 > 0)
+                            {
+                                break;
+                            }
+                            out |= compress_pairs(fine_word(fy, fz, 2 * wi - 1), fine_word(fy, fz, 2 * wi));
+                        }
+                    }
+                }
+            }
+            return out & v;
+        }
+
         // refine the cells flagged in rr (levels dlo .. dtop): levels dlo .. dtop + 1 change
         int grad_apply(Ctx& c, uint32_t* nc, const uint32_t* rr, int dlo, int dtop)
         {
@@ -962,6 +1061,25 @@ namespace sg
         // Levels min_level .. max_level-2 can hold such cells.
         const int dtop = maxl - 2;
         const int dlo  = c.cfg.min_level;
+        // radius 2: the contiguous-boundary cells refine leaves of levels min_level .. max_level-1 too
+        const bool contiguous = c.cfg.max_stencil_radius == 2;
+        const int rtop        = contiguous ? maxl - 1 : dtop; // rr covers levels dlo .. rtop
+        if (dtop < dlo && contiguous && maxl > dlo)
+        {
+            // no graduation between two levels, the contiguous-boundary pass alone
+            int st = launch_words(c, dlo, rtop,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                                  {
+                                      const uint32_t rv = contiguous_boundary_word(g, nc, l, w, row, wi);
+                                      rr[w]             = rv;
+                                      if (rv)
+                                      {
+                                          atomicOr(flag, 1);
+                                      }
+                                  },
+                                  "grad_boundary");
+            return st ? st : grad_apply(c, nc, rr, dlo, rtop);
+        }
         if (dtop < dlo)
         {
             return SG_OK;
@@ -1027,11 +1145,16 @@ namespace sg
             }
             if (!st)
             {
-                st = launch_words(c, dlo, dtop,
-                                  [=] __device__(const Geom&, int, long long w, long long, int)
+                const int dt = dtop;
+                st           = launch_words(c, dlo, rtop,
+                                  [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
                                   {
-                                      const uint32_t rv = nc[w] & d[w];
-                                      rr[w]             = rv;
+                                      uint32_t rv = l <= dt ? (nc[w] & d[w]) : 0u;
+                                      if (contiguous)
+                                      {
+                                          rv |= contiguous_boundary_word(g, nc, l, w, row, wi);
+                                      }
+                                      rr[w] = rv;
                                       if (rv)
                                       {
                                           atomicOr(flag, 1);
@@ -1043,7 +1166,7 @@ namespace sg
             {
                 return st;
             }
-            return grad_apply(c, nc, rr, dlo, dtop);
+            return grad_apply(c, nc, rr, dlo, rtop);
         }
         if (g.dim == 2)
         {
@@ -1105,7 +1228,28 @@ namespace sg
         {
             return st;
         }
-        return grad_apply(c, nc, rr, dlo, dtop);
+        if (contiguous)
+        {
+            // the contiguous-boundary cells join the chain's graduation flags (levels above dtop had none)
+            const int dt = dtop;
+            st           = launch_words(c, dlo, rtop,
+                              [=] __device__(const Geom& g, int l, long long w, long long row, int wi)
+                              {
+                                  const uint32_t add = contiguous_boundary_word(g, nc, l, w, row, wi);
+                                  const uint32_t rv  = (l <= dt ? rr[w] : 0u) | add;
+                                  rr[w]              = rv;
+                                  if (add)
+                                  {
+                                      atomicOr(flag, 1);
+                                  }
+                              },
+                              "grad_boundary");
+            if (st)
+            {
+                return st;
+            }
+        }
+        return grad_apply(c, nc, rr, dlo, rtop);
     }
 
     // make_graduation to the fixed point, with a host test after each pass

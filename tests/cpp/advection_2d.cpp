@@ -40,8 +40,10 @@ void init(Field& u)
                            });
 }
 
+// mode "default": samurai's default mesh configuration (no disable_minimal_ghost_width(): max_stencil_radius 2),
+// "refine_boundary": the same with samurai::args::refine_boundary (--refine-boundary)
 template <int pred>
-int run(const char* out_path, bool flux_form, bool periodic, const char* save_dir, const char* save_name)
+int run(const char* out_path, bool flux_form, bool periodic, bool default_config, const char* save_dir, const char* save_name)
 {
     constexpr std::size_t dim = 2;
     std::array<double, dim> a{{1, 1}};
@@ -50,7 +52,11 @@ int run(const char* out_path, bool flux_form, bool periodic, const char* save_di
     double t   = 0.;
 
     const samurai::Box<double, dim> box({0., 0.}, {1., 1.});
-    auto config = samurai::mesh_config<dim, pred>().min_level(4).max_level(10).max_stencil_size(2).disable_minimal_ghost_width();
+    auto config = samurai::mesh_config<dim, pred>().min_level(4).max_level(10);
+    if (!default_config)
+    {
+        config.max_stencil_size(2).disable_minimal_ghost_width();
+    }
     if (periodic)
     {
         config.periodic(true);
@@ -134,17 +140,20 @@ int main(int argc, char** argv)
 {
     if (argc < 3)
     {
-        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt> [upwind|convection|periodic [<dir> <name>]]\n");
+        std::fprintf(stderr, "usage: advection_2d <pred 0|1> <out.txt> [upwind|convection|periodic|default|refine_boundary [<dir> <name>]]\n");
         return 2;
     }
-    const bool flux_form = argc > 3 && std::string(argv[3]) == "convection";
-    const bool periodic  = argc > 3 && std::string(argv[3]) == "periodic";
+    const std::string mode = argc > 3 ? argv[3] : "";
+    const bool flux_form   = mode == "convection";
+    const bool periodic    = mode == "periodic";
+    const bool dflt        = mode == "default" || mode == "refine_boundary";
+    samurai::args::refine_boundary = mode == "refine_boundary";
     const char* save_dir  = argc > 5 ? argv[4] : nullptr;
     const char* save_name = argc > 5 ? argv[5] : nullptr;
     try
     {
-        return std::atoi(argv[1]) == 0 ? run<0>(argv[2], flux_form, periodic, save_dir, save_name)
-                                       : run<1>(argv[2], flux_form, periodic, save_dir, save_name);
+        return std::atoi(argv[1]) == 0 ? run<0>(argv[2], flux_form, periodic, dflt, save_dir, save_name)
+                                       : run<1>(argv[2], flux_form, periodic, dflt, save_dir, save_name);
     }
     catch (const std::exception& e)
     {

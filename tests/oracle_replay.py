@@ -75,13 +75,15 @@ def save_sequence(path, cells0, steps):
 
 
 def load_sequence(path):
-    f = np.load(path)
-    ends = np.cumsum(f["counts"])
-    meshes = [(f["level"][e - n:e], f["coords"][e - n:e]) for n, e in zip(f["counts"], ends)]
+    # each member of the archive is read once (indexing an NpzFile reads the member from the file again)
+    with np.load(path) as f:
+        level, coords, counts, per_step = f["level"], f["coords"], f["counts"], f["per_step"]
+    ends = np.cumsum(counts)
+    meshes = [(level[e - n:e], coords[e - n:e]) for n, e in zip(counts, ends)]
     steps, k = [], 1
-    for n in f["per_step"]:
+    for n in per_step:
         steps.append(meshes[k:k + n])
-        k += n
+        k += int(n)
     return meshes[0], steps
 
 

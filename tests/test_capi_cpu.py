@@ -75,7 +75,7 @@ def test_batch_argument_checks():
 
 def test_mesh_create_rejects_unsupported_configurations():
     """sg_mesh_create checks its configuration before touching a device:
-    dimension 2 or 3, 1 <= min_level <= max_level <= 23, stencil radius 1,
+    dimension 2 or 3, 1 <= min_level <= max_level <= 23, stencil radius 1 or 2,
     prediction radius 0 or 1 (include/samurai_gpu.h)."""
     import ctypes
 
@@ -89,7 +89,7 @@ def test_mesh_create_rejects_unsupported_configurations():
         (2, 0, 5, 1, 1, 1),   # min_level >= 1
         (2, 6, 5, 1, 1, 1),   # min_level <= max_level
         (2, 2, 24, 1, 1, 1),  # max_level <= 23
-        (2, 2, 5, 2, 1, 1),   # stencil radius 1 only
+        (2, 2, 5, 3, 1, 1),   # stencil radius 1 or 2
         (2, 2, 5, 1, 2, 1),   # prediction radius 0 or 1
     ]
     for args in bad:

@@ -171,6 +171,34 @@ def test_demo_periodic_matches_oracle(tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["default", "refine_boundary"])
+def test_demo_default_config_matches_oracle(tmp_path, mode):
+    """The demo with samurai's default configuration, mra::make_mesh(box,
+    mesh_config<2>().min_level(4).max_level(10)) without
+    disable_minimal_ghost_width() (max_stencil_radius 2), and with
+    samurai::args::refine_boundary, against the oracle running the same loop."""
+    from advection_cases import demo_time_loop, disc
+    from oracle.pyoracle import OracleSim
+
+    exe = compile_demo(tmp_path)
+    out = os.path.join(str(tmp_path), "out.txt")
+    subprocess.check_call([exe, "1", out, mode])
+    lines = open(out).read().split("\n")
+    rows = np.array([[float(v) for v in l.split()] for l in lines[1:] if l.strip()])
+    o = OracleSim(2, 4, 10, 2, 1)
+    o.set_refine_boundary(mode == "refine_boundary")
+    lv, co, _ = o.cells()
+    o.set_cell_values(disc(lv, co))
+    o.adapt(2e-4, 1.0)
+    nt = demo_time_loop(o, 0.5 / 1024, 0.01, 2e-4, 1.0, (1.0, 1.0))
+    assert int(lines[0]) == nt
+    lv, co, _ = o.cells()
+    assert np.array_equal(rows[:, 0].astype(int), lv)
+    assert np.array_equal(rows[:, 1:3].astype(int), co)
+    assert np.array_equal(rows[:, 3], o.cell_values())
+
+
+@pytest.mark.gpu
 def test_for_each_interval_through_the_header(tmp_path):
     """for_each_interval and u(level, i, j) of the C++ header after an
     adaptation: the oracle's leaf intervals and values."""

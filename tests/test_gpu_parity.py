@@ -457,7 +457,7 @@ def test_refine_boundary(sg, dim):
 
 def test_mesh_beyond_device_memory_is_refused(sg):
     """3D max_level 12: the dense level slabs of the mesh and of one field need
-    about 0.9 TB, more than the device holds: SG_ERR_CAPACITY (status 3) with
+    about 2.3 TB, more than the device holds: SG_ERR_CAPACITY (status 3) with
     the sizes, before any allocation"""
     with pytest.raises(sg.SamuraiGpuError, match=r"status 3\).*GB of device memory"):
         sg.MRMesh(3, 3, 12)
@@ -489,3 +489,30 @@ def test_adaptation_graph_matches_pass_by_pass(sg, dim, minl, maxl):
         for s in (a_graph, a_pass):
             s.update_ghost()
             s.upwind(vel, dt)
+
+
+@pytest.mark.parametrize("dim,scheme", [(2, 0), (2, 1), (2, 2), (3, 0)])
+def test_step_graph_matches_separate_calls(sg, dim, scheme):
+    """sg_step (the whole time step as one graph) gives what adapt,
+    update_ghost_mr, upwind and swap give as separate calls, bit for bit,
+    including the first step from the uniform mesh, whose last Harten pass
+    still changes the mesh"""
+    minl, maxl = (2, 8) if dim == 2 else (2, 5)
+    s_one, s_sep = sg.AdvectionSim(dim, minl, maxl), sg.AdvectionSim(dim, minl, maxl)
+    lv, co, _ = s_one.cells()
+    f = shapes_2d(29, 6, 6) if dim == 2 else ball_3d(13)
+    for s in (s_one, s_sep):
+        s.set_cell_values(f(lv, co))
+    vel = [1.0, -0.5] if dim == 2 else [1.0, -0.5, 0.75]
+    dt = 0.3 / (1 << maxl)
+    for it in range(8):
+        eps = 1e-4 if it % 3 else 5e-3
+        p1 = s_one.step(eps, 2.0, vel, dt, scheme)
+        p2 = s_sep.adapt(eps, 2.0)
+        s_sep.update_ghost()
+        s_sep.upwind(vel, dt, scheme)
+        assert p1 == p2, "it %d: Harten passes" % it
+        lg, cg, ig = s_one.cells()
+        lp, cp, ip = s_sep.cells()
+        assert np.array_equal(lg, lp) and np.array_equal(cg, cp) and np.array_equal(ig, ip), "it %d: cells" % it
+        assert np.array_equal(s_one.cell_values(), s_sep.cell_values()), "it %d: values" % it
