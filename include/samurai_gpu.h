@@ -102,10 +102,11 @@ int sg_mesh_version(sg_mesh_t mesh, unsigned long long* version);
  * as in samurai; it applies to the adaptations of this mesh (a process-wide flag in samurai). */
 int sg_mesh_set_refine_boundary(sg_mesh_t mesh, int enable);
 
-/* Without a samurai counterpart: how an adaptation runs.  enable = 1 (the default): the whole of sg_adapt /
- * sg_adapt_fields is one captured graph in which each Harten pass, the second half of a pass (new mesh,
- * update_fields) and the graduation iterations run under device-side conditions, with one host synchronisation at
- * the end; enable = 0: pass by pass, the host reading the fixed-point test after each pass.  Both give the same
+/* Without a samurai counterpart: how an adaptation runs.  enable = 1: the whole of sg_adapt / sg_adapt_fields (and
+ * of sg_step) is one captured graph in which each Harten pass, the second half of a pass (new mesh, update_fields)
+ * and the graduation iterations run under device-side conditions (conditional graph nodes), with one host
+ * synchronisation at the end; enable = 0 (the default, unless the launch-shape cache chose otherwise): pass by pass,
+ * one captured graph per half pass and the host reading the fixed-point test after each pass.  Both give the same
  * results; the named timers and the kernel trace use the pass-by-pass path while they are on. */
 int sg_mesh_set_adapt_graph(sg_mesh_t mesh, int enable);
 
@@ -119,9 +120,10 @@ int sg_mesh_set_adapt_graph(sg_mesh_t mesh, int enable);
 int sg_autotune(sg_field_t u, sg_field_t unp1, double eps, double regularity, const double* a, double dt, int scheme, int steps,
                 double* default_ms, double* tuned_ms);
 /* the mesh's launch shape: threads per block, grid limit (blocks of 8 warps), one-block chain limits in words per
- * level of the mesh, field and tag-finalisation chains */
+ * level of the mesh, field and tag-finalisation chains, and 1 when the adaptation runs as one graph with conditional
+ * nodes (0: pass by pass); any pointer may be NULL */
 int sg_launch_shape(sg_mesh_t mesh, int* block, long long* max_blocks, long long* fuse_mesh_words, long long* fuse_field_words,
-                    long long* fuse_max_words);
+                    long long* fuse_max_words, int* graphed_adapt);
 
 /* samurai's named timers (timers.hpp:111-1036, printed with --timers): CUDA-event timers per phase.
  * ids: 0 mesh adaptation, 1 ghost update, 2 detail computation, 3 tag cells, 4 tag finalization,

@@ -3,9 +3,10 @@
 // The level-serial chains of the step are latency-bound and the FP64 list
 // kernels compete for the narrow FP64 pipe, so the best launch shapes depend
 // on the device and on the size of the mesh: the threads per block of the
-// FP64 list kernels, the grid limit of the one-warp-per-word launches and the
+// FP64 list kernels, the grid limit of the one-warp-per-word launches, the
 // level sizes up to which a chain (ghost update, tag finalisation, mesh
-// construction) runs its levels in one block.  sg_autotune times the time
+// construction) runs its levels in one block, and whether the adaptation runs
+// as one graph with conditional nodes or pass by pass.  sg_autotune times the time
 // step of a given problem under candidate shapes (coordinate descent, each
 // candidate from the same saved state, its graphs captured afresh), keeps the
 // fastest on the mesh and caches it per device and level range; later meshes
@@ -36,6 +37,7 @@ namespace sg
         {
             int block;
             long long max_blocks, fuse_mesh, fuse_field, fuse_max;
+            int graphed; // the adaptation as one graph with conditional nodes (1) or pass by pass (0)
         };
 
         using TuneKey = std::tuple<std::string, int, int, int>; // device name, dim, min_level, max_level
@@ -57,7 +59,7 @@ namespace sg
             return n;
         }
 
-        // SG_TUNE_FILE: lines "device dim min max block max_blocks fuse_mesh fuse_field fuse_max" (the last line of a
+        // SG_TUNE_FILE: lines "device dim min max block max_blocks fuse_mesh fuse_field fuse_max graphed" (the last line of a
         // key wins); read once, under the cache mutex
         void read_tune_file()
         {
@@ -77,13 +79,13 @@ namespace sg
                 return;
             }
             char name[256];
-            int dim, lo, hi, block;
+            int dim, lo, hi, block, gr;
             long long mb, fm, ff, fx;
-            while (std::fscanf(f, "%255s %d %d %d %d %lld %lld %lld %lld", name, &dim, &lo, &hi, &block, &mb, &fm, &ff, &fx) == 9)
+            while (std::fscanf(f, "%255s %d %d %d %d %lld %lld %lld %lld %d", name, &dim, &lo, &hi, &block, &mb, &fm, &ff, &fx, &gr) == 10)
             {
-                if (block >= 32 && block <= 1024 && block % 32 == 0 && mb > 0 && fm >= 0 && ff >= 0 && fx >= 0)
+                if (block >= 32 && block <= 1024 && block % 32 == 0 && mb > 0 && fm >= 0 && ff >= 0 && fx >= 0 && (gr == 0 || gr == 1))
                 {
-                    g_tune_cache[TuneKey{name, dim, lo, hi}] = LaunchShape{block, mb, fm, ff, fx};
+                    g_tune_cache[TuneKey{name, dim, lo, hi}] = LaunchShape{block, mb, fm, ff, fx, gr};
                 }
             }
             std::fclose(f);
@@ -98,8 +100,8 @@ namespace sg
             }
             if (FILE* f = std::fopen(path, "a"))
             {
-                std::fprintf(f, "%s %d %d %d %d %lld %lld %lld %lld\n", std::get<0>(k).c_str(), std::get<1>(k), std::get<2>(k), std::get<3>(k),
-                             s.block, s.max_blocks, s.fuse_mesh, s.fuse_field, s.fuse_max);
+                std::fprintf(f, "%s %d %d %d %d %lld %lld %lld %lld %d\n", std::get<0>(k).c_str(), std::get<1>(k), std::get<2>(k), std::get<3>(k),
+                             s.block, s.max_blocks, s.fuse_mesh, s.fuse_field, s.fuse_max, s.graphed);
                 std::fclose(f);
             }
         }
@@ -117,14 +119,15 @@ namespace sg
 
         LaunchShape shape_of(const Ctx& c)
         {
-            return LaunchShape{c.block, c.max_blocks, c.fuse_words_mesh, c.fuse_words_field, c.fuse_words_max};
+            return LaunchShape{c.block, c.max_blocks, c.fuse_words_mesh, c.fuse_words_field, c.fuse_words_max, c.graphed_adapt ? 1 : 0};
         }
 
         // applies a shape to a mesh (its captured graphs were recorded with the old one and are dropped)
         void apply_shape(Ctx& c, const LaunchShape& s)
         {
-            c.block      = s.block;
-            c.max_blocks = s.max_blocks;
+            c.block         = s.block;
+            c.max_blocks    = s.max_blocks;
+            c.graphed_adapt = s.graphed != 0;
             set_fusion(c, s.fuse_mesh, s.fuse_field, s.fuse_max);
         }
     } // namespace
@@ -159,6 +162,10 @@ namespace sg
         if (!env_set("SG_FUSE_WORDS_MAX"))
         {
             c.fuse_words_max = s.fuse_max;
+        }
+        if (!env_set("SG_GRAPHED_ADAPT"))
+        {
+            c.graphed_adapt = s.graphed != 0;
         }
     }
 } // namespace sg
@@ -226,7 +233,7 @@ extern "C"
                 {
                     return st;
                 }
-                const int n = rep == 0 ? 2 : steps;
+                const int n = rep == 0 ? std::max(steps, 8) : steps; // rep 0 captures the graphs of every buffer combination
                 cudaStreamSynchronize(c.stream);
                 cudaEventRecord(e0, c.stream);
                 for (int k = 0; k < n; ++k)
@@ -261,22 +268,27 @@ extern "C"
         const std::vector<long long> blocks = {128, 256, 512};
         const std::vector<long long> grids  = {152LL * 4, 152LL * 8, 152LL * 16};
         const std::vector<long long> fuses  = {0, 32, 128, 512};
-        for (int param = 0; param < 4 && !st; ++param)
+        const std::vector<long long> paths  = {0, 1};
+        for (int param = 0; param < 5 && !st; ++param)
         {
-            const std::vector<long long>& cands = param == 0 ? blocks : (param == 1 ? grids : fuses);
+            const std::vector<long long>& cands = param == 0 ? paths : (param == 1 ? blocks : (param == 2 ? grids : fuses));
             const sg::LaunchShape from          = best;
             for (long long v : cands)
             {
                 sg::LaunchShape s = from;
                 if (param == 0)
                 {
-                    s.block = static_cast<int>(v);
+                    s.graphed = static_cast<int>(v);
                 }
                 else if (param == 1)
                 {
-                    s.max_blocks = v;
+                    s.block = static_cast<int>(v);
                 }
                 else if (param == 2)
+                {
+                    s.max_blocks = v;
+                }
+                else if (param == 3)
                 {
                     s.fuse_field = v;
                 }
@@ -284,7 +296,8 @@ extern "C"
                 {
                     s.fuse_max = v;
                 }
-                if (s.block == from.block && s.max_blocks == from.max_blocks && s.fuse_field == from.fuse_field && s.fuse_max == from.fuse_max)
+                if (s.graphed == from.graphed && s.block == from.block && s.max_blocks == from.max_blocks && s.fuse_field == from.fuse_field
+                    && s.fuse_max == from.fuse_max)
                 {
                     continue;
                 }
@@ -332,7 +345,7 @@ extern "C"
     SG_API_CATCH(sg_autotune)
 
     int sg_launch_shape(sg_mesh_t mesh, int* block, long long* max_blocks, long long* fuse_mesh_words, long long* fuse_field_words,
-                        long long* fuse_max_words)
+                        long long* fuse_max_words, int* graphed_adapt)
     try
     {
         if (!mesh)
@@ -359,6 +372,10 @@ extern "C"
         if (fuse_max_words)
         {
             *fuse_max_words = c.fuse_words_max;
+        }
+        if (graphed_adapt)
+        {
+            *graphed_adapt = c.graphed_adapt ? 1 : 0;
         }
         return SG_OK;
     }

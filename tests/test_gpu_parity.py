@@ -468,12 +468,14 @@ def test_mesh_beyond_device_memory_is_refused(sg):
 
 @pytest.mark.parametrize("dim,minl,maxl", [(2, 2, 9), (3, 2, 6)])
 def test_adaptation_graph_matches_pass_by_pass(sg, dim, minl, maxl):
-    """the adaptation as one graph with device-side conditions (the default)
-    and pass by pass with host tests give identical meshes, values and pass
+    """the adaptation as one graph with device-side conditions and pass by
+    pass with host tests (the default) give identical meshes, values and pass
     counts, from a uniform start (many passes, graduation loops) and along steps"""
     a_graph = sg.AdvectionSim(dim, minl, maxl)
     a_pass = sg.AdvectionSim(dim, minl, maxl)
+    a_graph.mesh.set_adapt_graph(True)
     a_pass.mesh.set_adapt_graph(False)
+    assert a_graph.mesh.launch_shape()["graphed_adapt"] and not a_pass.mesh.launch_shape()["graphed_adapt"]
     lv, co, _ = a_graph.cells()
     f = shapes_2d(23, 8, 8) if dim == 2 else ball_3d(11)
     for s in (a_graph, a_pass):
@@ -491,14 +493,17 @@ def test_adaptation_graph_matches_pass_by_pass(sg, dim, minl, maxl):
             s.upwind(vel, dt)
 
 
-@pytest.mark.parametrize("dim,scheme", [(2, 0), (2, 1), (2, 2), (3, 0)])
-def test_step_graph_matches_separate_calls(sg, dim, scheme):
-    """sg_step (the whole time step as one graph) gives what adapt,
-    update_ghost_mr, upwind and swap give as separate calls, bit for bit,
+@pytest.mark.parametrize("dim,scheme,graphed", [(2, 0, True), (2, 1, True), (2, 2, True), (3, 0, True), (2, 0, False), (3, 0, False)])
+def test_step_graph_matches_separate_calls(sg, dim, scheme, graphed):
+    """sg_step (the whole time step as one graph on the graphed adaptation
+    path, the per-pass graphs otherwise) gives what adapt, update_ghost_mr,
+    upwind and swap give as separate pass-by-pass calls, bit for bit,
     including the first step from the uniform mesh, whose last Harten pass
     still changes the mesh"""
     minl, maxl = (2, 8) if dim == 2 else (2, 5)
     s_one, s_sep = sg.AdvectionSim(dim, minl, maxl), sg.AdvectionSim(dim, minl, maxl)
+    s_one.mesh.set_adapt_graph(graphed)
+    s_sep.mesh.set_adapt_graph(False)
     lv, co, _ = s_one.cells()
     f = shapes_2d(29, 6, 6) if dim == 2 else ball_3d(13)
     for s in (s_one, s_sep):
