@@ -10,14 +10,13 @@
 // ValAcc is the plain forward: V = double, reads and writes go to the dense
 // slab, and the kernels compile to exactly the arithmetic they spell out.
 //
-// TapeAcc records the operator instead of applying it: V is a linear form
-// (a short list of (element, weight) terms; constants drop out), get(e) is the
-// form "1 * element e", and put(e, form) appends one record (e <- j, w) per
-// term to a device tape (one record with j = -1 when the form has no term, so
-// the transpose still knows that e was overwritten).  On a frozen mesh every
-// operator of the path is linear in the field (the Dirichlet constant is an
-// affine offset with no derivative), so the tape of a launch is its matrix,
-// and the adjoint applies the launches' transposes in reverse order.
+// RevAcc applies the transpose of the operator instead: V is a linear form (a
+// short list of (element, weight) terms; constants drop out), get(e) is the
+// form "1 * element e", and put(e, form) scatters the adjoint of e onto the
+// form's elements.  On a frozen mesh every operator of the path is linear in
+// the field (the Dirichlet constant is an affine offset with no derivative),
+// so a launch's puts are the rows of its matrix, and the adjoint runs the
+// launches with RevAcc in reverse order.
 #pragma once
 
 #include <cstdint>
@@ -108,22 +107,20 @@ namespace sg
         return a + (-b);
     }
 
-    // records of a tape, structure of arrays
-    struct TapeDev
-    {
-        int* dst;           // element written
-        int* src;           // element read, -1 for "overwritten with a constant"
-        double* w;          // weight
-        long long* count;   // records appended so far
-        long long cap;      // capacity in records
-        int* overflow;      // set when a record did not fit or a form overflowed
-    };
-
+    // RevAcc: put(e, form) adds w * lam_in[e] to
+    // lam_out[j] for every term (j, w) of the form and, for an operator that
+    // updates the field in place, clears lam_in[e] (e was overwritten).  Within
+    // one launch of the path's operators every element is written at most once
+    // and no written element is read, so the transpose of a launch is the set
+    // of its puts in any order; the launches themselves run in reverse order.
     template <int CAP>
-    struct TapeAcc
+    struct RevAcc
     {
         using V = LinForm<CAP>;
-        TapeDev t;
+        double* lam_in;  // adjoint of the elements the operator writes
+        double* lam_out; // adjoint of the elements it reads (accumulated)
+        int* overflow;   // set when a form overflowed
+        int in_place;    // lam_in == lam_out: clear lam_in[e] after scattering it
         __device__ __forceinline__ V get(long long e) const
         {
             V r;
@@ -136,28 +133,24 @@ namespace sg
         {
             if (v.n > CAP)
             {
-                atomicOr(t.overflow, 1);
+                atomicOr(overflow, 1);
                 return;
             }
-            const int n        = v.n > 0 ? v.n : 1;
-            const long long at = static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(t.count), static_cast<unsigned long long>(n)));
-            if (at + n > t.cap)
+            const double ld = lam_in[e];
+            if (ld != 0.)
             {
-                atomicOr(t.overflow, 2);
-                return;
+                for (int k = 0; k < v.n; ++k)
+                {
+                    const double t = v.w[k] * ld;
+                    if (t != 0.)
+                    {
+                        atomicAdd(lam_out + v.idx[k], t);
+                    }
+                }
             }
-            if (v.n == 0)
+            if (in_place)
             {
-                t.dst[at] = static_cast<int>(e);
-                t.src[at] = -1;
-                t.w[at]   = 0.;
-                return;
-            }
-            for (int k = 0; k < v.n; ++k)
-            {
-                t.dst[at + k] = static_cast<int>(e);
-                t.src[at + k] = v.idx[k];
-                t.w[at + k]   = v.w[k];
+                lam_in[e] = 0.;
             }
         }
         __device__ __forceinline__ static V konst(double)

@@ -11,12 +11,13 @@
 //   replay    the same steps on the recorded meshes from any u0 and velocity:
 //             the frozen-mesh map whose derivative the adjoint computes;
 //   backward  segment by segment from the last: recompute the segment from its
-//             checkpoint on the recorded meshes, recording every ghost-update
-//             and update_fields launch onto a tape (its matrix, see
-//             sg_access.cuh) and keeping the ghosted field of every step; then
-//             walk the segment backwards applying transposes: the upwind step
-//             (and its velocity derivative) by dedicated kernels, the tape
-//             launches by scatter kernels, in reverse launch order.
+//             checkpoint on the recorded meshes, keeping the ghosted field of
+//             every step; then walk the segment backwards applying transposes:
+//             the upwind step (and its velocity derivative) by dedicated
+//             kernels, the ghost update and update_fields by their own kernels
+//             on the transposing accessor (sg_access.cuh), launched in reverse
+//             order (a captured ghost update replayed backwards), rebuilding
+//             the recorded meshes on the way back.
 //
 // Every operator of a step is linear in the field on a frozen mesh; the
 // Dirichlet value only adds a constant.  The upwind step is bilinear in (a, u);
@@ -51,38 +52,6 @@ namespace sg
             return static_cast<long long>(gridDim.x) * blockDim.x;
         }
 
-        __global__ void k_tape_mark(const long long* count, long long* marks, int p)
-        {
-            marks[p] = *count;
-        }
-
-        // transpose of one recorded launch: lam_j[src] += w * lam_i[dst]
-        __global__ void k_tape_scatter(const int* __restrict__ dst, const int* __restrict__ src, const double* __restrict__ w, long long b,
-                                       long long e, const double* lam_i, double* lam_j)
-        {
-            for (long long r = b + gtid(); r < e; r += gstride())
-            {
-                const int j = src[r];
-                if (j >= 0)
-                {
-                    const double v = w[r] * lam_i[dst[r]];
-                    if (v != 0.)
-                    {
-                        atomicAdd(lam_j + j, v);
-                    }
-                }
-            }
-        }
-
-        // the entries a launch overwrote do not reach back past it
-        __global__ void k_tape_zero(const int* __restrict__ dst, long long b, long long e, double* lam)
-        {
-            for (long long r = b + gtid(); r < e; r += gstride())
-            {
-                lam[dst[r]] = 0.;
-            }
-        }
-
         __device__ __forceinline__ double pow2d(int l)
         {
             return __longlong_as_double(static_cast<long long>(1023 + l) << 52);
@@ -113,10 +82,10 @@ namespace sg
         // one mesh (the forward is k_upwind); gather form, one thread per
         // dense element, deterministic.
         template <int DIM>
-        __global__ void k_upwind_adjoint(const Geom* __restrict__ gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
+        __global__ void k_upwind_adjoint(const __grid_constant__ Geom gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
                                          double* __restrict__ mu, UpwindAdj p)
         {
-            const Geom& g       = *gp;
+            const Geom& g       = gp;
             const long long tot = 32 * g.total_words;
             for (long long k = gtid(); k < tot; k += gstride())
             {
@@ -156,10 +125,10 @@ namespace sg
 
         // per-block partial sums of lam . dU/da_d u for the leaf cells
         template <int DIM>
-        __global__ void k_upwind_da(const Geom* __restrict__ gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
+        __global__ void k_upwind_da(const __grid_constant__ Geom gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
                                     const double* __restrict__ u, UpwindAdj p, double* partial)
         {
-            const Geom& g       = *gp;
+            const Geom& g       = gp;
             const long long tot = 32 * g.total_words;
             double acc[3]       = {0., 0., 0.};
             for (long long k = gtid(); k < tot; k += gstride())
@@ -210,17 +179,38 @@ namespace sg
             }
         }
 
-        // ga[d] += sum of the partials, in block order (deterministic)
+        // ga[d] += sum of the partials: thread t of one ABLOCK-thread block sums partials t, t + ABLOCK, ... in that
+        // order, then a fixed tree adds the threads' sums (deterministic: the order depends on nb only)
         __global__ void k_sum_partials(const double* partial, int nb, double* ga)
         {
+            __shared__ double red[3][ABLOCK];
+            double acc[3] = {0., 0., 0.};
+            for (int k = static_cast<int>(threadIdx.x); k < nb; k += ABLOCK)
+            {
+                for (int d = 0; d < 3; ++d)
+                {
+                    acc[d] += partial[3 * k + d];
+                }
+            }
+            for (int d = 0; d < 3; ++d)
+            {
+                red[d][threadIdx.x] = acc[d];
+            }
+            __syncthreads();
+            for (int h = ABLOCK / 2; h > 0; h >>= 1)
+            {
+                if (static_cast<int>(threadIdx.x) < h)
+                {
+                    for (int d = 0; d < 3; ++d)
+                    {
+                        red[d][threadIdx.x] += red[d][threadIdx.x + h];
+                    }
+                }
+                __syncthreads();
+            }
             if (threadIdx.x < 3)
             {
-                double s = 0.;
-                for (int k = 0; k < nb; ++k)
-                {
-                    s += partial[3 * k + threadIdx.x];
-                }
-                ga[threadIdx.x] += s;
+                ga[threadIdx.x] += red[threadIdx.x][0];
             }
         }
 
@@ -280,13 +270,9 @@ struct sg_adjoint_s
     double* d_uT     = nullptr; // final leaf values of the last forward
     long long uT_cap = 0;
 
-    // tape and adjoint buffers
-    sg::TapeDev tape{};
-    long long tape_cap = 0;
-    long long* d_marks = nullptr;
-    long long* h_marks = nullptr;
-    int marks_cap      = 0;
-    double* lam[2]     = {nullptr, nullptr};
+    // adjoint buffers
+    int* d_overflow = nullptr; // set when a linear form of the transposed operators overflowed
+    double* lam[2]  = {nullptr, nullptr};
     std::vector<double*> ug; // ghosted field of each step of a segment
     double* d_partial = nullptr;
     double* d_ga      = nullptr;
@@ -505,35 +491,15 @@ namespace
     }
 
     // the recorded steps [s, e) on their meshes, value mode, from the field
-    // already in u (on the mesh of step s, loaded by the caller).  With a
-    // tape: every ghost/update_fields launch is also recorded (phases
-    // appended to `phases`), and the ghosted field of step n is kept in ug[n-s].
-    enum PhaseKind : int
-    {
-        PH_GHOST    = 0, // in place on the field
-        PH_TRANSFER = 1, // update_fields: new field from the old one
-        PH_UPWIND   = 2  // the upwind step of step `step`
-    };
-    struct Phase
-    {
-        int kind;
-        int step;
-        int mesh; // index in bits of the mesh the upwind ran on
-    };
-
-    int replay_range(sg_adjoint_t adj, int s, int e, bool taped, std::vector<Phase>* phases, bool store_ckpt)
+    // already in u (on the mesh of step s, loaded by the caller); with keep_ug
+    // the ghosted field of step n is kept in ug[n-s] (the velocity derivative
+    // of its upwind step reads it)
+    int replay_range(sg_adjoint_t adj, int s, int e, bool keep_ug, bool store_ckpt)
     {
         Ctx& c               = ctx_of(adj);
         sg::DeviceField& u   = adj->u->f;
         sg::DeviceField& up1 = adj->unp1->f;
         int st;
-        int np = 0;
-        auto mark = [&]()
-        {
-            sg::k_tape_mark<<<1, 1, 0, c.stream>>>(adj->tape.count, adj->d_marks, np);
-            ++np;
-        };
-        auto room = [&](int extra) { return np + extra < adj->marks_cap; };
         for (int n = s; n < e; ++n)
         {
             const auto& S = adj->steps[static_cast<size_t>(n)];
@@ -551,41 +517,11 @@ namespace
                 {
                     return st;
                 }
-                if (taped)
-                {
-                    if (!room(256))
-                    {
-                        c.err = "adjoint: too many launches in one segment";
-                        return SG_ERR_CAPACITY;
-                    }
-                    const int p0 = np;
-                    if ((st = sg::ghost_tape(c, c.m(), adj->tape, u.has_bc, u.bc_value, mark)))
-                    {
-                        return st;
-                    }
-                    for (int p = p0; p < np; ++p)
-                    {
-                        phases->push_back({PH_GHOST, n, -1});
-                    }
-                }
                 sg::DeviceMesh& nm = c.spare();
                 cudaMemcpyAsync(nm.cells, adj->bits[static_cast<size_t>(S.mesh0 + t)], bitmap_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
-                if ((st = sg::build_mesh(c, nm)))
+                if ((st = sg::build_mesh(c, nm)) || (st = sg::update_fields_value(c, c.m(), nm, u.data, u.spare)))
                 {
                     return st;
-                }
-                if ((st = sg::update_fields_value(c, c.m(), nm, u.data, u.spare)))
-                {
-                    return st;
-                }
-                if (taped)
-                {
-                    if ((st = sg::update_fields_tape(c, c.m(), nm, adj->tape)))
-                    {
-                        return st;
-                    }
-                    mark();
-                    phases->push_back({PH_TRANSFER, n, -1});
                 }
                 nm.host_valid = false;
                 std::swap(u.data, u.spare);
@@ -596,25 +532,9 @@ namespace
             {
                 return st;
             }
-            if (taped)
+            if (keep_ug)
             {
-                if (!room(256))
-                {
-                    c.err = "adjoint: too many launches in one segment";
-                    return SG_ERR_CAPACITY;
-                }
-                const int p0 = np;
-                if ((st = sg::ghost_tape(c, c.m(), adj->tape, u.has_bc, u.bc_value, mark)))
-                {
-                    return st;
-                }
-                for (int p = p0; p < np; ++p)
-                {
-                    phases->push_back({PH_GHOST, n, -1});
-                }
                 cudaMemcpyAsync(adj->ug[static_cast<size_t>(n - s)], u.data, dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
-                mark(); // empty phase: keeps marks and phases aligned
-                phases->push_back({PH_UPWIND, n, S.mesh0 + S.n_trans});
             }
             u.ghosts_valid = false;
             if ((st = sg::upwind(c, u, up1, adj->a, adj->dt, adj->scheme)))
@@ -649,28 +569,6 @@ namespace
         return cuda_ok(c, "adjoint final field");
     }
 
-    int ensure_tape(sg_adjoint_t adj, long long cap)
-    {
-        Ctx& c = ctx_of(adj);
-        if (cap <= adj->tape_cap)
-        {
-            return SG_OK;
-        }
-        dfree(adj->tape.dst);
-        dfree(adj->tape.src);
-        dfree(adj->tape.w);
-        if (dmalloc(&adj->tape.dst, static_cast<size_t>(cap)) || dmalloc(&adj->tape.src, static_cast<size_t>(cap))
-            || dmalloc(&adj->tape.w, static_cast<size_t>(cap)))
-        {
-            c.err = "adjoint: out of device memory for the tape";
-            adj->tape_cap = 0;
-            return SG_ERR_CUDA;
-        }
-        adj->tape_cap = cap;
-        adj->tape.cap = cap;
-        return SG_OK;
-    }
-
     sg::UpwindAdj upwind_adj(sg_adjoint_t adj)
     {
         sg::UpwindAdj p{};
@@ -685,64 +583,71 @@ namespace
         return p;
     }
 
-    // reverse pass over one segment whose phases and tape are recorded;
-    // lam[0] holds the adjoint of the field after the segment
-    int reverse_segment(sg_adjoint_t adj, int s, const std::vector<Phase>& phases)
+    // reverse pass over the steps [s, e) of one segment, replayed just before (the current mesh is the one the
+    // segment ends on, ug holds the ghosted field of each step); lam[0] holds the adjoint of the field after the
+    // segment and ends as the adjoint of the field at its start
+    int reverse_segment(sg_adjoint_t adj, int s, int e)
     {
-        Ctx& c = ctx_of(adj);
-        const long long tot = 32 * c.g.total_words;
-        const sg::UpwindAdj p = upwind_adj(adj);
-        const int nb_da = sg::grid_of(tot);
-        for (int k = static_cast<int>(phases.size()) - 1; k >= 0; --k)
+        Ctx& c                 = ctx_of(adj);
+        const sg::UpwindAdj p  = upwind_adj(adj);
+        const int nb_da        = sg::grid_of(32 * c.g.total_words);
+        const sg::DeviceField& u = adj->u->f;
+        int st;
+        for (int n = e - 1; n >= s; --n)
         {
-            const Phase& ph   = phases[static_cast<size_t>(k)];
-            const long long b = k > 0 ? adj->h_marks[k - 1] : 0;
-            const long long e = adj->h_marks[k];
-            if (ph.kind == PH_UPWIND)
+            const auto& S         = adj->steps[static_cast<size_t>(n)];
+            const uint32_t* cells = adj->bits[static_cast<size_t>(S.mesh0 + S.n_trans)];
+            const double* ugn     = adj->ug[static_cast<size_t>(n - s)];
+            // the upwind step u <- u - dt upwind(a, u) and its velocity derivative
+            if (p.scheme == 0)
             {
-                const uint32_t* cells = adj->bits[static_cast<size_t>(ph.mesh)];
-                if (p.scheme == 0)
-                {
-                    if (c.g.dim == 2)
-                    {
-                        sg::k_upwind_da<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->ug[static_cast<size_t>(ph.step - s)], p,
-                                                                              adj->d_partial);
-                    }
-                    else
-                    {
-                        sg::k_upwind_da<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->ug[static_cast<size_t>(ph.step - s)], p,
-                                                                              adj->d_partial);
-                    }
-                    sg::k_sum_partials<<<1, 32, 0, c.stream>>>(adj->d_partial, nb_da, adj->d_ga);
-                }
                 if (c.g.dim == 2)
                 {
-                    sg::k_upwind_adjoint<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->lam[1], p);
+                    sg::k_upwind_da<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], ugn, p, adj->d_partial);
                 }
                 else
                 {
-                    sg::k_upwind_adjoint<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.d_geom, cells, adj->lam[0], adj->lam[1], p);
+                    sg::k_upwind_da<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], ugn, p, adj->d_partial);
                 }
-                std::swap(adj->lam[0], adj->lam[1]);
+                sg::k_sum_partials<<<1, sg::ABLOCK, 0, c.stream>>>(adj->d_partial, nb_da, adj->d_ga);
             }
-            else if (ph.kind == PH_GHOST)
+            if (c.g.dim == 2)
             {
-                if (e > b)
-                {
-                    sg::k_tape_scatter<<<sg::grid_of(e - b), sg::ABLOCK, 0, c.stream>>>(adj->tape.dst, adj->tape.src, adj->tape.w, b, e, adj->lam[0],
-                                                                                         adj->lam[0]);
-                    sg::k_tape_zero<<<sg::grid_of(e - b), sg::ABLOCK, 0, c.stream>>>(adj->tape.dst, b, e, adj->lam[0]);
-                }
+                sg::k_upwind_adjoint<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], adj->lam[1], p);
             }
             else
             {
-                cudaMemsetAsync(adj->lam[1], 0, dense_bytes(c), c.stream);
-                if (e > b)
+                sg::k_upwind_adjoint<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], adj->lam[1], p);
+            }
+            std::swap(adj->lam[0], adj->lam[1]);
+            // the ghost update before it, on the step's last mesh
+            if ((st = sg::ghost_reverse(c, c.m(), adj->lam[0], adj->d_overflow, u.has_bc)))
+            {
+                return st;
+            }
+            // the adaptation's transitions, last first: update_fields from mesh t-1 to mesh t, then the ghost
+            // update that preceded it on mesh t-1
+            for (int t = S.n_trans; t >= 1; --t)
+            {
+                sg::DeviceMesh& om = c.spare();
+                cudaMemcpyAsync(om.cells, adj->bits[static_cast<size_t>(S.mesh0 + t - 1)], bitmap_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+                if ((st = sg::build_mesh(c, om)))
                 {
-                    sg::k_tape_scatter<<<sg::grid_of(e - b), sg::ABLOCK, 0, c.stream>>>(adj->tape.dst, adj->tape.src, adj->tape.w, b, e, adj->lam[0],
-                                                                                         adj->lam[1]);
+                    return st;
+                }
+                om.host_valid = false;
+                cudaMemsetAsync(adj->lam[1], 0, dense_bytes(c), c.stream);
+                if ((st = sg::update_fields_reverse(c, om, c.m(), adj->lam[0], adj->lam[1], adj->d_overflow)))
+                {
+                    return st;
                 }
                 std::swap(adj->lam[0], adj->lam[1]);
+                c.cur = 1 - c.cur;
+                ++c.mesh_version;
+                if ((st = sg::ghost_reverse(c, c.m(), adj->lam[0], adj->d_overflow, u.has_bc)))
+                {
+                    return st;
+                }
             }
         }
         return cuda_ok(c, "adjoint reverse");
@@ -804,7 +709,7 @@ extern "C"
         if (c.capacity >= (1LL << 31))
         {
             sg_adjoint_destroy(adj);
-            return afail(SG_ERR_CAPACITY, "sg_adjoint_create: the tape indexes elements with 32 bits; this mesh has more");
+            return afail(SG_ERR_CAPACITY, "sg_adjoint_create: the transposed operators index elements with 32 bits; this mesh has more");
         }
         if (sg::ensure_spare(c, adj->u->f) || push_current_bits(adj)
             || current_leaves(adj, adj->lev0, adj->co0, &adj->d_el0, &adj->n0, &adj->cap0) != SG_OK)
@@ -814,9 +719,7 @@ extern "C"
             sg_adjoint_destroy(adj);
             return code;
         }
-        adj->marks_cap = 1 << 16;
-        if (dmalloc(&adj->d_marks, static_cast<size_t>(adj->marks_cap)) || cudaMallocHost(reinterpret_cast<void**>(&adj->h_marks), sizeof(long long) * adj->marks_cap) != cudaSuccess
-            || dmalloc(&adj->tape.count, 1) || dmalloc(&adj->tape.overflow, 1) || dmalloc(&adj->lam[0], static_cast<size_t>(c.capacity))
+        if (dmalloc(&adj->d_overflow, 1) || dmalloc(&adj->lam[0], static_cast<size_t>(c.capacity))
             || dmalloc(&adj->lam[1], static_cast<size_t>(c.capacity)) || dmalloc(&adj->d_partial, static_cast<size_t>(3 * 152 * 16))
             || dmalloc(&adj->d_ga, 3))
         {
@@ -859,16 +762,7 @@ extern "C"
         dfree(adj->d_el0);
         dfree(adj->d_elT);
         dfree(adj->d_uT);
-        dfree(adj->tape.dst);
-        dfree(adj->tape.src);
-        dfree(adj->tape.w);
-        dfree(adj->tape.count);
-        dfree(adj->tape.overflow);
-        dfree(adj->d_marks);
-        if (adj->h_marks)
-        {
-            cudaFreeHost(adj->h_marks);
-        }
+        dfree(adj->d_overflow);
         dfree(adj->lam[0]);
         dfree(adj->lam[1]);
         dfree(adj->d_partial);
@@ -1090,7 +984,7 @@ extern "C"
         }
         int st;
         if ((st = load_mesh(adj, 0)) || (st = set_initial_field(adj, u0, adj->u->f.data))
-            || (st = replay_range(adj, 0, static_cast<int>(adj->steps.size()), false, nullptr, true)))
+            || (st = replay_range(adj, 0, static_cast<int>(adj->steps.size()), false, true)))
         {
             return afail(st, c.err.c_str());
         }
@@ -1137,54 +1031,29 @@ extern "C"
             }
             adj->ug.push_back(p);
         }
-        if ((st = ensure_tape(adj, std::max(adj->tape_cap, 8 * c.capacity))))
-        {
-            return afail(st, c.err.c_str());
-        }
-        std::vector<Phase> phases;
+        cudaMemsetAsync(adj->d_overflow, 0, sizeof(int), c.stream);
         for (int s = ((T - 1) / K) * K; s >= 0 && T > 0; s -= K)
         {
             const int e = std::min(T, s + K);
-            for (int attempt = 0;; ++attempt)
-            {
-                phases.clear();
-                cudaMemsetAsync(adj->tape.count, 0, sizeof(long long), c.stream);
-                cudaMemsetAsync(adj->tape.overflow, 0, sizeof(int), c.stream);
-                if ((st = load_mesh(adj, adj->steps[static_cast<size_t>(s)].mesh0)))
-                {
-                    return afail(st, c.err.c_str());
-                }
-                cudaMemcpyAsync(adj->u->f.data, adj->ckpt[static_cast<size_t>(s / K)], dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
-                if ((st = replay_range(adj, s, e, true, &phases, false)))
-                {
-                    return afail(st, c.err.c_str());
-                }
-                int overflow    = 0;
-                long long count = 0;
-                cudaMemcpyAsync(&overflow, adj->tape.overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
-                cudaMemcpyAsync(&count, adj->tape.count, sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
-                cudaMemcpyAsync(adj->h_marks, adj->d_marks, sizeof(long long) * phases.size(), cudaMemcpyDeviceToHost, c.stream);
-                if (cudaStreamSynchronize(c.stream) != cudaSuccess)
-                {
-                    return afail(SG_ERR_CUDA, "sg_adjoint_backward: CUDA error in the recomputation");
-                }
-                if (overflow & 1)
-                {
-                    return afail(SG_ERR_CAPACITY, "sg_adjoint_backward: a recorded operator has more terms than a form holds");
-                }
-                if (!(overflow & 2))
-                {
-                    break;
-                }
-                if (attempt > 4 || (st = ensure_tape(adj, std::max(2 * adj->tape_cap, count + count / 4))))
-                {
-                    return afail(SG_ERR_CUDA, "sg_adjoint_backward: the tape does not fit in device memory");
-                }
-            }
-            if ((st = reverse_segment(adj, s, phases)))
+            if ((st = load_mesh(adj, adj->steps[static_cast<size_t>(s)].mesh0)))
             {
                 return afail(st, c.err.c_str());
             }
+            cudaMemcpyAsync(adj->u->f.data, adj->ckpt[static_cast<size_t>(s / K)], dense_bytes(c), cudaMemcpyDeviceToDevice, c.stream);
+            if ((st = replay_range(adj, s, e, true, false)) || (st = reverse_segment(adj, s, e)))
+            {
+                return afail(st, c.err.c_str());
+            }
+        }
+        int overflow = 0;
+        cudaMemcpyAsync(&overflow, adj->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+        if (cudaStreamSynchronize(c.stream) != cudaSuccess)
+        {
+            return afail(SG_ERR_CUDA, "sg_adjoint_backward: CUDA error");
+        }
+        if (overflow)
+        {
+            return afail(SG_ERR_CAPACITY, "sg_adjoint_backward: an operator has more terms than a linear form holds");
         }
         if ((st = sg::device_error(c)))
         {

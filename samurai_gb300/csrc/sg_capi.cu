@@ -159,7 +159,6 @@ namespace
         dfree(c.block_sums);
         dfree(c.d_counts);
         dfree(c.d_flags);
-        dfree(c.d_geom);
         dfree(c.d_eps);
         dfree(c.d_absmax);
         dfree(c.g.err);
@@ -195,9 +194,9 @@ namespace
         delete h;
     }
 
-    __global__ void k_box_cells(const sg::Geom* __restrict__ gp, int l, uint32_t* cells)
+    __global__ void k_box_cells(const __grid_constant__ sg::Geom gp, int l, uint32_t* cells)
     {
-        const sg::Geom& g      = *gp;
+        const sg::Geom& g      = gp;
         const sg::LevelGeom& L = g.lv[l];
         for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < L.nwords; w += static_cast<long long>(gridDim.x) * blockDim.x)
         {
@@ -492,7 +491,6 @@ extern "C"
         st |= dalloc(c, &c.d_counts, static_cast<size_t>(sg::COUNTS));
         st |= dalloc(c, &c.d_flags, 8);
         st |= dalloc(c, &c.d_adapt, static_cast<size_t>(sg::A_COUNT));
-        st |= dalloc(c, &c.d_geom, 1);
         st |= dalloc(c, &c.d_ite, 1);
         st |= dalloc(c, &c.d_eps, sg::EPS_VELOCITY + 3);
         st |= dalloc(c, &c.d_absmax, 1);
@@ -516,7 +514,6 @@ extern "C"
             return fail(SG_ERR_CUDA, "sg_mesh_create: ", msg.c_str());
         }
         cudaMemsetAsync(c.g.err, 0, sizeof(int), c.stream);
-        cudaMemcpyAsync(c.d_geom, &c.g, sizeof(sg::Geom), cudaMemcpyHostToDevice, c.stream);
         // every bitmap starts empty: the mesh construction writes only the
         // levels where a set can be non-empty and relies on zeros elsewhere
         for (int k = 0; k < 2; ++k)
@@ -529,7 +526,7 @@ extern "C"
         }
         cudaMemsetAsync(c.detail, 0, static_cast<size_t>(c.capacity) * sizeof(double), c.stream);
         cudaMemsetAsync(c.tag, 0, static_cast<size_t>(c.capacity), c.stream);
-        k_box_cells<<<sg::grid_for(c.g.lv[max_level].nwords), 256, 0, c.stream>>>(c.d_geom, max_level, c.m().cells);
+        k_box_cells<<<sg::grid_for(c.g.lv[max_level].nwords), 256, 0, c.stream>>>(c.g, max_level, c.m().cells);
         st = sg::check(c, "initial cells");
         if (!st)
         {

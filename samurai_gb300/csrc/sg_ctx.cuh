@@ -130,8 +130,7 @@ namespace sg
         Timers timers;
         KernelTrace trace;
         MeshCfg cfg;
-        Geom g{};                // host copy
-        Geom* d_geom = nullptr;  // device copy: kernels read the geometry through this pointer
+        Geom g{};                // geometry: kernels take it by value as a __grid_constant__ parameter
         double* d_eps = nullptr; // per-level thresholds of the criteria (3 x MAXLEV)
         unsigned long long* d_absmax = nullptr; // bits of max |u| over the leaf cells (relative details)
         int detail_comps             = 1;       // dense detail slabs allocated (one per adapted field)
@@ -236,11 +235,10 @@ namespace sg
     int harten(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool* converged, bool relative_detail = false);
     int harten_begin(Ctx& c, DeviceField& f, int ite, double eps, double regularity, bool relative_detail = false); // no synchronisation
     // one step's linear operators on a frozen mesh (replay and adjoint)
-    struct TapeDev;
     int ghost_value(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv);
-    int ghost_tape(Ctx& c, DeviceMesh& m, const TapeDev& t, bool has_bc, double bcv, const std::function<void()>& mark);
+    int ghost_reverse(Ctx& c, DeviceMesh& m, double* lam, int* overflow, bool has_bc); // lam := G^T lam
     int update_fields_value(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un);
-    int update_fields_tape(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const TapeDev& t);
+    int update_fields_reverse(Ctx& c, DeviceMesh& m, DeviceMesh& nm, double* lam_new, double* lam_old, int* overflow); // lam_old += T^T lam_new
     int harten_end(Ctx& c, DeviceField& f, bool* converged);
     // the same for the fields fs driving the criteria and the fields os carried along
     int harten_begin_fields(Ctx& c, const std::vector<DeviceField*>& fs, int ite, double eps, double regularity, bool relative_detail);

@@ -332,10 +332,10 @@ namespace sg
         }
 
         // ----------------------------------------------------------- tags
-        __global__ void k_tag_init(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* cells,
+        __global__ void k_tag_init(const __grid_constant__ Geom gp, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* cells,
                                    uint8_t* tag, double* det)
         {
-            warp_list(wl, lo[LO_REF], lo[LO_REF + gp->nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; },
+            warp_list(wl, lo[LO_REF], lo[LO_REF + gp.nlev], warp_id(), warp_count(), [&](long long w) { return ref[w]; },
                       [&](long long w, int b)
                       {
                           const long long e = 32 * w + b;
@@ -700,10 +700,10 @@ namespace sg
         //    (update_outer_ghost.hpp:20-155) next to union cells;
         //  - projection of the reference cells of level l onto proj_cells[l-1].
         template <int DIM, class A>
-        __global__ void k_ghost_level(const Geom* __restrict__ gp, GhostLevelArgs a, const int* wl_ref, const long long* lo, const uint32_t* cells,
+        __global__ void k_ghost_level(const __grid_constant__ Geom gp, GhostLevelArgs a, const int* wl_ref, const long long* lo, const uint32_t* cells,
                                       const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, A u)
         {
-            const Geom& g = *gp;
+            const Geom& g = gp;
             const int l   = a.l;
             if (static_cast<int>(blockIdx.x) < a.nb_corner)
             {
@@ -773,9 +773,9 @@ namespace sg
         // update_ghost_periodic(level, field) (algorithm/update_periodic.hpp:19-25)
         // on one axis: both sides at once (they read inner cells and write
         // outer ghosts, so no item reads what another writes)
-        __global__ void k_periodic_copy(const Geom* __restrict__ gp, int l, int d, long long per_side, const uint32_t* ref, double* u)
+        __global__ void k_periodic_copy(const __grid_constant__ Geom gp, int l, int d, long long per_side, const uint32_t* ref, double* u)
         {
-            const Geom& g     = *gp;
+            const Geom& g     = gp;
             const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
             if (t >= 2 * per_side)
             {
@@ -791,9 +791,9 @@ namespace sg
 
         // update_tag_periodic(level, tag) (algorithm/update_periodic.hpp:178-300)
         // on one axis and side: both cells of a pair take the union of their tags
-        __global__ void k_periodic_tag(const Geom* __restrict__ gp, int l, int d, int side, long long per_side, const uint32_t* ref, uint8_t* tag)
+        __global__ void k_periodic_tag(const __grid_constant__ Geom gp, int l, int d, int side, long long per_side, const uint32_t* ref, uint8_t* tag)
         {
-            const Geom& g     = *gp;
+            const Geom& g     = gp;
             const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
             if (t >= per_side)
             {
@@ -821,7 +821,7 @@ namespace sg
             {
                 if ((g.periodic >> d) & 1)
                 {
-                    k_periodic_copy<<<static_cast<int>((2 * per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.d_geom, l, d, per, m.ref, u);
+                    k_periodic_copy<<<static_cast<int>((2 * per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.g, l, d, per, m.ref, u);
                     launched(c, "periodic_copy");
                 }
             }
@@ -841,7 +841,7 @@ namespace sg
                 {
                     for (int side = 0; side < 2; ++side)
                     {
-                        k_periodic_tag<<<static_cast<int>((per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.d_geom, l, d, side, per, m.ref, c.tag);
+                        k_periodic_tag<<<static_cast<int>((per + BLOCK - 1) / BLOCK), BLOCK, 0, c.stream>>>(c.g, l, d, side, per, m.ref, c.tag);
                         launched(c, "periodic_tag");
                     }
                 }
@@ -859,10 +859,10 @@ namespace sg
         // The small levels of the top-down pass in one block: the roles of
         // k_ghost_level one level after the other.
         template <int DIM>
-        __global__ void __launch_bounds__(1024, 1) k_ghost_levels_small(const Geom* __restrict__ gp, GhostChainArgs ca, const int* wl_ref, const long long* lo, const uint32_t* cells,
+        __global__ void __launch_bounds__(1024, 1) k_ghost_levels_small(const __grid_constant__ Geom gp, GhostChainArgs ca, const int* wl_ref, const long long* lo, const uint32_t* cells,
                                              const uint32_t* uni, const uint32_t* proj, const uint32_t* ref, ValAcc u)
         {
-            const Geom& g         = *gp;
+            const Geom& g         = gp;
             const int minl        = g.min_level, maxl = g.max_level;
             const int ndiag       = (DIM == 2) ? 4 : 20;
             const long long warp0 = threadIdx.x >> 5;
@@ -903,22 +903,22 @@ namespace sg
         }
 
         template <int DIM, class A>
-        __global__ void k_predict(const Geom* __restrict__ gp, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
+        __global__ void k_predict(const __grid_constant__ Geom gp, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
                                   const uint32_t* proj, const uint32_t* ref, A u)
         {
-            predict_level<DIM>(*gp, l, order, wl_ref, lo, cells, proj, ref, u, warp_id(), warp_count());
+            predict_level<DIM>(gp, l, order, wl_ref, lo, cells, proj, ref, u, warp_id(), warp_count());
         }
 
         // the small levels of the bottom-up pass in one block
         template <int DIM>
-        __global__ void __launch_bounds__(1024, 1) k_predict_small(const Geom* __restrict__ gp, int l_lo, int l_hi, int order, const int* wl_ref, const long long* lo,
+        __global__ void __launch_bounds__(1024, 1) k_predict_small(const __grid_constant__ Geom gp, int l_lo, int l_hi, int order, const int* wl_ref, const long long* lo,
                                         const uint32_t* cells, const uint32_t* proj, const uint32_t* ref, ValAcc u)
         {
             const long long warp0 = threadIdx.x >> 5;
             const long long nw    = blockDim.x >> 5;
             for (int l = l_lo; l <= l_hi; ++l)
             {
-                predict_level<DIM>(*gp, l, order, wl_ref, lo, cells, proj, ref, u, warp0, nw);
+                predict_level<DIM>(gp, l, order, wl_ref, lo, cells, proj, ref, u, warp0, nw);
                 __syncthreads();
             }
         }
@@ -927,10 +927,10 @@ namespace sg
         // compute_detail_op (mr/operators.hpp:139-540) on
         // intersection(all_cells[l], union(cells[l+1], cells[l+2])).on(l)
         template <int DIM>
-        __global__ void k_detail(const Geom* __restrict__ gp, int order, const int* wl, const long long* lo, int l0, int l1, const int* d_ite,
+        __global__ void k_detail(const __grid_constant__ Geom gp, int order, const int* wl, const long long* lo, int l0, int l1, const int* d_ite,
                                  const uint32_t* ref, const uint32_t* hc, const uint32_t* hc2, const double* u, double* det)
         {
-            const Geom& g = *gp;
+            const Geom& g = gp;
             // levels l0 .. min(l1, max_level - ite - 1) (mr/adapt.hpp:310-317)
             const int le = min(l1, g.max_level - *d_ite - 1);
             if (le < l0)
@@ -1001,7 +1001,7 @@ namespace sg
         // mr_criteria_op (mr/criteria.hpp:20-113) on
         // intersection(cells[l], all_cells[l-1]).on(l-1), fine levels l0..l1
         template <int DIM>
-        __global__ void k_criteria(const Geom* __restrict__ gp, const double* __restrict__ eps, const int* wl, const long long* lo, int l0, int l1,
+        __global__ void k_criteria(const __grid_constant__ Geom gp, const double* __restrict__ eps, const int* wl, const long long* lo, int l0, int l1,
                                    const int* d_ite, const uint32_t* ref, const uint32_t* hc, const double* det, uint8_t* tag, int ncomp,
                                    long long cstride)
         {
@@ -1018,7 +1018,7 @@ namespace sg
                 }
                 return false;
             };
-            const Geom& g = *gp;
+            const Geom& g = gp;
             // fine levels l0 .. min(l1, max_level - ite) (mr/adapt.hpp:325-339); the
             // operator runs on their parents
             const int le = min(l1, g.max_level - *d_ite);
@@ -1125,9 +1125,9 @@ namespace sg
         // -max_stencil_radius times the direction (domain_boundary_layer,
         // boundary.hpp:6-21), i.e. the leaves of max_level within r cells of
         // the boundary, are tagged keep (the tag is overwritten)
-        __global__ void k_keep_boundary(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* cells, int r, uint8_t* tag)
+        __global__ void k_keep_boundary(const __grid_constant__ Geom gp, const int* wl, const long long* lo, const uint32_t* cells, int r, uint8_t* tag)
         {
-            const Geom& g = *gp;
+            const Geom& g = gp;
             const int l   = g.max_level;
             warp_list(wl, lo[LO_CELLS + l], lo[LO_CELLS + l + 1], warp_id(), warp_count(),
                       [&](long long w)
@@ -1182,23 +1182,139 @@ namespace sg
                       });
         }
 
+        // byte-wise atomic OR / AND on the tag array (through its 32-bit word)
+        __device__ __forceinline__ void tag_or_atomic(uint8_t* t, unsigned v)
+        {
+            const unsigned long long a = reinterpret_cast<unsigned long long>(t);
+            atomicOr(reinterpret_cast<unsigned*>(a & ~3ull), v << (8 * (a & 3)));
+        }
+
+        __device__ __forceinline__ void tag_and_atomic(uint8_t* t, unsigned v)
+        {
+            const unsigned long long a = reinterpret_cast<unsigned long long>(t);
+            atomicAnd(reinterpret_cast<unsigned*>(a & ~3ull), ~((~v & 0xFFu) << (8 * (a & 3))));
+        }
+
+        // Two consecutive levels of maximum_op in one launch: the operator with children at level l (parents at
+        // l-1) and the one with children at level l-1 (parents at l-2), which in sequence runs after it.  A parent
+        // at l-2 needs the keep bits its children at l-1 carry after the first operator; it derives them itself
+        // from their children at l: keep(p) = keep bit of p, or p is a parent of leaves (reference and hc) whose
+        // children hold a keep bit or are all tagged coarsen.  Those inputs are the same before and after the
+        // first operator's writes (it sets keep bits on all children only when one already holds one, and clears
+        // coarsen bits only when not all hold one), so the two operators' threads run concurrently.  The bytes of
+        // level l-1, written by both, take atomic updates.
         template <int DIM>
-        __global__ void k_maximum(const Geom* __restrict__ gp, int l, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
+        __global__ void k_maximum2(const __grid_constant__ Geom gp, int l, const int* wl, const long long* lo, const uint32_t* ref,
+                                   const uint32_t* hc, uint8_t* tag)
+        {
+            const Geom& g      = gp;
+            const long long w1 = g.lv[l - 1].woff; // first word of level l-1
+            warp_list(wl, lo[LO_REF + l - 2], lo[LO_REF + l], warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
+                      [&](long long w, int b)
+                      {
+                          const long long co = 32 * w + b;
+                          if (w >= w1)
+                          {
+                              // parent at l-1, children at l (maximum_op, mr/operators.hpp:22-96)
+                              const Cell c  = cell_of(g, l - 1, w, b);
+                              const Box3 fb = box_at<DIM>(g, l, 2 * c.x, 2 * c.y, 2 * c.z, 2);
+                              long long fo[8];
+                              uint8_t keep = 0, coarsen = 2;
+                              for (int ch = 0; ch < (1 << DIM); ++ch)
+                              {
+                                  fo[ch]          = fb.base + (ch & 1) + ((ch >> 1) & 1) * fb.sy + ((ch >> 2) & 1) * fb.sz;
+                                  const uint8_t t = tag[fo[ch]];
+                                  keep |= t & 1;
+                                  coarsen &= t & 2;
+                              }
+                              if (keep)
+                              {
+                                  for (int ch = 0; ch < (1 << DIM); ++ch)
+                                  {
+                                      tag[fo[ch]] |= 1;
+                                  }
+                                  tag_or_atomic(tag + co, 1u);
+                              }
+                              else if (coarsen)
+                              {
+                                  tag_or_atomic(tag + co, 1u);
+                              }
+                              else
+                              {
+                                  for (int ch = 0; ch < (1 << DIM); ++ch)
+                                  {
+                                      tag[fo[ch]] &= static_cast<uint8_t>(~2);
+                                  }
+                              }
+                              return;
+                          }
+                          // parent at l-2, children p at l-1
+                          const Cell c  = cell_of(g, l - 2, w, b);
+                          const Box3 pb = box_at<DIM>(g, l - 1, 2 * c.x, 2 * c.y, 2 * c.z, 2);
+                          long long po[8];
+                          uint8_t keep = 0, coarsen = 2;
+                          for (int ch = 0; ch < (1 << DIM); ++ch)
+                          {
+                              const int px = 2 * c.x + (ch & 1), py = 2 * c.y + ((ch >> 1) & 1), pz = 2 * c.z + ((ch >> 2) & 1);
+                              po[ch]          = pb.base + (ch & 1) + ((ch >> 1) & 1) * pb.sy + ((ch >> 2) & 1) * pb.sz;
+                              const uint8_t t = tag[po[ch]];
+                              uint8_t k       = t & 1;
+                              const Pos pp    = pos_of(g, l - 1, px, py, DIM == 3 ? pz : 0);
+                              if (!k && test(ref, pp) && test(hc, pp))
+                              {
+                                  // p's own operator: a child's keep bit, or all children tagged coarsen
+                                  const Box3 fb = box_at<DIM>(g, l, 2 * px, 2 * py, 2 * pz, 2);
+                                  uint8_t ck = 0, cc = 2;
+                                  for (int gc = 0; gc < (1 << DIM); ++gc)
+                                  {
+                                      const uint8_t tt = tag[fb.base + (gc & 1) + ((gc >> 1) & 1) * fb.sy + ((gc >> 2) & 1) * fb.sz];
+                                      ck |= tt & 1;
+                                      cc &= tt & 2;
+                                  }
+                                  k = (ck | cc) ? 1 : 0;
+                              }
+                              keep |= k;
+                              coarsen &= t & 2;
+                          }
+                          if (keep)
+                          {
+                              for (int ch = 0; ch < (1 << DIM); ++ch)
+                              {
+                                  tag_or_atomic(tag + po[ch], 1u);
+                              }
+                              tag[co] |= 1;
+                          }
+                          else if (coarsen)
+                          {
+                              tag[co] |= 1;
+                          }
+                          else
+                          {
+                              for (int ch = 0; ch < (1 << DIM); ++ch)
+                              {
+                                  tag_and_atomic(tag + po[ch], static_cast<unsigned>(static_cast<uint8_t>(~2)));
+                              }
+                          }
+                      });
+        }
+
+        template <int DIM>
+        __global__ void k_maximum(const __grid_constant__ Geom gp, int l, const int* wl, const long long* lo, const uint32_t* ref, const uint32_t* hc,
                                   uint8_t* tag)
         {
-            maximum_level<DIM>(*gp, l, wl, lo, ref, hc, tag, warp_id(), warp_count());
+            maximum_level<DIM>(gp, l, wl, lo, ref, hc, tag, warp_id(), warp_count());
         }
 
         // the small levels of the tag finalisation in one block, l_hi down to l_lo
         template <int DIM>
-        __global__ void __launch_bounds__(1024, 1) k_maximum_small(const Geom* __restrict__ gp, int l_hi, int l_lo, const int* wl, const long long* lo,
+        __global__ void __launch_bounds__(1024, 1) k_maximum_small(const __grid_constant__ Geom gp, int l_hi, int l_lo, const int* wl, const long long* lo,
                                                                    const uint32_t* ref, const uint32_t* hc, uint8_t* tag)
         {
             const long long warp0 = threadIdx.x >> 5;
             const long long nw    = blockDim.x >> 5;
             for (int l = l_hi; l >= l_lo; --l)
             {
-                maximum_level<DIM>(*gp, l, wl, lo, ref, hc, tag, warp0, nw);
+                maximum_level<DIM>(gp, l, wl, lo, ref, hc, tag, warp0, nw);
                 __syncthreads();
             }
         }
@@ -1207,10 +1323,10 @@ namespace sg
         // reference ∩ new cells, projection on coarsened cells, prediction on
         // refined cells; every other reference entry of the new field is 0.
         template <int DIM, class A>
-        __global__ void k_update_fields(const Geom* __restrict__ gp, int order, const int* wl, const long long* lo, const uint32_t* nref,
+        __global__ void k_update_fields(const __grid_constant__ Geom gp, int order, const int* wl, const long long* lo, const uint32_t* nref,
                                         const uint32_t* ncells, const uint32_t* oref, const uint32_t* ocells, const uint32_t* ohc, A uo, A un)
         {
-            const Geom& g = *gp;
+            const Geom& g = gp;
             warp_list_compact(wl, lo[LO_REF], lo[LO_REF + g.nlev], warp_id(), warp_count(), [&](long long w) { return nref[w]; },
                       [&](long long w, int b)
                       {
@@ -1284,10 +1400,10 @@ namespace sg
         //    operations, same bits) and passed by a shuffle;
         //  - /dx and dt/dx use dx = 2^-l exactly: x / 2^-l == x * 2^l.
         template <int DIM>
-        __global__ void k_upwind(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* cells, const double* __restrict__ u,
+        __global__ void k_upwind(const __grid_constant__ Geom gp, const int* wl, const long long* lo, const uint32_t* cells, const double* __restrict__ u,
                                  double* __restrict__ unp1, UpwindArgs p)
         {
-            const Geom& g  = *gp;
+            const Geom& g  = gp;
             const int lane = threadIdx.x & 31;
             // the leaf cells compacted over the lanes (warp_items); a cell's left
             // flux is its left neighbour's right flux when that neighbour is the
@@ -1389,10 +1505,10 @@ namespace sg
         // coefficients (a, 0) for a >= 0, (0, a) otherwise; every factor is a
         // power of two.
         template <int DIM>
-        __global__ void k_convection(const Geom* __restrict__ gp, const int* wl, const long long* lo, const uint32_t* cells, const double* __restrict__ u,
+        __global__ void k_convection(const __grid_constant__ Geom gp, const int* wl, const long long* lo, const uint32_t* cells, const double* __restrict__ u,
                                      double* __restrict__ unp1, UpwindArgs p, const double* __restrict__ av)
         {
-            const Geom& g     = *gp;
+            const Geom& g     = gp;
             const long long n = lo[LO_CELLS + g.nlev];
             warp_list_compact(wl, lo[LO_CELLS], n, warp_id(), warp_count(), [&](long long w) { return __ldg(cells + w); },
                               [&](long long w, int b)
@@ -1732,6 +1848,147 @@ namespace sg
 
     namespace
     {
+        // A captured chain of kernel launches (one stream, no other node types) rebuilt with its kernels in the
+        // opposite order.  The kernel parameters are copied from the captured nodes.
+        cudaError_t reverse_chain(cudaGraph_t in, cudaGraph_t* out)
+        {
+            *out     = nullptr;
+            size_t n = 0, nr = 0;
+            cudaError_t e = cudaGraphGetNodes(in, nullptr, &n);
+            if (e == cudaSuccess)
+            {
+                e = cudaGraphGetRootNodes(in, nullptr, &nr);
+            }
+            if (e != cudaSuccess)
+            {
+                return e;
+            }
+            std::vector<cudaGraphNode_t> order;
+            if (n > 0)
+            {
+                if (nr != 1)
+                {
+                    return cudaErrorInvalidValue;
+                }
+                cudaGraphNode_t cur = nullptr;
+                if ((e = cudaGraphGetRootNodes(in, &cur, &nr)) != cudaSuccess)
+                {
+                    return e;
+                }
+                while (order.size() <= n)
+                {
+                    order.push_back(cur);
+                    size_t nd = 0;
+                    if ((e = cudaGraphNodeGetDependentNodes(cur, nullptr, nullptr, &nd)) != cudaSuccess)
+                    {
+                        return e;
+                    }
+                    if (nd == 0)
+                    {
+                        break;
+                    }
+                    if (nd != 1 || (e = cudaGraphNodeGetDependentNodes(cur, &cur, nullptr, &nd)) != cudaSuccess)
+                    {
+                        return nd != 1 ? cudaErrorInvalidValue : e;
+                    }
+                }
+                if (order.size() != n)
+                {
+                    return cudaErrorInvalidValue;
+                }
+            }
+            if ((e = cudaGraphCreate(out, 0)) != cudaSuccess)
+            {
+                return e;
+            }
+            cudaGraphNode_t prev = nullptr;
+            for (auto it = order.rbegin(); it != order.rend(); ++it)
+            {
+                cudaGraphNodeType t;
+                cudaKernelNodeParams kp{};
+                cudaGraphNode_t node = nullptr;
+                if ((e = cudaGraphNodeGetType(*it, &t)) != cudaSuccess || t != cudaGraphNodeTypeKernel
+                    || (e = cudaGraphKernelNodeGetParams(*it, &kp)) != cudaSuccess
+                    || (e = cudaGraphAddKernelNode(&node, *out, prev ? &prev : nullptr, prev ? 1 : 0, &kp)) != cudaSuccess)
+                {
+                    cudaGraphDestroy(*out);
+                    *out = nullptr;
+                    return e != cudaSuccess ? e : cudaErrorInvalidValue;
+                }
+                prev = node;
+            }
+            return cudaSuccess;
+        }
+    } // namespace
+
+    // run_cached for a launch sequence whose launches must run in the opposite order (the transpose of a chain of
+    // linear operators): captured once per key, reversed, cached and replayed.  Always a graph (the reversal needs
+    // the captured chain), and with no trace events inside.
+    template <class F>
+    int run_reversed(Ctx& c, unsigned long long k0, unsigned long long k1, unsigned long long k2, unsigned long long k3, F seq)
+    {
+        k0 |= 1ull << 62;
+        for (auto& e : c.graphs)
+        {
+            if (e.key[0] == k0 && e.key[1] == k1 && e.key[2] == k2 && e.key[3] == k3)
+            {
+                c.n_launches += e.kernels;
+                return cudaGraphLaunch(e.exec, c.stream) != cudaSuccess ? check(c, "cudaGraphLaunch") : SG_OK;
+            }
+        }
+        const bool traced = c.trace.enabled;
+        c.trace.enabled   = false;
+        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        {
+            c.trace.enabled = traced;
+            return check(c, "cudaStreamBeginCapture");
+        }
+        const int before  = c.n_launches;
+        int st            = seq();
+        cudaGraph_t graph = nullptr;
+        cudaError_t e     = cudaStreamEndCapture(c.stream, &graph);
+        c.trace.enabled   = traced;
+        cudaGraph_t rev   = nullptr;
+        if (!st && e == cudaSuccess)
+        {
+            e = reverse_chain(graph, &rev);
+        }
+        if (graph)
+        {
+            cudaGraphDestroy(graph);
+        }
+        if (st || e != cudaSuccess)
+        {
+            if (!st)
+            {
+                c.err = std::string("reversed graph: ") + cudaGetErrorString(e);
+                st    = SG_ERR_CUDA;
+            }
+            cudaGetLastError();
+            return st;
+        }
+        cudaGraphExec_t exec = nullptr;
+        e                    = cudaGraphInstantiate(&exec, rev, 0);
+        cudaGraphDestroy(rev);
+        if (e != cudaSuccess)
+        {
+            return check(c, "cudaGraphInstantiate");
+        }
+        if (c.graphs.size() >= 64)
+        {
+            cudaGraphExecDestroy(c.graphs.front().exec);
+            for (const auto& mk : c.graphs.front().marks)
+            {
+                give_event(c, mk.second);
+            }
+            c.graphs.erase(c.graphs.begin());
+        }
+        c.graphs.push_back({{k0, k1, k2, k3}, exec, c.n_launches - before, {}});
+        return cudaGraphLaunch(exec, c.stream) != cudaSuccess ? check(c, "cudaGraphLaunch") : SG_OK;
+    }
+
+    namespace
+    {
         // the Harten pass index and the criteria thresholds of one pass, baked
         // into a captured graph (the host computes them exactly as for the
         // staged copies of the per-pass path)
@@ -1953,11 +2210,11 @@ namespace sg
                 {
                     if (g.dim == 2)
                     {
-                        k_ghost_level<2><<<grid, c.block, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<2><<<grid, c.block, 0, c.stream>>>(c.g, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     else
                     {
-                        k_ghost_level<3><<<grid, c.block, 0, c.stream>>>(c.d_geom, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<3><<<grid, c.block, 0, c.stream>>>(c.g, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     launched(c, "ghost_level");
                     after();
@@ -1971,11 +2228,11 @@ namespace sg
                     b.do_proj        = 0;
                     if (g.dim == 2)
                     {
-                        k_ghost_level<2><<<b.nb_corner, c.block, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<2><<<b.nb_corner, c.block, 0, c.stream>>>(c.g, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     else
                     {
-                        k_ghost_level<3><<<b.nb_corner, c.block, 0, c.stream>>>(c.d_geom, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<3><<<b.nb_corner, c.block, 0, c.stream>>>(c.g, b, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     launched(c, "ghost_corner_projection");
                     after();
@@ -1991,11 +2248,11 @@ namespace sg
                     GhostChainArgs ca{l, lmin, lmin, has_bc ? 1 : 0, bcv};
                     if (g.dim == 2)
                     {
-                        k_ghost_levels_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_levels_small<2><<<1, 1024, 0, c.stream>>>(c.g, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     else
                     {
-                        k_ghost_levels_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_levels_small<3><<<1, 1024, 0, c.stream>>>(c.g, ca, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     launched(c, "ghost_levels_small");
                     after();
@@ -2005,11 +2262,11 @@ namespace sg
                     const int e = maxl < ft ? maxl : ft;
                     if (g.dim == 2)
                     {
-                        k_predict_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                        k_predict_small<2><<<1, 1024, 0, c.stream>>>(c.g, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
                     }
                     else
                     {
-                        k_predict_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
+                        k_predict_small<3><<<1, 1024, 0, c.stream>>>(c.g, lp, e, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj, m.ref, u);
                     }
                     launched(c, "predict_small");
                     after();
@@ -2020,12 +2277,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_predict<2><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<2><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.g, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 else
                 {
-                    k_predict<3><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.d_geom, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<3><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.g, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 launched(c, "predict");
@@ -2048,12 +2305,12 @@ namespace sg
             const Geom& g = c.g;
             if (g.dim == 2)
             {
-                k_update_fields<2><<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                k_update_fields<2><<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.g, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
                                                                                             nm.cells, m.ref, m.cells, m.hc, uo, un);
             }
             else
             {
-                k_update_fields<3><<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
+                k_update_fields<3><<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.g, c.cfg.prediction_radius, nm.wl_ref, nm.d_lo, nm.ref,
                                                                                             nm.cells, m.ref, m.cells, m.hc, uo, un);
             }
             launched(c, "update_fields");
@@ -2084,7 +2341,7 @@ namespace sg
                 cudaMemcpyAsync(c.d_eps, c.h_eps, 3 * MAXLEV * sizeof(double), cudaMemcpyHostToDevice, c.stream);
             }
             cudaMemsetAsync(c.d_flags, 0, F_COUNT * sizeof(int), c.stream);
-            k_tag_init<<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.d_geom, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
+            k_tag_init<<<blocks_words(c, 0, g.nlev - 1), c.block, 0, c.stream>>>(c.g, m.wl_ref, m.d_lo, m.ref, m.cells, c.tag, c.detail);
             launched(c, "tag_init");
             for (int k = 1; k < nf; ++k)
             {
@@ -2112,12 +2369,12 @@ namespace sg
                 double* det     = c.detail + k * c.capacity;
                 if (g.dim == 2)
                 {
-                    k_detail<2><<<blocks_words(c, dl0, dl1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                    k_detail<2><<<blocks_words(c, dl0, dl1), c.block, 0, c.stream>>>(c.g, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
                                                                                     m.ref, m.hc, m.hc2, u, det);
                 }
                 else
                 {
-                    k_detail<3><<<blocks_words(c, dl0, dl1), c.block, 0, c.stream>>>(c.d_geom, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
+                    k_detail<3><<<blocks_words(c, dl0, dl1), c.block, 0, c.stream>>>(c.g, c.cfg.prediction_radius, m.wl_ref, m.d_lo, dl0, dl1, c.d_ite,
                                                                                     m.ref, m.hc, m.hc2, u, det);
                 }
                 launched(c, "detail");
@@ -2136,12 +2393,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_criteria<2><<<blocks_words(c, minl - 1, maxl - 1), c.block, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                    k_criteria<2><<<blocks_words(c, minl - 1, maxl - 1), c.block, 0, c.stream>>>(c.g, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
                                                                                                 m.ref, m.hc, c.detail, c.tag, nf, c.capacity);
                 }
                 else
                 {
-                    k_criteria<3><<<blocks_words(c, minl - 1, maxl - 1), c.block, 0, c.stream>>>(c.d_geom, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
+                    k_criteria<3><<<blocks_words(c, minl - 1, maxl - 1), c.block, 0, c.stream>>>(c.g, c.d_eps, m.wl_ref, m.d_lo, minl, maxl, c.d_ite,
                                                                                                 m.ref, m.hc, c.detail, c.tag, nf, c.capacity);
                 }
                 launched(c, "criteria");
@@ -2149,7 +2406,7 @@ namespace sg
             if (c.refine_boundary)
             {
                 // "refine boundary" (mr/adapt.hpp:341-346), between tag cells and tag finalization
-                k_keep_boundary<<<blocks_words(c, maxl, maxl), c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, c.cfg.max_stencil_radius,
+                k_keep_boundary<<<blocks_words(c, maxl, maxl), c.block, 0, c.stream>>>(c.g, m.wl_cells, m.d_lo, m.cells, c.cfg.max_stencil_radius,
                                                                                    c.tag);
                 launched(c, "keep_boundary");
             }
@@ -2164,28 +2421,44 @@ namespace sg
                 // periodic axes: update_tag_periodic before each level's operator
                 // (mr/adapt.hpp:348-357), so no level is fused into a one-block chain
                 const int top   = g.periodic ? -2 * MAXLEV : c.fuse_top_max;
-                for (; l >= lstop && l - 1 > top; --l)
+                while (l >= lstop && l - 1 > top)
                 {
                     periodic_tags(c, m, l);
+                    if (!g.periodic && l - 1 >= lstop && l - 2 > top)
+                    {
+                        // children at levels l and l-1 in one launch
+                        if (g.dim == 2)
+                        {
+                            k_maximum2<2><<<blocks_words(c, l - 2, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        }
+                        else
+                        {
+                            k_maximum2<3><<<blocks_words(c, l - 2, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        }
+                        launched(c, "maximum2");
+                        l -= 2;
+                        continue;
+                    }
                     if (g.dim == 2)
                     {
-                        k_maximum<2><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<2><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     else
                     {
-                        k_maximum<3><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.d_geom, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<3><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     launched(c, "maximum");
+                    --l;
                 }
                 if (l >= lstop)
                 {
                     if (g.dim == 2)
                     {
-                        k_maximum_small<2><<<1, 1024, 0, c.stream>>>(c.d_geom, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum_small<2><<<1, 1024, 0, c.stream>>>(c.g, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     else
                     {
-                        k_maximum_small<3><<<1, 1024, 0, c.stream>>>(c.d_geom, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum_small<3><<<1, 1024, 0, c.stream>>>(c.g, l, lstop, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
                     }
                     launched(c, "maximum_small");
                 }
@@ -2473,20 +2746,28 @@ namespace sg
 
     // ---------------------------------------------------------------
     // Operators of one step on a given (frozen) mesh, for the replay and the
-    // adjoint: the ghost update and update_fields either applied (value) or
-    // recorded onto a tape, one tape phase per launch; mark(p) closes a phase.
+    // adjoint: the ghost update and update_fields applied (value) or
+    // transposed (reverse: the RevAcc accessor, launches in reverse order).
     int ghost_value(Ctx& c, DeviceMesh& m, double* u, bool has_bc, double bcv)
     {
         return ghost_launches(c, m, ValAcc{u}, has_bc, bcv, c.fuse_top_field, false, [] {});
     }
 
-    int ghost_tape(Ctx& c, DeviceMesh& m, const TapeDev& t, bool has_bc, double bcv, const std::function<void()>& mark)
+    // lam := G^T lam for the ghost update G of mesh m, in place.  The launch sequence is the one that separates
+    // every read from every write (corner projections in launches of their own, no one-block chains), captured
+    // once per mesh buffer and adjoint array and replayed backwards.
+    int ghost_reverse(Ctx& c, DeviceMesh& m, double* lam, int* overflow, bool has_bc)
     {
-        if (c.g.dim == 2)
-        {
-            return ghost_launches(c, m, TapeAcc<FormCap<2>::value>{t}, has_bc, bcv, -2, true, mark);
-        }
-        return ghost_launches(c, m, TapeAcc<FormCap<3>::value>{t}, has_bc, bcv, -2, true, mark);
+        const unsigned long long kind = 40ull | (has_bc ? 256ull : 0ull);
+        return run_reversed(c, kind, ptr_key(m.ref), ptr_key(lam), ptr_key(overflow),
+                            [&]()
+                            {
+                                if (c.g.dim == 2)
+                                {
+                                    return ghost_launches(c, m, RevAcc<FormCap<2>::value>{lam, lam, overflow, 1}, has_bc, 0., -2, true, [] {});
+                                }
+                                return ghost_launches(c, m, RevAcc<FormCap<3>::value>{lam, lam, overflow, 1}, has_bc, 0., -2, true, [] {});
+                            });
     }
 
     int update_fields_value(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const double* uo, double* un)
@@ -2495,17 +2776,20 @@ namespace sg
         return check(c, "update_fields");
     }
 
-    int update_fields_tape(Ctx& c, DeviceMesh& m, DeviceMesh& nm, const TapeDev& t)
+    // lam_old += T^T lam_new for update_fields T from mesh m to mesh nm (lam_old is not cleared here)
+    int update_fields_reverse(Ctx& c, DeviceMesh& m, DeviceMesh& nm, double* lam_new, double* lam_old, int* overflow)
     {
         if (c.g.dim == 2)
         {
-            update_fields_launch(c, m, nm, TapeAcc<FormCap<2>::value>{t}, TapeAcc<FormCap<2>::value>{t});
+            const RevAcc<FormCap<2>::value> r{lam_new, lam_old, overflow, 0};
+            update_fields_launch(c, m, nm, r, r);
         }
         else
         {
-            update_fields_launch(c, m, nm, TapeAcc<FormCap<3>::value>{t}, TapeAcc<FormCap<3>::value>{t});
+            const RevAcc<FormCap<3>::value> r{lam_new, lam_old, overflow, 0};
+            update_fields_launch(c, m, nm, r, r);
         }
-        return check(c, "update_fields (tape)");
+        return check(c, "update_fields (transpose)");
     }
 
     namespace
@@ -2903,20 +3187,20 @@ namespace sg
             }
             if (g.dim == 2)
             {
-                k_convection<2><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p, av);
+                k_convection<2><<<nb, c.block, 0, c.stream>>>(c.g, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p, av);
             }
             else
             {
-                k_convection<3><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p, av);
+                k_convection<3><<<nb, c.block, 0, c.stream>>>(c.g, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p, av);
             }
         }
         else if (g.dim == 2)
         {
-            k_upwind<2><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p);
+            k_upwind<2><<<nb, c.block, 0, c.stream>>>(c.g, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p);
         }
         else
         {
-            k_upwind<3><<<nb, c.block, 0, c.stream>>>(c.d_geom, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p);
+            k_upwind<3><<<nb, c.block, 0, c.stream>>>(c.g, m.wl_cells, m.d_lo, m.cells, ud, unp1d, p);
         }
         launched(c, scheme == 2 ? "convection" : "upwind");
         return check(c, "upwind");

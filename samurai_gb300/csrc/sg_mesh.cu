@@ -135,13 +135,13 @@ namespace sg
         // ------------------------------------------------------------- words
         // guard: when not null, the launch does nothing unless *guard != 0
         template <class F>
-        __global__ void k_words(const Geom* __restrict__ gp, int l0, int l1, F f, const int* guard)
+        __global__ void k_words(const __grid_constant__ Geom gp, int l0, int l1, F f, const int* guard)
         {
             if (guard && *guard == 0)
             {
                 return;
             }
-            const Geom& g         = *gp;
+            const Geom& g         = gp;
             const long long begin = g.lv[l0].woff;
             const long long end   = g.lv[l1].woff + g.lv[l1].nwords;
             for (long long w = begin + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < end;
@@ -159,13 +159,13 @@ namespace sg
 
         // one block walks the levels l_first -> l_last (either direction)
         template <class F>
-        __global__ void __launch_bounds__(1024, 1) k_words_chain(const Geom* __restrict__ gp, int l_first, int l_last, F f, const int* guard)
+        __global__ void __launch_bounds__(1024, 1) k_words_chain(const __grid_constant__ Geom gp, int l_first, int l_last, F f, const int* guard)
         {
             if (guard && *guard == 0)
             {
                 return;
             }
-            const Geom& g  = *gp;
+            const Geom& g  = gp;
             const int step = l_last >= l_first ? 1 : -1;
             for (int l = l_first;; l += step)
             {
@@ -206,7 +206,7 @@ namespace sg
                 }
                 if (l >= l_last)
                 {
-                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, l_last, f, c.guard);
+                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.g, l, l_last, f, c.guard);
                     launched(c, what);
                     st = check(c, what);
                 }
@@ -217,7 +217,7 @@ namespace sg
                 if (l <= ft)
                 {
                     const int e = l_last < ft ? l_last : ft;
-                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.d_geom, l, e, f, c.guard);
+                    k_words_chain<<<1, 1024, 0, c.stream>>>(c.g, l, e, f, c.guard);
                     launched(c, what);
                     if ((st = check(c, what)))
                     {
@@ -244,7 +244,7 @@ namespace sg
                 return SG_OK;
             }
             const long long n = c.g.lv[l1].woff + c.g.lv[l1].nwords - c.g.lv[l0].woff;
-            k_words<<<grid_for(n, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.d_geom, l0, l1, f, c.guard);
+            k_words<<<grid_for(n, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.g, l0, l1, f, c.guard);
             launched(c, what);
             return check(c, what);
         }
@@ -381,10 +381,10 @@ namespace sg
             }
         }
 
-        __global__ void k_scan_write(const Geom* __restrict__ gp, const uint32_t* ref, const uint32_t* cells, long long n, long long nb, const long long* sums, int* rank,
+        __global__ void k_scan_write(const __grid_constant__ Geom gp, const uint32_t* ref, const uint32_t* cells, long long n, long long nb, const long long* sums, int* rank,
                                      int* wl_ref, int* wl_cells, long long* counts)
         {
-            const Geom& g = *gp;
+            const Geom& g = gp;
             const long long base = static_cast<long long>(blockIdx.x) * SCAN_CHUNK + threadIdx.x * SCAN_PER;
             const Quad q         = thread_quad(ref, cells, base, n);
             long long off[4];
@@ -431,7 +431,7 @@ namespace sg
         launched(c, "scan_sums");
         k_scan_top<<<1, 1024, 0, c.stream>>>(c.block_sums, nb, m.d_lo, c.g.nlev);
         launched(c, "scan_top");
-        k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(c.d_geom, m.ref, m.cells, n, nb, c.block_sums, m.rank, m.wl_ref, m.wl_cells,
+        k_scan_write<<<static_cast<unsigned>(nb), SCAN_T, 0, c.stream>>>(c.g, m.ref, m.cells, n, nb, c.block_sums, m.rank, m.wl_ref, m.wl_cells,
                                                                           m.d_lo);
         launched(c, "scan_write");
         cudaMemcpyAsync(m.h_lo, m.d_lo, COUNTS * sizeof(long long), cudaMemcpyDeviceToHost, c.stream);
@@ -815,9 +815,9 @@ namespace sg
     {
         // refine / coarsen_even flags of leaf cells from the tags
         // (update_cell_array_from_tag, algorithm/graduation.hpp:743-842)
-        __global__ void k_tag_flags(const Geom* __restrict__ gp, const uint32_t* cells, const uint8_t* tag, uint32_t* rf, uint32_t* cf, int minl, int maxl)
+        __global__ void k_tag_flags(const __grid_constant__ Geom gp, const uint32_t* cells, const uint8_t* tag, uint32_t* rf, uint32_t* cf, int minl, int maxl)
         {
-            const Geom& g = *gp;
+            const Geom& g = gp;
             for (long long w = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; w < g.total_words;
                  w += static_cast<long long>(gridDim.x) * blockDim.x)
             {
@@ -854,7 +854,7 @@ namespace sg
     int new_cells_from_tags(Ctx& c, const DeviceMesh& m, uint32_t* nc)
     {
         const Geom g = c.g;
-        k_tag_flags<<<grid_for(g.total_words, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.d_geom, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
+        k_tag_flags<<<grid_for(g.total_words, 256, 4LL * c.max_blocks), 256, 0, c.stream>>>(c.g, m.cells, c.tag, c.rf, c.cf, c.cfg.min_level, c.cfg.max_level);
         launched(c, "tag_flags");
         int st = check(c, "tag_flags");
         if (st)
