@@ -679,6 +679,13 @@ def batch_record(args, steps, warmup, serial_steps, full=False):
     a = [p["a"] for p in probs]
     dt = [p["dt"] for p in probs]
     batch.adapt(eps, reg)
+    # the batch's launch-shape autotuner (sg_batch_autotune; the timed steps use its choice)
+    tune = None
+    if not args.no_tune:
+        d_ms, t_ms, shape = batch.autotune(eps, reg, a, dt, steps=3)
+        tune = {"default_ms_per_step": d_ms, "tuned_ms_per_step": t_ms, "shape": shape,
+                "how": "sg_batch_autotune: one-block chain limit shared by the instances, then threads per block; "
+                       "3 batched steps from the same state per candidate"}
     for _ in range(warmup):
         batch.step(eps, reg, a, dt)
     batch.synchronize()
@@ -745,6 +752,7 @@ def batch_record(args, steps, warmup, serial_steps, full=False):
         "serial": {"value": s_updates / s_s, "unit": UNIT, "steps": serial_steps, "ms_per_step": 1e3 * s_s / serial_steps,
                    "api": "sg_adapt + sg_update_ghost_mr + sg_upwind + sg_field_swap per instance, one after the other"},
         "speedup_vs_serial": (b_updates / b_s) / (s_updates / s_s),
+        "autotune": tune,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }

@@ -279,6 +279,16 @@ int sg_batch_step(sg_batch_t batch, const double* eps, const double* regularity,
                   int* n_harten);
 int sg_batch_synchronize(sg_batch_t batch);
 
+/* Without a samurai counterpart: the batch's launch-shape autotuner.  Times `steps` batched steps (sg_batch_step)
+ * from the instances' current state under candidate shapes (the level size, in words, up to which every instance's
+ * ghost-update, tag-finalisation and mesh chains run their levels in one block; the threads per block of their FP64
+ * list kernels), each from the same saved state; keeps the fastest and leaves every instance's mesh and values as
+ * they were.  default_ms / tuned_ms receive the batched step time under the starting and the chosen shape. */
+int sg_batch_autotune(sg_batch_t batch, const double* eps, const double* regularity, const double* a, const double* dt, int scheme,
+                      int steps, double* default_ms, double* tuned_ms);
+/* the batch's launch shape: one-block chain limit in words per level, threads per block (0: each instance's own) */
+int sg_batch_launch_shape(sg_batch_t batch, long long* fuse_words, int* block);
+
 /* Discrete adjoint of the time loop (no counterpart in samurai, which has no derivatives).  The loop of
  * demos/FiniteVolume/advection_2d.cpp:140-147 (MRadaptation(eps, regularity); update_ghost_mr; upwind; swap)
  * is recorded with its mesh sequence; derivatives are those of the loop on the recorded meshes (adaptation

@@ -106,6 +106,8 @@ def lib():
         "sg_batch_swap": (i, [vp]),
         "sg_batch_step": (i, [vp, vp, vp, vp, vp, i, vp]),
         "sg_batch_synchronize": (i, [vp]),
+        "sg_batch_autotune": (i, [vp, vp, vp, vp, vp, i, i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+        "sg_batch_launch_shape": (i, [vp, pl, pi]),
         "sg_adjoint_create": (i, [vp, i, ctypes.POINTER(vp)]),
         "sg_adjoint_destroy": (i, [vp]),
         "sg_adjoint_counts": (i, [vp, pl, pl, pi]),
@@ -919,6 +921,20 @@ class Batch:
 
     def synchronize(self):
         _check(lib().sg_batch_synchronize(self._h), "sg_batch_synchronize")
+
+    def autotune(self, eps, regularity, a, dt, steps=3, scheme=UPWIND_OP):
+        """sg_batch_autotune: (batched step ms with the starting shape, with the chosen one, the chosen shape)"""
+        e, r, av, dv = self._params(eps), self._params(regularity), self._velocities(a), self._params(dt)
+        d0, d1 = ctypes.c_double(), ctypes.c_double()
+        _check(lib().sg_batch_autotune(self._h, _ptr(e), _ptr(r), _ptr(av), _ptr(dv), int(scheme), int(steps), ctypes.byref(d0),
+                                       ctypes.byref(d1)), "sg_batch_autotune")
+        return d0.value, d1.value, self.launch_shape()
+
+    def launch_shape(self):
+        """{fuse_words, block} shared by the batch's instances (block 0: each instance's own)"""
+        fw, bl = ctypes.c_longlong(), ctypes.c_int()
+        _check(lib().sg_batch_launch_shape(self._h, ctypes.byref(fw), ctypes.byref(bl)), "sg_batch_launch_shape")
+        return {"fuse_words": fw.value, "block": bl.value}
 
     def close(self):
         if getattr(self, "_h", None) is not None and _lib is not None:

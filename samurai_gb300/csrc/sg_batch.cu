@@ -10,6 +10,7 @@
 // thread drives its share in the same lockstep order.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +32,7 @@ namespace sg
     int ensure_spare(Ctx& c, DeviceField& f);
     void set_fusion(Ctx& c, long long mesh_words, long long field_words, long long max_words);
     void set_fusion_tops(Ctx& c, int mesh_top, int field_top, int max_top);
+    void clear_graphs(Ctx& c);
 }
 
 struct sg_batch_s
@@ -38,7 +40,10 @@ struct sg_batch_s
     std::vector<sg_field_t> u, unp1;
     std::vector<size_t> order; // instances by decreasing size: the largest are launched first
     int n_threads = 1;
-    std::vector<int> saved_tops; // the instances' own one-block chain limits, restored on destroy
+    std::vector<int> saved_tops;   // the instances' own one-block chain limits, restored on destroy
+    std::vector<int> saved_blocks; // the instances' own threads per block, restored on destroy
+    long long fuse_words = sg::BATCH_FUSE_WORDS; // one-block chain limit of every instance (words per level)
+    int block            = 0;                    // threads per block of every instance's FP64 list kernels (0: their own)
 
     // worker pool: thread t runs job(t) for every new generation
     std::vector<std::thread> workers;
@@ -384,6 +389,7 @@ extern "C"
         {
             sg::Ctx& c = u[k]->mesh->ctx;
             b->saved_tops.insert(b->saved_tops.end(), {c.fuse_top, c.fuse_top_field, c.fuse_top_max});
+            b->saved_blocks.push_back(c.block);
             sg::set_fusion(c, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS, sg::BATCH_FUSE_WORDS);
         }
         b->n_threads = std::min(n_threads, n);
@@ -406,7 +412,9 @@ extern "C"
         {
             for (size_t k = 0; k < b->u.size(); ++k)
             {
-                sg::set_fusion_tops(b->u[k]->mesh->ctx, b->saved_tops[3 * k], b->saved_tops[3 * k + 1], b->saved_tops[3 * k + 2]);
+                sg::Ctx& c = b->u[k]->mesh->ctx;
+                c.block    = b->saved_blocks[k];
+                sg::set_fusion_tops(c, b->saved_tops[3 * k], b->saved_tops[3 * k + 1], b->saved_tops[3 * k + 2]);
             }
         }
         delete b;
@@ -534,4 +542,186 @@ extern "C"
         return SG_OK;
     }
     SG_API_CATCH(sg_batch_synchronize)
+
+    // The batch's launch-shape autotuner: times `steps` batched steps from the instances' current state under
+    // candidate shapes (coordinate descent over the one-block chain limit shared by the instances, then the
+    // threads per block of their FP64 list kernels), every candidate from the same saved state after one
+    // untimed run that captures its graphs; keeps the fastest and leaves every instance as it found it.
+    int sg_batch_autotune(sg_batch_t b, const double* eps, const double* regularity, const double* a, const double* dt, int scheme, int steps,
+                          double* default_ms, double* tuned_ms)
+    try
+    {
+        if (!b || !eps || !regularity || steps < 1 || steps > 1000)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_autotune: null argument or steps outside 1..1000");
+        }
+        if (int st = check_upwind_args(b, a, dt, scheme))
+        {
+            return st;
+        }
+        const size_t n = b->u.size();
+        struct Saved
+        {
+            std::vector<int> lv, co;
+            std::vector<double> vals;
+        };
+        std::vector<Saved> saved(n);
+        for (size_t k = 0; k < n; ++k)
+        {
+            long long nc = 0, nr = 0;
+            sg_mesh_t mesh = b->u[k]->mesh;
+            const int dim  = mesh->ctx.g.dim;
+            if (int st = sg_mesh_counts(mesh, &nc, &nr))
+            {
+                return st;
+            }
+            saved[k].lv.resize(static_cast<size_t>(nc));
+            saved[k].co.resize(static_cast<size_t>(nc) * dim);
+            saved[k].vals.resize(static_cast<size_t>(nc));
+            if (int st = sg_mesh_get_cells(mesh, saved[k].lv.data(), saved[k].co.data(), nullptr, nc))
+            {
+                return st;
+            }
+            if (int st = sg_field_get_cells(b->u[k], saved[k].vals.data(), nc))
+            {
+                return st;
+            }
+        }
+        auto restore = [&]() -> int
+        {
+            for (size_t k = 0; k < n; ++k)
+            {
+                const long long nc = static_cast<long long>(saved[k].lv.size());
+                if (int st = sg_mesh_set_cells(b->u[k]->mesh, nc, saved[k].lv.data(), saved[k].co.data()))
+                {
+                    return st;
+                }
+                if (int st = sg_field_set_cells(b->u[k], saved[k].vals.data(), nc))
+                {
+                    return st;
+                }
+            }
+            return sg_batch_synchronize(b);
+        };
+        auto apply = [&](long long fuse, int block)
+        {
+            for (size_t k = 0; k < n; ++k)
+            {
+                sg::Ctx& c = b->u[k]->mesh->ctx;
+                c.block    = block > 0 ? block : b->saved_blocks[k];
+                sg::set_fusion(c, fuse, fuse, fuse); // drops the captured graphs
+            }
+            b->fuse_words = fuse;
+            b->block      = block;
+        };
+        auto measure = [&](double* ms) -> int
+        {
+            for (int rep = 0; rep < 2; ++rep)
+            {
+                if (int st = restore())
+                {
+                    return st;
+                }
+                const auto t0 = std::chrono::steady_clock::now();
+                for (int k = 0; k < steps; ++k)
+                {
+                    if (int st = sg_batch_step(b, eps, regularity, a, dt, scheme, nullptr))
+                    {
+                        return st;
+                    }
+                }
+                if (int st = sg_batch_synchronize(b))
+                {
+                    return st;
+                }
+                *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count() / steps;
+            }
+            return SG_OK;
+        };
+        const long long fuse0 = b->fuse_words;
+        const int block0      = b->block;
+        double base           = 0.;
+        int st                = measure(&base);
+        long long best_fuse   = fuse0;
+        int best_block        = block0;
+        double best           = base;
+        const long long fuses[] = {0, 128, 1024, 10000, 100000};
+        for (long long f : fuses)
+        {
+            if (st || f == fuse0)
+            {
+                continue;
+            }
+            apply(f, best_block);
+            double ms = 0.;
+            if ((st = measure(&ms)))
+            {
+                break;
+            }
+            if (ms < best * 0.98)
+            {
+                best      = ms;
+                best_fuse = f;
+            }
+        }
+        const int blocks[] = {128, 256, 512};
+        for (int bl : blocks)
+        {
+            if (st || bl == best_block)
+            {
+                continue;
+            }
+            apply(best_fuse, bl);
+            double ms = 0.;
+            if ((st = measure(&ms)))
+            {
+                break;
+            }
+            if (ms < best * 0.98)
+            {
+                best       = ms;
+                best_block = bl;
+            }
+        }
+        if (st)
+        {
+            apply(fuse0, block0);
+            restore();
+            return st;
+        }
+        apply(best_fuse, best_block);
+        if ((st = restore()))
+        {
+            return st;
+        }
+        if (default_ms)
+        {
+            *default_ms = base;
+        }
+        if (tuned_ms)
+        {
+            *tuned_ms = best;
+        }
+        return SG_OK;
+    }
+    SG_API_CATCH(sg_batch_autotune)
+
+    int sg_batch_launch_shape(sg_batch_t b, long long* fuse_words, int* block)
+    try
+    {
+        if (!b)
+        {
+            return bfail(SG_ERR_ARG, "sg_batch_launch_shape: null batch");
+        }
+        if (fuse_words)
+        {
+            *fuse_words = b->fuse_words;
+        }
+        if (block)
+        {
+            *block = b->block;
+        }
+        return SG_OK;
+    }
+    SG_API_CATCH(sg_batch_launch_shape)
 }

@@ -50,6 +50,40 @@ def same_state(a, b, max_level, where):
     assert bad.size == 0, "%s: %d leaf values differ" % (where, bad.size)
 
 
+def test_batch_autotune_keeps_state_and_results(sg):
+    """sg_batch_autotune leaves every instance as it found it, and the
+    batch stepped under the chosen shape still matches the serial calls"""
+    probs, batched = make_problems(sg, 13, 6, with_3d=False)
+    _, serial = make_problems(sg, 13, 6, with_3d=False)
+    batch = sg.Batch(batched, n_threads=2)
+    eps = [p["eps"] for p in probs]
+    reg = [p["regularity"] for p in probs]
+    a = [p["a"] for p in probs]
+    dt = [p["dt"] for p in probs]
+    batch.adapt(eps, reg)
+    for p, s in zip(probs, serial):
+        s.adapt(p["eps"], p["regularity"])
+    batch.synchronize()
+    before = [(s.cells(), s.cell_values()) for s in batched]
+    d_ms, t_ms, shape = batch.autotune(eps, reg, a, dt, steps=2)
+    assert 0 < t_ms <= d_ms
+    assert shape["fuse_words"] in (0, 128, 1024, 10000, 100000) and shape["block"] in (0, 128, 256, 512)
+    for k, s in enumerate(batched):
+        (lv, co, ix), vals = s.cells(), s.cell_values()
+        assert np.array_equal(lv, before[k][0][0]) and np.array_equal(co, before[k][0][1]), "instance %d: cells changed" % k
+        assert np.array_equal(vals, before[k][1]), "instance %d: values changed" % k
+    for step in range(3):
+        batch.step(eps, reg, a, dt)
+        for p, s in zip(probs, serial):
+            s.adapt(p["eps"], p["regularity"])
+            s.update_ghost()
+            s.upwind(p["a"], p["dt"])
+        batch.synchronize()
+        for k, (p, s) in enumerate(zip(probs, serial)):
+            same_state(batched[k], s, p["max_level"], "tuned step %d, instance %d" % (step, k))
+    batch.close()
+
+
 @pytest.mark.parametrize("n_threads", [1, 4])
 def test_batch_matches_serial(sg, n_threads):
     probs, batched = make_problems(sg, 11, 9, with_3d=True)
