@@ -62,6 +62,18 @@ def workload_config(extra=None):
     return c
 
 
+def uniform_mesh(mesh, dim, level):
+    """make the leaf cells of `mesh` the uniform mesh of `level`"""
+    idx = np.arange(1 << level, dtype=np.int32)
+    if dim == 2:
+        y, x = np.meshgrid(idx, idx, indexing="ij")
+        coords = np.stack([x.ravel(), y.ravel()], axis=1)
+    else:
+        z, y, x = np.meshgrid(idx, idx, idx, indexing="ij")
+        coords = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    mesh.set_cells(np.full(coords.shape[0], level, np.int32), coords)
+
+
 def initial_values(level, coords):
     if CFG["dim"] == 3:
         return ball_3d(CFG["seed"])(level, coords)
@@ -288,9 +300,10 @@ def step_kernel_table(sim, step, dim, maxl, minl, halo, peak):
     return {"valid": valid, "harten_passes": passes, "launches": sum(r[1] for r in rows), "traced_ms": total_ms,
             "algorithmic_bytes": int(total_b), "kernels": table,
             "mesh_counts": counts,
-            "note": "one step traced inside its captured graphs: each launch's time runs from the previous launch's end event to its own "
-                    "(kernel time plus the gap before it); bytes: each array element once per kernel (FP64 kernels from the mesh-id "
-                    "counts, word kernels 4 B per bitmap word of the levels they cover)"}
+            "note": "one step traced inside its captured graphs: each launch's time runs from the previous launch's end event (or the "
+                    "head event of its graph: host round trips between graphs are charged to no kernel) to its own (kernel time plus "
+                    "the gap before it); bytes: each array element once per kernel (FP64 kernels from the mesh-id counts, word kernels "
+                    "4 B per bitmap word of the levels they cover)"}
 
 
 # --------------------------------------------------------------- GPU arm
@@ -312,6 +325,9 @@ def run_gpu(args):
     a = list(CFG["a"])
     dt = CFG["cfl"] / (1 << maxl)
     sim = sg.AdvectionSim(dim, minl, maxl, 1, 1)
+    if args.init_level is not None and args.init_level < maxl:
+        # the initial condition sampled on a coarser uniform mesh (the adaptation refines where the details ask)
+        uniform_mesh(sim.mesh, dim, args.init_level)
     lv, co, _ = sim.cells()
     sim.set_cell_values(initial_values(lv, co))
     sim.adapt(CFG["eps"], CFG["regularity"])  # initial adaptation, as the demo does before its loop
@@ -368,7 +384,10 @@ def run_gpu(args):
     if args.quick:
         # profiling runs: the timed steps only
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": total_ms_max / args.steps, "quick": True}))
+            free, total = torch.cuda.mem_get_info()
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": total_ms_max / args.steps, "quick": True,
+                              "config": workload_config({"cells_final": sim.nb_cells(), "initial_mesh_level": args.init_level or maxl}),
+                              "device_memory_used_gb": (total - free) / 1e9}))
         return
 
     # ---- end-to-end through the C ABI with host buffers
@@ -899,7 +918,9 @@ def main():
     p.add_argument("--workload", default="advection2d", choices=["advection2d", "advection3d", "batch", "adjoint"],
                    help="advection2d: the max_level-12 2D problem (default); batch: independent problems through sg_batch_step; "
                         "adjoint: the discrete adjoint of a max_level-10 loop")
-    p.add_argument("--max-level", type=int, default=None, help="a smaller max_level for the advection workloads (profiling captures)")
+    p.add_argument("--max-level", type=int, default=None, help="another max_level for the advection workloads")
+    p.add_argument("--init-level", type=int, default=None,
+                   help="advection workloads: sample the initial condition on the uniform mesh of this level (default: max_level)")
     p.add_argument("--adjoint-steps", type=int, default=256)
     p.add_argument("--fd-directions", type=int, default=64)
     p.add_argument("--instances", type=int, default=256)

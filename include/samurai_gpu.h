@@ -113,17 +113,21 @@ int sg_mesh_set_adapt_graph(sg_mesh_t mesh, int enable);
 /* Without a samurai counterpart: the launch-shape autotuner.  Times sg_step(u, unp1, eps, regularity, a, dt, scheme)
  * over `steps` steps from the problem's current state under candidate launch shapes (threads per block of the FP64
  * list kernels, grid limit of the word launches, level sizes up to which the ghost-update and tag-finalisation
- * chains run in one block), keeps the fastest on the mesh and caches it for this device and level range (later
- * meshes start from it; SG_TUNE_FILE names a file that keeps the cache across processes; the SG_BLOCK,
- * SG_MAX_BLOCKS, SG_FUSE_WORDS* environment variables override it).  The problem is left in the state it had.
- * default_ms / tuned_ms receive the step time under the starting and the chosen shape. */
+ * chains run in one block, the adaptation path of sg_mesh_set_adapt_graph, two levels per launch in the
+ * tag-finalisation chain), each step after an untimed 256 MiB
+ * write that empties the L2 (a scratch array held during the call), keeps the fastest on the mesh and caches it for
+ * this device and level range (later meshes start from it; SG_TUNE_FILE names a file that keeps the cache across
+ * processes; the SG_BLOCK, SG_MAX_BLOCKS, SG_FUSE_WORDS*, SG_GRAPHED_ADAPT, SG_LEVEL_PAIRS environment variables
+ * override it).  The
+ * problem is left in the state it had.  default_ms / tuned_ms receive the step time under the starting and the
+ * chosen shape. */
 int sg_autotune(sg_field_t u, sg_field_t unp1, double eps, double regularity, const double* a, double dt, int scheme, int steps,
                 double* default_ms, double* tuned_ms);
 /* the mesh's launch shape: threads per block, grid limit (blocks of 8 warps), one-block chain limits in words per
- * level of the mesh, field and tag-finalisation chains, and 1 when the adaptation runs as one graph with conditional
- * nodes (0: pass by pass); any pointer may be NULL */
+ * level of the mesh, field and tag-finalisation chains, 1 when the adaptation runs as one graph with conditional
+ * nodes (0: pass by pass), 1 when the tag-finalisation chain takes two levels per launch; any pointer may be NULL */
 int sg_launch_shape(sg_mesh_t mesh, int* block, long long* max_blocks, long long* fuse_mesh_words, long long* fuse_field_words,
-                    long long* fuse_max_words, int* graphed_adapt);
+                    long long* fuse_max_words, int* graphed_adapt, int* level_pairs);
 
 /* samurai's named timers (timers.hpp:111-1036, printed with --timers): CUDA-event timers per phase.
  * ids: 0 mesh adaptation, 1 ghost update, 2 detail computation, 3 tag cells, 4 tag finalization,
@@ -282,8 +286,9 @@ int sg_batch_synchronize(sg_batch_t batch);
 /* Without a samurai counterpart: the batch's launch-shape autotuner.  Times `steps` batched steps (sg_batch_step)
  * from the instances' current state under candidate shapes (the level size, in words, up to which every instance's
  * ghost-update, tag-finalisation and mesh chains run their levels in one block; the threads per block of their FP64
- * list kernels), each from the same saved state; keeps the fastest and leaves every instance's mesh and values as
- * they were.  default_ms / tuned_ms receive the batched step time under the starting and the chosen shape. */
+ * list kernels), each from the same saved state and each step after an untimed 256 MiB write that empties the L2;
+ * keeps the fastest and leaves every instance's mesh and values as they were.  default_ms / tuned_ms receive the
+ * batched step time under the starting and the chosen shape. */
 int sg_batch_autotune(sg_batch_t batch, const double* eps, const double* regularity, const double* a, const double* dt, int scheme,
                       int steps, double* default_ms, double* tuned_ms);
 /* the batch's launch shape: one-block chain limit in words per level, threads per block (0: each instance's own) */

@@ -94,7 +94,7 @@ def lib():
         "sg_upwind": (i, [vp, vp, vp, d, i]),
         "sg_step": (i, [vp, vp, d, d, vp, d, i, pi]),
         "sg_autotune": (i, [vp, vp, d, d, vp, d, i, i, ctypes.POINTER(d), ctypes.POINTER(d)]),
-        "sg_launch_shape": (i, [vp, pi, pl, pl, pl, pl, pi]),
+        "sg_launch_shape": (i, [vp, pi, pl, pl, pl, pl, pi, pi]),
         "sg_detail_download": (i, [vp, vp, ll]),
         "sg_tag_download": (i, [vp, vp, ll]),
         "sg_batch_create": (i, [i, vp, vp, i, ctypes.POINTER(vp)]),
@@ -379,13 +379,13 @@ class MRMesh:
         return out
 
     def launch_shape(self):
-        """{block, max_blocks, fuse_mesh_words, fuse_field_words, fuse_max_words, graphed_adapt} of this mesh's launches"""
+        """{block, max_blocks, fuse_mesh_words, fuse_field_words, fuse_max_words, graphed_adapt, level_pairs} of this mesh's launches"""
         b, mb, fm, ff, fx = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
-        gr = ctypes.c_int()
+        gr, lp = ctypes.c_int(), ctypes.c_int()
         _check(lib().sg_launch_shape(self.h, ctypes.byref(b), ctypes.byref(mb), ctypes.byref(fm), ctypes.byref(ff), ctypes.byref(fx),
-                                     ctypes.byref(gr)), "sg_launch_shape")
+                                     ctypes.byref(gr), ctypes.byref(lp)), "sg_launch_shape")
         return {"block": b.value, "max_blocks": mb.value, "fuse_mesh_words": fm.value, "fuse_field_words": ff.value, "fuse_max_words": fx.value,
-                "graphed_adapt": bool(gr.value)}
+                "graphed_adapt": bool(gr.value), "level_pairs": bool(lp.value)}
 
     def set_adapt_graph(self, enable):
         """each adaptation as one captured graph with conditional nodes (True) or pass by pass (False, the default)"""

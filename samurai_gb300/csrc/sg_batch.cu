@@ -546,7 +546,8 @@ extern "C"
     // The batch's launch-shape autotuner: times `steps` batched steps from the instances' current state under
     // candidate shapes (coordinate descent over the one-block chain limit shared by the instances, then the
     // threads per block of their FP64 list kernels), every candidate from the same saved state after one
-    // untimed run that captures its graphs; keeps the fastest and leaves every instance as it found it.
+    // untimed run that captures its graphs, every step after an L2 flush; keeps the fastest and leaves every
+    // instance as it found it.
     int sg_batch_autotune(sg_batch_t b, const double* eps, const double* regularity, const double* a, const double* dt, int scheme, int steps,
                           double* default_ms, double* tuned_ms)
     try
@@ -614,7 +615,16 @@ extern "C"
             b->fuse_words = fuse;
             b->block      = block;
         };
-        auto measure = [&](double* ms) -> int
+        // every timed step starts with a cold L2 (a 256 MiB write, not timed), as a step does that follows other work
+        const size_t flush_bytes = 256u << 20;
+        void* flush              = nullptr;
+        if (cudaMalloc(&flush, flush_bytes) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return bfail(SG_ERR_CUDA, "sg_batch_autotune: no device memory for the L2 flush");
+        }
+        cudaStream_t s0 = b->u[0]->mesh->ctx.stream;
+        auto measure    = [&](double* ms) -> int
         {
             for (int rep = 0; rep < 2; ++rep)
             {
@@ -622,19 +632,26 @@ extern "C"
                 {
                     return st;
                 }
-                const auto t0 = std::chrono::steady_clock::now();
+                double total = 0.;
                 for (int k = 0; k < steps; ++k)
                 {
+                    cudaMemsetAsync(flush, k & 0xFF, flush_bytes, s0);
+                    if (cudaStreamSynchronize(s0) != cudaSuccess)
+                    {
+                        return bfail(SG_ERR_CUDA, "sg_batch_autotune: L2 flush failed");
+                    }
+                    const auto t0 = std::chrono::steady_clock::now();
                     if (int st = sg_batch_step(b, eps, regularity, a, dt, scheme, nullptr))
                     {
                         return st;
                     }
+                    if (int st = sg_batch_synchronize(b))
+                    {
+                        return st;
+                    }
+                    total += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
                 }
-                if (int st = sg_batch_synchronize(b))
-                {
-                    return st;
-                }
-                *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count() / steps;
+                *ms = total / steps;
             }
             return SG_OK;
         };
@@ -683,6 +700,7 @@ extern "C"
                 best_block = bl;
             }
         }
+        cudaFree(flush);
         if (st)
         {
             apply(fuse0, block0);

@@ -457,11 +457,18 @@ extern "C"
         // the pass-by-pass path by default: on GB300 with driver 580 a conditional graph node costs about 9 us
         // (measured), more than the host round trip per Harten pass it replaces
         c.graphed_adapt = tuned("SG_GRAPHED_ADAPT", 0) != 0;
+        c.level_pairs   = tuned("SG_LEVEL_PAIRS", 1) != 0;
+        if (cudaGetDevice(&c.device) != cudaSuccess)
+        {
+            cudaGetLastError();
+            delete h;
+            return fail(SG_ERR_CUDA, "sg_mesh_create: no CUDA device");
+        }
         sg::apply_tuned_launch(c); // the autotuner's choice for this device and level range, unless overridden above
         c.fuse_top                 = sg::fuse_top_of(c.g, c.fuse_words_mesh);
         c.fuse_top_field           = sg::fuse_top_of(c.g, c.fuse_words_field);
         c.fuse_top_max             = sg::fuse_top_of(c.g, c.fuse_words_max);
-        if (cudaGetDevice(&c.device) != cudaSuccess || cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
+        if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
         {
             cudaGetLastError();
             delete h;
@@ -475,6 +482,7 @@ extern "C"
                 cs = nullptr;
             }
         }
+
         const size_t nw = static_cast<size_t>(c.g.total_words);
         int st          = alloc_mesh(c, c.mesh[0]);
         st |= alloc_mesh(c, c.mesh[1]);
@@ -966,6 +974,11 @@ extern "C"
         cudaEvent_t prev = c.trace.start;
         for (const auto& mk : c.trace.marks)
         {
+            if (!mk.first)
+            {
+                prev = mk.second; // the head of a launch sequence: the gap before it belongs to no kernel
+                continue;
+            }
             float ms = 0.f;
             if (cudaEventElapsedTime(&ms, prev, mk.second) != cudaSuccess)
             {

@@ -143,6 +143,7 @@ namespace sg
         static constexpr int CAPTURE_DEPTH = 4;
         cudaStream_t cap_streams[CAPTURE_DEPTH] = {};
         int cap_depth = 0;
+        bool level_pairs = true; // tag finalisation two levels per launch (k_maximum2)
         int* d_adapt  = nullptr; // device state of a graphed adaptation (AdaptSlot)
         int* h_adapt  = nullptr; // pinned mirror of d_adapt
         bool graphed_adapt = true; // the whole adaptation as one graph with conditional nodes
@@ -254,6 +255,7 @@ namespace sg
     // bookkeeping after every kernel launch: the launch counter and, while the
     // kernel trace is on, the trace event of the launch
     void launched(Ctx& c, const char* name, int count = 1);
+    void trace_mark(Ctx& c, const char* name); // a trace event (name null: the head of a launch sequence)
     void clear_graphs(Ctx& c); // drops the captured launch sequences (their trace events go back to the pool)
     void apply_tuned_launch(Ctx& c); // the autotuner's cached launch shape for the mesh's device and levels (sg_tune.cu)
     cudaEvent_t take_event(Ctx& c);

@@ -43,7 +43,11 @@ namespace sg
         // non-empty words of a superset (reference or leaf cells) in
         // ascending order; word_of(w) narrows it to the subset a kernel acts
         // on.  Consecutive cells of a word are consecutive doubles, so every
-        // field access of a warp is one 256-byte segment.
+        // field access of a warp is one 256-byte segment.  A null list means
+        // every word of [begin, end): the dense range of small levels, which
+        // a launch covers with one warp per word without loading the list
+        // or its offsets (two dependent loads fewer at the head of the
+        // launch; word_of is zero on the words the list leaves out).
         template <class WordF, class CellF>
         __device__ __forceinline__ void warp_list(const int* list, long long begin, long long end, long long warp0, long long nwarps, WordF word_of,
                                                   CellF cell)
@@ -51,7 +55,7 @@ namespace sg
             const int lane = threadIdx.x & 31;
             for (long long i = begin + warp0; i < end; i += nwarps)
             {
-                const long long w = __ldg(list + i);
+                const long long w = list ? __ldg(list + i) : i;
                 const uint32_t v  = word_of(w);
                 if ((v >> lane) & 1u)
                 {
@@ -97,7 +101,7 @@ namespace sg
                 uint32_t m  = 0u;
                 if (lane < ch && c0 + lane < end)
                 {
-                    w = __ldg(list + c0 + lane);
+                    w = list ? __ldg(list + c0 + lane) : c0 + lane;
                     m = word_of(w);
                 }
                 int incl = __popc(m); // inclusive prefix of the item counts over the lanes
@@ -657,7 +661,8 @@ namespace sg
                                                       const A& u, long long warp0, long long nwarps)
         {
             const int lc = l - 1;
-            warp_list_compact(wl_ref, lo[LO_REF + lc], lo[LO_REF + lc + 1], warp0, nwarps,
+            const LevelGeom& C = g.lv[lc];
+            warp_list_compact(lo ? wl_ref : nullptr, lo ? lo[LO_REF + lc] : C.woff, lo ? lo[LO_REF + lc + 1] : C.woff + C.nwords, warp0, nwarps,
                       [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, lc, w);
@@ -676,7 +681,8 @@ namespace sg
         __device__ __forceinline__ void predict_level(const Geom& g, int l, int order, const int* wl_ref, const long long* lo, const uint32_t* cells,
                                                       const uint32_t* proj, const uint32_t* ref, const A& u, long long warp0, long long nwarps)
         {
-            warp_list_compact(wl_ref, lo[LO_REF + l], lo[LO_REF + l + 1], warp0, nwarps,
+            const LevelGeom& L = g.lv[l];
+            warp_list_compact(lo ? wl_ref : nullptr, lo ? lo[LO_REF + l] : L.woff, lo ? lo[LO_REF + l + 1] : L.woff + L.nwords, warp0, nwarps,
                       [&](long long w)
                       {
                           const WordLoc loc = word_loc(g, l, w);
@@ -1144,7 +1150,8 @@ namespace sg
                                                       uint8_t* tag, long long warp0, long long nwarps)
         {
             const int lc = l - 1;
-            warp_list(wl, lo[LO_REF + lc], lo[LO_REF + l], warp0, nwarps,
+            const LevelGeom& C = g.lv[lc];
+            warp_list(lo ? wl : nullptr, lo ? lo[LO_REF + lc] : C.woff, lo ? lo[LO_REF + l] : C.woff + C.nwords, warp0, nwarps,
                       [&](long long w) { return ref[w] & hc[w]; },
                       [&](long long w, int b)
                       {
@@ -1209,7 +1216,9 @@ namespace sg
         {
             const Geom& g      = gp;
             const long long w1 = g.lv[l - 1].woff; // first word of level l-1
-            warp_list(wl, lo[LO_REF + l - 2], lo[LO_REF + l], warp_id(), warp_count(), [&](long long w) { return ref[w] & hc[w]; },
+            const LevelGeom& C = g.lv[l - 1];
+            warp_list(lo ? wl : nullptr, lo ? lo[LO_REF + l - 2] : g.lv[l - 2].woff, lo ? lo[LO_REF + l] : C.woff + C.nwords, warp_id(), warp_count(),
+                      [&](long long w) { return ref[w] & hc[w]; },
                       [&](long long w, int b)
                       {
                           const long long co = 32 * w + b;
@@ -1699,6 +1708,20 @@ namespace sg
         }
     } // namespace
 
+    namespace
+    {
+        // the offsets argument of a level-chain launch over levels l0..l1: null (the dense word range, no list)
+        // when the launch's grid gives every word of those levels a warp of its own, else the mesh's offsets
+        const long long* level_offsets(const Ctx& c, const DeviceMesh& m, int l0, int l1)
+        {
+            const Geom& g       = c.g;
+            const long long wpb = c.block / 32;
+            const long long cap = std::max(1LL, c.max_blocks * 8 / wpb) * wpb;
+            const long long n   = g.lv[l1].woff + g.lv[l1].nwords - g.lv[l0].woff;
+            return n <= cap ? nullptr : m.d_lo;
+        }
+    } // namespace
+
     cudaError_t launch_gather(Ctx& c, const DeviceMesh& m, const double* dense, double* compact)
     {
         k_gather<<<blocks_words(c, 0, c.g.nlev - 1), c.block, 0, c.stream>>>(m.wl_ref, m.d_lo, c.g.nlev, m.ref, m.rank, dense, compact);
@@ -1755,9 +1778,13 @@ namespace sg
     {
         if (!c.use_graphs || c.timers.enabled)
         {
+            if (c.trace.enabled)
+            {
+                trace_mark(c, nullptr);
+            }
             return seq();
         }
-        // a traced sequence carries its trace events as graph nodes: a graph of its own
+        // a traced sequence carries its trace events as graph nodes (a head event first): a graph of its own
         if (c.trace.enabled)
         {
             k0 |= 1ull << 63;
@@ -1791,6 +1818,10 @@ namespace sg
         }
         const int before      = c.n_launches;
         const size_t marks0   = c.trace.marks.size();
+        if (c.trace.enabled)
+        {
+            trace_mark(c, nullptr);
+        }
         int st                = seq();
         cudaGraph_t graph     = nullptr;
         cudaError_t e         = cudaStreamEndCapture(c.stream, &graph);
@@ -2205,16 +2236,17 @@ namespace sg
                 a.nb_face         = static_cast<int>((a.nfaces + c.block - 1) / c.block);
                 a.do_proj         = l > lmin;
                 const int nb_proj = a.do_proj ? blocks_words(c, l - 1, l - 1) : 0;
+                const long long* proj_lo = a.do_proj ? level_offsets(c, m, l - 1, l - 1) : m.d_lo;
                 const int grid    = a.nb_corner + a.nb_face + nb_proj;
                 if (grid > 0)
                 {
                     if (g.dim == 2)
                     {
-                        k_ghost_level<2><<<grid, c.block, 0, c.stream>>>(c.g, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<2><<<grid, c.block, 0, c.stream>>>(c.g, a, m.wl_ref, proj_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     else
                     {
-                        k_ghost_level<3><<<grid, c.block, 0, c.stream>>>(c.g, a, m.wl_ref, m.d_lo, m.cells, m.uni, m.proj, m.ref, u);
+                        k_ghost_level<3><<<grid, c.block, 0, c.stream>>>(c.g, a, m.wl_ref, proj_lo, m.cells, m.uni, m.proj, m.ref, u);
                     }
                     launched(c, "ghost_level");
                     after();
@@ -2277,12 +2309,12 @@ namespace sg
             {
                 if (g.dim == 2)
                 {
-                    k_predict<2><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.g, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<2><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.g, lp, c.cfg.prediction_radius, m.wl_ref, level_offsets(c, m, lp, lp), m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 else
                 {
-                    k_predict<3><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.g, lp, c.cfg.prediction_radius, m.wl_ref, m.d_lo, m.cells, m.proj,
+                    k_predict<3><<<blocks_words(c, lp, lp), c.block, 0, c.stream>>>(c.g, lp, c.cfg.prediction_radius, m.wl_ref, level_offsets(c, m, lp, lp), m.cells, m.proj,
                                                                                    m.ref, u);
                 }
                 launched(c, "predict");
@@ -2424,28 +2456,30 @@ namespace sg
                 while (l >= lstop && l - 1 > top)
                 {
                     periodic_tags(c, m, l);
-                    if (!g.periodic && l - 1 >= lstop && l - 2 > top)
+                    if (c.level_pairs && !g.periodic && l - 1 >= lstop && l - 2 > top)
                     {
                         // children at levels l and l-1 in one launch
                         if (g.dim == 2)
                         {
-                            k_maximum2<2><<<blocks_words(c, l - 2, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                            k_maximum2<2><<<blocks_words(c, l - 2, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, level_offsets(c, m, l - 2, l - 1), m.ref, m.hc,
+                                                                                         c.tag);
                         }
                         else
                         {
-                            k_maximum2<3><<<blocks_words(c, l - 2, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                            k_maximum2<3><<<blocks_words(c, l - 2, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, level_offsets(c, m, l - 2, l - 1), m.ref, m.hc,
+                                                                                         c.tag);
                         }
-                        launched(c, "maximum2");
+                        launched(c, "maximum"); // the trace groups the one- and two-level launches
                         l -= 2;
                         continue;
                     }
                     if (g.dim == 2)
                     {
-                        k_maximum<2><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<2><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, level_offsets(c, m, l - 1, l - 1), m.ref, m.hc, c.tag);
                     }
                     else
                     {
-                        k_maximum<3><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, m.d_lo, m.ref, m.hc, c.tag);
+                        k_maximum<3><<<blocks_words(c, l - 1, l - 1), c.block, 0, c.stream>>>(c.g, l, m.wl_ref, level_offsets(c, m, l - 1, l - 1), m.ref, m.hc, c.tag);
                     }
                     launched(c, "maximum");
                     --l;

@@ -59,21 +59,28 @@ namespace sg
         c.n_launches += count;
         if (c.trace.enabled)
         {
-            // inside a stream capture an external record becomes an event-record node of the graph (a plain
-            // record would only order the capture); outside a capture it is a plain record
-            cudaEvent_t e = take_event(c);
-            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-            cudaStreamIsCapturing(c.stream, &cs);
-            if (cs == cudaStreamCaptureStatusActive)
-            {
-                cudaEventRecordWithFlags(e, c.stream, cudaEventRecordExternal);
-            }
-            else
-            {
-                cudaEventRecord(e, c.stream);
-            }
-            c.trace.marks.push_back({name, e});
+            trace_mark(c, name);
         }
+    }
+
+    // a trace event after the work queued so far; name null for the head of a launch sequence (the time before
+    // it, a host round trip included, is charged to no kernel)
+    void trace_mark(Ctx& c, const char* name)
+    {
+        // inside a stream capture an external record becomes an event-record node of the graph (a plain
+        // record would only order the capture); outside a capture it is a plain record
+        cudaEvent_t e              = take_event(c);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(c.stream, &cs);
+        if (cs == cudaStreamCaptureStatusActive)
+        {
+            cudaEventRecordWithFlags(e, c.stream, cudaEventRecordExternal);
+        }
+        else
+        {
+            cudaEventRecord(e, c.stream);
+        }
+        c.trace.marks.push_back({name, e});
     }
 
     namespace

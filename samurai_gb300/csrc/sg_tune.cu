@@ -5,14 +5,16 @@
 // on the device and on the size of the mesh: the threads per block of the
 // FP64 list kernels, the grid limit of the one-warp-per-word launches, the
 // level sizes up to which a chain (ghost update, tag finalisation, mesh
-// construction) runs its levels in one block, and whether the adaptation runs
-// as one graph with conditional nodes or pass by pass.  sg_autotune times the time
+// construction) runs its levels in one block, whether the adaptation runs
+// as one graph with conditional nodes or pass by pass, and whether the
+// tag-finalisation chain takes two levels per launch.  sg_autotune times the time
 // step of a given problem under candidate shapes (coordinate descent, each
 // candidate from the same saved state, its graphs captured afresh), keeps the
 // fastest on the mesh and caches it per device and level range; later meshes
 // of the same device and levels start from the cached choice.  Environment
 // variables (SG_BLOCK, SG_MAX_BLOCKS, SG_FUSE_WORDS, SG_FUSE_WORDS_FIELD,
-// SG_FUSE_WORDS_MAX) override both the defaults and the cache.  With
+// SG_FUSE_WORDS_MAX, SG_GRAPHED_ADAPT, SG_LEVEL_PAIRS) override
+// both the defaults and the cache.  With
 // SG_TUNE_FILE set, the cache is also read from and appended to that file.
 #include <algorithm>
 #include <cstdio>
@@ -37,7 +39,8 @@ namespace sg
         {
             int block;
             long long max_blocks, fuse_mesh, fuse_field, fuse_max;
-            int graphed; // the adaptation as one graph with conditional nodes (1) or pass by pass (0)
+            int graphed;     // the adaptation as one graph with conditional nodes (1) or pass by pass (0)
+            int level_pairs; // tag finalisation two levels per launch (1) or one (0)
         };
 
         using TuneKey = std::tuple<std::string, int, int, int>; // device name, dim, min_level, max_level
@@ -59,7 +62,7 @@ namespace sg
             return n;
         }
 
-        // SG_TUNE_FILE: lines "device dim min max block max_blocks fuse_mesh fuse_field fuse_max graphed" (the last line of a
+        // SG_TUNE_FILE: lines "device dim min max block max_blocks fuse_mesh fuse_field fuse_max graphed level_pairs" (the last line of a
         // key wins); read once, under the cache mutex
         void read_tune_file()
         {
@@ -79,13 +82,14 @@ namespace sg
                 return;
             }
             char name[256];
-            int dim, lo, hi, block, gr;
+            int dim, lo, hi, block, gr, lp;
             long long mb, fm, ff, fx;
-            while (std::fscanf(f, "%255s %d %d %d %d %lld %lld %lld %lld %d", name, &dim, &lo, &hi, &block, &mb, &fm, &ff, &fx, &gr) == 10)
+            while (std::fscanf(f, "%255s %d %d %d %d %lld %lld %lld %lld %d %d", name, &dim, &lo, &hi, &block, &mb, &fm, &ff, &fx, &gr, &lp) == 11)
             {
-                if (block >= 32 && block <= 1024 && block % 32 == 0 && mb > 0 && fm >= 0 && ff >= 0 && fx >= 0 && (gr == 0 || gr == 1))
+                if (block >= 32 && block <= 1024 && block % 32 == 0 && mb > 0 && fm >= 0 && ff >= 0 && fx >= 0 && (gr == 0 || gr == 1)
+                    && (lp == 0 || lp == 1))
                 {
-                    g_tune_cache[TuneKey{name, dim, lo, hi}] = LaunchShape{block, mb, fm, ff, fx, gr};
+                    g_tune_cache[TuneKey{name, dim, lo, hi}] = LaunchShape{block, mb, fm, ff, fx, gr, lp};
                 }
             }
             std::fclose(f);
@@ -100,8 +104,8 @@ namespace sg
             }
             if (FILE* f = std::fopen(path, "a"))
             {
-                std::fprintf(f, "%s %d %d %d %d %lld %lld %lld %lld %d\n", std::get<0>(k).c_str(), std::get<1>(k), std::get<2>(k), std::get<3>(k),
-                             s.block, s.max_blocks, s.fuse_mesh, s.fuse_field, s.fuse_max, s.graphed);
+                std::fprintf(f, "%s %d %d %d %d %lld %lld %lld %lld %d %d\n", std::get<0>(k).c_str(), std::get<1>(k), std::get<2>(k), std::get<3>(k),
+                             s.block, s.max_blocks, s.fuse_mesh, s.fuse_field, s.fuse_max, s.graphed, s.level_pairs);
                 std::fclose(f);
             }
         }
@@ -119,7 +123,7 @@ namespace sg
 
         LaunchShape shape_of(const Ctx& c)
         {
-            return LaunchShape{c.block, c.max_blocks, c.fuse_words_mesh, c.fuse_words_field, c.fuse_words_max, c.graphed_adapt ? 1 : 0};
+            return LaunchShape{c.block, c.max_blocks, c.fuse_words_mesh, c.fuse_words_field, c.fuse_words_max, c.graphed_adapt ? 1 : 0, c.level_pairs ? 1 : 0};
         }
 
         // applies a shape to a mesh (its captured graphs were recorded with the old one and are dropped)
@@ -128,7 +132,8 @@ namespace sg
             c.block         = s.block;
             c.max_blocks    = s.max_blocks;
             c.graphed_adapt = s.graphed != 0;
-            set_fusion(c, s.fuse_mesh, s.fuse_field, s.fuse_max);
+            c.level_pairs   = s.level_pairs != 0;
+            set_fusion(c, s.fuse_mesh, s.fuse_field, s.fuse_max); // drops the captured graphs
         }
     } // namespace
 
@@ -166,6 +171,10 @@ namespace sg
         if (!env_set("SG_GRAPHED_ADAPT"))
         {
             c.graphed_adapt = s.graphed != 0;
+        }
+        if (!env_set("SG_LEVEL_PAIRS"))
+        {
+            c.level_pairs = s.level_pairs != 0;
         }
     }
 } // namespace sg
@@ -222,8 +231,19 @@ extern "C"
             }
             return sg_field_set_cells(u, vals.data(), nc);
         };
-        // ms per step of `steps` steps from the saved state (the best of two runs), after two untimed steps that
-        // capture the shape's graphs
+        // every timed step starts with a cold L2 (a 256 MiB write before it, not timed), as a step does that follows
+        // other work
+        const size_t flush_bytes = 256u << 20;
+        void* flush              = nullptr;
+        if (cudaMalloc(&flush, flush_bytes) != cudaSuccess)
+        {
+            cudaGetLastError();
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return tfail(SG_ERR_CUDA, "sg_autotune: no device memory for the L2 flush");
+        }
+        // ms per step of `steps` steps from the saved state (the best of two runs), after an untimed run that
+        // captures the shape's graphs
         auto measure = [&](double* ms) -> int
         {
             float best = 1e30f;
@@ -234,26 +254,28 @@ extern "C"
                     return st;
                 }
                 const int n = rep == 0 ? std::max(steps, 8) : steps; // rep 0 captures the graphs of every buffer combination
-                cudaStreamSynchronize(c.stream);
-                cudaEventRecord(e0, c.stream);
+                float total = 0.f;
                 for (int k = 0; k < n; ++k)
                 {
+                    cudaMemsetAsync(flush, k & 0xFF, flush_bytes, c.stream);
+                    cudaEventRecord(e0, c.stream);
                     int passes = 0;
                     if (int st = sg_step(u, unp1, eps, regularity, a, dt, scheme, &passes))
                     {
                         return st;
                     }
+                    cudaEventRecord(e1, c.stream);
+                    if (cudaEventSynchronize(e1) != cudaSuccess)
+                    {
+                        return tfail(SG_ERR_CUDA, "sg_autotune: CUDA error while timing");
+                    }
+                    float t = 0.f;
+                    cudaEventElapsedTime(&t, e0, e1);
+                    total += t;
                 }
-                cudaEventRecord(e1, c.stream);
-                if (cudaEventSynchronize(e1) != cudaSuccess)
-                {
-                    return tfail(SG_ERR_CUDA, "sg_autotune: CUDA error while timing");
-                }
-                float t = 0.f;
-                cudaEventElapsedTime(&t, e0, e1);
                 if (rep > 0)
                 {
-                    best = std::min(best, t / static_cast<float>(n));
+                    best = std::min(best, total / static_cast<float>(n));
                 }
             }
             *ms = best;
@@ -268,36 +290,25 @@ extern "C"
         const std::vector<long long> blocks = {128, 256, 512};
         const std::vector<long long> grids  = {152LL * 4, 152LL * 8, 152LL * 16};
         const std::vector<long long> fuses  = {0, 32, 128, 512};
-        const std::vector<long long> paths  = {0, 1};
-        for (int param = 0; param < 5 && !st; ++param)
+        const std::vector<long long> flags  = {0, 1};
+        for (int param = 0; param < 6 && !st; ++param)
         {
-            const std::vector<long long>& cands = param == 0 ? paths : (param == 1 ? blocks : (param == 2 ? grids : fuses));
+            const std::vector<long long>& cands = param <= 1 ? flags : (param == 2 ? blocks : (param == 3 ? grids : fuses));
             const sg::LaunchShape from          = best;
             for (long long v : cands)
             {
                 sg::LaunchShape s = from;
-                if (param == 0)
+                switch (param)
                 {
-                    s.graphed = static_cast<int>(v);
+                case 0: s.graphed = static_cast<int>(v); break;
+                case 1: s.level_pairs = static_cast<int>(v); break;
+                case 2: s.block = static_cast<int>(v); break;
+                case 3: s.max_blocks = v; break;
+                case 4: s.fuse_field = v; break;
+                default: s.fuse_max = v; break;
                 }
-                else if (param == 1)
-                {
-                    s.block = static_cast<int>(v);
-                }
-                else if (param == 2)
-                {
-                    s.max_blocks = v;
-                }
-                else if (param == 3)
-                {
-                    s.fuse_field = v;
-                }
-                else
-                {
-                    s.fuse_max = v;
-                }
-                if (s.graphed == from.graphed && s.block == from.block && s.max_blocks == from.max_blocks && s.fuse_field == from.fuse_field
-                    && s.fuse_max == from.fuse_max)
+                if (s.graphed == from.graphed && s.level_pairs == from.level_pairs && s.block == from.block
+                    && s.max_blocks == from.max_blocks && s.fuse_field == from.fuse_field && s.fuse_max == from.fuse_max)
                 {
                     continue;
                 }
@@ -316,6 +327,7 @@ extern "C"
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        cudaFree(flush);
         sg::apply_shape(c, st ? start : best);
         const int rs = restore();
         if (st)
@@ -345,7 +357,7 @@ extern "C"
     SG_API_CATCH(sg_autotune)
 
     int sg_launch_shape(sg_mesh_t mesh, int* block, long long* max_blocks, long long* fuse_mesh_words, long long* fuse_field_words,
-                        long long* fuse_max_words, int* graphed_adapt)
+                        long long* fuse_max_words, int* graphed_adapt, int* level_pairs)
     try
     {
         if (!mesh)
@@ -376,6 +388,10 @@ extern "C"
         if (graphed_adapt)
         {
             *graphed_adapt = c.graphed_adapt ? 1 : 0;
+        }
+        if (level_pairs)
+        {
+            *level_pairs = c.level_pairs ? 1 : 0;
         }
         return SG_OK;
     }
