@@ -152,8 +152,12 @@ class ClockSampler:
 
 
 UPWIND_ISSUED = {2: 10 * 2 + 3 + 2, 3: 10 * 3 + 5 + 2}
-# DRAM bytes per launch of the kernels named dominant, from ncu captures (profiles/)
-DOMINANT_TRAFFIC = {}
+# DRAM bytes per launch of the kernels named dominant, by (dim, max_level, kernel), from ncu captures (profiles/):
+# (bytes, how they were measured)
+DOMINANT_TRAFFIC = {
+    (2, 12, "ghost_level"): (959558.0, "ncu dram__bytes_read.sum + dram__bytes_write.sum averaged over the 22 k_ghost_level launches of one "
+                              "2D max_level-12 step (levels 12..2, twice; caches emptied by ncu before each launch)"),
+}
 
 
 def left_shared(level, coords):
@@ -483,7 +487,8 @@ def run_gpu(args):
     dom_launch_ms = dom["us"] / 1e3 / max(dom["launches"], 1)
     dom_bytes = dom["algorithmic_bytes"] / max(dom["launches"], 1)
     roofline = {"bound": "hbm", "kernel": dom["kernel"], "achieved": dom_bytes / (dom_launch_ms * 1e-3) / 1e9 if dom_launch_ms > 0 else None,
-                "peak": peak, "peak_source": peak_src, "unit": "GB/s", "traffic": DOMINANT_TRAFFIC.get(dom["kernel"]),
+                "peak": peak, "peak_source": peak_src, "unit": "GB/s", "traffic": DOMINANT_TRAFFIC.get((dim, maxl, dom["kernel"]), (None, None))[0],
+                "traffic_source": DOMINANT_TRAFFIC.get((dim, maxl, dom["kernel"]), (None, None))[1],
                 "algorithmic_bytes_per_launch": int(dom_bytes), "launch_ms": dom_launch_ms, "launches_per_step": dom["launches"],
                 "share_of_step": dom["us"] / 1e3 / ktab["traced_ms"] if ktab["traced_ms"] > 0 else None,
                 "timing": "per-launch trace events inside the captured graphs, one step"}

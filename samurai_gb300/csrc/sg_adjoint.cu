@@ -81,16 +81,26 @@ namespace sg
         // mu = U^T lam for unp1 = u - dt * upwind(a, u) on the leaf cells of
         // one mesh (the forward is k_upwind); gather form, one thread per
         // dense element, deterministic.
+        // Only the reference cells of the mesh are visited (the words of its reference list, a thread per bit):
+        // every value the upwind step reads is a reference cell (a leaf or a same-level neighbour of one), so mu
+        // is complete there; the transposes that follow read no other element.
         template <int DIM>
-        __global__ void k_upwind_adjoint(const __grid_constant__ Geom gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
+        __global__ void k_upwind_adjoint(const __grid_constant__ Geom gp, const int* __restrict__ wl_ref, const long long* __restrict__ lo,
+                                         const uint32_t* __restrict__ ref, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
                                          double* __restrict__ mu, UpwindAdj p)
         {
             const Geom& g       = gp;
-            const long long tot = 32 * g.total_words;
-            for (long long k = gtid(); k < tot; k += gstride())
+            const long long b0  = lo[LO_REF];
+            const long long tot = 32 * (lo[LO_REF + g.nlev] - b0);
+            for (long long t = gtid(); t < tot; t += gstride())
             {
-                const long long w = k >> 5;
-                const int b       = static_cast<int>(k & 31);
+                const long long w = wl_ref[b0 + (t >> 5)];
+                const int b       = static_cast<int>(t & 31);
+                if (!((ref[w] >> b) & 1u))
+                {
+                    continue;
+                }
+                const long long k = 32 * w + b;
                 const int l       = level_of(g, w);
                 const Cell c      = cell_of(g, l, w, b);
                 const double s    = p.dt * pow2d(l);
@@ -123,18 +133,21 @@ namespace sg
             }
         }
 
-        // per-block partial sums of lam . dU/da_d u for the leaf cells
+        // per-block partial sums of lam . dU/da_d u for the leaf cells (the words of the leaf list, a thread per bit)
         template <int DIM>
-        __global__ void k_upwind_da(const __grid_constant__ Geom gp, const uint32_t* __restrict__ cells, const double* __restrict__ lam,
-                                    const double* __restrict__ u, UpwindAdj p, double* partial)
+        __global__ void k_upwind_da(const __grid_constant__ Geom gp, const int* __restrict__ wl_cells, const long long* __restrict__ lo,
+                                    const uint32_t* __restrict__ cells, const double* __restrict__ lam, const double* __restrict__ u, UpwindAdj p,
+                                    double* partial)
         {
             const Geom& g       = gp;
-            const long long tot = 32 * g.total_words;
+            const long long b0  = lo[LO_CELLS];
+            const long long tot = 32 * (lo[LO_CELLS + g.nlev] - b0);
             double acc[3]       = {0., 0., 0.};
-            for (long long k = gtid(); k < tot; k += gstride())
+            for (long long t = gtid(); t < tot; t += gstride())
             {
-                const long long w = k >> 5;
-                const int b       = static_cast<int>(k & 31);
+                const long long w = wl_cells[b0 + (t >> 5)];
+                const int b       = static_cast<int>(t & 31);
+                const long long k = 32 * w + b;
                 if (!((cells[w] >> b) & 1u) || lam[k] == 0.)
                 {
                     continue;
@@ -590,34 +603,35 @@ namespace
     {
         Ctx& c                 = ctx_of(adj);
         const sg::UpwindAdj p  = upwind_adj(adj);
-        const int nb_da        = sg::grid_of(32 * c.g.total_words);
+        const int nb_da        = sg::grid_of(32 * c.g.total_words); // grid-stride loops over the lists: a fixed grid for every mesh
         const sg::DeviceField& u = adj->u->f;
         int st;
         for (int n = e - 1; n >= s; --n)
         {
             const auto& S         = adj->steps[static_cast<size_t>(n)];
-            const uint32_t* cells = adj->bits[static_cast<size_t>(S.mesh0 + S.n_trans)];
+            const sg::DeviceMesh& m = c.m(); // the step's last mesh (its leaves are bits[mesh0 + n_trans])
+            const uint32_t* cells = m.cells;
             const double* ugn     = adj->ug[static_cast<size_t>(n - s)];
             // the upwind step u <- u - dt upwind(a, u) and its velocity derivative
             if (p.scheme == 0)
             {
                 if (c.g.dim == 2)
                 {
-                    sg::k_upwind_da<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], ugn, p, adj->d_partial);
+                    sg::k_upwind_da<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, m.wl_cells, m.d_lo, cells, adj->lam[0], ugn, p, adj->d_partial);
                 }
                 else
                 {
-                    sg::k_upwind_da<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], ugn, p, adj->d_partial);
+                    sg::k_upwind_da<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, m.wl_cells, m.d_lo, cells, adj->lam[0], ugn, p, adj->d_partial);
                 }
                 sg::k_sum_partials<<<1, sg::ABLOCK, 0, c.stream>>>(adj->d_partial, nb_da, adj->d_ga);
             }
             if (c.g.dim == 2)
             {
-                sg::k_upwind_adjoint<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], adj->lam[1], p);
+                sg::k_upwind_adjoint<2><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, m.wl_ref, m.d_lo, m.ref, cells, adj->lam[0], adj->lam[1], p);
             }
             else
             {
-                sg::k_upwind_adjoint<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, cells, adj->lam[0], adj->lam[1], p);
+                sg::k_upwind_adjoint<3><<<nb_da, sg::ABLOCK, 0, c.stream>>>(c.g, m.wl_ref, m.d_lo, m.ref, cells, adj->lam[0], adj->lam[1], p);
             }
             std::swap(adj->lam[0], adj->lam[1]);
             // the ghost update before it, on the step's last mesh

@@ -654,6 +654,83 @@ namespace sg
             }
         }
 
+        template <class A>
+        struct IsRev
+        {
+            static constexpr bool value = false;
+        };
+        template <int CAP>
+        struct IsRev<RevAcc<CAP>>
+        {
+            static constexpr bool value = true;
+        };
+
+        // The transposes of one projection and one prediction, written out instead of through linear forms: the
+        // weights are those the forms would carry (2^-dim for each child; +-8^-k for each tap of the order-1
+        // stencil, the signs and k as in predict_one), so the adjoint is the same operator, without building a form
+        // in local memory per item.  lam[e] (e the written element) is read, scattered and, in place, cleared.
+        template <int DIM, int CAP>
+        __device__ __forceinline__ void project_transpose(const Geom& g, const RevAcc<CAP>& u, long long e, int lf, int x, int y, int z)
+        {
+            const double ld = u.lam_in[e];
+            if (u.in_place)
+            {
+                u.lam_in[e] = 0.;
+            }
+            if (ld == 0.)
+            {
+                return;
+            }
+            const double wch = ld * (1.0 / static_cast<double>(1 << DIM));
+            const Box3 bx    = box_at<DIM>(g, lf, 2 * x, 2 * y, 2 * z, 2);
+            for (int sz = 0; sz < (DIM == 3 ? 2 : 1); ++sz)
+            {
+                for (int sy = 0; sy < 2; ++sy)
+                {
+                    const long long b = bx.base + sy * bx.sy + sz * bx.sz;
+                    atomicAdd(u.lam_out + b, wch);
+                    atomicAdd(u.lam_out + b + 1, wch);
+                }
+            }
+        }
+
+        template <int DIM, int CAP>
+        __device__ __forceinline__ void predict_transpose(const Geom& g, const RevAcc<CAP>& u, long long e, int l, int x, int y, int z, int order)
+        {
+            const double ld = u.lam_in[e];
+            if (u.in_place)
+            {
+                u.lam_in[e] = 0.;
+            }
+            if (ld == 0.)
+            {
+                return;
+            }
+            const int px = x >> 1, py = y >> 1, pz = z >> 1;
+            if (order == 0)
+            {
+                atomicAdd(u.lam_out + elem_at(g, l - 1, px, py, pz), ld);
+                return;
+            }
+            const int qx = x & 1, qy = y & 1, qz = z & 1;
+            const Box3 bx = box_at<DIM>(g, l - 1, px - 1, py - 1, pz - 1, 3);
+            for (int sz = 0; sz < (DIM == 3 ? 3 : 1); ++sz)
+            {
+                for (int sy = 0; sy < 3; ++sy)
+                {
+                    const long long base = bx.base + sy * bx.sy + sz * bx.sz;
+                    for (int sx = 0; sx < 3; ++sx)
+                    {
+                        const int k    = (sx != 1) + (sy != 1) + (DIM == 3 && sz != 1);
+                        const bool neg = ((sx == 0 && qx) || (sx == 2 && !qx)) ^ ((sy == 0 && qy) || (sy == 2 && !qy))
+                                         ^ (DIM == 3 && ((sz == 0 && qz) || (sz == 2 && !qz)));
+                        const double w = (k == 0 ? 1.0 : (k == 1 ? 0.125 : (k == 2 ? 0.015625 : 0.001953125))) * (neg ? -1.0 : 1.0);
+                        atomicAdd(u.lam_out + base + sx, w * ld);
+                    }
+                }
+            }
+        }
+
         // projection of the reference cells of level l onto proj_cells[l-1]
         // (numeric/projection.hpp:15-65), warps warp0, warp0+nwarps, ...
         template <int DIM, class A>
@@ -671,7 +748,14 @@ namespace sg
                       [&](long long w, int b)
                       {
                           const Cell c = cell_of(g, lc, w, b);
-                          u.put(32 * w + b, project_one<DIM>(g, u, l, c.x, c.y, c.z));
+                          if constexpr (IsRev<A>::value)
+                          {
+                              project_transpose<DIM>(g, u, 32 * w + b, l, c.x, c.y, c.z);
+                          }
+                          else
+                          {
+                              u.put(32 * w + b, project_one<DIM>(g, u, l, c.x, c.y, c.z));
+                          }
                       });
         }
 
@@ -691,7 +775,14 @@ namespace sg
                       [&](long long w, int b)
                       {
                           const Cell c = cell_of(g, l, w, b);
-                          u.put(32 * w + b, predict_one<DIM>(g, u, l, c.x, c.y, c.z, order));
+                          if constexpr (IsRev<A>::value)
+                          {
+                              predict_transpose<DIM>(g, u, 32 * w + b, l, c.x, c.y, c.z, order);
+                          }
+                          else
+                          {
+                              u.put(32 * w + b, predict_one<DIM>(g, u, l, c.x, c.y, c.z, order));
+                          }
                       });
         }
 
