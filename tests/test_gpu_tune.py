@@ -56,20 +56,21 @@ def test_autotune_keeps_state_and_results(sg):
     assert problem(sg).mesh.launch_shape() == tuned.mesh.launch_shape()
 
 
-@pytest.mark.parametrize("block,fuse", [(128, 512), (512, 32)])
-def test_launch_shapes_give_identical_results(sg, monkeypatch, block, fuse):
-    """shapes set through the environment (an override of the cache) change no bit"""
+@pytest.mark.parametrize("block,fuse,pairs", [(128, 512, 1), (512, 32, 0), (256, 0, 0)])
+def test_launch_shapes_give_identical_results(sg, monkeypatch, block, fuse, pairs):
+    """shapes set through the environment (an override of the cache) change no
+    bit, including one-level tag finalisation launches instead of pairs"""
     monkeypatch.setenv("SG_BLOCK", str(block))
     monkeypatch.setenv("SG_FUSE_WORDS_FIELD", str(fuse))
     monkeypatch.setenv("SG_FUSE_WORDS_MAX", str(fuse))
     monkeypatch.setenv("SG_MAX_BLOCKS", "300")
+    monkeypatch.setenv("SG_LEVEL_PAIRS", str(pairs))
     a = problem(sg, 8)
-    monkeypatch.delenv("SG_BLOCK")
-    monkeypatch.delenv("SG_FUSE_WORDS_FIELD")
-    monkeypatch.delenv("SG_FUSE_WORDS_MAX")
-    monkeypatch.delenv("SG_MAX_BLOCKS")
+    for k in ("SG_BLOCK", "SG_FUSE_WORDS_FIELD", "SG_FUSE_WORDS_MAX", "SG_MAX_BLOCKS", "SG_LEVEL_PAIRS"):
+        monkeypatch.delenv(k)
     b = problem(sg, 8)
     assert a.mesh.launch_shape()["block"] == block
+    assert a.mesh.launch_shape()["level_pairs"] == bool(pairs)
     dt = 0.5 / (1 << 8)
     for it in range(5):
         assert a.step(EPS, REG, A, dt) == b.step(EPS, REG, A, dt)
