@@ -71,6 +71,10 @@ def test_batch_argument_checks():
     assert L.sg_batch_create(1, arr, arr, 0, ctypes.byref(h)) == 1
     assert L.sg_batch_step(None, None, None, None, None, 0, None) == 1
     assert L.sg_batch_synchronize(None) == 1
+    assert L.sg_batch_autotune(None, None, None, None, None, 0, 3, None, None) == 1
+    assert L.sg_batch_launch_shape(None, None, None) == 1
+    assert L.sg_launch_shape(None, None, None, None, None, None, None, None) == 1
+    assert L.sg_autotune(None, None, 1e-4, 2.0, None, 0.1, 0, 3, None, None) == 1
 
 
 def test_mesh_create_rejects_unsupported_configurations():
