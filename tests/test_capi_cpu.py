@@ -4,6 +4,8 @@ is made here (there is no GPU)."""
 import ctypes
 import os
 import re
+import shutil
+import subprocess
 
 import pytest
 
@@ -138,3 +140,18 @@ def test_vector_field_argument_checks():
     assert L.sg_vector_upwind(None, None, None, 0.1, 0) == 1
     assert L.sg_vector_field_download(None, None, 0) == 1
     assert L.sg_vector_field_destroy(None) == 0
+
+
+def test_header_is_c99_and_a_c_client_links(tmp_path):
+    """include/samurai_gpu.h is a C header (strict C99, no warnings) and a C
+    program making the demo's loop through it links against the library"""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from samurai_gb300 import build
+    lib = build.build()
+    exe = str(tmp_path / "abi_c_client")
+    src = os.path.join(ROOT, "tests", "cpp", "abi_c_client.c")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I" + os.path.join(ROOT, "include"), src, "-o", exe,
+                        lib, "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
